@@ -1,0 +1,180 @@
+/*
+ * sse_gb300.h -- C-ABI of the GB300 (sm_103a) semi-discrete residual library.
+ *
+ * Drop-in for the right-hand side that StableSpectralElements.jl's
+ * `semidiscretize(...)` hands to OrdinaryDiffEq:
+ *
+ *   semi_discrete_residual!(dudt, u, solver, t)   src/Solvers/Solvers.jl:474-514
+ *     -> nodal_values!(u, solver, k)              standard_form_first_order.jl:1-14,
+ *                                                 flux_differencing_form.jl:253-292
+ *     -> time_derivative!(dudt, solver, k)        standard_form_first_order.jl:16-63,
+ *                                                 flux_differencing_form.jl:294-347
+ *
+ * A Julia `Solver{..., GB300}` owns one handle; the operator and geometry
+ * arrays are the fields of `solver.operators` / `solver.mass_solver` and
+ * `solver.connectivity`, passed by pointer in the reference's own
+ * column-major layouts (no transposition).  All arithmetic of the plain form
+ * is FP64, as in the reference.
+ *
+ * Threading: one handle = one CUDA stream.  Calls on one handle must be
+ * serialised by the caller (OrdinaryDiffEq calls the RHS from one thread);
+ * distinct handles are independent.  No function throws; every function
+ * returns an sse_status and leaves a message for sse_last_error().
+ */
+#ifndef SSE_GB300_H
+#define SSE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SSE_ABI_VERSION 1
+
+typedef enum sse_status {
+  SSE_OK = 0,
+  SSE_ERR_INVALID_ARGUMENT = 1, /* null pointer, size mismatch, bad index */
+  SSE_ERR_UNSUPPORTED = 2,      /* combination the library does not implement */
+  SSE_ERR_CUDA = 3,             /* CUDA runtime error (message in sse_last_error) */
+  SSE_ERR_NONPHYSICAL = 4,      /* non-finite result or non-positive density/pressure */
+  SSE_ERR_OUT_OF_MEMORY = 5
+} sse_status;
+
+/* Residual form: StandardForm / FluxDifferencingForm (Solvers.jl:90-115). */
+enum sse_form { SSE_STANDARD_FORM = 0, SSE_FLUX_DIFFERENCING_FORM = 1 };
+/* Conservation law (ConservationLaws.jl:192-204). */
+enum sse_law { SSE_LINEAR_ADVECTION = 0, SSE_EULER = 1 };
+/* Interface numerical flux (ConservationLaws.jl:52-62). */
+enum sse_numerical_flux {
+  SSE_LAX_FRIEDRICHS = 0,        /* LaxFriedrichsNumericalFlux(λ): halfλ = λ/2 */
+  SSE_CENTRAL = 1,               /* CentralNumericalFlux */
+  SSE_ENTROPY_CONSERVATIVE = 2   /* EntropyConservativeNumericalFlux */
+};
+/* Two-point flux (ConservationLaws.jl:70-73). */
+enum sse_two_point_flux { SSE_CONSERVATIVE_FLUX = 0, SSE_EC_FLUX = 1 };
+/* Mass-matrix solver (mass_matrix.jl:1-17). */
+enum sse_mass_solver { SSE_WEIGHT_ADJUSTED = 0, SSE_DIAGONAL = 1 };
+/* Arithmetic of the bulk flux/operator work. */
+enum sse_precision { SSE_FP64 = 0, SSE_MIXED = 1 };
+/* Where the caller's state buffers live. */
+enum sse_memory { SSE_HOST = 0, SSE_DEVICE = 1 };
+/* Time integrators (OrdinaryDiffEq algorithms the reference's tests use). */
+enum sse_rk_scheme { SSE_CARPENTER_KENNEDY_2N54 = 0, SSE_RK4 = 1 };
+
+typedef struct sse_config {
+  int32_t d;              /* spatial dimension: 2 (Tri) or 3 (Tet) */
+  int32_t n_p;            /* solution coefficients per element (size(V, 2)) */
+  int32_t n_q;            /* volume quadrature nodes (size(V, 1)) */
+  int32_t n_f;            /* facet quadrature nodes (size(R, 1)) */
+  int32_t n_c;            /* conservative variables */
+  int32_t n_e;            /* elements */
+  int32_t num_faces;      /* 3 (Tri) or 4 (Tet) */
+  int32_t nodes_per_face; /* FluxDifferencingOperators.nodes_per_face */
+  int32_t form;           /* enum sse_form */
+  int32_t law;            /* enum sse_law */
+  int32_t numerical_flux; /* enum sse_numerical_flux */
+  int32_t two_point_flux; /* enum sse_two_point_flux (FluxDifferencingForm) */
+  int32_t mass_solver;    /* enum sse_mass_solver */
+  int32_t reserved;
+  double half_lambda;     /* LaxFriedrichsNumericalFlux.halfλ */
+  double gamma;           /* EulerEquations.γ */
+  double a[3];            /* LinearAdvectionEquation.a */
+} sse_config;
+
+/* SparseArrays.SparseMatrixCSC{Float64,Int64} fields, 1-based as in Julia. */
+typedef struct sse_csc {
+  int64_t m, n;
+  const int64_t *colptr; /* n + 1 entries */
+  const int64_t *rowval; /* nnz entries */
+  const double *nzval;   /* nnz entries */
+} sse_csc;
+
+typedef struct sse_operators {
+  /* V: WarpedTensorProductMap2D/3D factors (warped_product_2d.jl:2-23,
+   * warped_product_3d.jl:2-36), all NULL when V is the identity
+   * (NodalTensor's UniformScalingMap). */
+  int32_t vdm_p;             /* polynomial degree p */
+  int32_t vdm_m[3];          /* M1, M2, M3: 1-D quadrature sizes */
+  const double *vdm_A;       /* M1 x (p+1) */
+  const double *vdm_B;       /* M2 x (p+1) x (p+1) */
+  const double *vdm_C;       /* M3 x (p+1) x (p+1) x (p+1), Tet only */
+  const int64_t *vdm_sigma_in; /* (p+1)^d modal index, 1-based, 0 if unused */
+  /* R: volume -> facet interpolation, sparse(Matrix(R)), N_f x N_q */
+  sse_csc R;
+  /* StandardForm (ReferenceOperators.D, operators.jl:25): N_q x N_q each */
+  sse_csc D[3];
+  /* FluxDifferencingForm (FluxDifferencingOperators.S, C; operators.jl:192-200) */
+  sse_csc S[3];              /* N_q x N_q each */
+  sse_csc C;                 /* N_q x N_f; nnz = 0 means no facet correction */
+} sse_operators;
+
+typedef struct sse_geometry {
+  /* both forms */
+  const double *BJf;         /* N_f x N_e        : B .* J_f */
+  const double *n_f;         /* d x N_f x N_e    : nJf ./ J_f */
+  const int64_t *mapP;       /* N_f x N_e        : 1-based linear index into (N_f, N_e) */
+  /* StandardForm: ReferenceOperators.halfWΛ packed as N_q x d x d x N_e */
+  const double *halfWLambda;
+  /* FluxDifferencingForm */
+  const double *WJ;          /* N_q x N_e        : W .* J_q */
+  const double *Lambda_q;    /* N_q x d x d x N_e */
+  const double *halfnJf;     /* d x N_f x N_e */
+  const double *halfnJq;     /* d x num_faces x N_q x N_e */
+  /* mass solver */
+  const double *JinvW;       /* N_q x N_e : WeightAdjustedSolver.J⁻¹W (W ./ J_q) */
+  const double *WJinv;       /* N_q x N_e : DiagonalSolver.WJ⁻¹ (1 ./ (W .* J_q)) */
+} sse_geometry;
+
+typedef struct sse_solver sse_solver;
+
+/* Library ABI version (SSE_ABI_VERSION). */
+int32_t sse_abi_version(void);
+
+/* Build a handle: validates sizes and indices, deep-copies operators and
+ * geometry to the current CUDA device and allocates the per-element scratch
+ * (u_q, u_f) that Solver.preallocated_arrays holds in the reference
+ * (Solvers.jl:183-209).  Replaces Solver(...) + the Threaded/Serial parallelism
+ * tag (Solvers.jl:287-333, 429-452). */
+int32_t sse_create(const sse_config *cfg, const sse_operators *ops,
+                   const sse_geometry *geo, sse_solver **out);
+int32_t sse_destroy(sse_solver *s);
+
+/* dudt <- R(u): semi_discrete_residual!(dudt, u, solver, t), Solvers.jl:474-514.
+ * u and dudt are N_p x N_c x N_e column-major FP64, host or device memory. */
+int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t,
+                     int32_t memory);
+
+/* Phase A alone: nodal_values! for every element (standard_form_first_order.jl:
+ * 1-14, flux_differencing_form.jl:253-292).  u_q is N_q x N_c x N_e and u_f is
+ * N_f x N_e x N_c, the reference's PreAllocatedArraysFirstOrder layouts. */
+int32_t sse_nodal_values(sse_solver *s, const double *u, double *u_q, double *u_f,
+                         int32_t memory);
+
+/* n_steps fixed-step time steps of OrdinaryDiffEq's CarpenterKennedy2N54 or
+ * RK4 (solve(ode, alg; dt, adaptive=false)), entirely on the device; u is
+ * advanced in place and *t by n_steps*dt. */
+int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt,
+                     int32_t scheme, double *t, int32_t memory);
+
+/* FP64 reductions of Analysis/conservation.jl:145-189 for one (u, dudt):
+ * out[0..N_c-1] = sum_k 1' WJ V dudt[:, e, k]       (primary conservation)
+ * out[N_c]      = sum_k (P w)' M dudt               (entropy production, Euler)
+ *               = sum_k u' M dudt                   (energy, advection) */
+int32_t sse_conservation_residual(sse_solver *s, const double *u, const double *dudt,
+                                  double *out, int32_t memory);
+
+/* SSE_FP64 (default, the drop-in) or SSE_MIXED (FP32 fluxes and operator
+ * arithmetic, FP64 geometry, RK accumulation and reductions). */
+int32_t sse_set_precision(sse_solver *s, int32_t precision);
+
+/* Message of the last failing call on this handle ("" if none). */
+const char *sse_last_error(const sse_solver *s);
+/* Message of the last failing sse_create (no handle exists then). */
+const char *sse_create_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SSE_GB300_H */
