@@ -1,0 +1,251 @@
+"""Benchmark: DOF-stage updates per second of the semi-discrete residual on
+the 3-D Euler Taylor-Green workload (16^3 x 6 = 24,576 curved tetrahedra,
+ModalTensor(4), FluxDifferencingForm with the entropy-conservative volume
+flux and Lax-Friedrichs interface dissipation, CarpenterKennedy2N54).
+
+One step = one CarpenterKennedy2N54 time step = 5 residual evaluations and
+stage updates on the whole mesh; DOF = N_p * N_c * N_e (get_dof).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the reference's residual restated in C (OpenMP
+over elements on all host cores, the reference's ``Threaded()`` strategy)
+on the same workload; Julia is not available to run the reference itself.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__  # noqa: E402
+
+METRIC = "DOF-stage updates/s, 3D Euler p4 tets, FP64 vs mixed at fixed err; adj/fwd cost"
+UNIT = "DOF-stage updates/s"
+WORKLOAD = {"workload": "3-D Euler Taylor-Green vortex, Mach 0.1, periodic [0,2pi]^3",
+            "mesh": "16^3 hexahedra x 6 = 24576 curved tetrahedra (Chan warp 0.05)",
+            "approximation": "ModalTensor(4) on Tet, N_p=35, N_q=125, N_f=100",
+            "form": "FluxDifferencingForm, entropy-conservative (Ranocha) volume flux + Lax-Friedrichs",
+            "metrics": "ChanWilcox (conservative curl)",
+            "time_integrator": "CarpenterKennedy2N54 (5 stages per step)",
+            "dof": None,
+            "l2_policy": "inputs larger than L2: metric terms and states ~0.7 GB read per stage"}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_problem(cells: int):
+    pkg = __graft_entry__.load_package()
+    pb = pkg.setups.tgv_tet(cells=cells, p=4, lf=True)
+    return pkg, pb, pb.host_arrays()
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    from oracle.oracle import Oracle
+    pkg, pb, host = build_problem(args.cells)
+    o = Oracle(host)
+    u = pb.u0.copy()
+    for _ in range(args.warmup):
+        u = o.rk_steps(u, 1, pb.dt, 0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        u = o.rk_steps(u, 1, pb.dt, 0)
+    dt = time.perf_counter() - t0
+    value = host.dof * 5 * args.steps / dt
+    cfg = dict(WORKLOAD, dof=host.dof)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": o.nthreads, "kind": "port",
+                             "sample": f"{args.steps} full CarpenterKennedy2N54 steps on the whole "
+                                       f"mesh; reference restated in C (OpenMP), not the Julia "
+                                       f"reference itself"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def cpu_baseline(pb, host, budget_s: float):
+    from oracle.oracle import Oracle
+    o = Oracle(host)
+    u = pb.u0
+    o.residual(u)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.residual(u)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    t = (time.perf_counter() - t0) / n
+    return {"value": host.dof / t, "unit": UNIT, "cores": o.nthreads, "kind": "port",
+            "sample": f"{n} residual evaluations (one stage each) on the whole 24576-tet mesh; "
+                      f"reference restated in C with OpenMP over elements"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=16)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pkg, pb, host = build_problem(args.cells)
+    pkg.build.build()
+    gpu = pkg.GB300Solver(host)
+    stream = torch.cuda.current_stream()
+    gpu.set_stream(stream.cuda_stream)
+    u = torch.from_numpy(pb.u0).cuda()
+    dt = pb.dt
+
+    # ---- device-resident throughput (value)
+    for _ in range(args.warmup):
+        gpu.rk_steps(u, 1, dt)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        gpu.rk_steps(u, 1, dt)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * host.dof * 5 * args.steps / (ms * 1e-3)
+
+    # ---- per-kernel timings (CUDA events on the launching stream) and roofline
+    phases = gpu.phase_timings(u, 5)
+    work = pkg.flops_model.model(host)
+    fp64_peak, fp32_peak = pkg.gb300.measure_fma_peaks()
+    ne = host.N_e
+    dom = "B" if phases[1] >= phases[0] else "A"
+    dom_ms = phases[1] if dom == "B" else phases[0]
+    dom_flops = (work.flops_B if dom == "B" else work.flops_A) * ne
+    dom_bytes = (work.bytes_B if dom == "B" else work.bytes_A) * ne
+    achieved = dom_flops / (dom_ms * 1e-3) / 1e12
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak,
+                "kernel": "fd_time_derivative_kernel" if dom == "B" else "nodal_values_kernel",
+                "peak_source": "measured live: FP64 FMA-chain microbenchmark on this GPU",
+                "hbm_achieved_gbs": dom_bytes / (dom_ms * 1e-3) / 1e9,
+                "hbm_frac_of_measured": dom_bytes / (dom_ms * 1e-3) / 1e9 / hbm_peak,
+                "traffic": None,
+                "phase_ms": {"nodal_values": phases[0], "time_derivative": phases[1],
+                             "rk_stage_update": phases[2]},
+                "algorithmic_flops_per_element": {"nodal_values": work.flops_A,
+                                                  "time_derivative": work.flops_B},
+                "whole_stage_frac": (work.flops * ne) / ((phases[0] + phases[1]) * 1e-3) / 1e12 / fp64_peak,
+                "fp32_peak_tflops": fp32_peak}
+
+    # ---- end to end through the C-ABI with host (pinned) buffers
+    u_host = torch.from_numpy(pb.u0.copy()).pin_memory()
+    gpu.rk_steps(u_host, 1, dt)
+    torch.cuda.synchronize()
+    e2e_steps = max(2, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        gpu.rk_steps(u_host, 1, dt)           # H2D copy, 5 stages, D2H copy
+    e2e_s = time.perf_counter() - t0
+    nbytes = host.dof * 8
+    e2e = {"value": world * host.dof * 5 * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+
+    launches = args.steps * 5 * 3
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(WORKLOAD, dof=host.dof, form_precision="FP64 (drop-in form)",
+                           parallelism="replicas only" if world > 1 else "1 GPU"),
+            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(pb, host, args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

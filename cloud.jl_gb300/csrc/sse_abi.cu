@@ -1,0 +1,695 @@
+// sse_abi.cu -- C-ABI of the GB300 residual library (include/sse_gb300.h).
+//
+// Host side of the drop-in for `Solver{..., GB300}` + `semi_discrete_residual!`
+// (src/Solvers/Solvers.jl:259-333, 474-514): validates the caller's operator
+// and geometry arrays, converts the Julia CSC matrices into the pair and
+// CSR tables the kernels use, keeps everything resident on the device and
+// launches the two residual phases on the handle's stream.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sse_gb300.h"
+#include "sse_kernels.cuh"
+
+using namespace sse;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// Carpenter & Kennedy (1994), NASA TM-109112: five-stage fourth-order
+// 2N-storage Runge-Kutta coefficients (CarpenterKennedy2N54).
+const double kCKA[5] = {0.0, -567301805773.0 / 1357537059087.0,
+                        -2404267990393.0 / 2016746695238.0,
+                        -3550918686646.0 / 2091501179385.0,
+                        -1275806237668.0 / 842570457699.0};
+const double kCKB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                        1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                        2277821191437.0 / 14882151754819.0};
+
+struct Status {
+  int code = SSE_OK;
+  std::string msg;
+};
+
+struct CsrHost {
+  std::vector<int> ptr, idx;
+  std::vector<double> val;
+};
+
+}  // namespace
+
+struct sse_solver {
+  sse_config cfg{};
+  KernelArgs ka{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<void *> allocations;  // device buffers owned by the handle
+  double *d_u = nullptr, *d_dudt = nullptr, *d_tmp = nullptr, *d_acc = nullptr, *d_ust = nullptr;
+  double *d_partial = nullptr, *d_uf_ref = nullptr;
+  int *d_flag = nullptr;
+  int precision = SSE_FP64;
+  std::string last_error;
+};
+
+namespace {
+
+int fail(sse_solver *s, int code, const std::string &msg) {
+  if (s) s->last_error = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(sse_solver *s, cudaError_t e, const char *where) {
+  return fail(s, SSE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+cudaError_t upload(sse_solver *s, const T *host, size_t n, const T **dev) {
+  *dev = nullptr;
+  if (n == 0) return cudaSuccess;
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  s->allocations.push_back(p);
+  e = cudaMemcpy(p, host, n * sizeof(T), cudaMemcpyHostToDevice);
+  *dev = (const T *)p;
+  return e;
+}
+
+cudaError_t alloc(sse_solver *s, size_t bytes, void **out) {
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes > 0 ? bytes : 8);
+  if (e != cudaSuccess) return e;
+  s->allocations.push_back(p);
+  *out = p;
+  return cudaSuccess;
+}
+
+// validate a Julia CSC matrix of the expected shape
+bool csc_ok(const sse_csc &A, int64_t m, int64_t n, std::string &why, const char *name) {
+  if (A.m != m || A.n != n || !A.colptr) {
+    why = std::string(name) + ": expected " + std::to_string(m) + "x" + std::to_string(n) +
+          " CSC matrix";
+    return false;
+  }
+  if (A.colptr[0] != 1) { why = std::string(name) + ": colptr must start at 1"; return false; }
+  for (int64_t j = 0; j < n; ++j)
+    if (A.colptr[j + 1] < A.colptr[j]) { why = std::string(name) + ": colptr not monotone"; return false; }
+  int64_t nnz = A.colptr[n] - 1;
+  if (nnz > 0 && (!A.rowval || !A.nzval)) { why = std::string(name) + ": null rowval/nzval"; return false; }
+  for (int64_t q = 0; q < nnz; ++q)
+    if (A.rowval[q] < 1 || A.rowval[q] > m) { why = std::string(name) + ": row index out of range"; return false; }
+  return true;
+}
+
+// CSC (m x n) -> CSR rows of A (transpose = false) or of A^T (transpose = true)
+CsrHost csc_to_csr(const sse_csc &A, bool transpose) {
+  CsrHost out;
+  int64_t rows = transpose ? A.n : A.m;
+  out.ptr.assign(rows + 1, 0);
+  int64_t nnz = A.colptr[A.n] - 1;
+  if (transpose) {
+    for (int64_t j = 0; j < A.n; ++j) {
+      for (int64_t q = A.colptr[j] - 1; q < A.colptr[j + 1] - 1; ++q) {
+        out.idx.push_back((int)(A.rowval[q] - 1));
+        out.val.push_back(A.nzval[q]);
+      }
+      out.ptr[j + 1] = (int)out.idx.size();
+    }
+    return out;
+  }
+  std::vector<int> count(A.m, 0);
+  for (int64_t q = 0; q < nnz; ++q) count[A.rowval[q] - 1]++;
+  for (int64_t i = 0; i < A.m; ++i) out.ptr[i + 1] = out.ptr[i] + count[i];
+  out.idx.resize(nnz);
+  out.val.resize(nnz);
+  std::vector<int> fill(out.ptr.begin(), out.ptr.end() - 1);
+  for (int64_t j = 0; j < A.n; ++j)
+    for (int64_t q = A.colptr[j] - 1; q < A.colptr[j + 1] - 1; ++q) {
+      int i = (int)(A.rowval[q] - 1);
+      out.idx[fill[i]] = (int)j;
+      out.val[fill[i]] = A.nzval[q];
+      fill[i]++;
+    }
+  return out;
+}
+
+int upload_csr(sse_solver *s, const CsrHost &c, const int **ptr, const int **idx, const double **val) {
+  cudaError_t e;
+  if ((e = upload(s, c.ptr.data(), c.ptr.size(), ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");
+  if ((e = upload(s, c.idx.data(), c.idx.size(), idx)) != cudaSuccess) return cuda_fail(s, e, "upload");
+  if ((e = upload(s, c.val.data(), c.val.size(), val)) != cudaSuccess) return cuda_fail(s, e, "upload");
+  return SSE_OK;
+}
+
+size_t geo_len(const sse_config &c, int what) {
+  size_t d = c.d, nq = c.n_q, nf = c.n_f, ne = c.n_e;
+  switch (what) {
+    case 0: return nf * ne;                 // BJf
+    case 1: return d * nf * ne;             // n_f
+    case 2: return nq * d * d * ne;         // halfWLambda / Lambda_q
+    case 3: return nq * ne;                 // WJ / JinvW / WJinv
+    case 4: return d * nf * ne;             // halfnJf
+    case 5: return d * c.num_faces * nq * ne;  // halfnJq
+  }
+  return 0;
+}
+
+int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const sse_geometry *geo) {
+  const sse_config &c = *cfg;
+  std::string why;
+  if (!(c.d == 2 || c.d == 3)) return fail(s, SSE_ERR_UNSUPPORTED, "d must be 2 or 3");
+  if (!((c.law == SSE_LINEAR_ADVECTION && c.n_c == 1) || (c.law == SSE_EULER && c.n_c == c.d + 2)))
+    return fail(s, SSE_ERR_UNSUPPORTED, "law / n_c combination not supported");
+  if (c.n_p <= 0 || c.n_q <= 0 || c.n_f <= 0 || c.n_e <= 0 || c.num_faces <= 0 ||
+      c.nodes_per_face * c.num_faces != c.n_f)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "invalid sizes in sse_config");
+  if (c.n_q > 65535 || c.n_f > 65535) return fail(s, SSE_ERR_UNSUPPORTED, "n_q, n_f must be < 65536");
+  if (c.form != SSE_STANDARD_FORM && c.form != SSE_FLUX_DIFFERENCING_FORM)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown form");
+  if (c.numerical_flux < 0 || c.numerical_flux > 2) return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown numerical flux");
+  if (c.mass_solver != SSE_WEIGHT_ADJUSTED && c.mass_solver != SSE_DIAGONAL)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown mass solver");
+  if (c.law == SSE_EULER && !(c.gamma > 1.0)) return fail(s, SSE_ERR_INVALID_ARGUMENT, "gamma must exceed 1");
+  if ((double)c.n_f * c.n_e > 2.0e9 || (double)c.n_q * c.n_c * c.n_e > 4.0e18)
+    return fail(s, SSE_ERR_UNSUPPORTED, "mesh too large for 32-bit facet indices");
+  const bool fd = c.form == SSE_FLUX_DIFFERENCING_FORM;
+  const bool has_vdm = ops->vdm_A != nullptr;
+  if (!has_vdm && c.n_p != c.n_q) return fail(s, SSE_ERR_INVALID_ARGUMENT, "V = I requires n_p == n_q");
+  if (c.mass_solver == SSE_WEIGHT_ADJUSTED && !has_vdm)
+    return fail(s, SSE_ERR_UNSUPPORTED, "WeightAdjustedSolver requires a modal V");
+  if (!geo->BJf || !geo->n_f || !geo->mapP || !geo->WJ)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: BJf, n_f, mapP and WJ are required");
+  if (c.mass_solver == SSE_WEIGHT_ADJUSTED && !geo->JinvW)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: JinvW required for WeightAdjustedSolver");
+  if (c.mass_solver == SSE_DIAGONAL && !geo->WJinv)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: WJinv required for DiagonalSolver");
+  if (fd && (!geo->Lambda_q || !geo->halfnJf || !geo->halfnJq))
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: Lambda_q, halfnJf, halfnJq required for FluxDifferencingForm");
+  if (!fd && !geo->halfWLambda)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: halfWLambda required for StandardForm");
+  if (!csc_ok(ops->R, c.n_f, c.n_q, why, "R")) return fail(s, SSE_ERR_INVALID_ARGUMENT, why);
+  for (int m = 0; m < c.d; ++m) {
+    if (fd) {
+      if (!csc_ok(ops->S[m], c.n_q, c.n_q, why, "S")) return fail(s, SSE_ERR_INVALID_ARGUMENT, why);
+    } else if (!csc_ok(ops->D[m], c.n_q, c.n_q, why, "D")) {
+      return fail(s, SSE_ERR_INVALID_ARGUMENT, why);
+    }
+  }
+  const bool has_C = fd && ops->C.colptr && ops->C.n > 0;
+  if (has_C && !csc_ok(ops->C, c.n_q, c.n_f, why, "C")) return fail(s, SSE_ERR_INVALID_ARGUMENT, why);
+
+  // ---- warped tensor-product factors (validated before any device work)
+  int p1 = 0, M1 = 0, M2 = 0, M3 = 1;
+  std::vector<int> sigma, modes, b12, b12_index;
+  if (has_vdm) {
+    p1 = ops->vdm_p + 1;
+    M1 = ops->vdm_m[0]; M2 = ops->vdm_m[1]; M3 = c.d == 3 ? ops->vdm_m[2] : 1;
+    if (p1 < 1 || p1 > 16 || M1 < 1 || M2 < 1 || M3 < 1 || M1 * M2 * M3 != c.n_q || !ops->vdm_B ||
+        !ops->vdm_sigma_in || (c.d == 3 && !ops->vdm_C))
+      return fail(s, SSE_ERR_INVALID_ARGUMENT, "inconsistent warped tensor-product factors");
+    size_t nsig = (size_t)p1 * p1 * (c.d == 3 ? p1 : 1);
+    sigma.assign(nsig, -1);
+    modes.assign(c.n_p, -1);
+    b12_index.assign((size_t)p1 * p1, -1);
+    int count = 0;
+    for (size_t t = 0; t < nsig; ++t) {
+      int64_t l = ops->vdm_sigma_in[t];
+      if (l < 0 || l > c.n_p) return fail(s, SSE_ERR_INVALID_ARGUMENT, "sigma_in out of range");
+      if (l == 0) continue;
+      int b1 = (int)(t % p1), b2 = (int)((t / p1) % p1), b3 = c.d == 3 ? (int)(t / (p1 * p1)) : 0;
+      if (b1 + b2 + b3 >= p1) return fail(s, SSE_ERR_INVALID_ARGUMENT, "sigma_in outside the simplex");
+      if (modes[l - 1] != -1) return fail(s, SSE_ERR_INVALID_ARGUMENT, "sigma_in repeats a mode");
+      sigma[t] = (int)(l - 1);
+      modes[l - 1] = b1 | (b2 << 8) | (b3 << 16);
+      ++count;
+    }
+    if (count != c.n_p) return fail(s, SSE_ERR_INVALID_ARGUMENT, "sigma_in must enumerate n_p modes");
+    for (int b1 = 0; b1 < p1; ++b1)
+      for (int b2 = 0; b1 + b2 < p1; ++b2) {
+        b12_index[b1 + p1 * b2] = (int)b12.size();
+        b12.push_back(b1 | (b2 << 8));
+      }
+  }
+  // ---- connectivity (validated before any device work)
+  std::vector<int> mapP((size_t)c.n_f * c.n_e);
+  {
+    const int64_t lim = (int64_t)c.n_f * c.n_e;
+    for (size_t t = 0; t < mapP.size(); ++t) {
+      int64_t P = geo->mapP[t];
+      if (P < 1 || P > lim) return fail(s, SSE_ERR_INVALID_ARGUMENT, "mapP index out of range");
+      mapP[t] = (int)(P - 1);
+    }
+  }
+
+  s->cfg = c;
+  KernelArgs &ka = s->ka;
+  DevOps &op = ka.op;
+  op.d = c.d; op.nc = c.n_c; op.np = c.n_p; op.nq = c.n_q; op.nf = c.n_f;
+  op.nfac = c.num_faces; op.npf = c.nodes_per_face;
+  cudaError_t e;
+
+  op.has_vdm = has_vdm;
+  if (has_vdm) {
+    op.p1 = p1; op.M1 = M1; op.M2 = M2; op.M3 = M3;
+    op.nb12 = (int)b12.size();
+    if ((e = upload(s, ops->vdm_A, (size_t)M1 * p1, &op.A)) != cudaSuccess) return cuda_fail(s, e, "upload A");
+    if ((e = upload(s, ops->vdm_B, (size_t)M2 * p1 * p1, &op.B)) != cudaSuccess) return cuda_fail(s, e, "upload B");
+    if (c.d == 3 && (e = upload(s, ops->vdm_C, (size_t)M3 * p1 * p1 * p1, &op.C)) != cudaSuccess)
+      return cuda_fail(s, e, "upload C");
+    if ((e = upload(s, sigma.data(), sigma.size(), &op.sigma)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    if ((e = upload(s, modes.data(), modes.size(), &op.modes)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    if ((e = upload(s, b12.data(), b12.size(), &op.b12)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    if ((e = upload(s, b12_index.data(), b12_index.size(), &op.b12_index)) != cudaSuccess)
+      return cuda_fail(s, e, "upload");
+  }
+
+  // ---- R, R^T, D, D^T
+  int rc;
+  if ((rc = upload_csr(s, csc_to_csr(ops->R, false), &op.R_ptr, &op.R_idx, &op.R_val))) return rc;
+  if ((rc = upload_csr(s, csc_to_csr(ops->R, true), &op.Rt_ptr, &op.Rt_idx, &op.Rt_val))) return rc;
+  if (!fd) {
+    for (int m = 0; m < c.d; ++m) {
+      if ((rc = upload_csr(s, csc_to_csr(ops->D[m], false), &op.D_ptr[m], &op.D_idx[m], &op.D_val[m]))) return rc;
+      if ((rc = upload_csr(s, csc_to_csr(ops->D[m], true), &op.Dt_ptr[m], &op.Dt_idx[m], &op.Dt_val[m]))) return rc;
+    }
+  }
+
+  // ---- flux-differencing pair tables
+  if (fd) {
+    // unique pairs (i < j) over the union of the S_m patterns, ordered by (j, i)
+    std::vector<std::pair<int, int>> pairs;
+    for (int m = 0; m < c.d; ++m) {
+      const sse_csc &S = ops->S[m];
+      for (int64_t j = 0; j < S.n; ++j)
+        for (int64_t q = S.colptr[j] - 1; q < S.colptr[j + 1] - 1; ++q) {
+          int i = (int)(S.rowval[q] - 1);
+          if (i < j) pairs.emplace_back((int)j, i);
+        }
+    }
+    std::sort(pairs.begin(), pairs.end());
+    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+    const int nvp = (int)pairs.size();
+    std::vector<int> vp_ij(nvp);
+    std::vector<double> vp_S((size_t)nvp * c.d, 0.0);
+    for (int t = 0; t < nvp; ++t) vp_ij[t] = pairs[t].second | (pairs[t].first << 16);
+    for (int m = 0; m < c.d; ++m) {
+      const sse_csc &S = ops->S[m];
+      for (int64_t j = 0; j < S.n; ++j)
+        for (int64_t q = S.colptr[j] - 1; q < S.colptr[j + 1] - 1; ++q) {
+          int i = (int)(S.rowval[q] - 1);
+          if (i >= j) continue;
+          auto it = std::lower_bound(pairs.begin(), pairs.end(), std::make_pair((int)j, i));
+          vp_S[(size_t)(it - pairs.begin()) * c.d + m] = S.nzval[q];
+        }
+    }
+    std::vector<std::vector<int>> inc(c.n_q);
+    for (int t = 0; t < nvp; ++t) {
+      inc[pairs[t].second].push_back((t << 1) | 1);
+      inc[pairs[t].first].push_back(t << 1);
+    }
+    std::vector<int> inc_ptr(c.n_q + 1, 0), inc_flat;
+    for (int i = 0; i < c.n_q; ++i) {
+      inc_flat.insert(inc_flat.end(), inc[i].begin(), inc[i].end());
+      inc_ptr[i + 1] = (int)inc_flat.size();
+    }
+    op.nvp = nvp;
+    if ((e = upload(s, vp_ij.data(), vp_ij.size(), &op.vp_ij)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    if ((e = upload(s, vp_S.data(), vp_S.size(), &op.vp_S)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    if ((e = upload(s, inc_ptr.data(), inc_ptr.size(), &op.vp_inc_ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    if ((e = upload(s, inc_flat.data(), inc_flat.size(), &op.vp_inc)) != cudaSuccess) return cuda_fail(s, e, "upload");
+
+    op.nfp = 0;
+    if (has_C) {
+      const sse_csc &Cm = ops->C;
+      std::vector<int> fp_ij;
+      std::vector<double> fp_C;
+      std::vector<std::vector<int>> qinc(c.n_q), finc(c.n_f);
+      for (int64_t j = 0; j < Cm.n; ++j)
+        for (int64_t q = Cm.colptr[j] - 1; q < Cm.colptr[j + 1] - 1; ++q) {
+          int i = (int)(Cm.rowval[q] - 1);
+          int t = (int)fp_ij.size();
+          fp_ij.push_back(i | ((int)j << 16));
+          fp_C.push_back(Cm.nzval[q]);
+          qinc[i].push_back(t);
+          finc[j].push_back(t);
+        }
+      std::vector<int> qptr(c.n_q + 1, 0), qflat, fptr(c.n_f + 1, 0), fflat;
+      for (int i = 0; i < c.n_q; ++i) { qflat.insert(qflat.end(), qinc[i].begin(), qinc[i].end()); qptr[i + 1] = (int)qflat.size(); }
+      for (int j = 0; j < c.n_f; ++j) { fflat.insert(fflat.end(), finc[j].begin(), finc[j].end()); fptr[j + 1] = (int)fflat.size(); }
+      op.nfp = (int)fp_ij.size();
+      if ((e = upload(s, fp_ij.data(), fp_ij.size(), &op.fp_ij)) != cudaSuccess) return cuda_fail(s, e, "upload");
+      if ((e = upload(s, fp_C.data(), fp_C.size(), &op.fp_C)) != cudaSuccess) return cuda_fail(s, e, "upload");
+      if ((e = upload(s, qptr.data(), qptr.size(), &op.fp_q_ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");
+      if ((e = upload(s, qflat.data(), qflat.size(), &op.fp_q)) != cudaSuccess) return cuda_fail(s, e, "upload");
+      if ((e = upload(s, fptr.data(), fptr.size(), &op.fp_f_ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");
+      if ((e = upload(s, fflat.data(), fflat.size(), &op.fp_f)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    }
+  }
+
+  // ---- geometry
+  DevGeo &g = ka.geo;
+  if ((e = upload(s, mapP.data(), mapP.size(), &g.mapP)) != cudaSuccess) return cuda_fail(s, e, "upload mapP");
+  if ((e = upload(s, geo->BJf, geo_len(c, 0), &g.BJf)) != cudaSuccess) return cuda_fail(s, e, "upload BJf");
+  if ((e = upload(s, geo->n_f, geo_len(c, 1), &g.n_f)) != cudaSuccess) return cuda_fail(s, e, "upload n_f");
+  if ((e = upload(s, geo->WJ, geo_len(c, 3), &g.WJ)) != cudaSuccess) return cuda_fail(s, e, "upload WJ");
+  if (geo->JinvW && (e = upload(s, geo->JinvW, geo_len(c, 3), &g.JinvW)) != cudaSuccess) return cuda_fail(s, e, "upload");
+  if (geo->WJinv && (e = upload(s, geo->WJinv, geo_len(c, 3), &g.WJinv)) != cudaSuccess) return cuda_fail(s, e, "upload");
+  if (fd) {
+    if ((e = upload(s, geo->Lambda_q, geo_len(c, 2), &g.Lambda_q)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    if ((e = upload(s, geo->halfnJf, geo_len(c, 4), &g.halfnJf)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    if ((e = upload(s, geo->halfnJq, geo_len(c, 5), &g.halfnJq)) != cudaSuccess) return cuda_fail(s, e, "upload");
+  } else {
+    if ((e = upload(s, geo->halfWLambda, geo_len(c, 2), &g.halfWLambda)) != cudaSuccess) return cuda_fail(s, e, "upload");
+  }
+
+  // ---- physics
+  Physics &ph = ka.ph;
+  ph.law = c.law;
+  ph.nflux = c.numerical_flux;
+  ph.ec = (c.two_point_flux == SSE_EC_FLUX) ? 1 : 0;
+  ph.half_lambda = c.half_lambda;
+  ph.gamma = c.gamma;
+  ph.gm1 = c.gamma - 1.0;
+  ph.igm1 = c.law == SSE_EULER ? 1.0 / (c.gamma - 1.0) : 0.0;
+  for (int m = 0; m < 3; ++m) ph.a[m] = c.a[m];
+  ka.fd = fd;
+  ka.project_entropy = fd && c.law == SSE_EULER;
+  ka.mass_wa = c.mass_solver == SSE_WEIGHT_ADJUSTED;
+  ka.ne = c.n_e;
+
+  // ---- team geometry and shared-memory layouts
+  const int nc = c.n_c, np = c.n_p, nq = c.n_q, nf = c.n_f, d = c.d;
+  int tpe = nq >= 64 ? 128 : 32;
+  int zsz = 0, wsz = 0;
+  if (has_vdm) {
+    if (d == 2) zsz = nc * op.p1 * op.M2;
+    else { zsz = nc * op.nb12 * op.M3; wsz = nc * op.p1 * op.M2 * op.M3; }
+  }
+  auto finish = [](Layout &L, std::initializer_list<int> sizes) {
+    int off = 0, i = 0;
+    for (int sz : sizes) { L.off[i++] = off; off += (sz + 1) & ~1; }
+    for (; i < 12; ++i) L.off[i] = off;
+    L.team_doubles = off;
+  };
+  finish(ka.layA, {nc * std::max(np, nq), nc * nq, zsz, wsz, nc * std::max(np, nf), tpe * (nc + 1)});
+  if (fd) {
+    int diff = std::max({op.nvp * nc, op.nfp * nc, nc * (np + nq)});
+    int prim = (c.law == SSE_EULER) ? (nq + nf) * (3 + d) : 0;
+    finish(ka.layB, {nc * nq, nc * nf, nc * nf, nc * nq, diff, d * d * nq,
+                     op.nfp > 0 ? d * c.num_faces * nq : 0, prim, zsz, wsz});
+  } else {
+    finish(ka.layB, {nc * nq, nc * nf, nc * nf, nc * nq, d * nc * nq, nc * nq, nc * nq, 0, zsz, wsz});
+  }
+  int epb = (tpe == 32) ? 4 : 1;
+  const size_t smem_cap = 220 * 1024;
+  while (epb > 1 && (size_t)epb * std::max(ka.layA.team_doubles, ka.layB.team_doubles) * 8 > smem_cap) epb /= 2;
+  if ((size_t)epb * std::max(ka.layA.team_doubles, ka.layB.team_doubles) * 8 > smem_cap)
+    return fail(s, SSE_ERR_UNSUPPORTED, "element too large for shared memory");
+  ka.epb = epb;
+  ka.tpb = epb * tpe;
+
+  // ---- scratch and state buffers
+  size_t nstate = (size_t)np * nc * c.n_e;
+  void *p;
+  if ((e = alloc(s, (size_t)nq * nc * c.n_e * 8, &p))) return cuda_fail(s, e, "alloc u_q");
+  ka.u_q = (double *)p;
+  if ((e = alloc(s, (size_t)nf * nc * c.n_e * 8, &p))) return cuda_fail(s, e, "alloc u_f");
+  ka.u_f = (double *)p;
+  if ((e = alloc(s, nstate * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_u = (double *)p;
+  if ((e = alloc(s, nstate * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_dudt = (double *)p;
+  if ((e = alloc(s, nstate * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_tmp = (double *)p;
+  if ((e = alloc(s, (size_t)c.n_e * (nc + 1) * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_partial = (double *)p;
+  if ((e = alloc(s, sizeof(int), &p))) return cuda_fail(s, e, "alloc"); s->d_flag = (int *)p;
+  ka.flag = s->d_flag;
+  if ((e = cudaMemset(s->d_flag, 0, sizeof(int)))) return cuda_fail(s, e, "memset");
+  if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking))) return cuda_fail(s, e, "stream");
+  s->own_stream = true;
+
+  // opt in to large dynamic shared memory for every kernel instantiation used
+  size_t smA = (size_t)epb * ka.layA.team_doubles * 8, smB = (size_t)epb * ka.layB.team_doubles * 8;
+  if ((e = sse_set_smem_limits(ka, smA, smB)) != cudaSuccess) return cuda_fail(s, e, "cudaFuncSetAttribute");
+  return SSE_OK;
+}
+
+int check_flag(sse_solver *s) {
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "flag read");
+  if (h) {
+    cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream);
+    cudaStreamSynchronize(s->stream);
+    return fail(s, SSE_ERR_NONPHYSICAL, "non-physical state (density/pressure <= 0 or non-finite residual)");
+  }
+  return SSE_OK;
+}
+
+// one residual evaluation on device buffers (no synchronisation)
+cudaError_t residual_device(sse_solver *s, const double *u, double *dudt) {
+  KernelArgs ka = s->ka;
+  ka.u = u;
+  ka.dudt = dudt;
+  cudaError_t e = launch_nodal_values(ka, s->stream);
+  if (e != cudaSuccess) return e;
+  return launch_time_derivative(ka, s->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t sse_abi_version(void) { return SSE_ABI_VERSION; }
+
+const char *sse_create_error(void) { return g_create_error.c_str(); }
+
+const char *sse_last_error(const sse_solver *s) { return s ? s->last_error.c_str() : "null handle"; }
+
+int32_t sse_create(const sse_config *cfg, const sse_operators *ops, const sse_geometry *geo,
+                   sse_solver **out) {
+  g_create_error.clear();
+  if (!out) return fail(nullptr, SSE_ERR_INVALID_ARGUMENT, "out is null");
+  *out = nullptr;
+  if (!cfg || !ops || !geo) return fail(nullptr, SSE_ERR_INVALID_ARGUMENT, "null config/operators/geometry");
+  sse_solver *s = nullptr;
+  try {
+    s = new sse_solver();
+  } catch (const std::bad_alloc &) {
+    return fail(nullptr, SSE_ERR_OUT_OF_MEMORY, "host allocation failed");
+  }
+  int rc;
+  try {
+    rc = build(s, cfg, ops, geo);
+  } catch (const std::exception &ex) {
+    rc = fail(s, SSE_ERR_OUT_OF_MEMORY, ex.what());
+  }
+  if (rc != SSE_OK) {
+    g_create_error = s->last_error;
+    sse_destroy(s);
+    return rc;
+  }
+  *out = s;
+  return SSE_OK;
+}
+
+int32_t sse_destroy(sse_solver *s) {
+  if (!s) return SSE_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (void *p : s->allocations) cudaFree(p);
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return SSE_OK;
+}
+
+int32_t sse_set_stream(sse_solver *s, void *stream) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "sync");
+  if (s->own_stream) cudaStreamDestroy(s->stream);
+  s->own_stream = false;
+  s->stream = (cudaStream_t)stream;
+  return SSE_OK;
+}
+
+int32_t sse_set_precision(sse_solver *s, int32_t precision) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (precision != SSE_FP64) return fail(s, SSE_ERR_UNSUPPORTED, "only SSE_FP64 is available in this build");
+  s->precision = precision;
+  return SSE_OK;
+}
+
+int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t, int32_t memory) {
+  (void)t;  // the supported laws carry no source term
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!u || !dudt) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u/dudt");
+  size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
+  cudaError_t e;
+  if (memory == SSE_DEVICE) {
+    if ((e = residual_device(s, u, dudt)) != cudaSuccess) return cuda_fail(s, e, "residual");
+  } else if (memory == SSE_HOST) {
+    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    if ((e = residual_device(s, s->d_u, s->d_dudt)) != cudaSuccess) return cuda_fail(s, e, "residual");
+    if ((e = cudaMemcpyAsync(dudt, s->d_dudt, n * 8, cudaMemcpyDeviceToHost, s->stream))) return cuda_fail(s, e, "D2H");
+  } else {
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
+  }
+  return check_flag(s);
+}
+
+int32_t sse_nodal_values(sse_solver *s, const double *u, double *u_q, double *u_f, int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!u) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u");
+  const sse_config &c = s->cfg;
+  size_t n = (size_t)c.n_p * c.n_c * c.n_e, nq = (size_t)c.n_q * c.n_c * c.n_e, nf = (size_t)c.n_f * c.n_c * c.n_e;
+  cudaError_t e;
+  const double *du = u;
+  if (memory == SSE_HOST) {
+    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    du = s->d_u;
+  } else if (memory != SSE_DEVICE) {
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
+  }
+  KernelArgs ka = s->ka;
+  ka.u = du;
+  if ((e = launch_nodal_values(ka, s->stream))) return cuda_fail(s, e, "nodal values");
+  if (!s->d_uf_ref) {
+    void *p;
+    if ((e = alloc(s, nf * 8, &p))) return cuda_fail(s, e, "alloc");
+    s->d_uf_ref = (double *)p;
+  }
+  if ((e = launch_facet_layout(ka.u_f, s->d_uf_ref, c.n_f, c.n_e, c.n_c, s->stream))) return cuda_fail(s, e, "layout");
+  cudaMemcpyKind kind = memory == SSE_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (u_q && (e = cudaMemcpyAsync(u_q, ka.u_q, nq * 8, kind, s->stream))) return cuda_fail(s, e, "copy u_q");
+  if (u_f && (e = cudaMemcpyAsync(u_f, s->d_uf_ref, nf * 8, kind, s->stream))) return cuda_fail(s, e, "copy u_f");
+  return check_flag(s);
+}
+
+int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme, double *t,
+                     int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!u || n_steps < 0) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u or negative n_steps");
+  if (scheme != SSE_CARPENTER_KENNEDY_2N54 && scheme != SSE_RK4) return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown scheme");
+  const sse_config &c = s->cfg;
+  size_t n = (size_t)c.n_p * c.n_c * c.n_e;
+  cudaError_t e;
+  double *du = u;
+  if (memory == SSE_HOST) {
+    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    du = s->d_u;
+  } else if (memory != SSE_DEVICE) {
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
+  }
+  if (scheme == SSE_RK4 && !s->d_acc) {
+    void *p;
+    if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_acc = (double *)p;
+    if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_ust = (double *)p;
+  }
+  for (int step = 0; step < n_steps; ++step) {
+    if (scheme == SSE_CARPENTER_KENNEDY_2N54) {
+      for (int st = 0; st < 5; ++st) {
+        if ((e = residual_device(s, du, s->d_dudt))) return cuda_fail(s, e, "residual");
+        if ((e = launch_ck_stage(du, s->d_tmp, s->d_dudt, kCKA[st], kCKB[st], dt, st == 0, n, s->stream)))
+          return cuda_fail(s, e, "stage");
+      }
+    } else {
+      const double half = dt / 2;
+      if ((e = residual_device(s, du, s->d_dudt))) return cuda_fail(s, e, "residual");
+      if ((e = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 0.0, half, 1, n, s->stream))) return cuda_fail(s, e, "stage");
+      if ((e = residual_device(s, s->d_ust, s->d_dudt))) return cuda_fail(s, e, "residual");
+      if ((e = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 2.0, half, 0, n, s->stream))) return cuda_fail(s, e, "stage");
+      if ((e = residual_device(s, s->d_ust, s->d_dudt))) return cuda_fail(s, e, "residual");
+      if ((e = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 2.0, dt, 0, n, s->stream))) return cuda_fail(s, e, "stage");
+      if ((e = residual_device(s, s->d_ust, s->d_dudt))) return cuda_fail(s, e, "residual");
+      if ((e = launch_rk4_final(du, s->d_acc, s->d_dudt, dt / 6, n, s->stream))) return cuda_fail(s, e, "stage");
+    }
+  }
+  if (memory == SSE_HOST && (e = cudaMemcpyAsync(u, s->d_u, n * 8, cudaMemcpyDeviceToHost, s->stream)))
+    return cuda_fail(s, e, "D2H");
+  if (t) *t += n_steps * dt;
+  return check_flag(s);
+}
+
+int32_t sse_conservation_residual(sse_solver *s, const double *u, const double *dudt, double *out,
+                                  int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!u || !dudt || !out) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null argument");
+  const sse_config &c = s->cfg;
+  size_t n = (size_t)c.n_p * c.n_c * c.n_e;
+  cudaError_t e;
+  const double *du = u, *dd = dudt;
+  if (memory == SSE_HOST) {
+    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    if ((e = cudaMemcpyAsync(s->d_tmp, dudt, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    du = s->d_u;
+    dd = s->d_tmp;
+  } else if (memory != SSE_DEVICE) {
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
+  }
+  if ((e = launch_conservation(s->ka, du, dd, s->d_partial, s->stream))) return cuda_fail(s, e, "conservation");
+  std::vector<double> part((size_t)c.n_e * (c.n_c + 1));
+  if ((e = cudaMemcpyAsync(part.data(), s->d_partial, part.size() * 8, cudaMemcpyDeviceToHost, s->stream)))
+    return cuda_fail(s, e, "D2H");
+  if ((e = cudaStreamSynchronize(s->stream))) return cuda_fail(s, e, "sync");
+  for (int q = 0; q <= c.n_c; ++q) out[q] = 0.0;
+  for (int k = 0; k < c.n_e; ++k)
+    for (int q = 0; q <= c.n_c; ++q) out[q] += part[(size_t)k * (c.n_c + 1) + q];
+  return SSE_OK;
+}
+
+// Average device time (ms) of each residual phase over n_iter evaluations,
+// timed with CUDA events on the handle's stream: out[0] = phase A (nodal
+// values), out[1] = phase B (time derivative), out[2] = one RK stage update.
+int32_t sse_phase_timings(sse_solver *s, const double *u_dev, int32_t n_iter, double *out) {
+  if (!s || !u_dev || !out || n_iter <= 0) return SSE_ERR_INVALID_ARGUMENT;
+  KernelArgs ka = s->ka;
+  ka.u = u_dev;
+  ka.dudt = s->d_dudt;
+  size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
+  cudaEvent_t ev[4];
+  for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
+  float ta = 0, tb = 0, tc = 0;
+  cudaError_t e = cudaSuccess;
+  for (int it = 0; it < n_iter && e == cudaSuccess; ++it) {
+    cudaEventRecord(ev[0], s->stream);
+    e = launch_nodal_values(ka, s->stream);
+    cudaEventRecord(ev[1], s->stream);
+    if (e == cudaSuccess) e = launch_time_derivative(ka, s->stream);
+    cudaEventRecord(ev[2], s->stream);
+    // stage update into the host-staging buffer (never the caller's state)
+    if (e == cudaSuccess && s->d_u != u_dev)
+      e = launch_ck_stage(s->d_u, s->d_tmp, s->d_dudt, 0.5, 0.0, 1e-300, 0, n, s->stream);
+    cudaEventRecord(ev[3], s->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
+    float a, b, c2;
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
+    cudaEventElapsedTime(&b, ev[1], ev[2]);
+    cudaEventElapsedTime(&c2, ev[2], ev[3]);
+    ta += a; tb += b; tc += c2;
+  }
+  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  if (e != cudaSuccess) return cuda_fail(s, e, "timing");
+  out[0] = ta / n_iter;
+  out[1] = tb / n_iter;
+  out[2] = tc / n_iter;
+  return check_flag(s);
+}
+
+// sizeof checks for foreign-language bindings
+int32_t sse_struct_sizes(int32_t *out) {
+  out[0] = (int32_t)sizeof(sse_config);
+  out[1] = (int32_t)sizeof(sse_csc);
+  out[2] = (int32_t)sizeof(sse_operators);
+  out[3] = (int32_t)sizeof(sse_geometry);
+  return 4;
+}
+
+}  // extern "C"

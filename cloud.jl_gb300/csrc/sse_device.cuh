@@ -1,0 +1,241 @@
+// sse_device.cuh -- device-side data layout and pointwise physics of the
+// GB300 residual library.
+//
+// Pointwise physics restates src/ConservationLaws/ConservationLaws.jl:75-156,
+// src/ConservationLaws/euler_navierstokes.jl:58-225 and
+// src/ConservationLaws/linear_advection_diffusion.jl:54-128 in FP64.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sse {
+
+constexpr int kMaxC = 5;
+constexpr int kMaxD = 3;
+
+// Reference-element operators on the device, preprocessed from the caller's
+// CSC matrices and warped-product factors (all indices 0-based, int32).
+struct DevOps {
+  int d, nc, np, nq, nf, nfac, npf;
+  // warped tensor-product Vandermonde (has_vdm == 0: V = I)
+  int has_vdm, p1, M1, M2, M3;
+  const double *A;    // M1 x p1      (Julia column-major)
+  const double *B;    // M2 x p1 x p1
+  const double *C;    // M3 x p1^3
+  int nb12;           // number of (b1, b2) with b1 + b2 < p1 (3-D)
+  const int *b12;     // packed b1 | b2 << 8, 3-D stage list
+  const int *b12_index;  // p1 x p1 -> position in b12 list or -1
+  const int *modes;   // np packed b1 | b2 << 8 | b3 << 16 in modal order
+  const int *sigma;   // p1^d: modal index of (b1, b2[, b3]) or -1
+  // R (facet x volume) as CSR rows, and R^T as CSR rows
+  const int *R_ptr, *R_idx; const double *R_val;
+  const int *Rt_ptr, *Rt_idx; const double *Rt_val;
+  // StandardForm D_m and D_m^T as CSR rows
+  const int *D_ptr[kMaxD], *D_idx[kMaxD]; const double *D_val[kMaxD];
+  const int *Dt_ptr[kMaxD], *Dt_idx[kMaxD]; const double *Dt_val[kMaxD];
+  // FluxDifferencingForm volume pairs: unique (i < j) in the union of the
+  // S_m patterns; S values per direction (0 where S_m has no entry)
+  int nvp;
+  const int *vp_ij;      // i | j << 16
+  const double *vp_S;    // nvp x d (pair-major)
+  const int *vp_inc_ptr; // nq + 1
+  const int *vp_inc;     // (pair << 1) | (node is i ? 1 : 0)
+  // facet-correction pairs: nonzeros of C (volume node i, facet node j)
+  int nfp;
+  const int *fp_ij;      // i | j << 16
+  const double *fp_C;
+  const int *fp_q_ptr, *fp_q;  // per volume node: incident pair ids
+  const int *fp_f_ptr, *fp_f;  // per facet node: incident pair ids
+};
+
+__device__ __forceinline__ int modes_index2(const DevOps &op, int b1, int b2) {
+  return op.sigma[b1 + op.p1 * b2];
+}
+__device__ __forceinline__ int modes_index3(const DevOps &op, int b1, int b2, int b3) {
+  return op.sigma[b1 + op.p1 * (b2 + op.p1 * b3)];
+}
+
+struct DevGeo {
+  const double *BJf;          // nf x ne
+  const double *n_f;          // d x nf x ne
+  const int *mapP;            // nf x ne, 0-based linear index into (nf, ne)
+  const double *halfWLambda;  // nq x d x d x ne
+  const double *WJ;           // nq x ne
+  const double *Lambda_q;     // nq x d x d x ne
+  const double *halfnJf;      // d x nf x ne
+  const double *halfnJq;      // d x nfac x nq x ne
+  const double *JinvW;        // nq x ne
+  const double *WJinv;        // nq x ne
+};
+
+struct Physics {
+  int law;       // 0 advection, 1 Euler
+  int nflux;     // 0 LF, 1 central, 2 EC numerical flux
+  int ec;        // two-point flux: 1 entropy-conservative (Ranocha), 0 conservative
+  double half_lambda;
+  double gamma, gm1, igm1;
+  double a[3];
+};
+
+// ---------------------------------------------------------------------------
+// logmean / inverse logmean (ConservationLaws.jl:132-156)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double logmean(double x, double y) {
+  double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+  if (f2 < 1.0e-4) return (x + y) * 105 / (210 + f2 * (70 + f2 * (42 + f2 * 30)));
+  return (y - x) / log(y / x);
+}
+
+__device__ __forceinline__ double inv_logmean(double x, double y) {
+  double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+  if (f2 < 1.0e-4) return (210 + f2 * (70 + f2 * (42 + f2 * 30))) / ((x + y) * 105);
+  return log(y / x) / (y - x);
+}
+
+// Primitive quantities of one Euler state, computed once per node so that
+// the pairwise loops do no per-pair divisions for them.
+template <int D>
+struct Prim {
+  double rho, p, beta;  // beta = rho / p
+  double V[D];
+};
+
+template <int D>
+__device__ __forceinline__ Prim<D> euler_prim(const Physics &ph, const double *u) {
+  Prim<D> q;
+  q.rho = u[0];
+  double s = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) q.V[m] = u[m + 1] / u[0];
+#pragma unroll
+  for (int m = 0; m < D; ++m) s += q.V[m] * q.V[m];
+  q.p = ph.gm1 * (u[D + 1] - 0.5 * u[0] * s);
+  q.beta = u[0] / q.p;
+  return q;
+}
+
+// Ranocha's entropy-conservative flux tensor F[e][n] (euler_navierstokes.jl:171-195).
+template <int D>
+__device__ __forceinline__ void ec_flux(const Physics &ph, const Prim<D> &L, const Prim<D> &R,
+                                        double F[D + 2][D]) {
+  double rho_avg = logmean(L.rho, R.rho);
+  double Vavg[D];
+  double vv = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) Vavg[m] = 0.5 * (L.V[m] + R.V[m]);
+#pragma unroll
+  for (int m = 0; m < D; ++m) vv += L.V[m] * R.V[m];
+  double pavg = 0.5 * (L.p + R.p);
+  double C = 0.5 * vv + ph.igm1 * inv_logmean(L.beta, R.beta);
+#pragma unroll
+  for (int n = 0; n < D; ++n) {
+    double frho = rho_avg * Vavg[n];
+    F[0][n] = frho;
+#pragma unroll
+    for (int m = 0; m < D; ++m) F[m + 1][n] = rho_avg * Vavg[m] * Vavg[n] + (m == n ? pavg : 0.0);
+    F[D + 1][n] = frho * C + 0.5 * (L.p * R.V[n] + R.p * L.V[n]);
+  }
+}
+
+// Euler physical flux tensor (euler_navierstokes.jl:58-68).
+template <int D>
+__device__ __forceinline__ void euler_flux(const Physics &ph, const double *u, double F[D + 2][D]) {
+  double V[D], s = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) V[m] = u[m + 1] / u[0];
+#pragma unroll
+  for (int m = 0; m < D; ++m) s += u[m + 1] * V[m];
+  double p = ph.gm1 * (u[D + 1] - 0.5 * s);
+  double ht = u[D + 1] + p;
+#pragma unroll
+  for (int n = 0; n < D; ++n) {
+    F[0][n] = u[n + 1];
+#pragma unroll
+    for (int m = 0; m < D; ++m) F[m + 1][n] = u[m + 1] * V[n] + (m == n ? p : 0.0);
+    F[D + 1][n] = ht * V[n];
+  }
+}
+
+// Two-point flux tensor for a pair of states: Euler EC / conservative
+// average, or advection a_m (u_L + u_R)/2.
+template <int D, int NC>
+__device__ __forceinline__ void two_point(const Physics &ph, const double *uL, const double *uR,
+                                          double F[NC][D]) {
+  if constexpr (NC == 1) {
+    double f1 = 0.5 * (uL[0] + uR[0]);
+#pragma unroll
+    for (int m = 0; m < D; ++m) F[0][m] = ph.a[m] * f1;
+  } else {
+    if (ph.ec) {
+      Prim<D> L = euler_prim<D>(ph, uL), R = euler_prim<D>(ph, uR);
+      ec_flux<D>(ph, L, R, F);
+    } else {
+      double FL[D + 2][D], FR[D + 2][D];
+      euler_flux<D>(ph, uL, FL);
+      euler_flux<D>(ph, uR, FR);
+#pragma unroll
+      for (int e = 0; e < D + 2; ++e)
+#pragma unroll
+        for (int n = 0; n < D; ++n) F[e][n] = 0.5 * (FL[e][n] + FR[e][n]);
+    }
+  }
+}
+
+// wave_speed (euler_navierstokes.jl:133-150; linear_advection_diffusion.jl:106-111)
+template <int D, int NC>
+__device__ __forceinline__ double wave_speed(const Physics &ph, const double *ui, const double *uo,
+                                             const double *n) {
+  if constexpr (NC == 1) {
+    double s = 0.0;
+#pragma unroll
+    for (int m = 0; m < D; ++m) s += ph.a[m] * n[m];
+    return fabs(s);
+  } else {
+    double si = 0.0, so = 0.0, vni = 0.0, vno = 0.0;
+#pragma unroll
+    for (int m = 0; m < D; ++m) { si += ui[m + 1] * ui[m + 1]; so += uo[m + 1] * uo[m + 1]; }
+    double pin = ph.gm1 * (ui[D + 1] - (0.5 / ui[0]) * si);
+    double pout = ph.gm1 * (uo[D + 1] - (0.5 / uo[0]) * so);
+#pragma unroll
+    for (int m = 0; m < D; ++m) { vni += (ui[m + 1] / ui[0]) * n[m]; vno += (uo[m + 1] / uo[0]) * n[m]; }
+    double ci = sqrt(ph.gamma * pin / ui[0]);
+    double co = sqrt(ph.gamma * pout / uo[0]);
+    return fmax(fabs(vni), fabs(vno)) + fmax(ci, co);
+  }
+}
+
+// conservative_to_entropy! (euler_navierstokes.jl:100-113)
+template <int D>
+__device__ __forceinline__ void cons_to_entropy(const Physics &ph, const double *u, double *w) {
+  double s = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) s += u[m + 1] * u[m + 1];
+  double k = (0.5 / u[0]) * s;
+  double p = ph.gm1 * (u[D + 1] - k);
+  double ip = 1.0 / p;
+  w[0] = ph.igm1 * (ph.gamma - log(p / pow(u[0], ph.gamma))) - k * ip;
+#pragma unroll
+  for (int m = 0; m < D; ++m) w[m + 1] = u[m + 1] * ip;
+  w[D + 1] = -u[0] * ip;
+}
+
+// entropy_to_conservative! (euler_navierstokes.jl:115-131)
+template <int D>
+__device__ __forceinline__ void entropy_to_cons(const Physics &ph, const double *w_in, double *u) {
+  double w[D + 2];
+#pragma unroll
+  for (int e = 0; e < D + 2; ++e) w[e] = w_in[e] * ph.gm1;
+  double s = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) s += w[m + 1] * w[m + 1];
+  double k = s / (2 * w[D + 1]);
+  double sv = ph.gamma - w[0] + k;
+  double rhoe = pow(ph.gm1 / pow(-w[D + 1], ph.gamma), ph.igm1) * exp(-sv * ph.igm1);
+  u[0] = -w[D + 1] * rhoe;
+#pragma unroll
+  for (int m = 0; m < D; ++m) u[m + 1] = w[m + 1] * rhoe;
+  u[D + 1] = rhoe * (1 - k);
+}
+
+}  // namespace sse

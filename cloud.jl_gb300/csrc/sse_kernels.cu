@@ -1,0 +1,807 @@
+// sse_kernels.cu -- sm_103a kernels of the semi-discrete residual.
+//
+// Work decomposition: a CTA holds EPB elements; each element is handled by a
+// team of TPE = blockDim.x / EPB threads that keeps every per-element array
+// (states, fluxes, partial sums, sum-factorisation stages) in shared memory.
+// Global memory is touched once per array per phase: the element's modal
+// coefficients, its metric terms and, in phase B, the neighbours' facet
+// states gathered through mapP.  Pair sums are accumulated in two passes
+// (per-pair contributions, then a fixed-order per-node reduction), so the
+// result is deterministic run to run.
+//
+// Phase A  nodal_values_kernel     nodal_values! / entropy_projection!
+//          (standard_form_first_order.jl:1-14, flux_differencing_form.jl:190-292)
+// Phase B  fd_time_derivative_kernel   time_derivative! FD (flux_differencing_form.jl:294-347)
+//          std_time_derivative_kernel  time_derivative! StandardForm (standard_form_first_order.jl:16-63)
+#include "sse_device.cuh"
+#include "sse_kernels.cuh"
+
+namespace sse {
+
+// ---------------------------------------------------------------------------
+// team-parallel operator applications (all NC components at once)
+// ---------------------------------------------------------------------------
+
+// y (NC x nq) = V x (NC x np); warped_product_2d.jl:31-55 / _3d.jl:47-84
+template <int D, int NC>
+__device__ void vdm_mul(const DevOps &op, const double *x, double *y, double *Z, double *W,
+                        int lane, int tpe) {
+  if (!op.has_vdm) {
+    for (int t = lane; t < NC * op.nq; t += tpe) y[t] = x[t];
+    __syncthreads();
+    return;
+  }
+  const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
+  if constexpr (D == 2) {
+    // Z[e][b1][a2] = sum_b2 B[a2,b1,b2] x[sigma(b1,b2)]
+    for (int t = lane; t < NC * p1 * M2; t += tpe) {
+      int a2 = t % M2, r = t / M2, b1 = r % p1, e = r / p1;
+      double acc = 0.0;
+      for (int b2 = 0; b2 < p1 - b1; ++b2) {
+        int l = modes_index2(op, b1, b2);
+        acc = fma(op.B[a2 + M2 * (b1 + p1 * b2)], x[e * op.np + l], acc);
+      }
+      Z[(e * p1 + b1) * M2 + a2] = acc;
+    }
+    __syncthreads();
+    for (int t = lane; t < NC * M1 * M2; t += tpe) {
+      int a2 = t % M2, r = t / M2, a1 = r % M1, e = r / M1;
+      double acc = 0.0;
+      for (int b1 = 0; b1 < p1; ++b1) acc = fma(op.A[a1 + M1 * b1], Z[(e * p1 + b1) * M2 + a2], acc);
+      y[e * op.nq + M2 * a1 + a2] = acc;
+    }
+    __syncthreads();
+  } else {
+    const int M3 = op.M3, nb12 = op.nb12;
+    for (int t = lane; t < NC * nb12 * M3; t += tpe) {
+      int a3 = t % M3, r = t / M3, q = r % nb12, e = r / nb12;
+      int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
+      double acc = 0.0;
+      for (int b3 = 0; b3 < p1 - b1 - b2; ++b3) {
+        int l = modes_index3(op, b1, b2, b3);
+        acc = fma(op.C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], x[e * op.np + l], acc);
+      }
+      Z[(e * nb12 + q) * M3 + a3] = acc;
+    }
+    __syncthreads();
+    for (int t = lane; t < NC * p1 * M2 * M3; t += tpe) {
+      int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, b1 = r2 % p1, e = r2 / p1;
+      double acc = 0.0;
+      for (int b2 = 0; b2 < p1 - b1; ++b2) {
+        int q = op.b12_index[b1 + p1 * b2];
+        acc = fma(op.B[a2 + M2 * (b1 + p1 * b2)], Z[(e * nb12 + q) * M3 + a3], acc);
+      }
+      W[((e * p1 + b1) * M2 + a2) * M3 + a3] = acc;
+    }
+    __syncthreads();
+    for (int t = lane; t < NC * M1 * M2 * M3; t += tpe) {
+      int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, a1 = r2 % M1, e = r2 / M1;
+      double acc = 0.0;
+      for (int b1 = 0; b1 < p1; ++b1)
+        acc = fma(op.A[a1 + M1 * b1], W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc);
+      y[e * op.nq + (M2 * a1 + a2) * M3 + a3] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// x (NC x np) = V^T y (NC x nq); warped_product_2d.jl:61-89 / _3d.jl:94-136
+template <int D, int NC>
+__device__ void vdm_tmul(const DevOps &op, const double *y, double *x, double *Z, double *W,
+                         int lane, int tpe) {
+  if (!op.has_vdm) {
+    for (int t = lane; t < NC * op.nq; t += tpe) x[t] = y[t];
+    __syncthreads();
+    return;
+  }
+  const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
+  if constexpr (D == 2) {
+    for (int t = lane; t < NC * p1 * M2; t += tpe) {
+      int a2 = t % M2, r = t / M2, b1 = r % p1, e = r / p1;
+      double acc = 0.0;
+      for (int a1 = 0; a1 < M1; ++a1) acc = fma(op.A[a1 + M1 * b1], y[e * op.nq + M2 * a1 + a2], acc);
+      Z[(e * p1 + b1) * M2 + a2] = acc;
+    }
+    __syncthreads();
+    for (int t = lane; t < NC * op.np; t += tpe) {
+      int l = t % op.np, e = t / op.np;
+      int b1 = op.modes[l] & 0xff, b2 = (op.modes[l] >> 8) & 0xff;
+      double acc = 0.0;
+      for (int a2 = 0; a2 < M2; ++a2) acc = fma(op.B[a2 + M2 * (b1 + p1 * b2)], Z[(e * p1 + b1) * M2 + a2], acc);
+      x[e * op.np + l] = acc;
+    }
+    __syncthreads();
+  } else {
+    const int M3 = op.M3, nb12 = op.nb12;
+    for (int t = lane; t < NC * p1 * M2 * M3; t += tpe) {
+      int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, b1 = r2 % p1, e = r2 / p1;
+      double acc = 0.0;
+      for (int a1 = 0; a1 < M1; ++a1)
+        acc = fma(op.A[a1 + M1 * b1], y[e * op.nq + (M2 * a1 + a2) * M3 + a3], acc);
+      W[((e * p1 + b1) * M2 + a2) * M3 + a3] = acc;
+    }
+    __syncthreads();
+    for (int t = lane; t < NC * nb12 * M3; t += tpe) {
+      int a3 = t % M3, r = t / M3, q = r % nb12, e = r / nb12;
+      int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
+      double acc = 0.0;
+      for (int a2 = 0; a2 < M2; ++a2)
+        acc = fma(op.B[a2 + M2 * (b1 + p1 * b2)], W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc);
+      Z[(e * nb12 + q) * M3 + a3] = acc;
+    }
+    __syncthreads();
+    for (int t = lane; t < NC * op.np; t += tpe) {
+      int l = t % op.np, e = t / op.np;
+      int b1 = op.modes[l] & 0xff, b2 = (op.modes[l] >> 8) & 0xff, b3 = (op.modes[l] >> 16) & 0xff;
+      int q = op.b12_index[b1 + p1 * b2];
+      double acc = 0.0;
+      for (int a3 = 0; a3 < M3; ++a3)
+        acc = fma(op.C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], Z[(e * nb12 + q) * M3 + a3], acc);
+      x[e * op.np + l] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// y (NC x rows) = M x (NC x cols) for a CSR matrix
+template <int NC>
+__device__ void csr_mul(int rows, int cols, const int *ptr, const int *idx, const double *val,
+                        const double *x, double *y, int lane, int tpe) {
+  for (int t = lane; t < NC * rows; t += tpe) {
+    int r = t % rows, e = t / rows;
+    double acc = 0.0;
+    for (int q = ptr[r]; q < ptr[r + 1]; ++q) acc += val[q] * x[e * cols + idx[q]];
+    y[e * rows + r] = acc;
+  }
+}
+
+// WeightAdjustedSolver (M^-1 = I): x <- V^T diag(JinvW) V x;
+// DiagonalSolver: x <- WJinv .* x (mass_matrix.jl:177-196)
+template <int D, int NC>
+__device__ void mass_solve(const DevOps &op, const double *JinvW, const double *WJinv, int wa,
+                           double *x, double *Y, double *Z, double *W, int lane, int tpe) {
+  if (!wa) {
+    for (int t = lane; t < NC * op.np; t += tpe) x[t] *= WJinv[t % op.np];
+    __syncthreads();
+    return;
+  }
+  vdm_mul<D, NC>(op, x, Y, Z, W, lane, tpe);
+  for (int t = lane; t < NC * op.nq; t += tpe) Y[t] *= JinvW[t % op.nq];
+  __syncthreads();
+  vdm_tmul<D, NC>(op, Y, x, Z, W, lane, tpe);
+}
+
+// ---------------------------------------------------------------------------
+// Phase A: nodal_values!
+// ---------------------------------------------------------------------------
+template <int D, int NC>
+__global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Layout &L = ka.layA;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3],
+         *F = base + L.off[4];
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  const double *uk = ka.u + (size_t)kk * NC * np;
+  const bool project = ka.project_entropy;
+
+  for (int t = lane; t < NC * np; t += tpe) X[t] = uk[t];
+  __syncthreads();
+  vdm_mul<D, NC>(op, X, Y, Z, Wb, lane, tpe);  // Y = u_q = V u
+
+  double *uq_out = ka.u_q + (size_t)kk * NC * nq;
+  double *uf_out = ka.u_f + (size_t)kk * NC * nf;
+  if constexpr (NC > 1) {
+    if (project) {
+      const Physics &ph = ka.ph;
+      const double *WJ = ka.geo.WJ + (size_t)kk * nq;
+      // w_q = WJ .* c2e(u_q)   (entropy_projection!, flux_differencing_form.jl:229-235)
+      for (int i = lane; i < nq; i += tpe) {
+        double ui[NC], wi[NC];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) ui[e] = Y[e * nq + i];
+        if (!(ui[0] > 0.0)) ka.flag_nonphysical();
+        cons_to_entropy<D>(ph, ui, wi);
+        double s = op.has_vdm ? WJ[i] : 1.0;
+#pragma unroll
+        for (int e = 0; e < NC; ++e) X[e * (op.has_vdm ? nq : nq) + i] = wi[e] * s;
+      }
+      __syncthreads();
+      if (op.has_vdm) {
+        // X holds WJ w_q (NC x nq): w = V^T (WJ w_q); mass solve; w_q = V w
+        double *Wm = F;  // NC x np modal scratch (F is large enough, see layout)
+        vdm_tmul<D, NC>(op, X, Wm, Z, Wb, lane, tpe);
+        mass_solve<D, NC>(op, ka.geo.JinvW + (size_t)kk * nq, nullptr, 1, Wm, X, Z, Wb, lane, tpe);
+        vdm_mul<D, NC>(op, Wm, X, Z, Wb, lane, tpe);  // X = w_q (projected)
+        // u_q = e2c(w_q)
+        for (int i = lane; i < nq; i += tpe) {
+          double wi[NC], ui[NC];
+#pragma unroll
+          for (int e = 0; e < NC; ++e) wi[e] = X[e * nq + i];
+          entropy_to_cons<D>(ph, wi, ui);
+#pragma unroll
+          for (int e = 0; e < NC; ++e) {
+            if (live) uq_out[e * nq + i] = ui[e];
+            if (!(ui[0] > 0.0) || !isfinite(ui[e])) ka.flag_nonphysical();
+          }
+        }
+      } else {
+        // nodal: u_q stays u; X = w_q
+        for (int t = lane; t < NC * nq; t += tpe)
+          if (live) uq_out[t] = Y[t];
+      }
+      // w_f = R w_q ; u_f = e2c(w_f)
+      csr_mul<NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, X, F, lane, tpe);
+      __syncthreads();
+      for (int j = lane; j < nf; j += tpe) {
+        double wi[NC], ui[NC];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) wi[e] = F[e * nf + j];
+        entropy_to_cons<D>(ph, wi, ui);
+#pragma unroll
+        for (int e = 0; e < NC; ++e) {
+          if (live) uf_out[e * nf + j] = ui[e];
+          if (!(ui[0] > 0.0) || !isfinite(ui[e])) ka.flag_nonphysical();
+        }
+      }
+      return;
+    }
+  }
+  // no projection: u_q = V u; u_f = R u_q
+  for (int t = lane; t < NC * nq; t += tpe)
+    if (live) uq_out[t] = Y[t];
+  csr_mul<NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, Y, F, lane, tpe);
+  __syncthreads();
+  for (int t = lane; t < NC * nf; t += tpe)
+    if (live) uf_out[t] = F[t];
+}
+
+// ---------------------------------------------------------------------------
+// numerical flux at the element's facet nodes, scaled by BJf
+// (numerical_flux!, ConservationLaws.jl:75-128; lmul!(BJf[k], f_f))
+// ---------------------------------------------------------------------------
+template <int D, int NC>
+__device__ void facet_flux(const KernelArgs &ka, int kk, const double *uf, double *ff, int ec,
+                           int lane, int tpe) {
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const int nf = op.nf;
+  for (int j = lane; j < nf; j += tpe) {
+    int P = ka.geo.mapP[(size_t)kk * nf + j];
+    int jn = P % nf, kn = P / nf;
+    double ui[NC], uo[NC], n[D], F[NC][D];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      ui[e] = uf[e * nf + j];
+      uo[e] = ka.u_f[((size_t)kn * NC + e) * nf + jn];
+    }
+#pragma unroll
+    for (int m = 0; m < D; ++m) n[m] = ka.geo.n_f[m + D * (j + (size_t)nf * kk)];
+    Physics ph2 = ph;
+    ph2.ec = ec;
+    two_point<D, NC>(ph2, ui, uo, F);
+    double a = 0.0;
+    if (ph.nflux == 0) a = ph.half_lambda * wave_speed<D, NC>(ph, ui, uo, n);
+    double bjf = ka.geo.BJf[(size_t)kk * nf + j];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      double fn = 0.0;
+#pragma unroll
+      for (int m = 0; m < D; ++m) fn = fma(F[e][m], n[m], fn);
+      double fs = (ph.nflux == 0) ? fma(a, ui[e] - uo[e], fn) : fn;
+      ff[e * nf + j] = fs * bjf;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Phase B, FluxDifferencingForm
+// ---------------------------------------------------------------------------
+template <int D, int NC>
+__global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const Layout &L = ka.layB;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *uq = base + L.off[0], *uf = base + L.off[1], *ff = base + L.off[2], *rq = base + L.off[3],
+         *diff = base + L.off[4], *Lam = base + L.off[5], *hnq = base + L.off[6],
+         *prim = base + L.off[7], *Z = base + L.off[8], *Wb = base + L.off[9];
+
+  // stage the element's data
+  const double *uqg = ka.u_q + (size_t)kk * NC * nq;
+  const double *ufg = ka.u_f + (size_t)kk * NC * nf;
+  for (int t = lane; t < NC * nq; t += tpe) uq[t] = uqg[t];
+  for (int t = lane; t < NC * nf; t += tpe) uf[t] = ufg[t];
+  const double *Lg = ka.geo.Lambda_q + (size_t)kk * nq * D * D;
+  for (int t = lane; t < nq * D * D; t += tpe) Lam[t] = Lg[t];
+  const double *Hg = ka.geo.halfnJq + (size_t)kk * D * nfac * nq;
+  if (op.nfp > 0)
+    for (int t = lane; t < D * nfac * nq; t += tpe) hnq[t] = Hg[t];
+  __syncthreads();
+
+  const int ec = ph.ec;
+  // per-node primitive quantities for the Euler EC flux: [rho, p, beta, V_1..V_D]
+  const int PS = 3 + D;
+  if constexpr (NC > 1) {
+    if (ec) {
+      for (int i = lane; i < nq + nf; i += tpe) {
+        double u[NC];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) u[e] = (i < nq) ? uq[e * nq + i] : uf[e * nf + (i - nq)];
+        Prim<D> q = euler_prim<D>(ph, u);
+        double *pp = prim + (size_t)i * PS;
+        pp[0] = q.rho; pp[1] = q.p; pp[2] = q.beta;
+#pragma unroll
+        for (int m = 0; m < D; ++m) pp[3 + m] = q.V[m];
+      }
+    }
+  }
+  facet_flux<D, NC>(ka, kk, uf, ff, ec, lane, tpe);
+  __syncthreads();
+
+  // volume flux differencing, pass 1: per-pair contributions
+  // (flux_difference!, flux_differencing_form.jl:37-75, one flux per unique pair)
+  for (int pidx = lane; pidx < op.nvp; pidx += tpe) {
+    int ij = op.vp_ij[pidx];
+    int i = ij & 0xffff, j = ij >> 16;
+    double F[NC][D];
+    if constexpr (NC > 1) {
+      if (ec) {
+        Prim<D> Lp, Rp;
+        const double *pi_ = prim + (size_t)i * PS, *pj = prim + (size_t)j * PS;
+        Lp.rho = pi_[0]; Lp.p = pi_[1]; Lp.beta = pi_[2];
+        Rp.rho = pj[0]; Rp.p = pj[1]; Rp.beta = pj[2];
+#pragma unroll
+        for (int m = 0; m < D; ++m) { Lp.V[m] = pi_[3 + m]; Rp.V[m] = pj[3 + m]; }
+        ec_flux<D>(ph, Lp, Rp, F);
+      } else {
+        double ui[NC], uj[NC];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) { ui[e] = uq[e * nq + i]; uj[e] = uq[e * nq + j]; }
+        two_point<D, NC>(ph, ui, uj, F);
+      }
+    } else {
+      double ui[1] = {uq[i]}, uj[1] = {uq[j]};
+      two_point<D, NC>(ph, ui, uj, F);
+    }
+    double out[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) out[e] = 0.0;
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      double Sm = op.vp_S[pidx * D + m];
+      if (Sm == 0.0) continue;
+      double Lij[D];
+#pragma unroll
+      for (int n = 0; n < D; ++n) Lij[n] = Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        double Fm = 0.0;
+#pragma unroll
+        for (int n = 0; n < D; ++n) Fm = fma(Lij[n], F[e][n], Fm);
+        out[e] = fma(Sm, Fm, out[e]);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+  }
+  __syncthreads();
+  // pass 2: r_q[i] = sum over incident pairs (-diff if i is the first node, +diff otherwise)
+  for (int i = lane; i < nq; i += tpe) {
+    double acc[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) acc[e] = 0.0;
+    for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
+      int inc = op.vp_inc[q];
+      int pidx = inc >> 1;
+      double sgn = (inc & 1) ? -1.0 : 1.0;
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = fma(sgn, diff[(size_t)pidx * NC + e], acc[e]);
+    }
+#pragma unroll
+    for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
+  }
+  __syncthreads();
+
+  // facet correction (facet_correction!, flux_differencing_form.jl:126-168)
+  if (op.nfp > 0) {
+    const double *hnf = ka.geo.halfnJf + (size_t)kk * D * nf;
+    for (int pidx = lane; pidx < op.nfp; pidx += tpe) {
+      int ij = op.fp_ij[pidx];
+      int i = ij & 0xffff, j = ij >> 16;
+      int f = j / npf;
+      double F[NC][D];
+      if constexpr (NC > 1) {
+        if (ec) {
+          Prim<D> Lp, Rp;
+          const double *pi_ = prim + (size_t)i * PS, *pj = prim + (size_t)(nq + j) * PS;
+          Lp.rho = pi_[0]; Lp.p = pi_[1]; Lp.beta = pi_[2];
+          Rp.rho = pj[0]; Rp.p = pj[1]; Rp.beta = pj[2];
+#pragma unroll
+          for (int m = 0; m < D; ++m) { Lp.V[m] = pi_[3 + m]; Rp.V[m] = pj[3 + m]; }
+          ec_flux<D>(ph, Lp, Rp, F);
+        } else {
+          double ui[NC], uj[NC];
+#pragma unroll
+          for (int e = 0; e < NC; ++e) { ui[e] = uq[e * nq + i]; uj[e] = uf[e * nf + j]; }
+          two_point<D, NC>(ph, ui, uj, F);
+        }
+      } else {
+        double ui[1] = {uq[i]}, uj[1] = {uf[j]};
+        two_point<D, NC>(ph, ui, uj, F);
+      }
+      double nJ[D];
+#pragma unroll
+      for (int m = 0; m < D; ++m) nJ[m] = hnf[m + D * j] + hnq[m + D * (f + nfac * i)];
+      double Cij = op.fp_C[pidx];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        double Fn = 0.0;
+#pragma unroll
+        for (int m = 0; m < D; ++m) Fn = fma(nJ[m], F[e][m], Fn);
+        diff[(size_t)pidx * NC + e] = Cij * Fn;
+      }
+    }
+    __syncthreads();
+    for (int t = lane; t < nq + nf; t += tpe) {
+      double acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0.0;
+      const int *ptr = (t < nq) ? op.fp_q_ptr : op.fp_f_ptr;
+      const int *lst = (t < nq) ? op.fp_q : op.fp_f;
+      int r = (t < nq) ? t : t - nq;
+      for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+        int pidx = lst[q];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] += diff[(size_t)pidx * NC + e];
+      }
+      if (t < nq) {
+#pragma unroll
+        for (int e = 0; e < NC; ++e) rq[e * nq + r] -= acc[e];
+      } else {
+#pragma unroll
+        for (int e = 0; e < NC; ++e) ff[e * nf + r] -= acc[e];
+      }
+    }
+    __syncthreads();
+  }
+
+  // r_q -= R^T f_f
+  for (int t = lane; t < NC * nq; t += tpe) {
+    int i = t % nq, e = t / nq;
+    double acc = 0.0;
+    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * ff[e * nf + op.Rt_idx[q]];
+    rq[t] -= acc;
+  }
+  __syncthreads();
+
+  // dudt = V^T r_q ; mass solve  (scratch: diff region reused for modal / nodal buffers)
+  double *Xm = diff, *Yq = diff + (size_t)NC * np;
+  vdm_tmul<D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
+  mass_solve<D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
+                    ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq,
+                    Z, Wb, lane, tpe);
+  double *out = ka.dudt + (size_t)kk * NC * np;
+  if (live)
+    for (int t = lane; t < NC * np; t += tpe) {
+      out[t] = Xm[t];
+      if (!isfinite(Xm[t])) ka.flag_nonphysical();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Phase B, StandardForm with ReferenceOperators
+// ---------------------------------------------------------------------------
+template <int D, int NC>
+__global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const Layout &L = ka.layB;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *uq = base + L.off[0], *uf = base + L.off[1], *ff = base + L.off[2], *rq = base + L.off[3],
+         *fq = base + L.off[4], *tmp = base + L.off[5], *tmp2 = base + L.off[6], *Z = base + L.off[8],
+         *Wb = base + L.off[9];
+
+  const double *uqg = ka.u_q + (size_t)kk * NC * nq;
+  const double *ufg = ka.u_f + (size_t)kk * NC * nf;
+  for (int t = lane; t < NC * nq; t += tpe) uq[t] = uqg[t];
+  for (int t = lane; t < NC * nf; t += tpe) uf[t] = ufg[t];
+  __syncthreads();
+  // f_q[n][e][i] = physical flux
+  for (int i = lane; i < nq; i += tpe) {
+    if constexpr (NC == 1) {
+#pragma unroll
+      for (int n = 0; n < D; ++n) fq[n * nq + i] = ph.a[n] * uq[i];
+    } else {
+      double u[NC], F[NC][D];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) u[e] = uq[e * nq + i];
+      euler_flux<D>(ph, u, F);
+#pragma unroll
+      for (int n = 0; n < D; ++n)
+#pragma unroll
+        for (int e = 0; e < NC; ++e) fq[(n * NC + e) * nq + i] = F[e][n];
+    }
+  }
+  // numerical flux with the conservative two-point flux; not yet scaled by BJf
+  {
+    const int nff = nf;
+    for (int j = lane; j < nff; j += tpe) {
+      int P = ka.geo.mapP[(size_t)kk * nf + j];
+      int jn = P % nf, kn = P / nf;
+      double ui[NC], uo[NC], n[D], F[NC][D];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        ui[e] = uf[e * nf + j];
+        uo[e] = ka.u_f[((size_t)kn * NC + e) * nf + jn];
+      }
+#pragma unroll
+      for (int m = 0; m < D; ++m) n[m] = ka.geo.n_f[m + D * (j + (size_t)nf * kk)];
+      Physics ph2 = ph;
+      ph2.ec = 0;
+      two_point<D, NC>(ph2, ui, uo, F);
+      double a = 0.0;
+      if (ph.nflux == 0) a = ph.half_lambda * wave_speed<D, NC>(ph, ui, uo, n);
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        double fn = 0.0;
+#pragma unroll
+        for (int m = 0; m < D; ++m) fn = fma(F[e][m], n[m], fn);
+        ff[e * nf + j] = (ph.nflux == 0) ? fma(a, ui[e] - uo[e], fn) : fn;
+      }
+    }
+  }
+  for (int t = lane; t < NC * nq; t += tpe) rq[t] = 0.0;
+  __syncthreads();
+  const double *hwl = ka.geo.halfWLambda + (size_t)kk * nq * D * D;
+  for (int n = 0; n < D; ++n) {
+    const double *fn_ = fq + (size_t)n * NC * nq;
+    for (int m = 0; m < D; ++m) {
+      const double *hw = hwl + nq * (m + D * n);
+      // tmp = halfWLambda .* f_n ; tmp2 = D_m f_n
+      for (int t = lane; t < NC * nq; t += tpe) tmp[t] = hw[t % nq] * fn_[t];
+      csr_mul<NC>(nq, nq, op.D_ptr[m], op.D_idx[m], op.D_val[m], fn_, tmp2, lane, tpe);
+      __syncthreads();
+      // r_q += D_m^T tmp - halfWLambda .* tmp2
+      for (int t = lane; t < NC * nq; t += tpe) {
+        int i = t % nq, e = t / nq;
+        double acc = 0.0;
+        for (int q = op.Dt_ptr[m][i]; q < op.Dt_ptr[m][i + 1]; ++q)
+          acc += op.Dt_val[m][q] * tmp[e * nq + op.Dt_idx[m][q]];
+        rq[t] += acc;
+        rq[t] -= tmp2[t] * hw[i];
+      }
+      __syncthreads();
+    }
+    // f_f -= halfN[n] .* (R f_n)
+    for (int t = lane; t < NC * nf; t += tpe) {
+      int j = t % nf, e = t / nf;
+      double acc = 0.0;
+      for (int q = op.R_ptr[j]; q < op.R_ptr[j + 1]; ++q) acc += op.R_val[q] * fn_[e * nq + op.R_idx[q]];
+      double halfN = 0.5 * ka.geo.n_f[n + D * (j + (size_t)nf * kk)];
+      ff[t] -= acc * halfN;
+    }
+    __syncthreads();
+  }
+  // f_f .*= BJf ; r_q -= R^T f_f
+  for (int t = lane; t < NC * nf; t += tpe) ff[t] *= ka.geo.BJf[(size_t)kk * nf + t % nf];
+  __syncthreads();
+  for (int t = lane; t < NC * nq; t += tpe) {
+    int i = t % nq, e = t / nq;
+    double acc = 0.0;
+    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * ff[e * nf + op.Rt_idx[q]];
+    rq[t] -= acc;
+  }
+  __syncthreads();
+  double *Xm = tmp, *Yq = tmp2;
+  vdm_tmul<D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
+  mass_solve<D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
+                    ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq,
+                    Z, Wb, lane, tpe);
+  double *out = ka.dudt + (size_t)kk * NC * np;
+  if (live)
+    for (int t = lane; t < NC * np; t += tpe) {
+      out[t] = Xm[t];
+      if (!isfinite(Xm[t])) ka.flag_nonphysical();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// element-wise helpers: time-integration updates, layout conversion, reductions
+// ---------------------------------------------------------------------------
+
+// CarpenterKennedy2N54 stage: tmp = a tmp + dt k ; u = u + b tmp (a = 0 on stage 1)
+__global__ void ck_stage_kernel(double *__restrict__ u, double *__restrict__ tmp,
+                                const double *__restrict__ k, double a, double b, double dt,
+                                int first, size_t n) {
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) {
+    double t = first ? dt * k[x] : a * tmp[x] + dt * k[x];
+    tmp[x] = t;
+    u[x] = u[x] + b * t;
+  }
+}
+
+// classic RK4 stage helpers
+__global__ void rk4_stage_kernel(const double *__restrict__ u, double *__restrict__ ust,
+                                 double *__restrict__ acc, const double *__restrict__ k,
+                                 double acc_w, double c, int first, size_t n) {
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) {
+    double kx = k[x];
+    acc[x] = first ? kx : acc[x] + acc_w * kx;
+    ust[x] = u[x] + c * kx;
+  }
+}
+
+__global__ void rk4_final_kernel(double *__restrict__ u, const double *__restrict__ acc,
+                                 const double *__restrict__ k, double dt6, size_t n) {
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x)
+    u[x] = u[x] + dt6 * (acc[x] + k[x]);
+}
+
+// internal facet layout (ne, nc, nf) -> the reference's (nf, ne, nc)
+__global__ void facet_to_reference_layout(const double *__restrict__ in, double *__restrict__ out,
+                                          int nf, int ne, int nc) {
+  size_t n = (size_t)nf * ne * nc;
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) {
+    size_t j = x % nf, r = x / nf, k = r % ne, e = r / ne;
+    out[x] = in[(k * nc + e) * nf + j];
+  }
+}
+
+// per-element FP64 partial sums of the conservation and entropy residuals
+// (Analysis/conservation.jl:145-189); reduced on the host in element order
+template <int D, int NC>
+__global__ void __launch_bounds__(256) conservation_kernel(KernelArgs ka, const double *u,
+                                                           const double *dudt, double *partial) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Layout &L = ka.layA;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3],
+         *F = base + L.off[4];
+  const int np = op.np, nq = op.nq;
+  for (int t = lane; t < NC * np; t += tpe) X[t] = u[(size_t)kk * NC * np + t];
+  __syncthreads();
+  vdm_mul<D, NC>(op, X, Y, Z, Wb, lane, tpe);       // Y = V u
+  for (int t = lane; t < NC * np; t += tpe) X[t] = dudt[(size_t)kk * NC * np + t];
+  __syncthreads();
+  vdm_mul<D, NC>(op, X, F, Z, Wb, lane, tpe);       // F = V dudt
+  const double *WJ = ka.geo.WJ + (size_t)kk * nq;
+  // lane-ordered partial sums, reduced by lane 0 in a fixed order
+  double *red = base + L.off[5];  // tpe x (NC + 1)
+  {
+    double acc[NC + 1];
+#pragma unroll
+    for (int e = 0; e <= NC; ++e) acc[e] = 0.0;
+    for (int i = lane; i < nq; i += tpe) {
+      double ui[NC], wi[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) ui[e] = Y[e * nq + i];
+      if constexpr (NC > 1) cons_to_entropy<D>(ka.ph, ui, wi);
+      else wi[0] = ui[0];
+      double t = 0.0;
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        acc[e] += WJ[i] * F[e * nq + i];
+        t += wi[e] * F[e * nq + i];
+      }
+      acc[NC] += WJ[i] * t;
+    }
+#pragma unroll
+    for (int e = 0; e <= NC; ++e) red[lane * (NC + 1) + e] = acc[e];
+  }
+  __syncthreads();
+  if (lane == 0 && live) {
+    for (int e = 0; e <= NC; ++e) {
+      double s = 0.0;
+      for (int l = 0; l < tpe; ++l) s += red[l * (NC + 1) + e];
+      partial[(size_t)k * (NC + 1) + e] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------
+#define SSE_DISPATCH(D_, NC_, CALL)                                       \
+  if (ka.op.d == 2 && ka.op.nc == 1) { constexpr int D = 2, NC = 1; CALL; } \
+  else if (ka.op.d == 2 && ka.op.nc == 4) { constexpr int D = 2, NC = 4; CALL; } \
+  else if (ka.op.d == 3 && ka.op.nc == 1) { constexpr int D = 3, NC = 1; CALL; } \
+  else if (ka.op.d == 3 && ka.op.nc == 5) { constexpr int D = 3, NC = 5; CALL; } \
+  else return cudaErrorInvalidValue;
+
+cudaError_t sse_set_smem_limits(const KernelArgs &ka, size_t smA, size_t smB) {
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void *f, size_t bytes) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  };
+  SSE_DISPATCH(D, NC, {
+    set((const void *)nodal_values_kernel<D, NC>, smA);
+    set((const void *)conservation_kernel<D, NC>, smA);
+    if (ka.fd) set((const void *)fd_time_derivative_kernel<D, NC>, smB);
+    else set((const void *)std_time_derivative_kernel<D, NC>, smB);
+  });
+  return e;
+}
+
+cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st) {
+  int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  size_t sm = (size_t)ka.epb * ka.layA.team_doubles * sizeof(double);
+  SSE_DISPATCH(D, NC, (nodal_values_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st) {
+  int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  size_t sm = (size_t)ka.epb * ka.layB.team_doubles * sizeof(double);
+  if (ka.fd) {
+    SSE_DISPATCH(D, NC, (fd_time_derivative_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka)));
+  } else {
+    SSE_DISPATCH(D, NC, (std_time_derivative_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka)));
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conservation(const KernelArgs &ka, const double *u, const double *dudt,
+                                double *partial, cudaStream_t st) {
+  int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  size_t sm = (size_t)ka.epb * ka.layA.team_doubles * sizeof(double);
+  SSE_DISPATCH(D, NC, (conservation_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka, u, dudt, partial)));
+  return cudaGetLastError();
+}
+
+static int elementwise_grid(size_t n) {
+  size_t g = (n + 255) / 256;
+  return (int)(g > 152 * 16 ? 152 * 16 : (g < 1 ? 1 : g));
+}
+
+cudaError_t launch_ck_stage(double *u, double *tmp, const double *k, double a, double b, double dt,
+                            int first, size_t n, cudaStream_t st) {
+  ck_stage_kernel<<<elementwise_grid(n), 256, 0, st>>>(u, tmp, k, a, b, dt, first, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rk4_stage(const double *u, double *ust, double *acc, const double *k, double acc_w,
+                             double c, int first, size_t n, cudaStream_t st) {
+  rk4_stage_kernel<<<elementwise_grid(n), 256, 0, st>>>(u, ust, acc, k, acc_w, c, first, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rk4_final(double *u, const double *acc, const double *k, double dt6, size_t n,
+                             cudaStream_t st) {
+  rk4_final_kernel<<<elementwise_grid(n), 256, 0, st>>>(u, acc, k, dt6, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_facet_layout(const double *in, double *out, int nf, int ne, int nc, cudaStream_t st) {
+  size_t n = (size_t)nf * ne * nc;
+  facet_to_reference_layout<<<elementwise_grid(n), 256, 0, st>>>(in, out, nf, ne, nc);
+  return cudaGetLastError();
+}
+
+}  // namespace sse

@@ -1,0 +1,47 @@
+// sse_kernels.cuh -- kernel argument block and launchers.
+#pragma once
+
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "sse_device.cuh"
+
+namespace sse {
+
+// Per-team shared-memory layout (offsets in doubles) computed on the host.
+struct Layout {
+  int off[12];
+  int team_doubles;
+};
+
+struct KernelArgs {
+  DevOps op;
+  DevGeo geo;
+  Physics ph;
+  Layout layA, layB;
+  int ne, epb, tpb;
+  int fd, project_entropy, mass_wa;
+  const double *u;   // modal state (np x nc x ne)
+  double *dudt;      // residual   (np x nc x ne)
+  double *u_q;       // volume nodal scratch (nq x nc x ne)
+  double *u_f;       // facet nodal scratch, internal layout (nf x nc x ne) element-major
+  int *flag;         // nonzero: non-physical state met
+
+  __device__ __forceinline__ void flag_nonphysical() const { atomicOr(flag, 1); }
+};
+
+cudaError_t sse_set_smem_limits(const KernelArgs &ka, size_t smA, size_t smB);
+cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st);
+cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st);
+cudaError_t launch_conservation(const KernelArgs &ka, const double *u, const double *dudt,
+                                double *partial, cudaStream_t st);
+cudaError_t launch_ck_stage(double *u, double *tmp, const double *k, double a, double b, double dt,
+                            int first, size_t n, cudaStream_t st);
+cudaError_t launch_rk4_stage(const double *u, double *ust, double *acc, const double *k,
+                             double acc_w, double c, int first, size_t n, cudaStream_t st);
+cudaError_t launch_rk4_final(double *u, const double *acc, const double *k, double dt6, size_t n,
+                             cudaStream_t st);
+cudaError_t launch_facet_layout(const double *in, double *out, int nf, int ne, int nc,
+                                cudaStream_t st);
+
+}  // namespace sse

@@ -1,0 +1,116 @@
+"""Algorithmic work model of one residual evaluation, per element.
+
+Counting convention: add, subtract, multiply = 1 flop; fused multiply-add =
+2; divide, square root, log, exp, pow = 1 each.  Volume fluxes are counted
+once per unique node pair, contractions once per (pair, direction)
+incidence, as the reference's sparse loops perform them
+(flux_differencing_form.jl:37-75, 126-168).  Bytes are the minimal HBM
+traffic of the FP64 form: every array read or written once per phase.
+The same numbers feed ``roofline.achieved`` in bench.py and the reports.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+
+@dataclass
+class Work:
+    flops_A: float      # nodal values / entropy projection, per element
+    flops_B: float      # time derivative, per element
+    bytes_A: float
+    bytes_B: float
+    bytes_stage: float  # Runge-Kutta stage update, per element
+
+    @property
+    def flops(self):
+        return self.flops_A + self.flops_B
+
+    @property
+    def bytes(self):
+        return self.bytes_A + self.bytes_B + self.bytes_stage
+
+
+def vdm_flops(ra) -> float:
+    """One sum-factorised application of V (or V^T) to one component."""
+    if ra.V is None:
+        return 0.0
+    p1 = ra.p + 1
+    if ra.d == 2:
+        M1, M2 = ra.n1d
+        return 2.0 * (M2 * ra.N_p + M1 * M2 * p1)
+    M1, M2, M3 = ra.n1d
+    nb12 = p1 * (p1 + 1) // 2
+    return 2.0 * (M3 * ra.N_p + nb12 * M2 * M3 + M1 * p1 * M2 * M3)
+
+
+def ec_flux_flops(d: int) -> float:
+    """Ranocha's two-point flux tensor from per-node primitives
+    (euler_navierstokes.jl:171-195; logmean series branch)."""
+    logmeans = 2 * 19
+    return logmeans + 2 * d + (2 * d - 1) + 2 + 4 + d + 3 * d * d + 6 * d
+
+
+def model(host) -> Work:
+    """Work per element for the configuration held by ``host`` (HostArrays)."""
+    ra = host.sd.reference_approximation
+    d, nc, nq, nf, np_ = ra.d, host.N_c, host.N_q, host.N_f, host.N_p
+    nnzR = host.R.nnz
+    vf = vdm_flops(ra)
+    euler = nc > 1
+    fd = host.S != []
+    f8 = 8.0
+    # ---- phase A
+    if fd and euler:
+        c2e = 3 * d + 12
+        e2c = nc + 3 * d + 14
+        nV = 5 if ra.V is not None else 0
+        flops_A = nc * nV * vf + nc * 2 * nnzR + nq * (c2e + nc) + nq * nc + (nq + nf) * e2c
+        bytes_A = f8 * (np_ * nc + 2 * nq + nq * nc + nf * nc)
+    else:
+        flops_A = nc * (vf + 2 * nnzR)
+        bytes_A = f8 * (np_ * nc + nq * nc + nf * nc)
+    # ---- phase B
+    nV_B = 3 if ra.V is not None else 0
+    if fd:
+        npair = sum(1 for _ in range(0))
+        S_inc = sum(s.nnz for s in host.S) // 2          # (pair, m) incidences with i < j
+        pairs = _unique_pairs(host)
+        nfp = host.C.nnz if host.C is not None else 0
+        if euler:
+            prim = 3 * d + 4
+            pair_flux = ec_flux_flops(d)
+            wave = 40
+            flux_fac = 2 * prim + pair_flux + wave + nc * (2 * d + 3) + nc
+            flops_B = ((nq + nf) * prim + nf * flux_fac + pairs * pair_flux
+                       + S_inc * (d + nc * (2 * d + 2) + 2 * nc)
+                       + nfp * (pair_flux + d + nc * (2 * d + 3))
+                       + nc * 2 * nnzR + nq * nc + nc * nV_B * vf + nq * nc)
+        else:
+            pair_flux = 2 + d
+            flops_B = (nf * (pair_flux + 2 * d + 4) + pairs * pair_flux
+                       + S_inc * (d + 2 * d + 2 + 2) + nfp * (pair_flux + d + 2 * d + 3)
+                       + 2 * nnzR + nq + nV_B * vf + nq)
+        del npair
+        bytes_B = f8 * (nq * nc + 2 * nf * nc + d * d * nq + d * ra.reference_element.num_faces * nq
+                        + 2 * d * nf + nf + nq + np_ * nc) + 4.0 * nf
+    else:
+        nnzD = sum(D.nnz for D in host.D)
+        phys = (d + 2) * d * 2 if euler else d
+        flops_B = (nq * phys + nf * (4 * d + 10) * nc
+                   + d * d * nc * (2 * nq + 4 * nnzD / d)
+                   + d * nc * (2 * nnzR + 2 * nf) + nc * nf + nc * 2 * nnzR + nc * nq
+                   + nc * nV_B * vf + nq * nc)
+        bytes_B = f8 * (nq * nc + 2 * nf * nc + d * d * nq + d * nf + nf + nq + np_ * nc) + 4.0 * nf
+    bytes_stage = f8 * 5 * np_ * nc
+    return Work(float(flops_A), float(flops_B), bytes_A, bytes_B, bytes_stage)
+
+
+def _unique_pairs(host) -> int:
+    seen = set()
+    for S in host.S:
+        for j in range(S.n):
+            for q in range(S.colptr[j] - 1, S.colptr[j + 1] - 1):
+                i = S.rowval[q] - 1
+                if i < j:
+                    seen.add((i, j))
+    return len(seen)

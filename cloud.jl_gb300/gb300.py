@@ -1,0 +1,192 @@
+"""GB300 backend: the ``GB300 <: AbstractParallelism`` drop-in.
+
+``semidiscretize(..., parallelism=GB300())`` builds the reference's operator
+structs on the host (``HostArrays``), hands them once to the C-ABI library
+``libsse_gb300.so`` and returns an ``ODEProblem`` whose right-hand side
+``semi_discrete_residual(dudt, u, solver, t)`` runs entirely on the GPU
+(Solvers.jl:429-514).  There is no CPU path: if the library is missing or
+no CUDA device is present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from .solver import HostArrays, initialize
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libsse_gb300.so")
+
+EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual", "sse_nodal_values",
+            "sse_rk_steps", "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
+            "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
+            "sse_create_error"]
+
+_lib = None
+
+
+class SSEError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sse status {code}: {msg}")
+        self.code = code
+
+
+def load_library(path: str | None = None):
+    """Load libsse_gb300.so (built by build.build()); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build the CUDA library first (build.build())")
+    L = C.CDLL(path)
+    vp, i32, dp = C.c_void_p, C.c_int32, C.c_double
+    L.sse_abi_version.restype = i32
+    L.sse_create.argtypes = [vp, vp, vp, C.POINTER(vp)]
+    L.sse_create.restype = i32
+    L.sse_destroy.argtypes = [vp]
+    L.sse_destroy.restype = i32
+    L.sse_residual.argtypes = [vp, vp, vp, dp, i32]
+    L.sse_residual.restype = i32
+    L.sse_nodal_values.argtypes = [vp, vp, vp, vp, i32]
+    L.sse_nodal_values.restype = i32
+    L.sse_rk_steps.argtypes = [vp, vp, i32, dp, i32, C.POINTER(dp), i32]
+    L.sse_rk_steps.restype = i32
+    L.sse_conservation_residual.argtypes = [vp, vp, vp, vp, i32]
+    L.sse_conservation_residual.restype = i32
+    L.sse_set_precision.argtypes = [vp, i32]
+    L.sse_set_precision.restype = i32
+    L.sse_set_stream.argtypes = [vp, vp]
+    L.sse_set_stream.restype = i32
+    L.sse_phase_timings.argtypes = [vp, vp, i32, vp]
+    L.sse_phase_timings.restype = i32
+    L.sse_measure_fma_peaks.argtypes = [vp]
+    L.sse_measure_fma_peaks.restype = i32
+    L.sse_struct_sizes.argtypes = [vp]
+    L.sse_struct_sizes.restype = i32
+    L.sse_last_error.argtypes = [vp]
+    L.sse_last_error.restype = C.c_char_p
+    L.sse_create_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _addr(x):
+    """Raw address of a numpy array or a torch tensor (host or device)."""
+    if isinstance(x, np.ndarray):
+        assert x.dtype == np.float64 and x.flags.c_contiguous
+        return C.c_void_p(x.ctypes.data), abi.SSE_HOST
+    # torch tensor
+    assert x.dtype.__repr__() == "torch.float64" and x.is_contiguous()
+    return C.c_void_p(x.data_ptr()), (abi.SSE_DEVICE if x.is_cuda else abi.SSE_HOST)
+
+
+class GB300Solver:
+    """``Solver{..., GB300}``: owns one library handle."""
+
+    def __init__(self, host: HostArrays):
+        self.host = host
+        self.L = load_library()
+        h = C.c_void_p()
+        rc = self.L.sse_create(C.byref(host.cfg), C.byref(host.ops), C.byref(host.geo), C.byref(h))
+        if rc != abi.SSE_OK:
+            raise SSEError(rc, self.L.sse_create_error().decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sse_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != abi.SSE_OK:
+            raise SSEError(rc, self.L.sse_last_error(self.h).decode())
+
+    def residual(self, u, dudt=None, t: float = 0.0):
+        if dudt is None:
+            dudt = np.empty_like(u) if isinstance(u, np.ndarray) else u.new_empty(u.shape)
+        pu, mu = _addr(u)
+        pd, md = _addr(dudt)
+        assert mu == md, "u and dudt must live in the same memory"
+        self._check(self.L.sse_residual(self.h, pu, pd, t, mu))
+        return dudt
+
+    def nodal_values(self, u):
+        h = self.host
+        if isinstance(u, np.ndarray):
+            u_q = np.empty((h.N_e, h.N_c, h.N_q))
+            u_f = np.empty((h.N_c, h.N_e, h.N_f))
+        else:
+            u_q = u.new_empty((h.N_e, h.N_c, h.N_q))
+            u_f = u.new_empty((h.N_c, h.N_e, h.N_f))
+        pu, mu = _addr(u)
+        self._check(self.L.sse_nodal_values(self.h, pu, _addr(u_q)[0], _addr(u_f)[0], mu))
+        return u_q, u_f
+
+    def rk_steps(self, u, n_steps: int, dt: float, scheme: int = abi.SSE_CARPENTER_KENNEDY_2N54,
+                 t: float = 0.0) -> float:
+        pu, mu = _addr(u)
+        tt = C.c_double(t)
+        self._check(self.L.sse_rk_steps(self.h, pu, n_steps, dt, scheme, C.byref(tt), mu))
+        return tt.value
+
+    def conservation_residual(self, u, dudt) -> np.ndarray:
+        out = np.zeros(self.host.N_c + 1)
+        pu, mu = _addr(u)
+        pd, md = _addr(dudt)
+        assert mu == md
+        self._check(self.L.sse_conservation_residual(self.h, pu, pd, C.c_void_p(out.ctypes.data), mu))
+        return out
+
+    def set_precision(self, precision: int):
+        self._check(self.L.sse_set_precision(self.h, precision))
+
+    def set_stream(self, stream_handle: int):
+        self._check(self.L.sse_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    def phase_timings(self, u_dev, n_iter: int) -> np.ndarray:
+        out = np.zeros(3)
+        self._check(self.L.sse_phase_timings(self.h, _addr(u_dev)[0], n_iter, C.c_void_p(out.ctypes.data)))
+        return out
+
+
+def measure_fma_peaks():
+    """Measured (FP64, FP32) CUDA-core FMA throughput of the device, TFLOP/s."""
+    L = load_library()
+    out = np.zeros(2)
+    rc = L.sse_measure_fma_peaks(C.c_void_p(out.ctypes.data))
+    if rc != abi.SSE_OK:
+        raise SSEError(rc, "peak measurement failed")
+    return float(out[0]), float(out[1])
+
+
+@dataclass
+class ODEProblem:
+    """``ODEProblem(semi_discrete_residual!, u0, tspan, solver)``."""
+    f: object
+    u0: np.ndarray
+    tspan: tuple
+    p: GB300Solver
+
+
+def semi_discrete_residual(dudt, u, solver: GB300Solver, t: float = 0.0):
+    """``semi_discrete_residual!(dudt, u, solver, t)`` on the GPU."""
+    return solver.residual(u, dudt, t)
+
+
+def semidiscretize(conservation_law, spatial_discretization, initial_data, form, tspan,
+                   mass_matrix_solver="default") -> ODEProblem:
+    """``semidiscretize(...; parallelism = GB300())`` (Solvers.jl:429-452)."""
+    u0 = initialize(initial_data, spatial_discretization)
+    host = HostArrays(conservation_law, spatial_discretization, form, mass_matrix_solver)
+    return ODEProblem(semi_discrete_residual, u0, tuple(tspan), GB300Solver(host))

@@ -168,6 +168,28 @@ int32_t sse_conservation_residual(sse_solver *s, const double *u, const double *
  * arithmetic, FP64 geometry, RK accumulation and reductions). */
 int32_t sse_set_precision(sse_solver *s, int32_t precision);
 
+/* Run this handle's work on the caller's CUDA stream (a cudaStream_t; NULL
+ * selects the legacy default stream) instead of its own.  No counterpart in
+ * the reference, which has no device. */
+int32_t sse_set_stream(sse_solver *s, void *stream);
+
+/* Average device time in milliseconds of each residual phase over n_iter
+ * evaluations at the device state u_dev, timed with CUDA events on the
+ * handle's stream: out[0] nodal values (phase A), out[1] time derivative
+ * (phase B), out[2] one Runge-Kutta stage update.  No counterpart in the
+ * reference; mirrors the "nodal values" / "time deriv." TimerOutputs
+ * sections of Solvers.jl:474-489. */
+int32_t sse_phase_timings(sse_solver *s, const double *u_dev, int32_t n_iter, double *out);
+
+/* Measured FMA throughput of the current device in TFLOP/s (2 flops per
+ * FMA): out[0] FP64, out[1] FP32 CUDA-core pipes.  The roofline
+ * denominators of the residual kernels; no counterpart in the reference. */
+int32_t sse_measure_fma_peaks(double *out);
+
+/* sizeof(sse_config), sizeof(sse_csc), sizeof(sse_operators),
+ * sizeof(sse_geometry) into out[0..3], for checking foreign bindings. */
+int32_t sse_struct_sizes(int32_t *out);
+
 /* Message of the last failing call on this handle ("" if none). */
 const char *sse_last_error(const sse_solver *s);
 /* Message of the last failing sse_create (no handle exists then). */

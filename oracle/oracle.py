@@ -5,40 +5,56 @@ TEST INFRASTRUCTURE ONLY.  The oracle restates the reference's CPU residual
 warped_product_*.jl) and is used by tests/, __graft_entry__.smoke() and the
 cpu_baseline / --impl reference legs of bench.py to check and time the CUDA
 library.  The product never imports this module.
+
+Two builds exist: the default one (no floating-point contraction beyond the
+explicit fma() calls that mirror the reference's @muladd) and an ``fma``
+variant compiled with contraction enabled.  Both are valid FP64 evaluations
+of the same code; their difference measures the round-off floor of a
+residual on a given input, which calibrates the parity tolerance.
 """
 from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 import subprocess
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "sse_oracle.c")
-LIB = os.path.join(HERE, "_build", "libsse_oracle.so")
+HDR = os.path.join(HERE, "..", "include", "sse_gb300.h")
+BUILD = os.path.join(HERE, "_build")
+VARIANTS = {
+    "default": ["-ffp-contract=off"],
+    "fma": ["-ffp-contract=fast"] + (["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []),
+}
 
 
-def build(force: bool = False) -> str:
-    """Compile the oracle with gcc -O3 -fopenmp (no fast-math, no FP
-    contraction beyond the explicit fma() calls that mirror @muladd)."""
-    os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
-        return LIB
-    cmd = ["gcc", "-O3", "-std=c99", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-           SRC, "-o", LIB, "-lm"]
+def lib_path(variant: str = "default") -> str:
+    return os.path.join(BUILD, f"libsse_oracle_{variant}.so")
+
+
+def build(force: bool = False, variant: str = "default") -> str:
+    """Compile the oracle with gcc -O3 -fopenmp (no fast-math)."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = lib_path(variant)
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR))
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return out
+    cmd = ["gcc", "-O3", "-std=c99", "-fPIC", "-shared", "-fopenmp", *VARIANTS[variant],
+           SRC, "-o", out + ".tmp", "-lm"]
     subprocess.run(cmd, check=True)
-    return LIB
+    os.replace(out + ".tmp", out)
+    return out
 
 
-_lib = None
+_libs: dict = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = build()
-        L = C.CDLL(path)
+def lib(variant: str = "default"):
+    if variant not in _libs:
+        L = C.CDLL(build(variant=variant))
         L.oracle_create.restype = C.c_void_p
         L.oracle_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.oracle_destroy.argtypes = [C.c_void_p]
@@ -47,8 +63,8 @@ def lib():
         L.oracle_rk_steps.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int]
         L.oracle_conservation_residual.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_threads.restype = C.c_int
-        _lib = L
-    return _lib
+        _libs[variant] = L
+    return _libs[variant]
 
 
 def _ptr(a):
@@ -58,23 +74,23 @@ def _ptr(a):
 class Oracle:
     """CPU residual over the same HostArrays the CUDA library consumes."""
 
-    def __init__(self, host, nthreads: int | None = None):
-        L = lib()
+    def __init__(self, host, nthreads: int | None = None, variant: str = "default"):
+        self.L = lib(variant)
         self.host = host
-        self.nthreads = nthreads or L.oracle_threads()
-        self.h = L.oracle_create(C.byref(host.cfg), C.byref(host.ops), C.byref(host.geo),
-                                 self.nthreads)
+        self.nthreads = nthreads or self.L.oracle_threads()
+        self.h = self.L.oracle_create(C.byref(host.cfg), C.byref(host.ops), C.byref(host.geo),
+                                      self.nthreads)
 
     def __del__(self):
         if getattr(self, "h", None):
-            lib().oracle_destroy(self.h)
+            self.L.oracle_destroy(self.h)
             self.h = None
 
     def residual(self, u: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u, dtype=np.float64)
         assert u.shape == self.host.state_shape
         dudt = np.empty_like(u)
-        lib().oracle_residual(self.h, _ptr(u), _ptr(dudt))
+        self.L.oracle_residual(self.h, _ptr(u), _ptr(dudt))
         return dudt
 
     def nodal_values(self, u: np.ndarray):
@@ -82,17 +98,31 @@ class Oracle:
         h = self.host
         u_q = np.empty((h.N_e, h.N_c, h.N_q))
         u_f = np.empty((h.N_c, h.N_e, h.N_f))
-        lib().oracle_nodal_values(self.h, _ptr(u), _ptr(u_q), _ptr(u_f))
+        self.L.oracle_nodal_values(self.h, _ptr(u), _ptr(u_q), _ptr(u_f))
         return u_q, u_f
 
     def rk_steps(self, u: np.ndarray, n_steps: int, dt: float, scheme: int = 0) -> np.ndarray:
         u = np.array(u, dtype=np.float64, order="C", copy=True)
-        lib().oracle_rk_steps(self.h, _ptr(u), n_steps, dt, scheme)
+        self.L.oracle_rk_steps(self.h, _ptr(u), n_steps, dt, scheme)
         return u
 
     def conservation_residual(self, u: np.ndarray, dudt: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u, dtype=np.float64)
         dudt = np.ascontiguousarray(dudt, dtype=np.float64)
         out = np.zeros(self.host.N_c + 1)
-        lib().oracle_conservation_residual(self.h, _ptr(u), _ptr(dudt), _ptr(out))
+        self.L.oracle_conservation_residual(self.h, _ptr(u), _ptr(dudt), _ptr(out))
         return out
+
+
+def rel2(got, want) -> float:
+    """Whole-vector relative error ||got - want||_2 / ||want||_2."""
+    got = np.asarray(got, dtype=np.float64)
+    want = np.asarray(want, dtype=np.float64)
+    return float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
+
+
+def roundoff_floor(host, u) -> float:
+    """rel2 between the two oracle builds on the same input."""
+    a = Oracle(host).residual(u)
+    b = Oracle(host, variant="fma").residual(u)
+    return rel2(b, a)

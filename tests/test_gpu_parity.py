@@ -1,0 +1,116 @@
+"""GPU parity: the CUDA library through its C-ABI against the CPU oracle on
+identical seeded inputs.
+
+Tolerance (FP64 form): whole-vector relative error
+rel2 = ||x_gpu - x_oracle||_2 / ||x_oracle||_2 <= max(1e-12, 4 * floor),
+where floor is rel2 between two valid FP64 compilations of the oracle itself
+(with and without floating-point contraction) on the same input.  For most
+cases floor ~ 1e-14..1e-13 and the bound is the plain 1e-12; on the
+low-Mach 3-D Taylor-Green inputs with Lax-Friedrichs dissipation the
+oracle's own floor reaches ~1e-12 (the dissipation differences two
+entropy-projected facet states of magnitude ~1e2), and the GPU is held to
+the same round-off level.  A per-variable max-norm check at 1e-10 guards
+against a component-specific error hiding in the 2-norm.
+"""
+import numpy as np
+import pytest
+
+import cases
+from oracle.oracle import Oracle, rel2, roundoff_floor
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1.0e-12
+TOL_COMPONENT = 1.0e-10
+
+
+def relerr(got, want, axis_c=1):
+    """max over components of max|got - want| / max|want| (component axis 1)."""
+    got = np.asarray(got)
+    want = np.asarray(want)
+    errs = []
+    for c in range(want.shape[axis_c]):
+        w = np.take(want, c, axis=axis_c)
+        g = np.take(got, c, axis=axis_c)
+        errs.append(np.abs(g - w).max() / max(np.abs(w).max(), 1e-300))
+    return max(errs)
+
+
+@pytest.fixture(scope="module")
+def built(gpu_lib):
+    return gpu_lib
+
+
+@pytest.mark.parametrize("name", cases.NAMES)
+def test_residual_matches_oracle(built, pkg, name):
+    host, u = cases.make(name)
+    gpu = pkg.GB300Solver(host)
+    got = gpu.residual(u)
+    want = Oracle(host).residual(u)
+    floor = roundoff_floor(host, u)
+    err = rel2(got, want)
+    print(f"{name}: rel2 {err:.2e}  oracle floor {floor:.2e}")
+    assert err <= max(TOL, 4.0 * floor)
+    assert relerr(got, want) <= TOL_COMPONENT
+
+
+@pytest.mark.parametrize("name", ["adv_tri_modal", "vortex_tri_modal", "vortex_tri_nodal",
+                                  "tgv_tet_modal", "tgv_tet_p5"])
+def test_nodal_values_match_oracle(built, pkg, name):
+    host, u = cases.make(name)
+    gpu = pkg.GB300Solver(host)
+    uq_g, uf_g = gpu.nodal_values(u)
+    uq_o, uf_o = Oracle(host).nodal_values(u)
+    assert relerr(uq_g, uq_o) <= TOL
+    assert relerr(uf_g, uf_o, axis_c=0) <= TOL
+
+
+def test_device_memory_path_and_determinism(built, pkg):
+    import torch
+    host, u = cases.make("tgv_tet_modal")
+    gpu = pkg.GB300Solver(host)
+    ud = torch.from_numpy(u).cuda()
+    a = gpu.residual(ud)
+    b = gpu.residual(ud)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)                               # bitwise run-to-run
+    host_res = gpu.residual(u)
+    assert np.array_equal(a.cpu().numpy(), host_res)       # host and device paths agree
+
+
+@pytest.mark.parametrize("name,scheme,steps", [("adv_tri_modal", 1, 3), ("vortex_tri_modal", 0, 3),
+                                               ("tgv_tet_modal", 0, 2)])
+def test_rk_steps_match_oracle(built, pkg, name, scheme, steps):
+    host, u = cases.make(name)
+    gpu = pkg.GB300Solver(host)
+    dt = 1.0e-3
+    ug = u.copy()
+    t = gpu.rk_steps(ug, steps, dt, scheme)
+    assert abs(t - steps * dt) < 1e-15
+    uo = Oracle(host).rk_steps(u, steps, dt, scheme)
+    assert relerr(ug, uo) <= TOL
+
+
+@pytest.mark.parametrize("name", ["adv_tri_modal", "vortex_tri_ec", "tgv_tet_ec"])
+def test_conservation_residual_matches_oracle(built, pkg, name):
+    host, u = cases.make(name)
+    gpu = pkg.GB300Solver(host)
+    o = Oracle(host)
+    du = o.residual(u)
+    got = gpu.conservation_residual(u, du)
+    want = o.conservation_residual(u, du)
+    scale = np.abs(du).max() * np.abs(host.WJ).sum()
+    assert np.abs(got - want).max() <= 1e-12 * scale
+
+
+def test_nonphysical_state_is_reported(built, pkg):
+    host, u = cases.make("vortex_tri_modal")
+    gpu = pkg.GB300Solver(host)
+    bad = u.copy()
+    bad[3, 0, :] = -bad[3, 0, :]               # negative density modes on one element
+    with pytest.raises(pkg.SSEError) as ei:
+        gpu.residual(bad)
+    assert ei.value.code == pkg.abi.SSE_ERR_NONPHYSICAL
+    # the handle stays usable afterwards
+    good = gpu.residual(u)
+    assert np.isfinite(good).all()
