@@ -39,9 +39,14 @@ def _grid_vertices(M, limits):
 
 
 def uniform_tri_elements(Mx: int, My: int) -> np.ndarray:
-    """Two triangles per cell of an Mx x My grid, split along the diagonal
-    from (i+1, j) to (i, j+1); rows are 0-based vertex ids, counter-clockwise.
-    Elements are numbered cell by cell with x fastest."""
+    """Two triangles per cell of an Mx x My grid with corners
+    v1=(i,j), v2=(i+1,j), v3=(i+1,j+1), v4=(i,j+1): (v1, v2, v3) and
+    (v3, v4, v1), counter-clockwise, 0-based vertex ids, cells numbered with
+    x fastest.  This is StartUpDG's ``uniform_mesh(Tri(), Kx, Ky)`` split
+    and vertex order (which vertex is the collapsed one matters for
+    ModalTensor); the reference's own goldens pin it (test/runtests.jl:57,
+    :114-119 are reproduced to round-off with it and not with the other
+    diagonal or rotations)."""
     nx = Mx + 1
     ex, ey = np.meshgrid(np.arange(Mx), np.arange(My), indexing="xy")
     ex = ex.reshape(-1)
@@ -50,8 +55,8 @@ def uniform_tri_elements(Mx: int, My: int) -> np.ndarray:
     v2 = v1 + 1
     v3 = v1 + 1 + nx
     v4 = v1 + nx
-    t1 = np.stack([v1, v2, v4], axis=1)
-    t2 = np.stack([v2, v3, v4], axis=1)
+    t1 = np.stack([v1, v2, v3], axis=1)
+    t2 = np.stack([v3, v4, v1], axis=1)
     return np.stack([t1, t2], axis=1).reshape(-1, 3)
 
 

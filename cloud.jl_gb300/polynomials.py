@@ -260,11 +260,6 @@ def tet_basis(n: int, r, s, t):
 # Interpolation nodes on simplices
 # ---------------------------------------------------------------------------
 
-_ALPHA_OPT_TRI = [0.0000, 0.0000, 1.4152, 0.1001, 0.2751, 0.9800, 1.0999,
-                  1.2832, 1.3648, 1.4773, 1.4959, 1.5743, 1.5770, 1.6223,
-                  1.6258]
-
-
 def _warp_factor(n: int, rout: np.ndarray) -> np.ndarray:
     """1-D warp from equispaced to LGL nodes, blended to vanish at +-1."""
     lgl = gauss_lobatto_nodes(n)
@@ -278,15 +273,19 @@ def _warp_factor(n: int, rout: np.ndarray) -> np.ndarray:
     return warp / np.where(sf != 0.0, sf, 1.0) + warp * (zerof - 1.0)
 
 
-def tri_nodes(n: int):
+def tri_nodes(n: int, alpha: float = 0.0):
     """Warp-and-blend interpolation nodes of degree ``n`` on the triangle.
 
+    ``alpha`` is the interior blending exponent of Warburton's construction.
+    The mapping nodes of the reference's ``RefElemData`` use alpha = 0: with
+    it the reference's degree-4 curved-triangle golden (test/runtests.jl:57)
+    is reproduced to 2e-15, and not with the optimised alpha(4) = 0.1001 of
+    Hesthaven & Warburton's table; degrees <= 3 do not depend on alpha.
     Ordering: the equispaced loop (L1 outer, L3 inner), which for n = 1
     gives the vertices (-1,-1), (1,-1), (-1,1).
     """
     if n == 0:
         return np.array([-1.0 / 3.0]), np.array([-1.0 / 3.0])
-    alpha = _ALPHA_OPT_TRI[n - 1] if n < 16 else 5.0 / 3.0
     l1, l3 = [], []
     for i in range(n + 1):
         for j in range(n + 1 - i):

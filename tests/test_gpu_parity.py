@@ -103,6 +103,31 @@ def test_conservation_residual_matches_oracle(built, pkg, name):
     assert np.abs(got - want).max() <= 1e-12 * scale
 
 
+def test_reference_goldens_through_gpu(built, pkg):
+    """The reference's own end-to-end goldens (test/runtests.jl:57, :114-119)
+    reproduced with every residual evaluated on the GPU (time stepping
+    with sse_rk_steps), at the reference's tolerance 1e-10."""
+    import json
+    import os
+    import reference_scenarios as RS
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+    sc = RS.advection_2d()
+    gpu = pkg.GB300Solver(sc["host"])
+    u = sc["u0"].copy()
+    gpu.rk_steps(u, sc["steps"], sc["dt"], pkg.abi.SSE_CARPENTER_KENNEDY_2N54)
+    l2 = RS.l2_error(sc["sd"], u, sc["exact"])[0]
+    assert abs(l2 - gold["advection_2d_modal_tensor_tri"]["l2"]) < gold["tol"]
+    sc = RS.euler_vortex_2d()
+    gpu = pkg.GB300Solver(sc["host"])
+    u = sc["u0"].copy()
+    gpu.rk_steps(u, sc["steps"], sc["dt"], pkg.abi.SSE_CARPENTER_KENNEDY_2N54)
+    l2 = RS.l2_error(sc["sd"], u, sc["exact"])
+    want = np.array(gold["euler_vortex_2d_modal_tensor_tri_fd_lf"]["l2"])
+    assert np.abs(l2 - want).max() < gold["tol"]
+    E0 = RS.conserved_totals(sc["host"], sc["u0"])
+    assert np.abs(RS.conserved_totals(sc["host"], u) - E0).max() < gold["tol"]
+
+
 def test_nonphysical_state_is_reported(built, pkg):
     host, u = cases.make("vortex_tri_modal")
     gpu = pkg.GB300Solver(host)
