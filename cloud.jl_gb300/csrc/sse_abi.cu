@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <exception>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -464,6 +465,41 @@ cudaError_t residual_device(sse_solver *s, const double *u, double *dudt) {
   return launch_time_derivative(ka, s->stream);
 }
 
+// ---------------------------------------------------------------------------
+// Fixed device scratch for sse_residual_static_scratch.
+//
+// The residual's two phases hand the element's volume and facet nodal states
+// (u_q, u_f) from one kernel to the next through global memory.  For callers
+// that must not allocate, that hand-over buffer is this file-scope array,
+// present on every GPU that loads the library for the life of the process.
+// Host code cannot use the symbol as a pointer: its device address is looked
+// up with cudaGetSymbolAddress once per device, with that device current.
+// ---------------------------------------------------------------------------
+constexpr size_t kStaticScratchDoubles = SSE_STATIC_SCRATCH_BYTES / sizeof(double);
+static __device__ __align__(256) double g_static_scratch[kStaticScratchDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_scratch_mutex;
+double *g_static_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device (looked up on
+// the first call per device).
+int static_scratch_address(sse_solver *s, double **out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(s, e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(s, SSE_ERR_UNSUPPORTED, "device ordinal too large");
+  std::lock_guard<std::mutex> lock(g_static_scratch_mutex);
+  if (!g_static_scratch_addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return cuda_fail(s, e, "cudaGetSymbolAddress(static scratch)");
+    g_static_scratch_addr[dev] = (double *)p;
+  }
+  *out = g_static_scratch_addr[dev];
+  return SSE_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -542,6 +578,30 @@ int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t, int
   } else {
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
   }
+  return check_flag(s);
+}
+
+int32_t sse_residual_static_scratch(sse_solver *s, const double *u_dev, double *dudt_dev) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!u_dev || !dudt_dev) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u/dudt");
+  const sse_config &c = s->cfg;
+  const size_t nq = (size_t)c.n_q * c.n_c * c.n_e, nf = (size_t)c.n_f * c.n_c * c.n_e;
+  if (nq + nf > kStaticScratchDoubles)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT,
+                "mesh too large for the static scratch: needs " + std::to_string((nq + nf) * 8) +
+                    " bytes of nodal states, the fixed buffer holds " +
+                    std::to_string(kStaticScratchDoubles * 8) + " (use sse_residual)");
+  double *scratch = nullptr;
+  int rc = static_scratch_address(s, &scratch);
+  if (rc != SSE_OK) return rc;
+  KernelArgs ka = s->ka;
+  ka.u = u_dev;
+  ka.dudt = dudt_dev;
+  ka.u_q = scratch;       // fully written by phase A before phase B reads it:
+  ka.u_f = scratch + nq;  // no clearing needed between calls
+  cudaError_t e = launch_nodal_values(ka, s->stream);
+  if (e == cudaSuccess) e = launch_time_derivative(ka, s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "residual (static scratch)");
   return check_flag(s);
 }
 

@@ -21,7 +21,8 @@ from .solver import HostArrays, initialize
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libsse_gb300.so")
 
-EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual", "sse_nodal_values",
+EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual",
+            "sse_residual_static_scratch", "sse_nodal_values",
             "sse_rk_steps", "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
             "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
             "sse_create_error"]
@@ -52,6 +53,8 @@ def load_library(path: str | None = None):
     L.sse_destroy.restype = i32
     L.sse_residual.argtypes = [vp, vp, vp, dp, i32]
     L.sse_residual.restype = i32
+    L.sse_residual_static_scratch.argtypes = [vp, vp, vp]
+    L.sse_residual_static_scratch.restype = i32
     L.sse_nodal_values.argtypes = [vp, vp, vp, vp, i32]
     L.sse_nodal_values.restype = i32
     L.sse_rk_steps.argtypes = [vp, vp, i32, dp, i32, C.POINTER(dp), i32]
