@@ -6,6 +6,7 @@
 // CSR tables the kernels use, keeps everything resident on the device and
 // launches the two residual phases on the handle's stream.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -382,6 +383,7 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   ph.gamma = c.gamma;
   ph.gm1 = c.gamma - 1.0;
   ph.igm1 = c.law == SSE_EULER ? 1.0 / (c.gamma - 1.0) : 0.0;
+  ph.log_gm1 = c.law == SSE_EULER ? std::log(c.gamma - 1.0) : 0.0;
   for (int m = 0; m < 3; ++m) ph.a[m] = c.a[m];
   ka.fd = fd;
   ka.project_entropy = fd && c.law == SSE_EULER;

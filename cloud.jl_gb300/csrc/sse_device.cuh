@@ -74,7 +74,7 @@ struct Physics {
   int nflux;     // 0 LF, 1 central, 2 EC numerical flux
   int ec;        // two-point flux: 1 entropy-conservative (Ranocha), 0 conservative
   double half_lambda;
-  double gamma, gm1, igm1;
+  double gamma, gm1, igm1, log_gm1;
   double a[3];
 };
 
@@ -91,6 +91,134 @@ __device__ __forceinline__ double inv_logmean(double x, double y) {
   double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
   if (f2 < 1.0e-4) return (210 + f2 * (70 + f2 * (42 + f2 * 30))) / ((x + y) * 105);
   return log(y / x) / (y - x);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 fast path.  GB300 issues FP64 at 1/62 of its FP32 rate, so the
+// residual's cost is its FP64 instruction count.  The functions below compute
+// the reference's quantities with fewer FP64 instructions: one correctly
+// rounded reciprocal shared by the logarithmic mean's series branch, the
+// two-point flux contracted with its metric vector before the flux tensor is
+// formed, and logarithms/exponentials instead of pow.  They agree with the
+// reference's formulas to a few ulps (checked on the host in
+// tests/test_device_math.py and against the oracle on the GPU).
+// ---------------------------------------------------------------------------
+#define SSE_HD __host__ __device__ __forceinline__
+
+SSE_HD double sse_rcp(double s) {
+#ifdef __CUDA_ARCH__
+  return __drcp_rn(s);
+#else
+  return 1.0 / s;
+#endif
+}
+
+// 1/q(z) for q(z) = 1 + z/3 + z^2/5 + z^3/7 by its power series; for
+// z < 1e-4 the first omitted term is below 1e-17 relative.
+constexpr double kInvQ1 = -1.0 / 3.0;
+constexpr double kInvQ2 = -4.0 / 45.0;
+constexpr double kInvQ3 = -44.0 / 945.0;
+
+// logmean(x, y) of ConservationLaws.jl:132-145: (x + y) / (2 q(f^2)) with
+// f = (x - y)/(x + y) on the series branch, (y - x)/log(y/x) otherwise.
+SSE_HD double logmean_fast(double x, double y) {
+  const double s = x + y;
+  const double f = (x - y) * sse_rcp(s);
+  const double z = f * f;
+  if (z < 1.0e-4) return 0.5 * s * fma(z, fma(z, fma(z, kInvQ3, kInvQ2), kInvQ1), 1.0);
+  return (y - x) / log(y / x);
+}
+
+// inv_logmean(x, y) of ConservationLaws.jl:147-156: 2 q(f^2) / (x + y).
+SSE_HD double inv_logmean_fast(double x, double y) {
+  const double s = x + y;
+  const double r = sse_rcp(s);
+  const double f = (x - y) * r;
+  const double z = f * f;
+  if (z < 1.0e-4) return 2.0 * r * fma(z, fma(z, fma(z, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+  return log(y / x) / (y - x);
+}
+
+// Per-node primitives in the layout [rho, p, beta = rho/p, V_1..V_D].
+template <int D>
+SSE_HD void euler_prim_fast(double gm1, const double *u, double *P) {
+  const double rr = sse_rcp(u[0]);
+  double s = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    P[3 + m] = u[m + 1] * rr;
+    s = fma(P[3 + m], P[3 + m], s);
+  }
+  const double p = gm1 * (u[D + 1] - 0.5 * u[0] * s);
+  P[0] = u[0];
+  P[1] = p;
+  P[2] = u[0] * sse_rcp(p);
+}
+
+// out[e] = sum_n G[n] F_ec(i, j)[e][n] for Ranocha's flux tensor
+// (euler_navierstokes.jl:171-195) without forming the tensor:
+//   out[0]     = rho_hat (Vbar . G)
+//   out[1 + m] = rho_hat Vbar_m (Vbar . G) + pbar G_m
+//   out[D + 1] = C rho_hat (Vbar . G) + (p_i (G . V_j) + p_j (G . V_i)) / 2
+template <int D>
+SSE_HD void ec_flux_dot(double igm1, const double *Pi, const double *Pj, const double *G,
+                        double *out) {
+  const double rho_hat = logmean_fast(Pi[0], Pj[0]);
+  const double ilm = inv_logmean_fast(Pi[2], Pj[2]);
+  double vs[D];
+  double vv = 0.0, gvs = 0.0, gvi = 0.0, gvj = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    vs[m] = Pi[3 + m] + Pj[3 + m];
+    vv = fma(Pi[3 + m], Pj[3 + m], vv);
+    gvs = fma(G[m], vs[m], gvs);
+    gvi = fma(G[m], Pi[3 + m], gvi);
+    gvj = fma(G[m], Pj[3 + m], gvj);
+  }
+  const double f0 = 0.5 * rho_hat * gvs;
+  const double pbar = 0.5 * (Pi[1] + Pj[1]);
+  const double C = fma(igm1, ilm, 0.5 * vv);
+  const double t = 0.5 * f0;
+  out[0] = f0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) out[1 + m] = fma(t, vs[m], pbar * G[m]);
+  out[D + 1] = fma(C, f0, 0.5 * fma(Pi[1], gvj, Pj[1] * gvi));
+}
+
+// conservative_to_entropy! (euler_navierstokes.jl:100-113) with
+// log(p / rho^gamma) = log(p) - gamma log(rho).
+template <int D>
+SSE_HD void cons_to_entropy_fast(double gamma, double gm1, double igm1, const double *u, double *w) {
+  double s = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) s = fma(u[m + 1], u[m + 1], s);
+  const double k = 0.5 * s * sse_rcp(u[0]);
+  const double p = gm1 * (u[D + 1] - k);
+  const double ip = sse_rcp(p);
+  w[0] = fma(igm1, gamma - (log(p) - gamma * log(u[0])), -k * ip);
+#pragma unroll
+  for (int m = 0; m < D; ++m) w[m + 1] = u[m + 1] * ip;
+  w[D + 1] = -u[0] * ip;
+}
+
+// entropy_to_conservative! (euler_navierstokes.jl:115-131) with
+// (gm1/(-w_E)^gamma)^(1/gm1) exp(-s/gm1) = exp((log gm1 - gamma log(-w_E) - s)/gm1).
+template <int D>
+SSE_HD void entropy_to_cons_fast(double gamma, double gm1, double igm1, double log_gm1,
+                                 const double *w_in, double *u) {
+  double w[D + 2];
+#pragma unroll
+  for (int e = 0; e < D + 2; ++e) w[e] = w_in[e] * gm1;
+  double s = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) s = fma(w[m + 1], w[m + 1], s);
+  const double k = 0.5 * s * sse_rcp(w[D + 1]);
+  const double sv = gamma - w[0] + k;
+  const double rhoe = exp(igm1 * (log_gm1 - gamma * log(-w[D + 1]) - sv));
+  u[0] = -w[D + 1] * rhoe;
+#pragma unroll
+  for (int m = 0; m < D; ++m) u[m + 1] = w[m + 1] * rhoe;
+  u[D + 1] = rhoe * (1 - k);
 }
 
 // Primitive quantities of one Euler state, computed once per node so that

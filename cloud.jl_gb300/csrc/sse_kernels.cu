@@ -207,10 +207,10 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
 #pragma unroll
         for (int e = 0; e < NC; ++e) ui[e] = Y[e * nq + i];
         if (!(ui[0] > 0.0)) ka.flag_nonphysical();
-        cons_to_entropy<D>(ph, ui, wi);
+        cons_to_entropy_fast<D>(ph.gamma, ph.gm1, ph.igm1, ui, wi);
         double s = op.has_vdm ? WJ[i] : 1.0;
 #pragma unroll
-        for (int e = 0; e < NC; ++e) X[e * (op.has_vdm ? nq : nq) + i] = wi[e] * s;
+        for (int e = 0; e < NC; ++e) X[e * nq + i] = wi[e] * s;
       }
       __syncthreads();
       if (op.has_vdm) {
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
           double wi[NC], ui[NC];
 #pragma unroll
           for (int e = 0; e < NC; ++e) wi[e] = X[e * nq + i];
-          entropy_to_cons<D>(ph, wi, ui);
+          entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui);
 #pragma unroll
           for (int e = 0; e < NC; ++e) {
             if (live) uq_out[e * nq + i] = ui[e];
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
         double wi[NC], ui[NC];
 #pragma unroll
         for (int e = 0; e < NC; ++e) wi[e] = F[e * nf + j];
-        entropy_to_cons<D>(ph, wi, ui);
+        entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui);
 #pragma unroll
         for (int e = 0; e < NC; ++e) {
           if (live) uf_out[e * nf + j] = ui[e];
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
 // ---------------------------------------------------------------------------
 template <int D, int NC>
 __device__ void facet_flux(const KernelArgs &ka, int kk, const double *uf, double *ff, int ec,
-                           int lane, int tpe) {
+                           int lane, int tpe, const double *prim_f) {
   const DevOps &op = ka.op;
   const Physics &ph = ka.ph;
   const int nf = op.nf;
@@ -283,6 +283,31 @@ __device__ void facet_flux(const KernelArgs &ka, int kk, const double *uf, doubl
     }
 #pragma unroll
     for (int m = 0; m < D; ++m) n[m] = ka.geo.n_f[m + D * (j + (size_t)nf * kk)];
+    if constexpr (NC > 1) {
+      if (ec && prim_f) {
+        // entropy-conservative flux . n from per-node primitives, plus LF
+        const double *Pi = prim_f + (size_t)j * (3 + D);
+        double Po[3 + D], out[NC];
+        euler_prim_fast<D>(ph.gm1, uo, Po);
+        ec_flux_dot<D>(ph.igm1, Pi, Po, n, out);
+        double a = 0.0;
+        if (ph.nflux == 0) {
+          double vni = 0.0, vno = 0.0;
+#pragma unroll
+          for (int m = 0; m < D; ++m) { vni = fma(Pi[3 + m], n[m], vni); vno = fma(Po[3 + m], n[m], vno); }
+          double ci = sqrt(ph.gamma * Pi[1] * sse_rcp(Pi[0]));
+          double co = sqrt(ph.gamma * Po[1] * sse_rcp(Po[0]));
+          a = ph.half_lambda * (fmax(fabs(vni), fabs(vno)) + fmax(ci, co));
+        }
+        double bjf = ka.geo.BJf[(size_t)kk * nf + j];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) {
+          double fs = (ph.nflux == 0) ? fma(a, ui[e] - uo[e], out[e]) : out[e];
+          ff[e * nf + j] = fs * bjf;
+        }
+        continue;
+      }
+    }
     Physics ph2 = ph;
     ph2.ec = ec;
     two_point<D, NC>(ph2, ui, uo, F);
@@ -341,33 +366,43 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
         double u[NC];
 #pragma unroll
         for (int e = 0; e < NC; ++e) u[e] = (i < nq) ? uq[e * nq + i] : uf[e * nf + (i - nq)];
-        Prim<D> q = euler_prim<D>(ph, u);
-        double *pp = prim + (size_t)i * PS;
-        pp[0] = q.rho; pp[1] = q.p; pp[2] = q.beta;
-#pragma unroll
-        for (int m = 0; m < D; ++m) pp[3 + m] = q.V[m];
+        euler_prim_fast<D>(ph.gm1, u, prim + (size_t)i * PS);
       }
+      __syncthreads();
     }
   }
-  facet_flux<D, NC>(ka, kk, uf, ff, ec, lane, tpe);
-  __syncthreads();
+  facet_flux<D, NC>(ka, kk, uf, ff, ec, lane, tpe, (NC > 1 && ec) ? prim + (size_t)nq * PS : nullptr);
 
   // volume flux differencing, pass 1: per-pair contributions
-  // (flux_difference!, flux_differencing_form.jl:37-75, one flux per unique pair)
+  // (flux_difference!, flux_differencing_form.jl:37-75, one flux per unique
+  // pair).  For the EC flux the metric vector G[n] = sum_m S_m (Lambda_i +
+  // Lambda_j)[m, n] is formed first and contracted inside the flux.
   for (int pidx = lane; pidx < op.nvp; pidx += tpe) {
     int ij = op.vp_ij[pidx];
     int i = ij & 0xffff, j = ij >> 16;
-    double F[NC][D];
     if constexpr (NC > 1) {
       if (ec) {
-        Prim<D> Lp, Rp;
-        const double *pi_ = prim + (size_t)i * PS, *pj = prim + (size_t)j * PS;
-        Lp.rho = pi_[0]; Lp.p = pi_[1]; Lp.beta = pi_[2];
-        Rp.rho = pj[0]; Rp.p = pj[1]; Rp.beta = pj[2];
+        double G[D];
 #pragma unroll
-        for (int m = 0; m < D; ++m) { Lp.V[m] = pi_[3 + m]; Rp.V[m] = pj[3 + m]; }
-        ec_flux<D>(ph, Lp, Rp, F);
-      } else {
+        for (int n = 0; n < D; ++n) G[n] = 0.0;
+#pragma unroll
+        for (int m = 0; m < D; ++m) {
+          const double Sm = op.vp_S[pidx * D + m];
+          if (Sm == 0.0) continue;
+#pragma unroll
+          for (int n = 0; n < D; ++n)
+            G[n] = fma(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
+        }
+        double out[NC];
+        ec_flux_dot<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, out);
+#pragma unroll
+        for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+        continue;
+      }
+    }
+    double F[NC][D];
+    if constexpr (NC > 1) {
+      {
         double ui[NC], uj[NC];
 #pragma unroll
         for (int e = 0; e < NC; ++e) { ui[e] = uq[e * nq + i]; uj[e] = uq[e * nq + j]; }
@@ -423,17 +458,21 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
       int ij = op.fp_ij[pidx];
       int i = ij & 0xffff, j = ij >> 16;
       int f = j / npf;
-      double F[NC][D];
       if constexpr (NC > 1) {
         if (ec) {
-          Prim<D> Lp, Rp;
-          const double *pi_ = prim + (size_t)i * PS, *pj = prim + (size_t)(nq + j) * PS;
-          Lp.rho = pi_[0]; Lp.p = pi_[1]; Lp.beta = pi_[2];
-          Rp.rho = pj[0]; Rp.p = pj[1]; Rp.beta = pj[2];
+          const double Cij = op.fp_C[pidx];
+          double G[D], out[NC];
 #pragma unroll
-          for (int m = 0; m < D; ++m) { Lp.V[m] = pi_[3 + m]; Rp.V[m] = pj[3 + m]; }
-          ec_flux<D>(ph, Lp, Rp, F);
-        } else {
+          for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+          ec_flux_dot<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, out);
+#pragma unroll
+          for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+          continue;
+        }
+      }
+      double F[NC][D];
+      if constexpr (NC > 1) {
+        {
           double ui[NC], uj[NC];
 #pragma unroll
           for (int e = 0; e < NC; ++e) { ui[e] = uq[e * nq + i]; uj[e] = uf[e * nf + j]; }

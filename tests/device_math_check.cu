@@ -1,0 +1,125 @@
+// Host-side check of the FP64 fast-path math in sse_device.cuh against the
+// reference's formulas (ConservationLaws.jl:132-156,
+// euler_navierstokes.jl:100-131, 171-195), on seeded random states.
+// Built and run by tests/test_device_math.py with nvcc; needs no GPU.
+#include <cmath>
+#include <cstdio>
+#include <random>
+
+#include "../cloud.jl_gb300/csrc/sse_device.cuh"
+
+using namespace sse;
+
+static double ref_logmean(double x, double y) {
+  double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+  if (f2 < 1.0e-4) return (x + y) * 105 / (210 + f2 * (70 + f2 * (42 + f2 * 30)));
+  return (y - x) / std::log(y / x);
+}
+static double ref_inv_logmean(double x, double y) {
+  double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+  if (f2 < 1.0e-4) return (210 + f2 * (70 + f2 * (42 + f2 * 30))) / ((x + y) * 105);
+  return std::log(y / x) / (y - x);
+}
+
+template <int D>
+static void ref_ec_tensor(double g, const double *uL, const double *uR, double F[D + 2][D]) {
+  const double gm1 = g - 1, igm1 = 1 / (g - 1);
+  double VL[D], VR[D], sL = 0, sR = 0, vv = 0;
+  for (int m = 0; m < D; ++m) { VL[m] = uL[m + 1] / uL[0]; VR[m] = uR[m + 1] / uR[0]; }
+  for (int m = 0; m < D; ++m) { sL += VL[m] * VL[m]; sR += VR[m] * VR[m]; vv += VL[m] * VR[m]; }
+  double pL = gm1 * (uL[D + 1] - 0.5 * uL[0] * sL), pR = gm1 * (uR[D + 1] - 0.5 * uR[0] * sR);
+  double rho = ref_logmean(uL[0], uR[0]), pavg = 0.5 * (pL + pR);
+  double C = 0.5 * vv + igm1 * ref_inv_logmean(uL[0] / pL, uR[0] / pR);
+  for (int n = 0; n < D; ++n) {
+    double va = 0.5 * (VL[n] + VR[n]);
+    F[0][n] = rho * va;
+    for (int m = 0; m < D; ++m) F[m + 1][n] = rho * 0.5 * (VL[m] + VR[m]) * va + (m == n ? pavg : 0);
+    F[D + 1][n] = rho * va * C + 0.5 * (pL * VR[n] + pR * VL[n]);
+  }
+}
+
+template <int D>
+static void ref_c2e(double g, const double *u, double *w) {
+  double s = 0;
+  for (int m = 0; m < D; ++m) s += u[m + 1] * u[m + 1];
+  double k = (0.5 / u[0]) * s, p = (g - 1) * (u[D + 1] - k), ip = 1 / p;
+  w[0] = (g - std::log(p / std::pow(u[0], g))) / (g - 1) - k * ip;
+  for (int m = 0; m < D; ++m) w[m + 1] = u[m + 1] * ip;
+  w[D + 1] = -u[0] * ip;
+}
+
+template <int D>
+static void ref_e2c(double g, const double *wi, double *u) {
+  double w[D + 2], s = 0;
+  for (int e = 0; e < D + 2; ++e) w[e] = wi[e] * (g - 1);
+  for (int m = 0; m < D; ++m) s += w[m + 1] * w[m + 1];
+  double k = s / (2 * w[D + 1]), sv = g - w[0] + k;
+  double rhoe = std::pow((g - 1) / std::pow(-w[D + 1], g), 1 / (g - 1)) * std::exp(-sv / (g - 1));
+  u[0] = -w[D + 1] * rhoe;
+  for (int m = 0; m < D; ++m) u[m + 1] = w[m + 1] * rhoe;
+  u[D + 1] = rhoe * (1 - k);
+}
+
+template <int D>
+static void random_state(std::mt19937_64 &rng, double g, double pscale, double *u) {
+  std::uniform_real_distribution<double> U(-1, 1);
+  double rho = 1.0 + 0.3 * U(rng), p = pscale * (1.0 + 0.3 * U(rng)), ke = 0;
+  u[0] = rho;
+  for (int m = 0; m < D; ++m) { double v = U(rng); u[m + 1] = rho * v; ke += 0.5 * rho * v * v; }
+  u[D + 1] = p / (g - 1) + ke;
+}
+
+static double rel(double a, double b) { return std::fabs(a - b) / std::fmax(std::fabs(b), 1e-300); }
+
+template <int D>
+static void check(std::mt19937_64 &rng, double *worst) {
+  const double g = 1.4;
+  std::uniform_real_distribution<double> U(-1, 1);
+  for (int trial = 0; trial < 20000; ++trial) {
+    double pscale = (trial % 2) ? 71.4 : 1.0;
+    double uL[D + 2], uR[D + 2];
+    random_state<D>(rng, g, pscale, uL);
+    // near pairs (series branch) and far pairs (log branch)
+    if (trial % 3) {
+      for (int e = 0; e < D + 2; ++e) uR[e] = uL[e] * (1.0 + 1e-3 * U(rng));
+    } else {
+      random_state<D>(rng, g, pscale, uR);
+    }
+    double x = uL[0], y = uR[0];
+    worst[0] = std::fmax(worst[0], rel(logmean_fast(x, y), ref_logmean(x, y)));
+    worst[1] = std::fmax(worst[1], rel(inv_logmean_fast(x, y), ref_inv_logmean(x, y)));
+    double PL[3 + D], PR[3 + D], G[D];
+    euler_prim_fast<D>(g - 1, uL, PL);
+    euler_prim_fast<D>(g - 1, uR, PR);
+    for (int m = 0; m < D; ++m) G[m] = U(rng);
+    double out[D + 2], F[D + 2][D];
+    ec_flux_dot<D>(1 / (g - 1), PL, PR, G, out);
+    ref_ec_tensor<D>(g, uL, uR, F);
+    double scale = 0;
+    for (int e = 0; e < D + 2; ++e)
+      for (int n = 0; n < D; ++n) scale = std::fmax(scale, std::fabs(F[e][n]));
+    for (int e = 0; e < D + 2; ++e) {
+      double want = 0;
+      for (int n = 0; n < D; ++n) want += G[n] * F[e][n];
+      worst[2] = std::fmax(worst[2], std::fabs(out[e] - want) / scale);
+    }
+    double w1[D + 2], w2[D + 2], u1[D + 2], u2[D + 2];
+    cons_to_entropy_fast<D>(g, g - 1, 1 / (g - 1), uL, w1);
+    ref_c2e<D>(g, uL, w2);
+    for (int e = 0; e < D + 2; ++e) worst[3] = std::fmax(worst[3], rel(w1[e], w2[e]));
+    entropy_to_cons_fast<D>(g, g - 1, 1 / (g - 1), std::log(g - 1), w2, u1);
+    ref_e2c<D>(g, w2, u2);
+    for (int e = 0; e < D + 2; ++e) worst[4] = std::fmax(worst[4], std::fabs(u1[e] - u2[e]) / std::fabs(u2[D + 1]));
+  }
+}
+
+int main() {
+  std::mt19937_64 rng(20261203);
+  double worst[5] = {0, 0, 0, 0, 0};
+  check<2>(rng, worst);
+  check<3>(rng, worst);
+  std::printf("{\"logmean\": %.3e, \"inv_logmean\": %.3e, \"ec_flux_dot\": %.3e, "
+              "\"cons_to_entropy\": %.3e, \"entropy_to_cons\": %.3e}\n",
+              worst[0], worst[1], worst[2], worst[3], worst[4]);
+  return 0;
+}

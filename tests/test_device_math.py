@@ -1,0 +1,38 @@
+"""The FP64 fast-path device math (logmean with a shared reciprocal, the
+two-point flux contracted with its metric vector, log/exp entropy maps)
+against the reference's formulas, compiled by nvcc as host code (no GPU)."""
+import json
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def results(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.fail("nvcc is required")
+    exe = str(tmp_path_factory.mktemp("devmath") / "device_math_check")
+    subprocess.run([nvcc, "-std=c++17", "-O2", os.path.join(HERE, "device_math_check.cu"), "-o", exe],
+                   check=True, capture_output=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    return json.loads(out)
+
+
+def test_logmeans(results):
+    assert results["logmean"] < 5e-15
+    assert results["inv_logmean"] < 5e-15
+
+
+def test_contracted_ec_flux(results):
+    # relative to the largest flux-tensor entry; the contraction sums D terms
+    assert results["ec_flux_dot"] < 2e-14
+
+
+def test_entropy_variable_maps(results):
+    assert results["cons_to_entropy"] < 5e-14
+    assert results["entropy_to_cons"] < 5e-14
