@@ -221,6 +221,50 @@ def main():
                 "whole_stage_frac": (work.flops * ne) / ((phases[0] + phases[1]) * 1e-3) / 1e12 / fp64_peak,
                 "fp32_peak_tflops": fp32_peak}
 
+    # ---- mixed FP32/FP64 form on the same handle: same steps from the same
+    # initial state, error against the FP64 trajectory at equal step count
+    abi = pkg.abi
+    mixed = None
+    try:
+        gpu.set_precision(abi.SSE_MIXED)
+        um = torch.from_numpy(pb.u0).cuda()
+        torch.cuda.synchronize()
+        for _ in range(args.warmup):
+            gpu.rk_steps(um, 1, dt)
+        torch.cuda.synchronize()
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        for _ in range(args.steps):
+            gpu.rk_steps(um, 1, dt)
+        m1.record(stream)
+        torch.cuda.synchronize()
+        mms = m0.elapsed_time(m1)
+        mphases = gpu.phase_timings(um, 5)
+        u0d = torch.from_numpy(pb.u0).cuda()
+        torch.cuda.synchronize()
+        r_mixed = gpu.residual(u0d).cpu().numpy()
+        gpu.set_precision(abi.SSE_FP64)
+        r_fp64 = gpu.residual(u0d).cpu().numpy()
+        state_err = float(torch.linalg.norm(um - u) / torch.linalg.norm(u))
+        res_err = float(np.linalg.norm(r_mixed - r_fp64) / np.linalg.norm(r_fp64))
+        cons = gpu.conservation_residual(u0d, torch.from_numpy(r_mixed).cuda())
+        mvalue = world * host.dof * 5 * args.steps / (mms * 1e-3)
+        mixed = {"value": mvalue, "unit": UNIT, "ms_per_step": mms / args.steps,
+                 "speedup_vs_fp64": mvalue / value,
+                 "state_rel_err_vs_fp64": state_err,
+                 "state_err_after_steps": args.warmup + args.steps,
+                 "residual_rel_err_vs_fp64": res_err,
+                 "conservation_residual_fp64_reduction": [float(x) for x in cons[: host.N_c]],
+                 "entropy_production_fp64_reduction": float(cons[host.N_c]),
+                 "phase_ms": {"nodal_values_fp64": mphases[0], "time_derivative_fp32": mphases[1],
+                              "rk_stage_update_compensated": mphases[2]},
+                 "precision": "entropy projection FP64; fluxes, flux differencing, facet correction, "
+                              "lifting and mass solve FP32 on perturbations from a constant reference "
+                              "state; FP64 compensated stage accumulation and reductions"}
+    except pkg.SSEError as ex:
+        mixed = {"unavailable": str(ex)}
+        gpu.set_precision(abi.SSE_FP64)
+
     # ---- end to end through the C-ABI with host (pinned) buffers
     u_host = torch.from_numpy(pb.u0.copy()).pin_memory()
     gpu.rk_steps(u_host, 1, dt)
@@ -240,7 +284,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": dict(WORKLOAD, dof=host.dof, form_precision="FP64 (drop-in form)",
                            parallelism="replicas only" if world > 1 else "1 GPU"),
-            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline}
+            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+            "mixed": mixed}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pb, host, args.cpu_budget)
     if rank == 0:

@@ -60,6 +60,12 @@ struct sse_solver {
   int *d_flag = nullptr;
   int precision = SSE_FP64;
   std::string last_error;
+  // element counts of the device operator arrays (for the FP32 roundings)
+  size_t nA = 0, nB = 0, nC = 0, nnzR = 0, nvpS = 0, nfpC = 0;
+  double volume = 0.0;      // sum of W .* J_q over the mesh
+  bool mixed_ready = false; // FP32 copies allocated
+  bool ref_ready = false;   // reference state of the mixed form chosen
+  double *d_comp = nullptr; // compensation of the mixed form's stage accumulation
 };
 
 namespace {
@@ -273,7 +279,12 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
     if ((e = upload(s, b12.data(), b12.size(), &op.b12)) != cudaSuccess) return cuda_fail(s, e, "upload");
     if ((e = upload(s, b12_index.data(), b12_index.size(), &op.b12_index)) != cudaSuccess)
       return cuda_fail(s, e, "upload");
+    s->nA = (size_t)M1 * p1;
+    s->nB = (size_t)M2 * p1 * p1;
+    s->nC = c.d == 3 ? (size_t)M3 * p1 * p1 * p1 : 0;
   }
+  s->nnzR = (size_t)(ops->R.colptr[ops->R.n] - 1);
+  for (size_t t = 0; t < (size_t)c.n_q * c.n_e; ++t) s->volume += geo->WJ[t];
 
   // ---- R, R^T, D, D^T
   int rc;
@@ -325,6 +336,7 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
       inc_ptr[i + 1] = (int)inc_flat.size();
     }
     op.nvp = nvp;
+    s->nvpS = (size_t)nvp * c.d;
     if ((e = upload(s, vp_ij.data(), vp_ij.size(), &op.vp_ij)) != cudaSuccess) return cuda_fail(s, e, "upload");
     if ((e = upload(s, vp_S.data(), vp_S.size(), &op.vp_S)) != cudaSuccess) return cuda_fail(s, e, "upload");
     if ((e = upload(s, inc_ptr.data(), inc_ptr.size(), &op.vp_inc_ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");
@@ -349,6 +361,7 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
       for (int i = 0; i < c.n_q; ++i) { qflat.insert(qflat.end(), qinc[i].begin(), qinc[i].end()); qptr[i + 1] = (int)qflat.size(); }
       for (int j = 0; j < c.n_f; ++j) { fflat.insert(fflat.end(), finc[j].begin(), finc[j].end()); fptr[j + 1] = (int)fflat.size(); }
       op.nfp = (int)fp_ij.size();
+      s->nfpC = fp_C.size();
       if ((e = upload(s, fp_ij.data(), fp_ij.size(), &op.fp_ij)) != cudaSuccess) return cuda_fail(s, e, "upload");
       if ((e = upload(s, fp_C.data(), fp_C.size(), &op.fp_C)) != cudaSuccess) return cuda_fail(s, e, "upload");
       if ((e = upload(s, qptr.data(), qptr.size(), &op.fp_q_ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");
@@ -457,11 +470,107 @@ int check_flag(sse_solver *s) {
   return SSE_OK;
 }
 
-// one residual evaluation on device buffers (no synchronisation)
+// Mixed form: FP32 roundings of the metric terms and operator values, FP32
+// perturbation scratch, FP64 compensation buffer.  Allocated once.
+int enable_mixed(sse_solver *s) {
+  const sse_config &c = s->cfg;
+  if (!(c.form == SSE_FLUX_DIFFERENCING_FORM && c.law == SSE_EULER && c.two_point_flux == SSE_EC_FLUX))
+    return fail(s, SSE_ERR_UNSUPPORTED,
+                "SSE_MIXED covers FluxDifferencingForm with the entropy-conservative flux (Euler)");
+  if (s->mixed_ready) return SSE_OK;
+  KernelArgs &ka = s->ka;
+  DevOps &op = ka.op;
+  DevGeo &g = ka.geo;
+  cudaError_t e;
+  void *p;
+  auto rounded = [&](const double *src, size_t n, const float **dst) -> cudaError_t {
+    *dst = nullptr;
+    if (!src || n == 0) return cudaSuccess;
+    void *q = nullptr;
+    cudaError_t err = alloc(s, n * sizeof(float), &q);
+    if (err != cudaSuccess) return err;
+    *dst = (const float *)q;
+    return launch_round_to_float(src, (float *)q, n, s->stream);
+  };
+  const size_t nq = c.n_q, nf = c.n_f, ne = c.n_e, d = c.d;
+  if ((e = rounded(op.A, s->nA, &op.Af)) || (e = rounded(op.B, s->nB, &op.Bf)) ||
+      (e = rounded(op.C, s->nC, &op.Cf)) || (e = rounded(op.R_val, s->nnzR, &op.R_valf)) ||
+      (e = rounded(op.Rt_val, s->nnzR, &op.Rt_valf)) || (e = rounded(op.vp_S, s->nvpS, &op.vp_Sf)) ||
+      (e = rounded(op.fp_C, s->nfpC, &op.fp_Cf)))
+    return cuda_fail(s, e, "mixed operators");
+  if ((e = rounded(g.BJf, nf * ne, &g.BJff)) || (e = rounded(g.n_f, d * nf * ne, &g.n_ff)) ||
+      (e = rounded(g.Lambda_q, nq * d * d * ne, &g.Lambda_qf)) ||
+      (e = rounded(g.halfnJf, d * nf * ne, &g.halfnJff)) ||
+      (e = rounded(g.halfnJq, d * c.num_faces * nq * ne, &g.halfnJqf)) ||
+      (e = rounded(g.JinvW, g.JinvW ? nq * ne : 0, &g.JinvWf)) ||
+      (e = rounded(g.WJinv, g.WJinv ? nq * ne : 0, &g.WJinvf)))
+    return cuda_fail(s, e, "mixed metric terms");
+  if ((e = alloc(s, nq * c.n_c * ne * sizeof(float), &p))) return cuda_fail(s, e, "alloc");
+  ka.u_qf = (float *)p;
+  if ((e = alloc(s, nf * c.n_c * ne * sizeof(float), &p))) return cuda_fail(s, e, "alloc");
+  ka.u_ff = (float *)p;
+  if ((e = alloc(s, (size_t)c.n_p * c.n_c * ne * sizeof(double), &p))) return cuda_fail(s, e, "alloc");
+  s->d_comp = (double *)p;
+  // phase-B layout in floats (primitives carry p - p_ref as well)
+  const int nc = c.n_c, np = c.n_p;
+  int zsz = 0, wsz = 0;
+  if (op.has_vdm) {
+    if (c.d == 2) zsz = nc * op.p1 * op.M2;
+    else { zsz = nc * op.nb12 * op.M3; wsz = nc * op.p1 * op.M2 * op.M3; }
+  }
+  const int sizes[10] = {nc * (int)nq, nc * (int)nf, nc * (int)nf, nc * (int)nq,
+                         std::max({op.nvp * nc, op.nfp * nc, nc * (np + (int)nq)}), (int)(d * d * nq),
+                         op.nfp > 0 ? (int)(d * c.num_faces * nq) : 0, (int)((nq + nf) * (4 + d)), zsz, wsz};
+  int off = 0, i = 0;
+  for (int sz : sizes) { ka.layBm.off[i++] = off; off += (sz + 3) & ~3; }
+  for (; i < 12; ++i) ka.layBm.off[i] = off;
+  ka.layBm.team_doubles = off;  // counted in floats for this layout
+  size_t smm = (size_t)ka.epb * off * sizeof(float);
+  if (smm > 220 * 1024) return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed kernel");
+  if ((e = sse_set_smem_limit_mixed(ka, smm))) return cuda_fail(s, e, "cudaFuncSetAttribute");
+  if ((e = cudaStreamSynchronize(s->stream))) return cuda_fail(s, e, "sync");
+  s->mixed_ready = true;
+  return SSE_OK;
+}
+
+// Choose the mixed form's reference state from the first state it sees:
+// volume means of density and total energy, zero momentum.  Any constant
+// state gives the same residual in exact arithmetic; a close one keeps the
+// FP32 perturbations small.
+int ensure_reference(sse_solver *s, const double *u_dev) {
+  if (s->ref_ready) return SSE_OK;
+  const sse_config &c = s->cfg;
+  cudaError_t e = launch_conservation(s->ka, u_dev, u_dev, s->d_partial, s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "reference state");
+  std::vector<double> part((size_t)c.n_e * (c.n_c + 1));
+  if ((e = cudaMemcpyAsync(part.data(), s->d_partial, part.size() * 8, cudaMemcpyDeviceToHost, s->stream)) ||
+      (e = cudaStreamSynchronize(s->stream)))
+    return cuda_fail(s, e, "reference state");
+  double rho = 0.0, E = 0.0;
+  for (int k = 0; k < c.n_e; ++k) {
+    rho += part[(size_t)k * (c.n_c + 1)];
+    E += part[(size_t)k * (c.n_c + 1) + c.n_c - 1];
+  }
+  Physics &ph = s->ka.ph;
+  ph.rho_ref = rho / s->volume;
+  ph.E_ref = E / s->volume;
+  ph.p_ref = ph.gm1 * ph.E_ref;
+  if (!(ph.rho_ref > 0.0) || !(ph.p_ref > 0.0))
+    return fail(s, SSE_ERR_NONPHYSICAL, "mixed form: mean density or energy not positive");
+  s->ref_ready = true;
+  return SSE_OK;
+}
+
+// one residual evaluation on device buffers (no synchronisation in the FP64
+// form; the mixed form synchronises once, on its first call)
 cudaError_t residual_device(sse_solver *s, const double *u, double *dudt) {
   KernelArgs ka = s->ka;
   ka.u = u;
   ka.dudt = dudt;
+  if (ka.mixed && !s->ref_ready) {
+    if (ensure_reference(s, u) != SSE_OK) return cudaErrorInvalidValue;
+    ka.ph = s->ka.ph;
+  }
   cudaError_t e = launch_nodal_values(ka, s->stream);
   if (e != cudaSuccess) return e;
   return launch_time_derivative(ka, s->stream);
@@ -560,7 +669,15 @@ int32_t sse_set_stream(sse_solver *s, void *stream) {
 
 int32_t sse_set_precision(sse_solver *s, int32_t precision) {
   if (!s) return SSE_ERR_INVALID_ARGUMENT;
-  if (precision != SSE_FP64) return fail(s, SSE_ERR_UNSUPPORTED, "only SSE_FP64 is available in this build");
+  if (precision == SSE_FP64) {
+    s->ka.mixed = 0;
+  } else if (precision == SSE_MIXED) {
+    int rc = enable_mixed(s);
+    if (rc != SSE_OK) return rc;
+    s->ka.mixed = 1;
+  } else {
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "precision must be SSE_FP64 or SSE_MIXED");
+  }
   s->precision = precision;
   return SSE_OK;
 }
@@ -597,6 +714,7 @@ int32_t sse_residual_static_scratch(sse_solver *s, const double *u_dev, double *
   int rc = static_scratch_address(s, &scratch);
   if (rc != SSE_OK) return rc;
   KernelArgs ka = s->ka;
+  ka.mixed = 0;           // FP64 form
   ka.u = u_dev;
   ka.dudt = dudt_dev;
   ka.u_q = scratch;       // fully written by phase A before phase B reads it:
@@ -621,6 +739,7 @@ int32_t sse_nodal_values(sse_solver *s, const double *u, double *u_q, double *u_
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
   }
   KernelArgs ka = s->ka;
+  ka.mixed = 0;  // FP64 nodal values in the reference's layouts
   ka.u = du;
   if ((e = launch_nodal_values(ka, s->stream))) return cuda_fail(s, e, "nodal values");
   if (!s->d_uf_ref) {
@@ -655,12 +774,16 @@ int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt, int32
     if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_acc = (double *)p;
     if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_ust = (double *)p;
   }
+  const bool mixed = s->ka.mixed;
+  if (mixed && (e = cudaMemsetAsync(s->d_comp, 0, n * 8, s->stream))) return cuda_fail(s, e, "memset");
   for (int step = 0; step < n_steps; ++step) {
     if (scheme == SSE_CARPENTER_KENNEDY_2N54) {
       for (int st = 0; st < 5; ++st) {
         if ((e = residual_device(s, du, s->d_dudt))) return cuda_fail(s, e, "residual");
-        if ((e = launch_ck_stage(du, s->d_tmp, s->d_dudt, kCKA[st], kCKB[st], dt, st == 0, n, s->stream)))
-          return cuda_fail(s, e, "stage");
+        e = mixed ? launch_ck_stage_compensated(du, s->d_comp, s->d_tmp, s->d_dudt, kCKA[st], kCKB[st],
+                                                dt, st == 0, n, s->stream)
+                  : launch_ck_stage(du, s->d_tmp, s->d_dudt, kCKA[st], kCKB[st], dt, st == 0, n, s->stream);
+        if (e) return cuda_fail(s, e, "stage");
       }
     } else {
       const double half = dt / 2;
@@ -712,6 +835,10 @@ int32_t sse_conservation_residual(sse_solver *s, const double *u, const double *
 // values), out[1] = phase B (time derivative), out[2] = one RK stage update.
 int32_t sse_phase_timings(sse_solver *s, const double *u_dev, int32_t n_iter, double *out) {
   if (!s || !u_dev || !out || n_iter <= 0) return SSE_ERR_INVALID_ARGUMENT;
+  if (s->ka.mixed) {
+    int rc = ensure_reference(s, u_dev);
+    if (rc != SSE_OK) return rc;
+  }
   KernelArgs ka = s->ka;
   ka.u = u_dev;
   ka.dudt = s->d_dudt;

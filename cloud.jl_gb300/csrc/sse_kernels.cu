@@ -19,66 +19,68 @@
 namespace sse {
 
 // ---------------------------------------------------------------------------
-// team-parallel operator applications (all NC components at once)
+// team-parallel operator applications (all NC components at once), in the
+// scalar type T of the form (double: FP64 form; float: mixed form)
 // ---------------------------------------------------------------------------
 
 // y (NC x nq) = V x (NC x np); warped_product_2d.jl:31-55 / _3d.jl:47-84
-template <int D, int NC>
-__device__ void vdm_mul(const DevOps &op, const double *x, double *y, double *Z, double *W,
-                        int lane, int tpe) {
+template <typename T, int D, int NC>
+__device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane, int tpe) {
   if (!op.has_vdm) {
     for (int t = lane; t < NC * op.nq; t += tpe) y[t] = x[t];
     __syncthreads();
     return;
   }
+  const T *A = OpVals<T>::A(op), *B = OpVals<T>::B(op);
   const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
   if constexpr (D == 2) {
     // Z[e][b1][a2] = sum_b2 B[a2,b1,b2] x[sigma(b1,b2)]
     for (int t = lane; t < NC * p1 * M2; t += tpe) {
       int a2 = t % M2, r = t / M2, b1 = r % p1, e = r / p1;
-      double acc = 0.0;
+      T acc = 0;
       for (int b2 = 0; b2 < p1 - b1; ++b2) {
         int l = modes_index2(op, b1, b2);
-        acc = fma(op.B[a2 + M2 * (b1 + p1 * b2)], x[e * op.np + l], acc);
+        acc = fma(B[a2 + M2 * (b1 + p1 * b2)], x[e * op.np + l], acc);
       }
       Z[(e * p1 + b1) * M2 + a2] = acc;
     }
     __syncthreads();
     for (int t = lane; t < NC * M1 * M2; t += tpe) {
       int a2 = t % M2, r = t / M2, a1 = r % M1, e = r / M1;
-      double acc = 0.0;
-      for (int b1 = 0; b1 < p1; ++b1) acc = fma(op.A[a1 + M1 * b1], Z[(e * p1 + b1) * M2 + a2], acc);
+      T acc = 0;
+      for (int b1 = 0; b1 < p1; ++b1) acc = fma(A[a1 + M1 * b1], Z[(e * p1 + b1) * M2 + a2], acc);
       y[e * op.nq + M2 * a1 + a2] = acc;
     }
     __syncthreads();
   } else {
+    const T *C = OpVals<T>::C(op);
     const int M3 = op.M3, nb12 = op.nb12;
     for (int t = lane; t < NC * nb12 * M3; t += tpe) {
       int a3 = t % M3, r = t / M3, q = r % nb12, e = r / nb12;
       int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
-      double acc = 0.0;
+      T acc = 0;
       for (int b3 = 0; b3 < p1 - b1 - b2; ++b3) {
         int l = modes_index3(op, b1, b2, b3);
-        acc = fma(op.C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], x[e * op.np + l], acc);
+        acc = fma(C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], x[e * op.np + l], acc);
       }
       Z[(e * nb12 + q) * M3 + a3] = acc;
     }
     __syncthreads();
     for (int t = lane; t < NC * p1 * M2 * M3; t += tpe) {
       int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, b1 = r2 % p1, e = r2 / p1;
-      double acc = 0.0;
+      T acc = 0;
       for (int b2 = 0; b2 < p1 - b1; ++b2) {
         int q = op.b12_index[b1 + p1 * b2];
-        acc = fma(op.B[a2 + M2 * (b1 + p1 * b2)], Z[(e * nb12 + q) * M3 + a3], acc);
+        acc = fma(B[a2 + M2 * (b1 + p1 * b2)], Z[(e * nb12 + q) * M3 + a3], acc);
       }
       W[((e * p1 + b1) * M2 + a2) * M3 + a3] = acc;
     }
     __syncthreads();
     for (int t = lane; t < NC * M1 * M2 * M3; t += tpe) {
       int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, a1 = r2 % M1, e = r2 / M1;
-      double acc = 0.0;
+      T acc = 0;
       for (int b1 = 0; b1 < p1; ++b1)
-        acc = fma(op.A[a1 + M1 * b1], W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc);
+        acc = fma(A[a1 + M1 * b1], W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc);
       y[e * op.nq + (M2 * a1 + a2) * M3 + a3] = acc;
     }
     __syncthreads();
@@ -86,47 +88,48 @@ __device__ void vdm_mul(const DevOps &op, const double *x, double *y, double *Z,
 }
 
 // x (NC x np) = V^T y (NC x nq); warped_product_2d.jl:61-89 / _3d.jl:94-136
-template <int D, int NC>
-__device__ void vdm_tmul(const DevOps &op, const double *y, double *x, double *Z, double *W,
-                         int lane, int tpe) {
+template <typename T, int D, int NC>
+__device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lane, int tpe) {
   if (!op.has_vdm) {
     for (int t = lane; t < NC * op.nq; t += tpe) x[t] = y[t];
     __syncthreads();
     return;
   }
+  const T *A = OpVals<T>::A(op), *B = OpVals<T>::B(op);
   const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
   if constexpr (D == 2) {
     for (int t = lane; t < NC * p1 * M2; t += tpe) {
       int a2 = t % M2, r = t / M2, b1 = r % p1, e = r / p1;
-      double acc = 0.0;
-      for (int a1 = 0; a1 < M1; ++a1) acc = fma(op.A[a1 + M1 * b1], y[e * op.nq + M2 * a1 + a2], acc);
+      T acc = 0;
+      for (int a1 = 0; a1 < M1; ++a1) acc = fma(A[a1 + M1 * b1], y[e * op.nq + M2 * a1 + a2], acc);
       Z[(e * p1 + b1) * M2 + a2] = acc;
     }
     __syncthreads();
     for (int t = lane; t < NC * op.np; t += tpe) {
       int l = t % op.np, e = t / op.np;
       int b1 = op.modes[l] & 0xff, b2 = (op.modes[l] >> 8) & 0xff;
-      double acc = 0.0;
-      for (int a2 = 0; a2 < M2; ++a2) acc = fma(op.B[a2 + M2 * (b1 + p1 * b2)], Z[(e * p1 + b1) * M2 + a2], acc);
+      T acc = 0;
+      for (int a2 = 0; a2 < M2; ++a2) acc = fma(B[a2 + M2 * (b1 + p1 * b2)], Z[(e * p1 + b1) * M2 + a2], acc);
       x[e * op.np + l] = acc;
     }
     __syncthreads();
   } else {
+    const T *C = OpVals<T>::C(op);
     const int M3 = op.M3, nb12 = op.nb12;
     for (int t = lane; t < NC * p1 * M2 * M3; t += tpe) {
       int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, b1 = r2 % p1, e = r2 / p1;
-      double acc = 0.0;
+      T acc = 0;
       for (int a1 = 0; a1 < M1; ++a1)
-        acc = fma(op.A[a1 + M1 * b1], y[e * op.nq + (M2 * a1 + a2) * M3 + a3], acc);
+        acc = fma(A[a1 + M1 * b1], y[e * op.nq + (M2 * a1 + a2) * M3 + a3], acc);
       W[((e * p1 + b1) * M2 + a2) * M3 + a3] = acc;
     }
     __syncthreads();
     for (int t = lane; t < NC * nb12 * M3; t += tpe) {
       int a3 = t % M3, r = t / M3, q = r % nb12, e = r / nb12;
       int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
-      double acc = 0.0;
+      T acc = 0;
       for (int a2 = 0; a2 < M2; ++a2)
-        acc = fma(op.B[a2 + M2 * (b1 + p1 * b2)], W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc);
+        acc = fma(B[a2 + M2 * (b1 + p1 * b2)], W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc);
       Z[(e * nb12 + q) * M3 + a3] = acc;
     }
     __syncthreads();
@@ -134,9 +137,9 @@ __device__ void vdm_tmul(const DevOps &op, const double *y, double *x, double *Z
       int l = t % op.np, e = t / op.np;
       int b1 = op.modes[l] & 0xff, b2 = (op.modes[l] >> 8) & 0xff, b3 = (op.modes[l] >> 16) & 0xff;
       int q = op.b12_index[b1 + p1 * b2];
-      double acc = 0.0;
+      T acc = 0;
       for (int a3 = 0; a3 < M3; ++a3)
-        acc = fma(op.C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], Z[(e * nb12 + q) * M3 + a3], acc);
+        acc = fma(C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], Z[(e * nb12 + q) * M3 + a3], acc);
       x[e * op.np + l] = acc;
     }
     __syncthreads();
@@ -144,12 +147,12 @@ __device__ void vdm_tmul(const DevOps &op, const double *y, double *x, double *Z
 }
 
 // y (NC x rows) = M x (NC x cols) for a CSR matrix
-template <int NC>
-__device__ void csr_mul(int rows, int cols, const int *ptr, const int *idx, const double *val,
-                        const double *x, double *y, int lane, int tpe) {
+template <typename T, int NC>
+__device__ void csr_mul(int rows, int cols, const int *ptr, const int *idx, const T *val,
+                        const T *x, T *y, int lane, int tpe) {
   for (int t = lane; t < NC * rows; t += tpe) {
     int r = t % rows, e = t / rows;
-    double acc = 0.0;
+    T acc = 0;
     for (int q = ptr[r]; q < ptr[r + 1]; ++q) acc += val[q] * x[e * cols + idx[q]];
     y[e * rows + r] = acc;
   }
@@ -157,18 +160,31 @@ __device__ void csr_mul(int rows, int cols, const int *ptr, const int *idx, cons
 
 // WeightAdjustedSolver (M^-1 = I): x <- V^T diag(JinvW) V x;
 // DiagonalSolver: x <- WJinv .* x (mass_matrix.jl:177-196)
-template <int D, int NC>
-__device__ void mass_solve(const DevOps &op, const double *JinvW, const double *WJinv, int wa,
-                           double *x, double *Y, double *Z, double *W, int lane, int tpe) {
+template <typename T, int D, int NC>
+__device__ void mass_solve(const DevOps &op, const T *JinvW, const T *WJinv, int wa, T *x, T *Y,
+                           T *Z, T *W, int lane, int tpe) {
   if (!wa) {
     for (int t = lane; t < NC * op.np; t += tpe) x[t] *= WJinv[t % op.np];
     __syncthreads();
     return;
   }
-  vdm_mul<D, NC>(op, x, Y, Z, W, lane, tpe);
+  vdm_mul<T, D, NC>(op, x, Y, Z, W, lane, tpe);
   for (int t = lane; t < NC * op.nq; t += tpe) Y[t] *= JinvW[t % op.nq];
   __syncthreads();
-  vdm_tmul<D, NC>(op, Y, x, Z, W, lane, tpe);
+  vdm_tmul<T, D, NC>(op, Y, x, Z, W, lane, tpe);
+}
+
+// Store one nodal state value: FP64 form -> the double scratch; mixed form ->
+// the float scratch as a perturbation from the reference state.
+template <int NC>
+__device__ __forceinline__ void store_state(const KernelArgs &ka, double *d, float *f, size_t idx,
+                                            int e, double v) {
+  if (ka.mixed) {
+    double ref = (e == 0) ? ka.ph.rho_ref : ((e == NC - 1) ? ka.ph.E_ref : 0.0);
+    f[idx] = (float)(v - ref);
+  } else {
+    d[idx] = v;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -193,7 +209,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
 
   for (int t = lane; t < NC * np; t += tpe) X[t] = uk[t];
   __syncthreads();
-  vdm_mul<D, NC>(op, X, Y, Z, Wb, lane, tpe);  // Y = u_q = V u
+  vdm_mul<double, D, NC>(op, X, Y, Z, Wb, lane, tpe);  // Y = u_q = V u
 
   double *uq_out = ka.u_q + (size_t)kk * NC * nq;
   double *uf_out = ka.u_f + (size_t)kk * NC * nf;
@@ -216,9 +232,9 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
       if (op.has_vdm) {
         // X holds WJ w_q (NC x nq): w = V^T (WJ w_q); mass solve; w_q = V w
         double *Wm = F;  // NC x np modal scratch (F is large enough, see layout)
-        vdm_tmul<D, NC>(op, X, Wm, Z, Wb, lane, tpe);
-        mass_solve<D, NC>(op, ka.geo.JinvW + (size_t)kk * nq, nullptr, 1, Wm, X, Z, Wb, lane, tpe);
-        vdm_mul<D, NC>(op, Wm, X, Z, Wb, lane, tpe);  // X = w_q (projected)
+        vdm_tmul<double, D, NC>(op, X, Wm, Z, Wb, lane, tpe);
+        mass_solve<double, D, NC>(op, ka.geo.JinvW + (size_t)kk * nq, nullptr, 1, Wm, X, Z, Wb, lane, tpe);
+        vdm_mul<double, D, NC>(op, Wm, X, Z, Wb, lane, tpe);  // X = w_q (projected)
         // u_q = e2c(w_q)
         for (int i = lane; i < nq; i += tpe) {
           double wi[NC], ui[NC];
@@ -227,17 +243,17 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
           entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui);
 #pragma unroll
           for (int e = 0; e < NC; ++e) {
-            if (live) uq_out[e * nq + i] = ui[e];
+            if (live) store_state<NC>(ka, ka.u_q, ka.u_qf, (size_t)kk * NC * nq + e * nq + i, e, ui[e]);
             if (!(ui[0] > 0.0) || !isfinite(ui[e])) ka.flag_nonphysical();
           }
         }
       } else {
         // nodal: u_q stays u; X = w_q
         for (int t = lane; t < NC * nq; t += tpe)
-          if (live) uq_out[t] = Y[t];
+          if (live) store_state<NC>(ka, ka.u_q, ka.u_qf, (size_t)kk * NC * nq + t, t / nq, Y[t]);
       }
       // w_f = R w_q ; u_f = e2c(w_f)
-      csr_mul<NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, X, F, lane, tpe);
+      csr_mul<double, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, X, F, lane, tpe);
       __syncthreads();
       for (int j = lane; j < nf; j += tpe) {
         double wi[NC], ui[NC];
@@ -246,7 +262,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
         entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui);
 #pragma unroll
         for (int e = 0; e < NC; ++e) {
-          if (live) uf_out[e * nf + j] = ui[e];
+          if (live) store_state<NC>(ka, ka.u_f, ka.u_ff, (size_t)kk * NC * nf + e * nf + j, e, ui[e]);
           if (!(ui[0] > 0.0) || !isfinite(ui[e])) ka.flag_nonphysical();
         }
       }
@@ -256,7 +272,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
   // no projection: u_q = V u; u_f = R u_q
   for (int t = lane; t < NC * nq; t += tpe)
     if (live) uq_out[t] = Y[t];
-  csr_mul<NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, Y, F, lane, tpe);
+  csr_mul<double, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, Y, F, lane, tpe);
   __syncthreads();
   for (int t = lane; t < NC * nf; t += tpe)
     if (live) uf_out[t] = F[t];
@@ -529,8 +545,8 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
 
   // dudt = V^T r_q ; mass solve  (scratch: diff region reused for modal / nodal buffers)
   double *Xm = diff, *Yq = diff + (size_t)NC * np;
-  vdm_tmul<D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
-  mass_solve<D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
+  vdm_tmul<double, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
+  mass_solve<double, D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
                     ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq,
                     Z, Wb, lane, tpe);
   double *out = ka.dudt + (size_t)kk * NC * np;
@@ -619,7 +635,7 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
       const double *hw = hwl + nq * (m + D * n);
       // tmp = halfWLambda .* f_n ; tmp2 = D_m f_n
       for (int t = lane; t < NC * nq; t += tpe) tmp[t] = hw[t % nq] * fn_[t];
-      csr_mul<NC>(nq, nq, op.D_ptr[m], op.D_idx[m], op.D_val[m], fn_, tmp2, lane, tpe);
+      csr_mul<double, NC>(nq, nq, op.D_ptr[m], op.D_idx[m], op.D_val[m], fn_, tmp2, lane, tpe);
       __syncthreads();
       // r_q += D_m^T tmp - halfWLambda .* tmp2
       for (int t = lane; t < NC * nq; t += tpe) {
@@ -653,14 +669,189 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
   }
   __syncthreads();
   double *Xm = tmp, *Yq = tmp2;
-  vdm_tmul<D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
-  mass_solve<D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
+  vdm_tmul<double, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
+  mass_solve<double, D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
                     ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq,
                     Z, Wb, lane, tpe);
   double *out = ka.dudt + (size_t)kk * NC * np;
   if (live)
     for (int t = lane; t < NC * np; t += tpe) {
       out[t] = Xm[t];
+      if (!isfinite(Xm[t])) ka.flag_nonphysical();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Phase B of the mixed form, FluxDifferencingForm with the EC flux (Euler):
+// the same steps as fd_time_derivative_kernel in FP32 on the perturbation
+// states u_qf/u_ff written by phase A, FP32 metric terms and operators; the
+// residual is written in FP64 for the FP64 stage accumulation.
+// ---------------------------------------------------------------------------
+template <int D, int NC>
+__global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArgs ka) {
+  static_assert(NC == D + 2, "the mixed form covers the Euler equations");
+  extern __shared__ double smem_raw[];
+  float *smem = reinterpret_cast<float *>(smem_raw);
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const DevGeo &g = ka.geo;
+  const Layout &L = ka.layBm;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  float *base = smem + (size_t)team * L.team_doubles;  // team size in floats for this layout
+  float *uq = base + L.off[0], *uf = base + L.off[1], *ff = base + L.off[2], *rq = base + L.off[3],
+        *diff = base + L.off[4], *Lam = base + L.off[5], *hnq = base + L.off[6],
+        *prim = base + L.off[7], *Z = base + L.off[8], *Wb = base + L.off[9];
+  const int PS = 4 + D;
+  const float gm1 = (float)ph.gm1, igm1 = (float)ph.igm1, gam = (float)ph.gamma;
+  const float rho_ref = (float)ph.rho_ref, p_ref = (float)ph.p_ref, hl = (float)ph.half_lambda;
+
+  const float *uqg = ka.u_qf + (size_t)kk * NC * nq;
+  const float *ufg = ka.u_ff + (size_t)kk * NC * nf;
+  for (int t = lane; t < NC * nq; t += tpe) uq[t] = uqg[t];
+  for (int t = lane; t < NC * nf; t += tpe) uf[t] = ufg[t];
+  const float *Lg = g.Lambda_qf + (size_t)kk * nq * D * D;
+  for (int t = lane; t < nq * D * D; t += tpe) Lam[t] = Lg[t];
+  const float *Hg = g.halfnJqf + (size_t)kk * D * nfac * nq;
+  if (op.nfp > 0)
+    for (int t = lane; t < D * nfac * nq; t += tpe) hnq[t] = Hg[t];
+  __syncthreads();
+  for (int i = lane; i < nq + nf; i += tpe) {
+    float du[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) du[e] = (i < nq) ? uq[e * nq + i] : uf[e * nf + (i - nq)];
+    euler_prim_mixed<D>(gm1, rho_ref, p_ref, du, prim + (size_t)i * PS);
+  }
+  __syncthreads();
+
+  // interface flux: EC flux . n + Lax-Friedrichs, scaled by BJf
+  for (int j = lane; j < nf; j += tpe) {
+    int P = g.mapP[(size_t)kk * nf + j];
+    int jn = P % nf, kn = P / nf;
+    float uo[NC], n[D], Po[4 + D], out[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) uo[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
+#pragma unroll
+    for (int m = 0; m < D; ++m) n[m] = g.n_ff[m + D * (j + (size_t)nf * kk)];
+    const float *Pi = prim + (size_t)(nq + j) * PS;
+    euler_prim_mixed<D>(gm1, rho_ref, p_ref, uo, Po);
+    ec_flux_dot_mixed<D>(igm1, Pi, Po, n, out);
+    float a = 0.f;
+    if (ph.nflux == 0) {
+      float vni = 0.f, vno = 0.f;
+#pragma unroll
+      for (int m = 0; m < D; ++m) { vni = fmaf(Pi[3 + m], n[m], vni); vno = fmaf(Po[3 + m], n[m], vno); }
+      float ci = sqrtf(gam * Pi[1] / Pi[0]), co = sqrtf(gam * Po[1] / Po[0]);
+      a = hl * (fmaxf(fabsf(vni), fabsf(vno)) + fmaxf(ci, co));
+    }
+    const float bjf = g.BJff[(size_t)kk * nf + j];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      float fs = (ph.nflux == 0) ? fmaf(a, uf[e * nf + j] - uo[e], out[e]) : out[e];
+      ff[e * nf + j] = fs * bjf;
+    }
+  }
+
+  // volume flux differencing: one contracted EC flux per unique pair
+  const float *vpS = OpVals<float>::vpS(op);
+  for (int pidx = lane; pidx < op.nvp; pidx += tpe) {
+    int ij = op.vp_ij[pidx];
+    int i = ij & 0xffff, j = ij >> 16;
+    float G[D], out[NC];
+#pragma unroll
+    for (int n = 0; n < D; ++n) G[n] = 0.f;
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      const float Sm = vpS[pidx * D + m];
+      if (Sm == 0.f) continue;
+#pragma unroll
+      for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
+    }
+    ec_flux_dot_mixed<D>(igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, out);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+  }
+  __syncthreads();
+  for (int i = lane; i < nq; i += tpe) {
+    float acc[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) acc[e] = 0.f;
+    for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
+      int inc = op.vp_inc[q];
+      const float *dp = diff + (size_t)(inc >> 1) * NC;
+      if (inc & 1) {
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] -= dp[e];
+      } else {
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
+  }
+  __syncthreads();
+
+  // facet correction
+  if (op.nfp > 0) {
+    const float *hnf = g.halfnJff + (size_t)kk * D * nf;
+    const float *fpC = OpVals<float>::fpC(op);
+    for (int pidx = lane; pidx < op.nfp; pidx += tpe) {
+      int ij = op.fp_ij[pidx];
+      int i = ij & 0xffff, j = ij >> 16;
+      int f = j / npf;
+      const float Cij = fpC[pidx];
+      float G[D], out[NC];
+#pragma unroll
+      for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+      ec_flux_dot_mixed<D>(igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, out);
+#pragma unroll
+      for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+    }
+    __syncthreads();
+    for (int t = lane; t < nq + nf; t += tpe) {
+      float acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0.f;
+      const int *ptr = (t < nq) ? op.fp_q_ptr : op.fp_f_ptr;
+      const int *lst = (t < nq) ? op.fp_q : op.fp_f;
+      int r = (t < nq) ? t : t - nq;
+      for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+        const float *dp = diff + (size_t)lst[q] * NC;
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+      }
+      float *dst = (t < nq) ? rq + r : ff + r;
+      const int stride = (t < nq) ? nq : nf;
+#pragma unroll
+      for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+    }
+    __syncthreads();
+  }
+
+  // r_q -= R^T f_f
+  const float *Rt = OpVals<float>::Rt(op);
+  for (int t = lane; t < NC * nq; t += tpe) {
+    int i = t % nq, e = t / nq;
+    float acc = 0.f;
+    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc = fmaf(Rt[q], ff[e * nf + op.Rt_idx[q]], acc);
+    rq[t] -= acc;
+  }
+  __syncthreads();
+
+  float *Xm = diff, *Yq = diff + (size_t)NC * np;
+  vdm_tmul<float, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
+  mass_solve<float, D, NC>(op, g.JinvWf ? g.JinvWf + (size_t)kk * nq : nullptr,
+                           g.WJinvf ? g.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq, Z,
+                           Wb, lane, tpe);
+  double *outp = ka.dudt + (size_t)kk * NC * np;
+  if (live)
+    for (int t = lane; t < NC * np; t += tpe) {
+      outp[t] = (double)Xm[t];
       if (!isfinite(Xm[t])) ka.flag_nonphysical();
     }
 }
@@ -678,6 +869,28 @@ __global__ void ck_stage_kernel(double *__restrict__ u, double *__restrict__ tmp
     tmp[x] = t;
     u[x] = u[x] + b * t;
   }
+}
+
+// The same stage with the update u += b tmp accumulated by compensated
+// (Kahan) summation: comp carries the low-order part lost when the small
+// increment is added to the state.  Used by the mixed form.
+__global__ void ck_stage_compensated_kernel(double *__restrict__ u, double *__restrict__ comp,
+                                            double *__restrict__ tmp, const double *__restrict__ k,
+                                            double a, double b, double dt, int first, size_t n) {
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) {
+    double t = first ? dt * k[x] : a * tmp[x] + dt * k[x];
+    tmp[x] = t;
+    double y = b * t - comp[x];
+    double s = u[x] + y;
+    comp[x] = (s - u[x]) - y;
+    u[x] = s;
+  }
+}
+
+// FP64 -> FP32 rounding of metric terms and operator values for the mixed form
+__global__ void round_to_float_kernel(const double *__restrict__ in, float *__restrict__ out, size_t n) {
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x)
+    out[x] = (float)in[x];
 }
 
 // classic RK4 stage helpers
@@ -726,10 +939,10 @@ __global__ void __launch_bounds__(256) conservation_kernel(KernelArgs ka, const 
   const int np = op.np, nq = op.nq;
   for (int t = lane; t < NC * np; t += tpe) X[t] = u[(size_t)kk * NC * np + t];
   __syncthreads();
-  vdm_mul<D, NC>(op, X, Y, Z, Wb, lane, tpe);       // Y = V u
+  vdm_mul<double, D, NC>(op, X, Y, Z, Wb, lane, tpe);       // Y = V u
   for (int t = lane; t < NC * np; t += tpe) X[t] = dudt[(size_t)kk * NC * np + t];
   __syncthreads();
-  vdm_mul<D, NC>(op, X, F, Z, Wb, lane, tpe);       // F = V dudt
+  vdm_mul<double, D, NC>(op, X, F, Z, Wb, lane, tpe);       // F = V dudt
   const double *WJ = ka.geo.WJ + (size_t)kk * nq;
   // lane-ordered partial sums, reduced by lane 0 in a fixed order
   double *red = base + L.off[5];  // tpe x (NC + 1)
@@ -795,9 +1008,27 @@ cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+cudaError_t sse_set_smem_limit_mixed(const KernelArgs &ka, size_t smBm) {
+  cudaError_t e = cudaErrorInvalidValue;
+  if (ka.op.d == 2 && ka.op.nc == 4)
+    e = cudaFuncSetAttribute((const void *)fd_time_derivative_mixed_kernel<2, 4>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smBm);
+  else if (ka.op.d == 3 && ka.op.nc == 5)
+    e = cudaFuncSetAttribute((const void *)fd_time_derivative_mixed_kernel<3, 5>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smBm);
+  return e;
+}
+
 cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st) {
   int grid = (ka.ne + ka.epb - 1) / ka.epb;
   size_t sm = (size_t)ka.epb * ka.layB.team_doubles * sizeof(double);
+  if (ka.mixed) {
+    size_t smm = (size_t)ka.epb * ka.layBm.team_doubles * sizeof(float);
+    if (ka.op.d == 2 && ka.op.nc == 4) fd_time_derivative_mixed_kernel<2, 4><<<grid, ka.tpb, smm, st>>>(ka);
+    else if (ka.op.d == 3 && ka.op.nc == 5) fd_time_derivative_mixed_kernel<3, 5><<<grid, ka.tpb, smm, st>>>(ka);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+  }
   if (ka.fd) {
     SSE_DISPATCH(D, NC, (fd_time_derivative_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka)));
   } else {
@@ -822,6 +1053,19 @@ static int elementwise_grid(size_t n) {
 cudaError_t launch_ck_stage(double *u, double *tmp, const double *k, double a, double b, double dt,
                             int first, size_t n, cudaStream_t st) {
   ck_stage_kernel<<<elementwise_grid(n), 256, 0, st>>>(u, tmp, k, a, b, dt, first, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, const double *k,
+                                        double a, double b, double dt, int first, size_t n,
+                                        cudaStream_t st) {
+  ck_stage_compensated_kernel<<<elementwise_grid(n), 256, 0, st>>>(u, comp, tmp, k, a, b, dt, first, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  round_to_float_kernel<<<elementwise_grid(n), 256, 0, st>>>(in, out, n);
   return cudaGetLastError();
 }
 

@@ -19,18 +19,27 @@ struct KernelArgs {
   DevGeo geo;
   Physics ph;
   Layout layA, layB;
+  Layout layBm;      // mixed-form phase B layout, offsets and team size in floats
   int ne, epb, tpb;
   int fd, project_entropy, mass_wa;
   const double *u;   // modal state (np x nc x ne)
   double *dudt;      // residual   (np x nc x ne)
   double *u_q;       // volume nodal scratch (nq x nc x ne)
   double *u_f;       // facet nodal scratch, internal layout (nf x nc x ne) element-major
+  float *u_qf;       // mixed form: FP32 perturbations of u_q from the reference state
+  float *u_ff;       // mixed form: FP32 perturbations of u_f
+  int mixed;         // 1: phase A writes u_qf/u_ff and phase B runs in FP32
   int *flag;         // nonzero: non-physical state met
 
   __device__ __forceinline__ void flag_nonphysical() const { atomicOr(flag, 1); }
 };
 
 cudaError_t sse_set_smem_limits(const KernelArgs &ka, size_t smA, size_t smB);
+cudaError_t sse_set_smem_limit_mixed(const KernelArgs &ka, size_t smBm);
+cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, const double *k,
+                                        double a, double b, double dt, int first, size_t n,
+                                        cudaStream_t st);
+cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st);
 cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_conservation(const KernelArgs &ka, const double *u, const double *dudt,

@@ -1,0 +1,80 @@
+"""Size-independent properties at the full benchmark sizes, where the CPU
+oracle would take too long: the 2-D Euler vortex mesh (64x64 cells = 8192
+curved triangles, p = 4) and the 3-D Taylor-Green mesh (16^3 x 6 = 24,576
+curved tetrahedra, p = 4).
+
+* discrete conservation: sum_k 1' WJ V dudt = 0 to round-off
+  (the reference asserts it at 1e-10, test/runtests.jl:120);
+* entropy conservation of the EC-only scheme: sum_k w' WJ V dudt = 0;
+* free-stream preservation: a constant state has zero residual;
+* bitwise determinism run to run;
+* the FP64 residual of a few sampled elements against the oracle, with
+  the oracle evaluated on the whole mesh once.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import cases
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tgv(pkg):
+    pb = pkg.setups.tgv_tet(cells=16, p=4, lf=False)
+    return pb, pb.host_arrays()
+
+
+@pytest.fixture(scope="module")
+def vortex(pkg):
+    pb = pkg.setups.vortex_tri(cells=64, p=4)
+    return pb, pb.host_arrays()
+
+
+def _scale(host, du):
+    return np.abs(du).max() * np.abs(host.WJ).sum()
+
+
+def test_tgv_24576_conservation_entropy_determinism(gpu_lib, pkg, tgv):
+    import torch
+    pb, host = tgv
+    gpu = pkg.GB300Solver(host)
+    u = torch.from_numpy(pkg.setups.perturbed(pb.u0, 7, 1e-3)).cuda()
+    torch.cuda.synchronize()
+    a = gpu.residual(u)
+    b = gpu.residual(u)
+    assert torch.equal(a, b)
+    out = gpu.conservation_residual(u, a)
+    s = _scale(host, a.cpu().numpy())
+    assert np.abs(out[:host.N_c]).max() < 1e-12 * s
+    assert abs(out[host.N_c]) < 1e-11 * s
+
+
+def test_tgv_24576_free_stream(gpu_lib, pkg, tgv):
+    pb, host = tgv
+    gpu = pkg.GB300Solver(host)
+
+    class Const:
+        N_c = 5
+
+        def evaluate(self, x, t=0.0):
+            one = np.ones_like(x[0])
+            return np.stack([one, 0.1 * one, -0.2 * one, 0.05 * one, 180.0 * one], -1)
+    u = pkg.solver.initialize(Const(), host.sd)
+    du = gpu.residual(u)
+    assert np.abs(du).max() < 1e-10 * 180.0
+
+
+def test_vortex_8192_matches_oracle_and_conserves(gpu_lib, pkg, vortex):
+    pb, host = vortex
+    gpu = pkg.GB300Solver(host)
+    u = pkg.setups.perturbed(pb.u0, 11, 1e-3)
+    got = gpu.residual(u)
+    want = Oracle(host).residual(u)
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert err < 1e-12
+    out = gpu.conservation_residual(u, got)
+    assert np.abs(out[:host.N_c]).max() < 1e-12 * _scale(host, got)
