@@ -417,7 +417,9 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
     for (; i < 12; ++i) L.off[i] = off;
     L.team_doubles = off;
   };
-  finish(ka.layA, {nc * std::max(np, nq), nc * nq, zsz, wsz, nc * std::max(np, nf), tpe * (nc + 1)});
+  // phase-A layout: X, Y, Z, W, F, lane partials; F holds NC x max(N_p, N_q,
+  // N_f) (modal scratch, facet values, or V dudt in the conservation kernel)
+  finish(ka.layA, {nc * std::max(np, nq), nc * nq, zsz, wsz, nc * std::max({np, nq, nf}), tpe * (nc + 1)});
   if (fd) {
     int diff = std::max({op.nvp * nc, op.nfp * nc, nc * (np + nq)});
     int prim = (c.law == SSE_EULER) ? (nq + nf) * (3 + d) : 0;
@@ -555,6 +557,8 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
   ph.rho_ref = rho / s->volume;
   ph.E_ref = E / s->volume;
   ph.p_ref = ph.gm1 * ph.E_ref;
+  ph.theta_ref = ph.p_ref / ph.rho_ref;
+  ph.H_ref = ph.gamma / ph.gm1 * ph.theta_ref;
   if (!(ph.rho_ref > 0.0) || !(ph.p_ref > 0.0))
     return fail(s, SSE_ERR_NONPHYSICAL, "mixed form: mean density or energy not positive");
   s->ref_ready = true;

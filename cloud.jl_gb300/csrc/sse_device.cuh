@@ -105,6 +105,8 @@ struct Physics {
   // mixed form: constant reference state (rho_ref, 0, ..., 0, E_ref) that the
   // FP32 nodal states are stored relative to, and p_ref = (gamma-1) E_ref
   double rho_ref, E_ref, p_ref;
+  double theta_ref;  // p_ref / rho_ref
+  double H_ref;      // gamma/(gamma-1) theta_ref: enthalpy removed from the energy fluxes
 };
 
 // ---------------------------------------------------------------------------
@@ -286,8 +288,19 @@ SSE_HD float inv_logmean_mixed(float x, float y) {
   return logf(y / x) / (y - x);
 }
 
+// The energy flux carries a large enthalpy part: Ranocha's energy flux is
+// f_E = f_rho C + (p_i V_j + p_j V_i)/2 with C ~ theta/(gamma-1), theta =
+// p/rho.  With H_ref = gamma/(gamma-1) theta_ref (theta_ref = p_ref/rho_ref)
+// the reduced flux f_E - H_ref f_rho is, exactly,
+//   f_rho (C - C_ref) + (Vbar . G)(rho_ref - rho_hat) theta_ref
+//   + (p'_i V_j + p'_j V_i)/2,          C_ref = theta_ref/(gamma-1),
+// a sum of products of fluctuations.  Every energy flux (volume pairs, facet
+// correction, interface flux including its dissipation) is reduced the same
+// way, so the energy residual equals H_ref times the density residual plus
+// the residual of the reduced fluxes; that sum is formed in FP64 at the end.
+
 // FP32 primitives from a perturbation du = u - u_ref, layout
-// [rho, p, beta, V_1..V_D, p - p_ref].
+// [rho, rho - rho_ref, theta - theta_ref, V_1..V_D, p - p_ref].
 template <int D>
 SSE_HD void euler_prim_mixed(float gm1, float rho_ref, float p_ref, const float *du, float *P) {
   const float rho = rho_ref + du[0];
@@ -299,19 +312,51 @@ SSE_HD void euler_prim_mixed(float gm1, float rho_ref, float p_ref, const float 
     s = fmaf(P[3 + m], P[3 + m], s);
   }
   const float pp = gm1 * (du[D + 1] - 0.5f * rho * s);
-  const float p = p_ref + pp;
   P[0] = rho;
-  P[1] = p;
-  P[2] = rho / p;
+  P[1] = du[0];
+  P[2] = (pp * rho_ref - p_ref * du[0]) * rr / rho_ref;  // p/rho - p_ref/rho_ref
   P[3 + D] = pp;
 }
 
-// ec_flux_dot in FP32 with the momentum pressure term taken as pbar - p_ref.
+// q(z) - 1 = z/3 + z^2/5 + ... (series of the FP32 branch)
+SSE_HD float q_minus_one_f(float z) {
+  return z * fmaf(z, fmaf(z, fmaf(z, fmaf(z, 1.f / 11.f, 1.f / 9.f), 1.f / 7.f), 0.2f), 1.f / 3.f);
+}
+
+// logmean(rho_i, rho_j) - rho_ref from density perturbations
+SSE_HD float logmean_minus_ref(float rho_ref, float ri, float rj, float dri, float drj) {
+  const float s = 2.f * rho_ref + (dri + drj);
+  const float f = (dri - drj) / s;
+  const float z = f * f;
+  if (z < 0.05f) {
+    const float qm1 = q_minus_one_f(z);
+    return (0.5f * (dri + drj) - rho_ref * qm1) / (1.f + qm1);
+  }
+  return (rj - ri) / logf(rj / ri) - rho_ref;
+}
+
+// inv_logmean(beta_i, beta_j) - theta_ref with beta = 1/theta, from
+// temperature perturbations dti = theta_i - theta_ref
+SSE_HD float inv_logmean_beta_minus_ref(float theta_ref, float dti, float dtj) {
+  const float ti = theta_ref + dti, tj = theta_ref + dtj;
+  const float sig = dti + dtj;
+  const float den = 2.f * theta_ref + sig;
+  const float f = (dtj - dti) / den;
+  const float z = f * f;
+  if (z < 0.05f) {
+    const float hm_minus = (theta_ref * sig + 2.f * dti * dtj) / den;  // 2 ti tj/(ti+tj) - theta_ref
+    const float hm = theta_ref + hm_minus;
+    return fmaf(q_minus_one_f(z), hm, hm_minus);
+  }
+  return ti * tj * logf(ti / tj) / (ti - tj) - theta_ref;
+}
+
+// ec_flux_dot in FP32: momentum with pbar - p_ref, energy reduced by H_ref f_rho.
 template <int D>
-SSE_HD void ec_flux_dot_mixed(float igm1, const float *Pi, const float *Pj, const float *G,
-                              float *out) {
-  const float rho_hat = logmean_mixed(Pi[0], Pj[0]);
-  const float ilm = inv_logmean_mixed(Pi[2], Pj[2]);
+SSE_HD void ec_flux_dot_mixed(float igm1, float rho_ref, float theta_ref, const float *Pi,
+                              const float *Pj, const float *G, float *out) {
+  const float drho_hat = logmean_minus_ref(rho_ref, Pi[0], Pj[0], Pi[1], Pj[1]);
+  const float dilm = inv_logmean_beta_minus_ref(theta_ref, Pi[2], Pj[2]);
   float vs[D];
   float vv = 0.f, gvs = 0.f, gvi = 0.f, gvj = 0.f;
 #pragma unroll
@@ -322,14 +367,16 @@ SSE_HD void ec_flux_dot_mixed(float igm1, const float *Pi, const float *Pj, cons
     gvi = fmaf(G[m], Pi[3 + m], gvi);
     gvj = fmaf(G[m], Pj[3 + m], gvj);
   }
+  const float rho_hat = rho_ref + drho_hat;
   const float f0 = 0.5f * rho_hat * gvs;
   const float pbar_pert = 0.5f * (Pi[3 + D] + Pj[3 + D]);
-  const float C = fmaf(igm1, ilm, 0.5f * vv);
+  const float dC = fmaf(igm1, dilm, 0.5f * vv);  // C - C_ref
   const float t = 0.5f * f0;
   out[0] = f0;
 #pragma unroll
   for (int m = 0; m < D; ++m) out[1 + m] = fmaf(t, vs[m], pbar_pert * G[m]);
-  out[D + 1] = fmaf(C, f0, 0.5f * fmaf(Pi[1], gvj, Pj[1] * gvi));
+  out[D + 1] = fmaf(dC, f0, fmaf(-0.5f * gvs * theta_ref, drho_hat,
+                                 0.5f * fmaf(Pi[3 + D], gvj, Pj[3 + D] * gvi)));
 }
 
 // Primitive quantities of one Euler state, computed once per node so that

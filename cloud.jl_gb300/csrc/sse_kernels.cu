@@ -709,6 +709,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   const int PS = 4 + D;
   const float gm1 = (float)ph.gm1, igm1 = (float)ph.igm1, gam = (float)ph.gamma;
   const float rho_ref = (float)ph.rho_ref, p_ref = (float)ph.p_ref, hl = (float)ph.half_lambda;
+  const float theta_ref = (float)ph.theta_ref, H_ref = (float)ph.H_ref;
 
   const float *uqg = ka.u_qf + (size_t)kk * NC * nq;
   const float *ufg = ka.u_ff + (size_t)kk * NC * nf;
@@ -739,19 +740,23 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
     for (int m = 0; m < D; ++m) n[m] = g.n_ff[m + D * (j + (size_t)nf * kk)];
     const float *Pi = prim + (size_t)(nq + j) * PS;
     euler_prim_mixed<D>(gm1, rho_ref, p_ref, uo, Po);
-    ec_flux_dot_mixed<D>(igm1, Pi, Po, n, out);
+    ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, Pi, Po, n, out);
     float a = 0.f;
     if (ph.nflux == 0) {
       float vni = 0.f, vno = 0.f;
 #pragma unroll
       for (int m = 0; m < D; ++m) { vni = fmaf(Pi[3 + m], n[m], vni); vno = fmaf(Po[3 + m], n[m], vno); }
-      float ci = sqrtf(gam * Pi[1] / Pi[0]), co = sqrtf(gam * Po[1] / Po[0]);
+      float ci = sqrtf(gam * (theta_ref + Pi[2])), co = sqrtf(gam * (theta_ref + Po[2]));
       a = hl * (fmaxf(fabsf(vni), fabsf(vno)) + fmaxf(ci, co));
     }
     const float bjf = g.BJff[(size_t)kk * nf + j];
+    float jump[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) jump[e] = uf[e * nf + j] - uo[e];
+    jump[NC - 1] = fmaf(-H_ref, jump[0], jump[NC - 1]);  // reduced energy: E' - H_ref rho'
 #pragma unroll
     for (int e = 0; e < NC; ++e) {
-      float fs = (ph.nflux == 0) ? fmaf(a, uf[e * nf + j] - uo[e], out[e]) : out[e];
+      float fs = (ph.nflux == 0) ? fmaf(a, jump[e], out[e]) : out[e];
       ff[e * nf + j] = fs * bjf;
     }
   }
@@ -771,7 +776,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
 #pragma unroll
       for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
     }
-    ec_flux_dot_mixed<D>(igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, out);
+    ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)j * PS, G, out);
 #pragma unroll
     for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
   }
@@ -808,7 +813,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
       float G[D], out[NC];
 #pragma unroll
       for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
-      ec_flux_dot_mixed<D>(igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, out);
+      ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, out);
 #pragma unroll
       for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
     }
@@ -848,10 +853,13 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   mass_solve<float, D, NC>(op, g.JinvWf ? g.JinvWf + (size_t)kk * nq : nullptr,
                            g.WJinvf ? g.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq, Z,
                            Wb, lane, tpe);
+  // energy residual = H_ref x density residual + reduced-flux residual, in FP64
   double *outp = ka.dudt + (size_t)kk * NC * np;
   if (live)
     for (int t = lane; t < NC * np; t += tpe) {
-      outp[t] = (double)Xm[t];
+      double v = (double)Xm[t];
+      if (t >= (NC - 1) * np) v = fma(ph.H_ref, (double)Xm[t - (NC - 1) * np], v);
+      outp[t] = v;
       if (!isfinite(Xm[t])) ka.flag_nonphysical();
     }
 }

@@ -53,6 +53,19 @@ def test_tgv_24576_conservation_entropy_determinism(gpu_lib, pkg, tgv):
     assert abs(out[host.N_c]) < 1e-11 * s
 
 
+def test_tgv_24576_matches_oracle(gpu_lib, pkg, tgv):
+    pb, host = tgv
+    gpu = pkg.GB300Solver(host)
+    u = pkg.setups.perturbed(pb.u0, 7, 1e-3)
+    got = gpu.residual(u)
+    want = Oracle(host).residual(u)
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-12
+    # the FP64 reductions of the GPU and of the oracle agree on the same residual
+    g = gpu.conservation_residual(u, got)
+    o = Oracle(host).conservation_residual(u, got)
+    assert np.abs(g - o).max() < 1e-12 * _scale(host, got)
+
+
 def test_tgv_24576_free_stream(gpu_lib, pkg, tgv):
     pb, host = tgv
     gpu = pkg.GB300Solver(host)
