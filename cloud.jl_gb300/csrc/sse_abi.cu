@@ -66,6 +66,25 @@ struct sse_solver {
   bool mixed_ready = false; // FP32 copies allocated
   bool ref_ready = false;   // reference state of the mixed form chosen
   double *d_comp = nullptr; // compensation of the mixed form's stage accumulation
+  // discrete adjoint: VJP scratch (allocated on first use)
+  bool adj_ready = false;
+  bool mapP_involution = false;  // mapP(mapP(x)) == x: each interface seen from both sides
+  double *d_lam = nullptr, *d_mu = nullptr;
+  // trajectory recorded by sse_rk_record for sse_rk_adjoint
+  struct Tape {
+    bool valid = false;
+    int n_steps = 0, every = 0, scheme = 0, stages = 0, nseg = 0;
+    bool mixed = false;  // recorded (and recomputed) in SSE_MIXED
+    bool nodal = false;  // FP64 phase-A outputs kept per stage (FP64 recordings)
+    double dt = 0.0;
+    size_t bytes = 0;
+    std::vector<void *> bufs;  // freed when re-recorded and by sse_destroy
+    double *ckpt = nullptr, *ckpt_comp = nullptr;  // nseg states (+ compensation)
+    double *seg_y = nullptr, *seg_uq = nullptr, *seg_uf = nullptr;  // every*stages slots
+    double *w_u = nullptr, *w_tmp = nullptr, *w_comp = nullptr, *w_dudt = nullptr;
+    double *w_acc = nullptr, *w_ust = nullptr;
+    double *ybar = nullptr, *qbar = nullptr, *yp = nullptr;
+  } tape;
 };
 
 namespace {
@@ -201,6 +220,8 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: JinvW required for WeightAdjustedSolver");
   if (c.mass_solver == SSE_DIAGONAL && !geo->WJinv)
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: WJinv required for DiagonalSolver");
+  if (fd && c.law == SSE_EULER && has_vdm && !geo->JinvW)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: JinvW required for the entropy projection");
   if (fd && (!geo->Lambda_q || !geo->halfnJf || !geo->halfnJq))
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "geometry: Lambda_q, halfnJf, halfnJq required for FluxDifferencingForm");
   if (!fd && !geo->halfWLambda)
@@ -257,6 +278,9 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
       if (P < 1 || P > lim) return fail(s, SSE_ERR_INVALID_ARGUMENT, "mapP index out of range");
       mapP[t] = (int)(P - 1);
     }
+    s->mapP_involution = true;
+    for (size_t t = 0; t < mapP.size(); ++t)
+      if ((size_t)mapP[mapP[t]] != t) { s->mapP_involution = false; break; }
   }
 
   s->cfg = c;
@@ -566,11 +590,17 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
 }
 
 // one residual evaluation on device buffers (no synchronisation in the FP64
-// form; the mixed form synchronises once, on its first call)
-cudaError_t residual_device(sse_solver *s, const double *u, double *dudt) {
+// form; the mixed form synchronises once, on its first call).  u_q / u_f,
+// when given, receive the FP64 nodal states instead of the handle's scratch.
+cudaError_t residual_device(sse_solver *s, const double *u, double *dudt, double *u_q = nullptr,
+                            double *u_f = nullptr) {
   KernelArgs ka = s->ka;
   ka.u = u;
   ka.dudt = dudt;
+  if (u_q) {
+    ka.u_q = u_q;
+    ka.u_f = u_f;
+  }
   if (ka.mixed && !s->ref_ready) {
     if (ensure_reference(s, u) != SSE_OK) return cudaErrorInvalidValue;
     ka.ph = s->ka.ph;
@@ -578,6 +608,133 @@ cudaError_t residual_device(sse_solver *s, const double *u, double *dudt) {
   cudaError_t e = launch_nodal_values(ka, s->stream);
   if (e != cudaSuccess) return e;
   return launch_time_derivative(ka, s->stream);
+}
+
+// ---------------------------------------------------------------------------
+// Discrete adjoint
+// ---------------------------------------------------------------------------
+
+// VJP scratch and shared-memory layouts of the three adjoint kernels.
+int enable_adjoint(sse_solver *s) {
+  const sse_config &c = s->cfg;
+  if (!(c.form == SSE_FLUX_DIFFERENCING_FORM && c.law == SSE_EULER && c.two_point_flux == SSE_EC_FLUX))
+    return fail(s, SSE_ERR_UNSUPPORTED,
+                "the discrete adjoint covers FluxDifferencingForm with the entropy-conservative flux (Euler)");
+  if (!s->mapP_involution)
+    return fail(s, SSE_ERR_UNSUPPORTED, "the discrete adjoint needs mapP to pair facet nodes (mapP(mapP(x)) == x)");
+  if (s->adj_ready) return SSE_OK;
+  KernelArgs &ka = s->ka;
+  const DevOps &op = ka.op;
+  const int nc = c.n_c, np = c.n_p, nq = c.n_q, nf = c.n_f, d = c.d, ps = 3 + d;
+  int zsz = 0, wsz = 0;
+  if (op.has_vdm) {
+    if (d == 2) zsz = nc * op.p1 * op.M2;
+    else { zsz = nc * op.nb12 * op.M3; wsz = nc * op.p1 * op.M2 * op.M3; }
+  }
+  auto finish = [](Layout &L, std::initializer_list<int> sizes) {
+    int off = 0, i = 0;
+    for (int sz : sizes) { L.off[i++] = off; off += (sz + 1) & ~1; }
+    for (; i < 12; ++i) L.off[i] = off;
+    L.team_doubles = off;
+  };
+  const size_t cap = (size_t)220 * 1024 / 8 / ka.epb;  // doubles per team
+  // lift: X, Y, Z, W, F as in phase A
+  ka.layAdjB1 = ka.layA;
+  // projection transpose: X, Y, Z, W, F, u_q0, w_q, w_f, ubar_q, ubar_f
+  finish(ka.layAdjA, {nc * std::max(np, nq), nc * nq, zsz, wsz, nc * std::max({np, nq, nf}), nc * nq,
+                      nc * nq, nc * nf, nc * nq, nc * nf});
+  // pair transposes: fixed arrays, then a chunk of per-pair primitive cotangents
+  const int hsz = op.nfp > 0 ? d * c.num_faces * nq : 0;
+  Layout base{};
+  finish(base, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf, d * d * nq, hsz});
+  const int max_pairs = std::max(op.nvp, op.nfp);
+  // chunk: keep the team no larger than the forward flux-differencing team
+  // when that leaves room for at least 64 pairs, else as large as fits
+  long room = (long)std::max<size_t>(ka.layB.team_doubles, base.team_doubles + 64 * 2 * ps) - base.team_doubles;
+  room = std::min<long>(room, (long)cap - base.team_doubles);
+  int chunk = (int)std::min<long>(max_pairs, room / (2 * ps));
+  if (chunk < 1 || ka.layAdjA.team_doubles > (int)cap)
+    return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the adjoint kernels' shared memory");
+  ka.pair_chunk = chunk;
+  finish(ka.layAdjB2, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf,
+                       d * d * nq, hsz, chunk * 2 * ps});
+  cudaError_t e;
+  void *p;
+  const size_t ne = c.n_e, n = (size_t)np * nc * ne;
+  if ((e = alloc(s, (size_t)nq * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.rbar_q = (double *)p;
+  if ((e = alloc(s, (size_t)nf * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.gbar_f = (double *)p;
+  if ((e = alloc(s, (size_t)nq * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.ubar_q = (double *)p;
+  if ((e = alloc(s, (size_t)nf * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.ubar_f = (double *)p;
+  if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_lam = (double *)p;
+  if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_mu = (double *)p;
+  if ((e = sse_set_smem_limits_adjoint(ka))) return cuda_fail(s, e, "cudaFuncSetAttribute (adjoint)");
+  s->adj_ready = true;
+  return SSE_OK;
+}
+
+// mu = (dR/du)^T lam on device buffers.  u_q / u_f: the FP64 nodal states of
+// u when already computed (a recorded stage), else phase A runs first.
+cudaError_t vjp_device(sse_solver *s, const double *u, const double *lam, double *mu,
+                       const double *u_q = nullptr, const double *u_f = nullptr) {
+  KernelArgs ka = s->ka;
+  ka.mixed = 0;
+  ka.u = u;
+  ka.lam = lam;
+  ka.mu = mu;
+  cudaError_t e;
+  if (u_q) {
+    ka.u_q = const_cast<double *>(u_q);
+    ka.u_f = const_cast<double *>(u_f);
+  } else if ((e = launch_nodal_values(ka, s->stream)) != cudaSuccess) {
+    return e;
+  }
+  return launch_residual_vjp_kernels(ka, s->stream);
+}
+
+void free_tape(sse_solver *s) {
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (void *p : s->tape.bufs) cudaFree(p);
+  s->tape = sse_solver::Tape{};
+}
+
+// one Runge-Kutta step of u (device) using the tape's work buffers; with
+// slot >= 0 every stage's input state (and, for FP64 recordings, its nodal
+// states) is stored in the segment slots slot*stages + stage
+cudaError_t tape_step(sse_solver *s, double *u, int slot) {
+  sse_solver::Tape &T = s->tape;
+  const sse_config &c = s->cfg;
+  const size_t n = (size_t)c.n_p * c.n_c * c.n_e;
+  const size_t nqs = (size_t)c.n_q * c.n_c * c.n_e, nfs = (size_t)c.n_f * c.n_c * c.n_e;
+  const double dt = T.dt;
+  cudaError_t e;
+  auto stage_residual = [&](const double *y, int st) -> cudaError_t {
+    if (slot < 0) return residual_device(s, y, T.w_dudt);
+    const size_t q = (size_t)slot * T.stages + st;
+    double *ys = T.seg_y + q * n;
+    cudaError_t err = cudaMemcpyAsync(ys, y, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+    if (err != cudaSuccess) return err;
+    if (T.nodal) return residual_device(s, ys, T.w_dudt, T.seg_uq + q * nqs, T.seg_uf + q * nfs);
+    return residual_device(s, ys, T.w_dudt);
+  };
+  if (T.scheme == SSE_CARPENTER_KENNEDY_2N54) {
+    for (int st = 0; st < 5; ++st) {
+      if ((e = stage_residual(u, st))) return e;
+      e = T.mixed ? launch_ck_stage_compensated(u, T.w_comp, T.w_tmp, T.w_dudt, kCKA[st], kCKB[st], dt,
+                                                st == 0, n, s->stream)
+                  : launch_ck_stage(u, T.w_tmp, T.w_dudt, kCKA[st], kCKB[st], dt, st == 0, n, s->stream);
+      if (e) return e;
+    }
+    return cudaSuccess;
+  }
+  const double half = dt / 2;
+  if ((e = stage_residual(u, 0))) return e;
+  if ((e = launch_rk4_stage(u, T.w_ust, T.w_acc, T.w_dudt, 0.0, half, 1, n, s->stream))) return e;
+  if ((e = stage_residual(T.w_ust, 1))) return e;
+  if ((e = launch_rk4_stage(u, T.w_ust, T.w_acc, T.w_dudt, 2.0, half, 0, n, s->stream))) return e;
+  if ((e = stage_residual(T.w_ust, 2))) return e;
+  if ((e = launch_rk4_stage(u, T.w_ust, T.w_acc, T.w_dudt, 2.0, dt, 0, n, s->stream))) return e;
+  if ((e = stage_residual(T.w_ust, 3))) return e;
+  return launch_rk4_final(u, T.w_acc, T.w_dudt, dt / 6, n, s->stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -655,6 +812,7 @@ int32_t sse_create(const sse_config *cfg, const sse_operators *ops, const sse_ge
 int32_t sse_destroy(sse_solver *s) {
   if (!s) return SSE_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
+  for (void *p : s->tape.bufs) cudaFree(p);
   for (void *p : s->allocations) cudaFree(p);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -804,6 +962,179 @@ int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt, int32
   if (memory == SSE_HOST && (e = cudaMemcpyAsync(u, s->d_u, n * 8, cudaMemcpyDeviceToHost, s->stream)))
     return cuda_fail(s, e, "D2H");
   if (t) *t += n_steps * dt;
+  return check_flag(s);
+}
+
+int32_t sse_residual_vjp(sse_solver *s, const double *u, const double *lam, double *mu, int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!u || !lam || !mu) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u/lam/mu");
+  if (memory != SSE_HOST && memory != SSE_DEVICE)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
+  int rc = enable_adjoint(s);
+  if (rc != SSE_OK) return rc;
+  const size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
+  cudaError_t e;
+  if (memory == SSE_DEVICE) {
+    if ((e = vjp_device(s, u, lam, mu))) return cuda_fail(s, e, "residual vjp");
+  } else {
+    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream)) ||
+        (e = cudaMemcpyAsync(s->d_lam, lam, n * 8, cudaMemcpyHostToDevice, s->stream)))
+      return cuda_fail(s, e, "H2D");
+    if ((e = vjp_device(s, s->d_u, s->d_lam, s->d_mu))) return cuda_fail(s, e, "residual vjp");
+    if ((e = cudaMemcpyAsync(mu, s->d_mu, n * 8, cudaMemcpyDeviceToHost, s->stream))) return cuda_fail(s, e, "D2H");
+  }
+  return check_flag(s);
+}
+
+int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme,
+                      int32_t checkpoint_every, double *t, int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!u || n_steps < 1 || checkpoint_every < 0)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u, n_steps < 1 or negative checkpoint_every");
+  if (scheme != SSE_CARPENTER_KENNEDY_2N54 && scheme != SSE_RK4)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown scheme");
+  if (memory != SSE_HOST && memory != SSE_DEVICE)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
+  int rc = enable_adjoint(s);
+  if (rc != SSE_OK) return rc;
+  free_tape(s);
+  const sse_config &c = s->cfg;
+  const size_t n = (size_t)c.n_p * c.n_c * c.n_e;
+  const size_t nqs = (size_t)c.n_q * c.n_c * c.n_e, nfs = (size_t)c.n_f * c.n_c * c.n_e;
+  sse_solver::Tape &T = s->tape;
+  T.n_steps = n_steps;
+  T.scheme = scheme;
+  T.stages = scheme == SSE_RK4 ? 4 : 5;
+  T.mixed = s->ka.mixed != 0;
+  T.nodal = !T.mixed;
+  T.dt = dt;
+  const size_t ckpt_state = (T.mixed ? 2 : 1) * n * 8;
+  const size_t stage_bytes = (n + (T.nodal ? nqs + nfs : 0)) * 8;
+  // fixed work buffers: u, tmp, comp, dudt, acc, ust, ybar, qbar, ybar'
+  const size_t fixed = 9 * n * 8;
+  auto need = [&](int every) {
+    const size_t nseg = (n_steps + every - 1) / every;
+    return nseg * ckpt_state + (size_t)every * T.stages * stage_bytes + fixed;
+  };
+  int every = checkpoint_every > 0 ? std::min(checkpoint_every, (int)n_steps) : 1;
+  if (checkpoint_every == 0)
+    for (int c2 = 2; c2 <= n_steps; ++c2)
+      if (need(c2) < need(every)) every = c2;
+  size_t free_b = 0, total_b = 0;
+  cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+  if (e != cudaSuccess) return cuda_fail(s, e, "cudaMemGetInfo");
+  const size_t bytes = need(every);
+  if (bytes + ((size_t)256 << 20) > free_b)
+    return fail(s, SSE_ERR_OUT_OF_MEMORY,
+                "recording needs " + std::to_string(bytes >> 20) + " MiB of device memory, " +
+                    std::to_string(free_b >> 20) + " MiB free (choose another checkpoint_every)");
+  T.every = every;
+  T.nseg = (n_steps + every - 1) / every;
+  T.bytes = bytes;
+  auto get = [&](size_t count, double **out) -> cudaError_t {
+    void *p = nullptr;
+    cudaError_t err = cudaMalloc(&p, std::max<size_t>(count, 1) * 8);
+    if (err != cudaSuccess) return err;
+    T.bufs.push_back(p);
+    *out = (double *)p;
+    return cudaSuccess;
+  };
+  const size_t slots = (size_t)every * T.stages;
+  if ((e = get(T.nseg * n, &T.ckpt)) || (T.mixed && (e = get(T.nseg * n, &T.ckpt_comp))) ||
+      (e = get(slots * n, &T.seg_y)) || (T.nodal && (e = get(slots * nqs, &T.seg_uq))) ||
+      (T.nodal && (e = get(slots * nfs, &T.seg_uf))) || (e = get(n, &T.w_u)) || (e = get(n, &T.w_tmp)) ||
+      (e = get(n, &T.w_comp)) || (e = get(n, &T.w_dudt)) || (e = get(n, &T.w_acc)) ||
+      (e = get(n, &T.w_ust)) || (e = get(n, &T.ybar)) || (e = get(n, &T.qbar)) || (e = get(n, &T.yp))) {
+    free_tape(s);
+    return fail(s, SSE_ERR_OUT_OF_MEMORY, std::string("recording: ") + cudaGetErrorString(e));
+  }
+  double *du = u;
+  if (memory == SSE_HOST) {
+    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    du = s->d_u;
+  }
+  if (T.mixed && (e = cudaMemsetAsync(T.w_comp, 0, n * 8, s->stream))) return cuda_fail(s, e, "memset");
+  for (int step = 0; step < n_steps; ++step) {
+    if (step % every == 0) {
+      const size_t g = step / every;
+      if ((e = cudaMemcpyAsync(T.ckpt + g * n, du, n * 8, cudaMemcpyDeviceToDevice, s->stream)))
+        return cuda_fail(s, e, "checkpoint");
+      if (T.mixed && (e = cudaMemcpyAsync(T.ckpt_comp + g * n, T.w_comp, n * 8, cudaMemcpyDeviceToDevice,
+                                          s->stream)))
+        return cuda_fail(s, e, "checkpoint");
+    }
+    if ((e = tape_step(s, du, -1))) return cuda_fail(s, e, "step");
+  }
+  if (memory == SSE_HOST && (e = cudaMemcpyAsync(u, s->d_u, n * 8, cudaMemcpyDeviceToHost, s->stream)))
+    return cuda_fail(s, e, "D2H");
+  if (t) *t += n_steps * dt;
+  rc = check_flag(s);
+  T.valid = rc == SSE_OK;
+  return rc;
+}
+
+int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double *out_info, int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!lam_T || !lam_0) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null lam_T/lam_0");
+  if (memory != SSE_HOST && memory != SSE_DEVICE)
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
+  sse_solver::Tape &T = s->tape;
+  if (!T.valid) return fail(s, SSE_ERR_INVALID_ARGUMENT, "no recorded trajectory (call sse_rk_record first)");
+  const sse_config &c = s->cfg;
+  const size_t n = (size_t)c.n_p * c.n_c * c.n_e;
+  const size_t nqs = (size_t)c.n_q * c.n_c * c.n_e, nfs = (size_t)c.n_f * c.n_c * c.n_e;
+  const double dt = T.dt;
+  cudaError_t e;
+  cudaMemcpyKind kin = memory == SSE_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  if ((e = cudaMemcpyAsync(T.ybar, lam_T, n * 8, kin, s->stream))) return cuda_fail(s, e, "copy lam_T");
+  // the recomputation runs in the recorded precision; the stage adjoints in FP64
+  const int saved_mixed = s->ka.mixed;
+  s->ka.mixed = T.mixed ? 1 : 0;
+  auto stage_vjp = [&](size_t q, const double *lam) -> cudaError_t {
+    const double *uq = T.nodal ? T.seg_uq + q * nqs : nullptr;
+    const double *uf = T.nodal ? T.seg_uf + q * nfs : nullptr;
+    return vjp_device(s, T.seg_y + q * n, lam, s->d_mu, uq, uf);
+  };
+  for (int seg = T.nseg - 1; seg >= 0 && e == cudaSuccess; --seg) {
+    const int s0 = seg * T.every, m = std::min(T.n_steps, s0 + T.every) - s0;
+    e = cudaMemcpyAsync(T.w_u, T.ckpt + (size_t)seg * n, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+    if (e == cudaSuccess && T.mixed)
+      e = cudaMemcpyAsync(T.w_comp, T.ckpt_comp + (size_t)seg * n, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+    for (int i = 0; i < m && e == cudaSuccess; ++i) e = tape_step(s, T.w_u, i);
+    for (int i = m - 1; i >= 0 && e == cudaSuccess; --i) {
+      const size_t q0 = (size_t)i * T.stages;
+      if (T.scheme == SSE_CARPENTER_KENNEDY_2N54) {
+        e = launch_adj_lincomb(T.qbar, T.ybar, 0.0, kCKB[4], n, s->stream);
+        for (int st = 4; st >= 0 && e == cudaSuccess; --st) {
+          e = stage_vjp(q0 + st, T.qbar);
+          if (e == cudaSuccess)
+            e = launch_adj_ck_stage(T.ybar, T.qbar, s->d_mu, dt, kCKA[st], st > 0 ? kCKB[st - 1] : 0.0, n,
+                                    s->stream);
+        }
+      } else {
+        // u' = u + dt/6 (k1 + 2 k2 + 2 k3 + k4), stages y1 = u, y2 = u + dt/2 k1,
+        // y3 = u + dt/2 k2, y4 = u + dt k3
+        e = cudaMemcpyAsync(T.yp, T.ybar, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess) e = launch_adj_lincomb(T.qbar, T.ybar, 0.0, dt / 6, n, s->stream);
+        const double cy[4] = {0.0, dt / 6, dt / 3, dt / 3};  // kbar of stage st-1: cy ybar' + cm mu
+        const double cm[4] = {0.0, dt / 2, dt / 2, dt};
+        for (int st = 3; st >= 0 && e == cudaSuccess; --st) {
+          e = stage_vjp(q0 + st, T.qbar);
+          if (e == cudaSuccess)
+            e = launch_adj_rk4_stage(T.ybar, T.qbar, s->d_mu, T.yp, cy[st], cm[st], st == 0, n, s->stream);
+        }
+      }
+    }
+  }
+  s->ka.mixed = saved_mixed;
+  if (e != cudaSuccess) return cuda_fail(s, e, "adjoint sweep");
+  cudaMemcpyKind kout = memory == SSE_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if ((e = cudaMemcpyAsync(lam_0, T.ybar, n * 8, kout, s->stream))) return cuda_fail(s, e, "copy lam_0");
+  if (out_info) {
+    out_info[0] = T.nseg;
+    out_info[1] = T.every;
+    out_info[2] = (double)T.bytes;
+  }
   return check_flag(s);
 }
 

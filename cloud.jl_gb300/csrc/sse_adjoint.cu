@@ -1,0 +1,483 @@
+// sse_adjoint.cu -- discrete adjoint of the FP64 flux-differencing residual
+// (Euler, entropy-conservative volume flux, Lax-Friedrichs or EC interface
+// flux): mu = (dR/du)^T lam for the residual of flux_differencing_form.jl:
+// 253-347, with no counterpart in the reference (which has no AD).
+//
+// Three kernels per vector-Jacobian product, after the forward phase A has
+// written u_q, u_f for the state:
+//   adj_lift_kernel     rbar_q = V M lam, interface cotangent gbar = -BJf R rbar_q
+//   adj_flux_kernel     per-pair transposes of the contracted EC flux, the
+//                       interface flux seen from both sides (no cross-element
+//                       atomics: each element differentiates its own flux
+//                       w.r.t. its inner state and its neighbour's flux w.r.t.
+//                       the neighbour's outer state), deterministic chunked
+//                       two-pass accumulation -> ubar_q, ubar_f
+//   adj_projection_kernel  recomputes the entropy projection and applies its
+//                       transpose (symmetric Jacobians of the entropy maps) -> mu
+#include "sse_device.cuh"
+#include "sse_kernels.cuh"
+#include "sse_ops.cuh"
+
+namespace sse {
+
+// ---------------------------------------------------------------------------
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_lift_kernel(KernelArgs ka) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Layout &L = ka.layAdjB1;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3],
+         *F = base + L.off[4];
+  const double *lk = ka.lam + (size_t)kk * NC * np;
+  for (int t = lane; t < NC * np; t += tpe) X[t] = lk[t];
+  __syncthreads();
+  // dudt = M V^T r_q  =>  rbar_q = V M^T lam (M symmetric)
+  mass_solve<double, D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
+                            ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, X, Y,
+                            Z, Wb, lane, tpe);
+  vdm_mul<double, D, NC>(op, X, Y, Z, Wb, lane, tpe);
+  if (live)
+    for (int t = lane; t < NC * nq; t += tpe) ka.rbar_q[(size_t)kk * NC * nq + t] = Y[t];
+  // r_q -= R^T f_f  =>  fbar_f = -R rbar_q ; f_f = BJf f*  =>  gbar = BJf fbar_f
+  csr_mul<double, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, Y, F, lane, tpe);
+  __syncthreads();
+  if (live)
+    for (int t = lane; t < NC * nf; t += tpe)
+      ka.gbar_f[(size_t)kk * NC * nf + t] = -F[t] * ka.geo.BJf[(size_t)kk * nf + t % nf];
+}
+
+// ---------------------------------------------------------------------------
+// transpose of the Lax-Friedrichs interface flux
+//   f* = ECdot(P(u_in), P(u_out), n) + a (u_in - u_out),
+//   a = halfλ (max(|V_in.n|, |V_out.n|) + max(c_in, c_out)),
+// with respect to one side: side = 0 inner, 1 outer.  Adds to Pb (primitive
+// cotangent of that side) and ub_direct (cotangent of its conservative state
+// through the a (u_in - u_out) term).
+template <int D, int NC>
+__device__ void lf_flux_bwd(const Physics &ph, const double *uin, const double *uout,
+                            const double *Pin, const double *Pout, const double *n, const double *g,
+                            int side, double *Pb, double *ub_direct) {
+  double Pbi[3 + D], Pbo[3 + D];
+  ec_flux_dot_bwd<D>(ph.igm1, Pin, Pout, n, g, Pbi, Pbo);
+  const double *Pself = side ? Pbo : Pbi;
+#pragma unroll
+  for (int c = 0; c < 3 + D; ++c) Pb[c] += Pself[c];
+  if (ph.nflux != 0) return;
+  double vni = 0.0, vno = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) { vni = fma(Pin[3 + m], n[m], vni); vno = fma(Pout[3 + m], n[m], vno); }
+  const double ci = sqrt(ph.gamma * Pin[1] * sse_rcp(Pin[0]));
+  const double co = sqrt(ph.gamma * Pout[1] * sse_rcp(Pout[0]));
+  const double a = ph.half_lambda * (fmax(fabs(vni), fabs(vno)) + fmax(ci, co));
+  double abar = 0.0;
+#pragma unroll
+  for (int e = 0; e < NC; ++e) {
+    abar = fma(g[e], uin[e] - uout[e], abar);
+    ub_direct[e] += side ? -a * g[e] : a * g[e];
+  }
+  const double hb = ph.half_lambda * abar;
+  // max(|vni|, |vno|): the inner side owns ties (fmax returns its first argument's value)
+  const bool v_in = fabs(vni) >= fabs(vno);
+  const bool c_in = ci >= co;
+  if (v_in == (side == 0)) {
+    const double vn = side ? vno : vni;
+    const double sg = vn >= 0.0 ? 1.0 : -1.0;
+#pragma unroll
+    for (int m = 0; m < D; ++m) Pb[3 + m] += hb * sg * n[m];
+  }
+  if (c_in == (side == 0)) {
+    const double *P = side ? Pout : Pin;
+    const double c = side ? co : ci;
+    Pb[1] += hb * ph.gamma / (2.0 * c * P[0]);
+    Pb[0] -= hb * c / (2.0 * P[0]);
+  }
+}
+
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_flux_kernel(KernelArgs ka) {
+  static_assert(NC == D + 2, "adjoint of the Euler flux-differencing residual");
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const DevGeo &g = ka.geo;
+  const Layout &L = ka.layAdjB2;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  const int PS = 3 + D;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *uq = base + L.off[0], *uf = base + L.off[1], *rb = base + L.off[2], *fb = base + L.off[3],
+         *prim = base + L.off[4], *Pb = base + L.off[5], *ubd = base + L.off[6], *Lam = base + L.off[7],
+         *hnq = base + L.off[8], *buf = base + L.off[9];
+
+  for (int t = lane; t < NC * nq; t += tpe) {
+    uq[t] = ka.u_q[(size_t)kk * NC * nq + t];
+    rb[t] = ka.rbar_q[(size_t)kk * NC * nq + t];
+  }
+  for (int t = lane; t < NC * nf; t += tpe) {
+    uf[t] = ka.u_f[(size_t)kk * NC * nf + t];
+    ubd[t] = 0.0;
+  }
+  for (int t = lane; t < nq * D * D; t += tpe) Lam[t] = g.Lambda_q[(size_t)kk * nq * D * D + t];
+  if (op.nfp > 0)
+    for (int t = lane; t < D * nfac * nq; t += tpe) hnq[t] = g.halfnJq[(size_t)kk * D * nfac * nq + t];
+  for (int t = lane; t < (nq + nf) * PS; t += tpe) Pb[t] = 0.0;
+  __syncthreads();
+  for (int i = lane; i < nq + nf; i += tpe) {
+    double u[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) u[e] = (i < nq) ? uq[e * nq + i] : uf[e * nf + (i - nq)];
+    euler_prim_fast<D>(ph.gm1, u, prim + (size_t)i * PS);
+  }
+  // fbar_f = -R rbar_q
+  csr_mul<double, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, rb, fb, lane, tpe);
+  __syncthreads();
+  for (int t = lane; t < NC * nf; t += tpe) fb[t] = -fb[t];
+
+  // interface flux: own flux w.r.t. the inner state, neighbour's flux w.r.t. its outer state
+  for (int j = lane; j < nf; j += tpe) {
+    const int P = g.mapP[(size_t)kk * nf + j];
+    const int jn = P % nf, kn = P / nf;
+    double ui[NC], uo[NC], Po[3 + D], n[D], nn[D], gown[NC], gnb[NC], ub[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      ui[e] = uf[e * nf + j];
+      uo[e] = ka.u_f[((size_t)kn * NC + e) * nf + jn];
+      gown[e] = ka.gbar_f[((size_t)kk * NC + e) * nf + j];
+      gnb[e] = ka.gbar_f[((size_t)kn * NC + e) * nf + jn];
+      ub[e] = 0.0;
+    }
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      n[m] = g.n_f[m + D * (j + (size_t)nf * kk)];
+      nn[m] = g.n_f[m + D * (jn + (size_t)nf * kn)];
+    }
+    euler_prim_fast<D>(ph.gm1, uo, Po);
+    double *Pself = Pb + (size_t)(nq + j) * PS;
+    const double *Pi = prim + (size_t)(nq + j) * PS;
+    lf_flux_bwd<D, NC>(ph, ui, uo, Pi, Po, n, gown, 0, Pself, ub);
+    lf_flux_bwd<D, NC>(ph, uo, ui, Po, Pi, nn, gnb, 1, Pself, ub);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) ubd[e * nf + j] += ub[e];
+  }
+  __syncthreads();
+
+  // volume pairs: dbar_p = rbar[j] - rbar[i]
+  const int CH = ka.pair_chunk;
+  for (int c0 = 0; c0 < op.nvp; c0 += CH) {
+    const int c1 = min(op.nvp, c0 + CH);
+    for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+      const int ij = op.vp_ij[pidx];
+      const int i = ij & 0xffff, j = ij >> 16;
+      double G[D], db[NC];
+#pragma unroll
+      for (int n_ = 0; n_ < D; ++n_) G[n_] = 0.0;
+#pragma unroll
+      for (int m = 0; m < D; ++m) {
+        const double Sm = op.vp_S[pidx * D + m];
+        if (Sm == 0.0) continue;
+#pragma unroll
+        for (int n_ = 0; n_ < D; ++n_)
+          G[n_] = fma(Sm, Lam[i + nq * (m + D * n_)] + Lam[j + nq * (m + D * n_)], G[n_]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) db[e] = rb[e * nq + j] - rb[e * nq + i];
+      double *slot = buf + (size_t)(pidx - c0) * 2 * PS;
+      ec_flux_dot_bwd<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, db, slot, slot + PS);
+    }
+    __syncthreads();
+    for (int i = lane; i < nq; i += tpe) {
+      double acc[3 + D];
+#pragma unroll
+      for (int c = 0; c < PS; ++c) acc[c] = 0.0;
+      for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
+        const int inc = op.vp_inc[q];
+        const int pidx = inc >> 1;
+        if (pidx < c0) continue;
+        if (pidx >= c1) break;
+        const double *slot = buf + (size_t)(pidx - c0) * 2 * PS + ((inc & 1) ? 0 : PS);
+#pragma unroll
+        for (int c = 0; c < PS; ++c) acc[c] += slot[c];
+      }
+#pragma unroll
+      for (int c = 0; c < PS; ++c) Pb[(size_t)i * PS + c] += acc[c];
+    }
+    __syncthreads();
+  }
+
+  // facet correction pairs: dbar_p = -rbar[i] - fbar_f[j]
+  if (op.nfp > 0) {
+    const double *hnf = g.halfnJf + (size_t)kk * D * nf;
+    for (int c0 = 0; c0 < op.nfp; c0 += CH) {
+      const int c1 = min(op.nfp, c0 + CH);
+      for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+        const int ij = op.fp_ij[pidx];
+        const int i = ij & 0xffff, j = ij >> 16;
+        const int f = j / npf;
+        const double Cij = op.fp_C[pidx];
+        double G[D], db[NC];
+#pragma unroll
+        for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+#pragma unroll
+        for (int e = 0; e < NC; ++e) db[e] = -rb[e * nq + i] - fb[e * nf + j];
+        double *slot = buf + (size_t)(pidx - c0) * 2 * PS;
+        ec_flux_dot_bwd<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, db, slot,
+                           slot + PS);
+      }
+      __syncthreads();
+      for (int t = lane; t < nq + nf; t += tpe) {
+        const bool vol = t < nq;
+        const int r = vol ? t : t - nq;
+        const int *ptr = vol ? op.fp_q_ptr : op.fp_f_ptr;
+        const int *lst = vol ? op.fp_q : op.fp_f;
+        double acc[3 + D];
+#pragma unroll
+        for (int c = 0; c < PS; ++c) acc[c] = 0.0;
+        for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+          const int pidx = lst[q];
+          if (pidx < c0) continue;
+          if (pidx >= c1) break;
+          const double *slot = buf + (size_t)(pidx - c0) * 2 * PS + (vol ? 0 : PS);
+#pragma unroll
+          for (int c = 0; c < PS; ++c) acc[c] += slot[c];
+        }
+#pragma unroll
+        for (int c = 0; c < PS; ++c) Pb[(size_t)t * PS + c] += acc[c];
+      }
+      __syncthreads();
+    }
+  }
+
+  // primitive cotangents -> conservative cotangents of u_q and u_f
+  if (live) {
+    for (int t = lane; t < nq + nf; t += tpe) {
+      const bool vol = t < nq;
+      const int r = vol ? t : t - nq;
+      double u[NC], ub[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        u[e] = vol ? uq[e * nq + r] : uf[e * nf + r];
+        ub[e] = vol ? 0.0 : ubd[e * nf + r];
+      }
+      euler_prim_bwd<D>(ph.gm1, u, prim + (size_t)t * PS, Pb + (size_t)t * PS, ub);
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        if (vol) ka.ubar_q[(size_t)kk * NC * nq + e * nq + r] = ub[e];
+        else ka.ubar_f[((size_t)kk * NC + e) * nf + r] = ub[e];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// transpose of the entropy projection (flux_differencing_form.jl:190-250)
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const Layout &L = ka.layAdjA;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3],
+         *F = base + L.off[4], *Uq0 = base + L.off[5], *Wq = base + L.off[6], *Wf = base + L.off[7],
+         *Bq = base + L.off[8], *Bf = base + L.off[9];
+  const double *WJ = ka.geo.WJ + (size_t)kk * nq;
+  const double *JinvW = ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr;
+
+  // ---- forward recompute
+  for (int t = lane; t < NC * np; t += tpe) X[t] = ka.u[(size_t)kk * NC * np + t];
+  __syncthreads();
+  vdm_mul<double, D, NC>(op, X, Uq0, Z, Wb, lane, tpe);  // u_q0 = V u (= u for nodal)
+  for (int i = lane; i < nq; i += tpe) {
+    double ui[NC], wi[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) ui[e] = Uq0[e * nq + i];
+    cons_to_entropy_fast<D>(ph.gamma, ph.gm1, ph.igm1, ui, wi);
+    const double s = op.has_vdm ? WJ[i] : 1.0;
+#pragma unroll
+    for (int e = 0; e < NC; ++e) X[e * nq + i] = wi[e] * s;
+  }
+  __syncthreads();
+  if (op.has_vdm) {
+    vdm_tmul<double, D, NC>(op, X, F, Z, Wb, lane, tpe);
+    mass_solve<double, D, NC>(op, JinvW, nullptr, 1, F, X, Z, Wb, lane, tpe);
+    vdm_mul<double, D, NC>(op, F, Wq, Z, Wb, lane, tpe);  // projected w_q
+  } else {
+    for (int t = lane; t < NC * nq; t += tpe) Wq[t] = X[t];
+    __syncthreads();
+  }
+  csr_mul<double, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, Wq, Wf, lane, tpe);
+  for (int t = lane; t < NC * nq; t += tpe) Bq[t] = ka.ubar_q[(size_t)kk * NC * nq + t];
+  for (int t = lane; t < NC * nf; t += tpe) Bf[t] = ka.ubar_f[(size_t)kk * NC * nf + t];
+  __syncthreads();
+
+  // ---- backward
+  // facet: wbar_f = J_e2c(w_f)^T ubar_f
+  for (int j = lane; j < nf; j += tpe) {
+    double wi[NC], bi[NC], ri[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) { wi[e] = Wf[e * nf + j]; bi[e] = Bf[e * nf + j]; }
+    entropy_to_cons_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, bi, ri);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) Bf[e * nf + j] = ri[e];
+  }
+  if (op.has_vdm) {
+    // volume: wbar_q = J_e2c(w_q)^T ubar_q
+    for (int i = lane; i < nq; i += tpe) {
+      double wi[NC], bi[NC], ri[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) { wi[e] = Wq[e * nq + i]; bi[e] = Bq[e * nq + i]; }
+      entropy_to_cons_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, bi, ri);
+#pragma unroll
+      for (int e = 0; e < NC; ++e) Bq[e * nq + i] = ri[e];
+    }
+  }
+  __syncthreads();
+  // wbar_q += R^T wbar_f   (into Y)
+  for (int t = lane; t < NC * nq; t += tpe) {
+    const int i = t % nq, e = t / nq;
+    double acc = 0.0;
+    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * Bf[e * nf + op.Rt_idx[q]];
+    Y[t] = op.has_vdm ? Bq[t] + acc : acc;
+  }
+  __syncthreads();
+  if (op.has_vdm) {
+    // w_q = V M V^T (WJ c2e(u_q0))  =>  wbar_c2e = WJ .* V M V^T wbar_q
+    vdm_tmul<double, D, NC>(op, Y, F, Z, Wb, lane, tpe);
+    mass_solve<double, D, NC>(op, JinvW, nullptr, 1, F, X, Z, Wb, lane, tpe);
+    vdm_mul<double, D, NC>(op, F, Y, Z, Wb, lane, tpe);
+    for (int t = lane; t < NC * nq; t += tpe) Y[t] *= WJ[t % nq];
+    __syncthreads();
+  }
+  // ubar_q0 = J_c2e(u_q0)^T wbar
+  for (int i = lane; i < nq; i += tpe) {
+    double ui[NC], bi[NC], ri[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) { ui[e] = Uq0[e * nq + i]; bi[e] = Y[e * nq + i]; }
+    cons_to_entropy_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ui, bi, ri);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) Y[e * nq + i] = op.has_vdm ? ri[e] : ri[e] + Bq[e * nq + i];
+  }
+  __syncthreads();
+  vdm_tmul<double, D, NC>(op, Y, F, Z, Wb, lane, tpe);  // mu = V^T ubar_q0
+  if (live)
+    for (int t = lane; t < NC * np; t += tpe) ka.mu[(size_t)kk * NC * np + t] = F[t];
+}
+
+// ---------------------------------------------------------------------------
+// elementwise pieces of the adjoint Runge-Kutta sweep
+//
+// CarpenterKennedy2N54 stage s (forward: tmp = a_s tmp + dt k_s, u += b_s tmp,
+// k_s = R(u_s)) reversed, with ybar the state adjoint and qbar the adjoint of
+// tmp after the stage:
+//   qbar += b_s ybar  (done by the previous reversal, or at the step's start)
+//   ybar += dt (dR/du(u_s))^T qbar   <- mu
+//   qbar  = a_s qbar + b_{s-1} ybar   (b_{-1} = 0, a_1 = 0 ends the step)
+__global__ void adj_ck_stage_kernel(double *__restrict__ ybar, double *__restrict__ qbar,
+                                    const double *__restrict__ mu, double dt, double a, double b_prev,
+                                    size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double y = fma(dt, mu[i], ybar[i]);
+    ybar[i] = y;
+    qbar[i] = fma(a, qbar[i], b_prev * y);
+  }
+}
+
+// y = beta x  (alpha == 0, y not read)  or  y = alpha y + beta x
+__global__ void adj_lincomb_kernel(double *__restrict__ y, const double *__restrict__ x, double alpha,
+                                   double beta, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = alpha == 0.0 ? beta * x[i] : fma(alpha, y[i], beta * x[i]);
+}
+
+// classic RK4 stage reversed: ybar += mu ; kbar = cy ybar' + cm mu (not on the last)
+__global__ void adj_rk4_stage_kernel(double *__restrict__ ybar, double *__restrict__ kbar,
+                                     const double *__restrict__ mu, const double *__restrict__ yp,
+                                     double cy, double cm, int last, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double m = mu[i];
+    ybar[i] += m;
+    if (!last) kbar[i] = fma(cy, yp[i], cm * m);
+  }
+}
+
+static int grid_for(size_t n) {
+  size_t g = (n + 255) / 256;
+  return (int)(g > 152 * 16 ? 152 * 16 : (g < 1 ? 1 : g));
+}
+
+cudaError_t launch_adj_ck_stage(double *ybar, double *qbar, const double *mu, double dt, double a,
+                                double b_prev, size_t n, cudaStream_t st) {
+  adj_ck_stage_kernel<<<grid_for(n), 256, 0, st>>>(ybar, qbar, mu, dt, a, b_prev, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_lincomb(double *y, const double *x, double alpha, double beta, size_t n,
+                               cudaStream_t st) {
+  adj_lincomb_kernel<<<grid_for(n), 256, 0, st>>>(y, x, alpha, beta, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_rk4_stage(double *ybar, double *kbar, const double *mu, const double *yp,
+                                 double cy, double cm, int last, size_t n, cudaStream_t st) {
+  adj_rk4_stage_kernel<<<grid_for(n), 256, 0, st>>>(ybar, kbar, mu, yp, cy, cm, last, n);
+  return cudaGetLastError();
+}
+
+cudaError_t sse_set_smem_limits_adjoint(const KernelArgs &ka) {
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void *f, const Layout &L) {
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)((size_t)ka.epb * L.team_doubles * sizeof(double)));
+  };
+  if (ka.op.d == 2 && ka.op.nc == 4) {
+    set((const void *)adj_lift_kernel<2, 4>, ka.layAdjB1);
+    set((const void *)adj_flux_kernel<2, 4>, ka.layAdjB2);
+    set((const void *)adj_projection_kernel<2, 4>, ka.layAdjA);
+  } else if (ka.op.d == 3 && ka.op.nc == 5) {
+    set((const void *)adj_lift_kernel<3, 5>, ka.layAdjB1);
+    set((const void *)adj_flux_kernel<3, 5>, ka.layAdjB2);
+    set((const void *)adj_projection_kernel<3, 5>, ka.layAdjA);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  return e;
+}
+
+cudaError_t launch_residual_vjp_kernels(const KernelArgs &ka, cudaStream_t st) {
+  const int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  const size_t s1 = (size_t)ka.epb * ka.layAdjB1.team_doubles * sizeof(double);
+  const size_t s2 = (size_t)ka.epb * ka.layAdjB2.team_doubles * sizeof(double);
+  const size_t s3 = (size_t)ka.epb * ka.layAdjA.team_doubles * sizeof(double);
+  if (ka.op.d == 2 && ka.op.nc == 4) {
+    adj_lift_kernel<2, 4><<<grid, ka.tpb, s1, st>>>(ka);
+    adj_flux_kernel<2, 4><<<grid, ka.tpb, s2, st>>>(ka);
+    adj_projection_kernel<2, 4><<<grid, ka.tpb, s3, st>>>(ka);
+  } else if (ka.op.d == 3 && ka.op.nc == 5) {
+    adj_lift_kernel<3, 5><<<grid, ka.tpb, s1, st>>>(ka);
+    adj_flux_kernel<3, 5><<<grid, ka.tpb, s2, st>>>(ka);
+    adj_projection_kernel<3, 5><<<grid, ka.tpb, s3, st>>>(ka);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace sse

@@ -253,6 +253,180 @@ SSE_HD void entropy_to_cons_fast(double gamma, double gm1, double igm1, double l
 }
 
 // ---------------------------------------------------------------------------
+// Reverse-mode derivatives (discrete adjoint of the FP64 residual).  Each
+// function below is the hand-written transpose of the forward function of
+// the same name above; tests/device_math_check.cu checks them against
+// central differences.
+// ---------------------------------------------------------------------------
+
+// partial derivatives of logmean_fast(x, y)
+SSE_HD void logmean_fast_grad(double x, double y, double *dx, double *dy) {
+  const double s = x + y;
+  const double r = sse_rcp(s);
+  const double f = (x - y) * r;
+  const double z = f * f;
+  if (z < 1.0e-4) {
+    const double P = fma(z, fma(z, fma(z, kInvQ3, kInvQ2), kInvQ1), 1.0);
+    const double dP = fma(z, fma(z, 3.0 * kInvQ3, 2.0 * kInvQ2), kInvQ1);
+    const double c = 0.5 * s * dP * 4.0 * f * r * r;  // (s/2) P'(z) * 4 f / s^2
+    *dx = 0.5 * P + c * y;
+    *dy = 0.5 * P - c * x;
+    return;
+  }
+  const double N = y - x, Dl = log(y / x);
+  const double iD2 = 1.0 / (Dl * Dl);
+  *dx = (-Dl + N / x) * iD2;
+  *dy = (Dl - N / y) * iD2;
+}
+
+// partial derivatives of inv_logmean_fast(x, y)
+SSE_HD void inv_logmean_fast_grad(double x, double y, double *dx, double *dy) {
+  const double s = x + y;
+  const double r = sse_rcp(s);
+  const double f = (x - y) * r;
+  const double z = f * f;
+  if (z < 1.0e-4) {
+    const double Q = fma(z, fma(z, fma(z, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+    const double dQ = fma(z, fma(z, 3.0 / 7.0, 0.4), 1.0 / 3.0);
+    const double base = -2.0 * r * r * Q;
+    const double c = 2.0 * r * dQ * 4.0 * f * r * r;
+    *dx = base + c * y;
+    *dy = base - c * x;
+    return;
+  }
+  const double N = y - x, Dl = log(y / x);
+  const double iN2 = 1.0 / (N * N);
+  *dx = (Dl - N / x) * iN2;
+  *dy = (N / y - Dl) * iN2;
+}
+
+// Transpose of ec_flux_dot with respect to the two primitive vectors:
+// given ob = d(objective)/d(out), returns Pbi, Pbj (layout [rho, p, beta, V]).
+template <int D>
+SSE_HD void ec_flux_dot_bwd(double igm1, const double *Pi, const double *Pj, const double *G,
+                            const double *ob, double *Pbi, double *Pbj) {
+  const double rho_hat = logmean_fast(Pi[0], Pj[0]);
+  const double ilm = inv_logmean_fast(Pi[2], Pj[2]);
+  double vs[D];
+  double vv = 0.0, gvs = 0.0, gvi = 0.0, gvj = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    vs[m] = Pi[3 + m] + Pj[3 + m];
+    vv = fma(Pi[3 + m], Pj[3 + m], vv);
+    gvs = fma(G[m], vs[m], gvs);
+    gvi = fma(G[m], Pi[3 + m], gvi);
+    gvj = fma(G[m], Pj[3 + m], gvj);
+  }
+  const double f0 = 0.5 * rho_hat * gvs;
+  const double C = fma(igm1, ilm, 0.5 * vv);
+  const double t = 0.5 * f0;
+  const double oE = ob[D + 1];
+  // reverse sweep
+  double ovs_dot = 0.0, pbar_b = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    ovs_dot = fma(ob[1 + m], vs[m], ovs_dot);
+    pbar_b = fma(ob[1 + m], G[m], pbar_b);
+  }
+  const double f0b = ob[0] + C * oE + 0.5 * ovs_dot;
+  const double Cb = oE * f0;
+  const double gvjb = 0.5 * oE * Pi[1];
+  const double gvib = 0.5 * oE * Pj[1];
+  const double gvsb = 0.5 * rho_hat * f0b;
+  const double rhob = 0.5 * gvs * f0b;
+  const double ilmb = igm1 * Cb;
+  const double vvb = 0.5 * Cb;
+  double dlx, dly, dix, diy;
+  logmean_fast_grad(Pi[0], Pj[0], &dlx, &dly);
+  inv_logmean_fast_grad(Pi[2], Pj[2], &dix, &diy);
+  Pbi[0] = rhob * dlx;
+  Pbj[0] = rhob * dly;
+  Pbi[1] = 0.5 * pbar_b + 0.5 * oE * gvj;
+  Pbj[1] = 0.5 * pbar_b + 0.5 * oE * gvi;
+  Pbi[2] = ilmb * dix;
+  Pbj[2] = ilmb * diy;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    const double vsb = fma(t, ob[1 + m], G[m] * gvsb);
+    Pbi[3 + m] = vsb + Pj[3 + m] * vvb + G[m] * gvib;
+    Pbj[3 + m] = vsb + Pi[3 + m] * vvb + G[m] * gvjb;
+  }
+}
+
+// Transpose of euler_prim_fast: accumulate ub += (dP/du)^T Pb.
+template <int D>
+SSE_HD void euler_prim_bwd(double gm1, const double *u, const double *P, const double *Pb, double *ub) {
+  const double rho = P[0], p = P[1];
+  const double rr = sse_rcp(rho);
+  const double pb = Pb[1] - Pb[2] * rho / (p * p);
+  double v2 = 0.0, vvb = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    v2 = fma(P[3 + m], P[3 + m], v2);
+    vvb = fma(Pb[3 + m], P[3 + m], vvb);
+  }
+  ub[0] += Pb[0] + Pb[2] / p + 0.5 * gm1 * pb * v2 - vvb * rr;
+#pragma unroll
+  for (int m = 0; m < D; ++m) ub[m + 1] += fma(-gm1 * pb, P[3 + m], Pb[3 + m] * rr);
+  ub[D + 1] += gm1 * pb;
+  (void)u;
+}
+
+// Directional derivative of cons_to_entropy_fast at u along du.  The map is
+// the gradient of the entropy function, so its Jacobian is symmetric and
+// this is also the transpose product.
+template <int D>
+SSE_HD void cons_to_entropy_jvp(double gamma, double gm1, double igm1, const double *u,
+                                const double *du, double *dw) {
+  const double rho = u[0], rr = sse_rcp(rho);
+  double s = 0.0, vdm = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    s = fma(u[m + 1], u[m + 1], s);
+    vdm = fma(u[m + 1] * rr, du[m + 1], vdm);
+  }
+  const double k = 0.5 * s * rr;
+  const double dk = vdm - 0.5 * s * rr * rr * du[0];
+  const double p = gm1 * (u[D + 1] - k);
+  const double dp = gm1 * (du[D + 1] - dk);
+  const double ip = sse_rcp(p);
+  dw[0] = -igm1 * (dp * ip - gamma * du[0] * rr) - (dk * ip - k * dp * ip * ip);
+#pragma unroll
+  for (int m = 0; m < D; ++m) dw[m + 1] = du[m + 1] * ip - u[m + 1] * dp * ip * ip;
+  dw[D + 1] = -du[0] * ip + rho * dp * ip * ip;
+}
+
+// Directional derivative of entropy_to_cons_fast at w along dw (symmetric
+// Jacobian: the inverse of the entropy Hessian).
+template <int D>
+SSE_HD void entropy_to_cons_jvp(double gamma, double gm1, double igm1, double log_gm1,
+                                const double *w_in, const double *dw_in, double *du) {
+  double w[D + 2], dw[D + 2];
+#pragma unroll
+  for (int e = 0; e < D + 2; ++e) {
+    w[e] = w_in[e] * gm1;
+    dw[e] = dw_in[e] * gm1;
+  }
+  double s = 0.0, ds = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    s = fma(w[m + 1], w[m + 1], s);
+    ds = fma(w[m + 1], dw[m + 1], ds);
+  }
+  const double iwE = sse_rcp(w[D + 1]);
+  const double k = 0.5 * s * iwE;
+  const double dk = ds * iwE - k * dw[D + 1] * iwE;
+  const double sv = gamma - w[0] + k;
+  const double dsv = -dw[0] + dk;
+  const double rhoe = exp(igm1 * (log_gm1 - gamma * log(-w[D + 1]) - sv));
+  const double drhoe = rhoe * igm1 * (-gamma * dw[D + 1] * iwE - dsv);
+  du[0] = -dw[D + 1] * rhoe - w[D + 1] * drhoe;
+#pragma unroll
+  for (int m = 0; m < D; ++m) du[m + 1] = dw[m + 1] * rhoe + w[m + 1] * drhoe;
+  du[D + 1] = drhoe * (1 - k) - rhoe * dk;
+}
+
+// ---------------------------------------------------------------------------
 // Mixed form: FP32 arithmetic on perturbations u' = u - u_ref from a constant
 // reference state u_ref = (rho_ref, 0, ..., 0, E_ref) with p_ref =
 // (gamma - 1) E_ref.  At Mach 0.1 the pressure (~71) exceeds its fluctuations

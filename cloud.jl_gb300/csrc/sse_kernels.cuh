@@ -30,6 +30,15 @@ struct KernelArgs {
   float *u_ff;       // mixed form: FP32 perturbations of u_f
   int mixed;         // 1: phase A writes u_qf/u_ff and phase B runs in FP32
   int *flag;         // nonzero: non-physical state met
+  // discrete adjoint (vector-Jacobian product of the FP64 residual)
+  const double *lam; // cotangent of dudt            (np x nc x ne)
+  double *mu;        // result (dR/du)^T lam          (np x nc x ne)
+  double *rbar_q;    // adjoint of r_q                (nq x nc x ne)
+  double *gbar_f;    // adjoint of the interface flux  (nf x nc x ne, element-major)
+  double *ubar_q;    // adjoint of u_q                (nq x nc x ne)
+  double *ubar_f;    // adjoint of u_f                (nf x nc x ne, element-major)
+  Layout layAdjB1, layAdjB2, layAdjA;
+  int pair_chunk;    // pairs per shared-memory chunk in the pair-adjoint passes
 
   __device__ __forceinline__ void flag_nonphysical() const { atomicOr(flag, 1); }
 };
@@ -52,5 +61,15 @@ cudaError_t launch_rk4_final(double *u, const double *acc, const double *k, doub
                              cudaStream_t st);
 cudaError_t launch_facet_layout(const double *in, double *out, int nf, int ne, int nc,
                                 cudaStream_t st);
+
+// discrete adjoint (sse_adjoint.cu)
+cudaError_t sse_set_smem_limits_adjoint(const KernelArgs &ka);
+cudaError_t launch_residual_vjp_kernels(const KernelArgs &ka, cudaStream_t st);
+cudaError_t launch_adj_ck_stage(double *ybar, double *qbar, const double *mu, double dt, double a,
+                                double b_prev, size_t n, cudaStream_t st);
+cudaError_t launch_adj_lincomb(double *y, const double *x, double alpha, double beta, size_t n,
+                               cudaStream_t st);
+cudaError_t launch_adj_rk4_stage(double *ybar, double *kbar, const double *mu, const double *yp,
+                                 double cy, double cm, int last, size_t n, cudaStream_t st);
 
 }  // namespace sse

@@ -23,7 +23,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "libsse_gb300.so")
 
 EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual",
             "sse_residual_static_scratch", "sse_nodal_values",
-            "sse_rk_steps", "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
+            "sse_rk_steps", "sse_residual_vjp", "sse_rk_record", "sse_rk_adjoint",
+            "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
             "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
             "sse_create_error"]
 
@@ -59,6 +60,12 @@ def load_library(path: str | None = None):
     L.sse_nodal_values.restype = i32
     L.sse_rk_steps.argtypes = [vp, vp, i32, dp, i32, C.POINTER(dp), i32]
     L.sse_rk_steps.restype = i32
+    L.sse_residual_vjp.argtypes = [vp, vp, vp, vp, i32]
+    L.sse_residual_vjp.restype = i32
+    L.sse_rk_record.argtypes = [vp, vp, i32, dp, i32, i32, C.POINTER(dp), i32]
+    L.sse_rk_record.restype = i32
+    L.sse_rk_adjoint.argtypes = [vp, vp, vp, vp, i32]
+    L.sse_rk_adjoint.restype = i32
     L.sse_conservation_residual.argtypes = [vp, vp, vp, vp, i32]
     L.sse_conservation_residual.restype = i32
     L.sse_set_precision.argtypes = [vp, i32]
@@ -142,6 +149,39 @@ class GB300Solver:
         tt = C.c_double(t)
         self._check(self.L.sse_rk_steps(self.h, pu, n_steps, dt, scheme, C.byref(tt), mu))
         return tt.value
+
+    def residual_vjp(self, u, lam, mu=None):
+        """(dR/du)^T lam at u: the discrete adjoint of ``residual``."""
+        if mu is None:
+            mu = np.empty_like(u) if isinstance(u, np.ndarray) else u.new_empty(u.shape)
+        pu, mu_u = _addr(u)
+        pl, mu_l = _addr(lam)
+        pm, mu_m = _addr(mu)
+        assert mu_u == mu_l == mu_m, "u, lam and mu must live in the same memory"
+        self._check(self.L.sse_residual_vjp(self.h, pu, pl, pm, mu_u))
+        return mu
+
+    def rk_record(self, u, n_steps: int, dt: float, scheme: int = abi.SSE_CARPENTER_KENNEDY_2N54,
+                  checkpoint_every: int = 0, t: float = 0.0) -> float:
+        """``rk_steps`` that records checkpoints for ``rk_adjoint``."""
+        pu, mu = _addr(u)
+        tt = C.c_double(t)
+        self._check(self.L.sse_rk_record(self.h, pu, n_steps, dt, scheme, checkpoint_every,
+                                         C.byref(tt), mu))
+        return tt.value
+
+    def rk_adjoint(self, lam_T, lam_0=None) -> dict:
+        """(du(T)/du(0))^T lam_T for the last ``rk_record``; returns
+        {"lam_0", "segments", "checkpoint_every", "bytes"}."""
+        if lam_0 is None:
+            lam_0 = np.empty_like(lam_T) if isinstance(lam_T, np.ndarray) else lam_T.new_empty(lam_T.shape)
+        pl, ml = _addr(lam_T)
+        p0, m0 = _addr(lam_0)
+        assert ml == m0
+        info = np.zeros(3)
+        self._check(self.L.sse_rk_adjoint(self.h, pl, p0, C.c_void_p(info.ctypes.data), ml))
+        return {"lam_0": lam_0, "segments": int(info[0]), "checkpoint_every": int(info[1]),
+                "bytes": int(info[2])}
 
     def conservation_residual(self, u, dudt) -> np.ndarray:
         out = np.zeros(self.host.N_c + 1)

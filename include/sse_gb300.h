@@ -181,6 +181,38 @@ int32_t sse_nodal_values(sse_solver *s, const double *u, double *u_q, double *u_
 int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt,
                      int32_t scheme, double *t, int32_t memory);
 
+/* Discrete adjoint of the FP64 residual: mu <- (dR/du)^T lam at the state u
+ * (all three N_p x N_c x N_e, host or device).  Covers FluxDifferencingForm
+ * with the entropy-conservative two-point flux (Euler) and any of the three
+ * interface fluxes; other configurations return SSE_ERR_UNSUPPORTED.  The
+ * vector-Jacobian product of semi_discrete_residual!; no counterpart in the
+ * reference, whose residual is typed Float64 throughout and has no AD or
+ * adjoint code (Solvers.jl:474-514). */
+int32_t sse_residual_vjp(sse_solver *s, const double *u, const double *lam, double *mu,
+                         int32_t memory);
+
+/* sse_rk_steps that also records the trajectory for sse_rk_adjoint: the
+ * state at every checkpoint_every-th step (and the compensation term in
+ * SSE_MIXED) is kept in device memory owned by the handle, replacing the
+ * previous recording.  checkpoint_every = 0 picks the interval that
+ * minimises checkpoint plus one segment's stage storage.  Fails with
+ * SSE_ERR_OUT_OF_MEMORY (nothing advanced) when the recording does not fit
+ * in free device memory.  The forward half of the stepper's rrule; no
+ * counterpart in the reference. */
+int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme,
+                      int32_t checkpoint_every, double *t, int32_t memory);
+
+/* Reverse sweep of the last sse_rk_record: lam_0 <- (du(T)/du(0))^T lam_T,
+ * the gradient of J(u(T)) w.r.t. the initial state when lam_T = dJ/du(T)
+ * (both N_p x N_c x N_e, host or device).  Each checkpoint segment is
+ * recomputed once, in the precision it was recorded in, storing its RK
+ * stage states; the stage adjoints use sse_residual_vjp's kernels at those
+ * states.  The recording stays valid for further calls.  out_info, if not
+ * NULL, receives {segments, checkpoint_every, stored stage bytes}.  The
+ * pullback half of the stepper's rrule; no counterpart in the reference. */
+int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double *out_info,
+                       int32_t memory);
+
 /* FP64 reductions of Analysis/conservation.jl:145-189 for one (u, dudt):
  * out[0..N_c-1] = sum_k 1' WJ V dudt[:, e, k]       (primary conservation)
  * out[N_c]      = sum_k (P w)' M dudt               (entropy production, Euler)

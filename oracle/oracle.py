@@ -114,6 +114,73 @@ class Oracle:
         return out
 
 
+TANGENT_SRC = os.path.join(HERE, "sse_oracle_tangent.cpp")
+
+
+def build_tangent(force: bool = False) -> str:
+    """Compile the dual-number build of the same oracle source (g++ -O3
+    -fopenmp, no contraction beyond the explicit fma() calls)."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = os.path.join(BUILD, "libsse_oracle_tangent.so")
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR), os.path.getmtime(TANGENT_SRC))
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return out
+    cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           TANGENT_SRC, "-o", out + ".tmp", "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+_tangent_lib = None
+
+
+def tangent_lib():
+    global _tangent_lib
+    if _tangent_lib is None:
+        L = C.CDLL(build_tangent())
+        L.oracle_tangent_create.restype = C.c_void_p
+        L.oracle_tangent_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.oracle_tangent_destroy.argtypes = [C.c_void_p]
+        L.oracle_tangent_residual.argtypes = [C.c_void_p] * 5
+        L.oracle_tangent_rk_steps.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                              C.c_double, C.c_int]
+        _tangent_lib = L
+    return _tangent_lib
+
+
+class TangentOracle:
+    """Forward-mode derivatives of the oracle: J(u) v and the tangent of a
+    whole fixed-step trajectory (dual numbers through sse_oracle.c)."""
+
+    def __init__(self, host, nthreads: int | None = None):
+        self.L = tangent_lib()
+        self.host = host
+        self.h = self.L.oracle_tangent_create(C.byref(host.cfg), C.byref(host.ops), C.byref(host.geo),
+                                              nthreads or lib().oracle_threads())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.oracle_tangent_destroy(self.h)
+            self.h = None
+
+    def jvp(self, u: np.ndarray, v: np.ndarray):
+        """(R(u), J(u) v)."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        assert u.shape == v.shape == self.host.state_shape
+        r, jv = np.empty_like(u), np.empty_like(u)
+        self.L.oracle_tangent_residual(self.h, _ptr(u), _ptr(v), _ptr(r), _ptr(jv))
+        return r, jv
+
+    def rk_jvp(self, u: np.ndarray, v: np.ndarray, n_steps: int, dt: float, scheme: int = 0):
+        """(u(T), (du(T)/du(0)) v)."""
+        u = np.array(u, dtype=np.float64, order="C", copy=True)
+        v = np.array(v, dtype=np.float64, order="C", copy=True)
+        self.L.oracle_tangent_rk_steps(self.h, _ptr(u), _ptr(v), n_steps, dt, scheme)
+        return u, v
+
+
 def rel2(got, want) -> float:
     """Whole-vector relative error ||got - want||_2 / ||want||_2."""
     got = np.asarray(got, dtype=np.float64)

@@ -41,12 +41,21 @@
 #define MAXC 5
 #define MAXD 3
 
+/* Scalar type of every state-dependent quantity: double here.  The tangent
+ * build (sse_oracle_tangent.cpp) compiles this same file as C++ with a
+ * dual-number type, so its derivatives are those of exactly this
+ * restatement.  Operator and geometry values stay double. */
+#ifndef SSE_ORACLE_REAL
+#define SSE_ORACLE_REAL double
+#endif
+typedef SSE_ORACLE_REAL sse_real;
+
 typedef struct {
   sse_config cfg;
   sse_operators ops;
   sse_geometry geo;
-  double *u_q; /* N_q x N_c x N_e */
-  double *u_f; /* N_f x N_e x N_c */
+  sse_real *u_q; /* N_q x N_c x N_e */
+  sse_real *u_f; /* N_f x N_e x N_c */
   int nthreads;
 } oracle_t;
 
@@ -55,19 +64,19 @@ typedef struct {
 /* ------------------------------------------------------------------ */
 
 /* y = A x (CSC), y zeroed first */
-static void csc_mul(const sse_csc *A, const double *x, double *y) {
+static void csc_mul(const sse_csc *A, const sse_real *x, sse_real *y) {
   for (int64_t i = 0; i < A->m; ++i) y[i] = 0.0;
   for (int64_t j = 0; j < A->n; ++j) {
-    double xj = x[j];
+    sse_real xj = x[j];
     for (int64_t ii = A->colptr[j] - 1; ii < A->colptr[j + 1] - 1; ++ii)
       y[A->rowval[ii] - 1] += A->nzval[ii] * xj;
   }
 }
 
 /* y = A^T x (CSC) */
-static void csc_tmul(const sse_csc *A, const double *x, double *y) {
+static void csc_tmul(const sse_csc *A, const sse_real *x, sse_real *y) {
   for (int64_t j = 0; j < A->n; ++j) {
-    double acc = 0.0;
+    sse_real acc = 0.0;
     for (int64_t ii = A->colptr[j] - 1; ii < A->colptr[j + 1] - 1; ++ii)
       acc += A->nzval[ii] * x[A->rowval[ii] - 1];
     y[j] = acc;
@@ -76,16 +85,16 @@ static void csc_tmul(const sse_csc *A, const double *x, double *y) {
 
 /* V x for the warped tensor-product Vandermonde; x has N_p entries, y N_q.
  * warped_product_2d.jl:31-55, warped_product_3d.jl:47-84 */
-static void vdm_mul(const oracle_t *o, const double *x, double *y) {
+static void vdm_mul(const oracle_t *o, const sse_real *x, sse_real *y) {
   const sse_operators *op = &o->ops;
-  if (!op->vdm_A) { memcpy(y, x, sizeof(double) * o->cfg.n_q); return; }
+  if (!op->vdm_A) { memcpy(y, x, sizeof(sse_real) * o->cfg.n_q); return; }
   const int p1 = op->vdm_p + 1;
   const int M1 = op->vdm_m[0], M2 = op->vdm_m[1], M3 = op->vdm_m[2];
   if (o->cfg.d == 2) {
-    double Z[16 * 16];
+    sse_real Z[16 * 16];
     for (int a2 = 0; a2 < M2; ++a2)
       for (int b1 = 0; b1 < p1; ++b1) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int b2 = 0; b2 < p1 - b1; ++b2) {
           int64_t l = op->vdm_sigma_in[b1 + p1 * b2] - 1;
           t = fma(op->vdm_B[a2 + M2 * (b1 + p1 * b2)], x[l], t);
@@ -94,17 +103,17 @@ static void vdm_mul(const oracle_t *o, const double *x, double *y) {
       }
     for (int a1 = 0; a1 < M1; ++a1)
       for (int a2 = 0; a2 < M2; ++a2) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int b1 = 0; b1 < p1; ++b1) t = fma(op->vdm_A[a1 + M1 * b1], Z[b1 + p1 * a2], t);
         y[M2 * a1 + a2] = t;
       }
     return;
   }
-  double Z[8 * 8 * 8], W[8 * 8 * 8];
+  sse_real Z[8 * 8 * 8], W[8 * 8 * 8];
   for (int b1 = 0; b1 < p1; ++b1)
     for (int b2 = 0; b2 < p1 - b1; ++b2)
       for (int a3 = 0; a3 < M3; ++a3) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int b3 = 0; b3 < p1 - b1 - b2; ++b3) {
           int64_t l = op->vdm_sigma_in[b1 + p1 * (b2 + p1 * b3)] - 1;
           t = fma(op->vdm_C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], x[l], t);
@@ -114,7 +123,7 @@ static void vdm_mul(const oracle_t *o, const double *x, double *y) {
   for (int b1 = 0; b1 < p1; ++b1)
     for (int a2 = 0; a2 < M2; ++a2)
       for (int a3 = 0; a3 < M3; ++a3) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int b2 = 0; b2 < p1 - b1; ++b2)
           t = fma(op->vdm_B[a2 + M2 * (b1 + p1 * b2)], Z[b1 + p1 * (b2 + p1 * a3)], t);
         W[b1 + p1 * (a2 + M2 * a3)] = t;
@@ -122,39 +131,39 @@ static void vdm_mul(const oracle_t *o, const double *x, double *y) {
   for (int a1 = 0; a1 < M1; ++a1)
     for (int a2 = 0; a2 < M2; ++a2)
       for (int a3 = 0; a3 < M3; ++a3) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int b1 = 0; b1 < p1; ++b1) t = fma(op->vdm_A[a1 + M1 * b1], W[b1 + p1 * (a2 + M2 * a3)], t);
         y[M2 * M3 * a1 + M3 * a2 + a3] = t;
       }
 }
 
 /* V^T x; warped_product_2d.jl:61-89, warped_product_3d.jl:94-136 */
-static void vdm_tmul(const oracle_t *o, const double *x, double *y) {
+static void vdm_tmul(const oracle_t *o, const sse_real *x, sse_real *y) {
   const sse_operators *op = &o->ops;
-  if (!op->vdm_A) { memcpy(y, x, sizeof(double) * o->cfg.n_q); return; }
+  if (!op->vdm_A) { memcpy(y, x, sizeof(sse_real) * o->cfg.n_q); return; }
   const int p1 = op->vdm_p + 1;
   const int M1 = op->vdm_m[0], M2 = op->vdm_m[1], M3 = op->vdm_m[2];
   if (o->cfg.d == 2) {
-    double Z[16 * 16];
+    sse_real Z[16 * 16];
     for (int b1 = 0; b1 < p1; ++b1)
       for (int a2 = 0; a2 < M2; ++a2) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int a1 = 0; a1 < M1; ++a1) t = fma(op->vdm_A[a1 + M1 * b1], x[M2 * a1 + a2], t);
         Z[b1 + p1 * a2] = t;
       }
     for (int b1 = 0; b1 < p1; ++b1)
       for (int b2 = 0; b2 < p1 - b1; ++b2) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int a2 = 0; a2 < M2; ++a2) t = fma(op->vdm_B[a2 + M2 * (b1 + p1 * b2)], Z[b1 + p1 * a2], t);
         y[op->vdm_sigma_in[b1 + p1 * b2] - 1] = t;
       }
     return;
   }
-  double Z[8 * 8 * 8], W[8 * 8 * 8];
+  sse_real Z[8 * 8 * 8], W[8 * 8 * 8];
   for (int b1 = 0; b1 < p1; ++b1)
     for (int a2 = 0; a2 < M2; ++a2)
       for (int a3 = 0; a3 < M3; ++a3) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int a1 = 0; a1 < M1; ++a1)
           t = fma(op->vdm_A[a1 + M1 * b1], x[M2 * M3 * a1 + M3 * a2 + a3], t);
         W[b1 + p1 * (a2 + M2 * a3)] = t;
@@ -162,7 +171,7 @@ static void vdm_tmul(const oracle_t *o, const double *x, double *y) {
   for (int b1 = 0; b1 < p1; ++b1)
     for (int b2 = 0; b2 < p1 - b1; ++b2)
       for (int a3 = 0; a3 < M3; ++a3) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int a2 = 0; a2 < M2; ++a2)
           t = fma(op->vdm_B[a2 + M2 * (b1 + p1 * b2)], W[b1 + p1 * (a2 + M2 * a3)], t);
         Z[b1 + p1 * (b2 + p1 * a3)] = t;
@@ -170,7 +179,7 @@ static void vdm_tmul(const oracle_t *o, const double *x, double *y) {
   for (int b1 = 0; b1 < p1; ++b1)
     for (int b2 = 0; b2 < p1 - b1; ++b2)
       for (int b3 = 0; b3 < p1 - b1 - b2; ++b3) {
-        double t = 0.0;
+        sse_real t = 0.0;
         for (int a3 = 0; a3 < M3; ++a3)
           t = fma(op->vdm_C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], Z[b1 + p1 * (b2 + p1 * a3)], t);
         y[op->vdm_sigma_in[b1 + p1 * (b2 + p1 * b3)] - 1] = t;
@@ -182,15 +191,15 @@ static void vdm_tmul(const oracle_t *o, const double *x, double *y) {
 /* ------------------------------------------------------------------ */
 
 /* ConservationLaws.jl:132-145 */
-static double logmean(double x, double y) {
-  double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+static sse_real logmean(sse_real x, sse_real y) {
+  sse_real f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
   if (f2 < 1.0e-4) return (x + y) * 105 / (210 + f2 * (70 + f2 * (42 + f2 * 30)));
   return (y - x) / log(y / x);
 }
 
 /* ConservationLaws.jl:147-156 */
-static double inv_logmean(double x, double y) {
-  double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+static sse_real inv_logmean(sse_real x, sse_real y) {
+  sse_real f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
   if (f2 < 1.0e-4) return (210 + f2 * (70 + f2 * (42 + f2 * 30))) / ((x + y) * 105);
   return log(y / x) / (y - x);
 }
@@ -198,30 +207,30 @@ static double inv_logmean(double x, double y) {
 /* two-point flux tensor F[e + MAXC*n] (e = 0..N_c-1, n = 0..d-1).
  * Euler EC: euler_navierstokes.jl:171-195 (Ranocha); conservative:
  * :152-158; advection: linear_advection_diffusion.jl:113-119. */
-static void two_point_flux(const sse_config *c, int ec, const double *uL, const double *uR,
-                           double *F) {
+static void two_point_flux(const sse_config *c, int ec, const sse_real *uL, const sse_real *uR,
+                           sse_real *F) {
   const int d = c->d;
   if (c->law == SSE_LINEAR_ADVECTION) {
-    double f1 = 0.5 * (uL[0] + uR[0]);
+    sse_real f1 = 0.5 * (uL[0] + uR[0]);
     for (int m = 0; m < d; ++m) F[MAXC * m] = c->a[m] * f1;
     return;
   }
   const double gm1 = c->gamma - 1.0, igm1 = 1.0 / (c->gamma - 1.0);
   const int E = d + 1;
   if (ec) {
-    double VL[MAXD], VR[MAXD], sL = 0.0, sR = 0.0, vv = 0.0;
+    sse_real VL[MAXD], VR[MAXD], sL = 0.0, sR = 0.0, vv = 0.0;
     for (int m = 0; m < d; ++m) { VL[m] = uL[m + 1] / uL[0]; VR[m] = uR[m + 1] / uR[0]; }
     for (int m = 0; m < d; ++m) { sL += VL[m] * VL[m]; sR += VR[m] * VR[m]; }
-    double pL = gm1 * (uL[E] - 0.5 * uL[0] * sL);
-    double pR = gm1 * (uR[E] - 0.5 * uR[0] * sR);
-    double rho_avg = logmean(uL[0], uR[0]);
-    double Vavg[MAXD];
+    sse_real pL = gm1 * (uL[E] - 0.5 * uL[0] * sL);
+    sse_real pR = gm1 * (uR[E] - 0.5 * uR[0] * sR);
+    sse_real rho_avg = logmean(uL[0], uR[0]);
+    sse_real Vavg[MAXD];
     for (int m = 0; m < d; ++m) Vavg[m] = 0.5 * (VL[m] + VR[m]);
-    double pavg = 0.5 * (pL + pR);
+    sse_real pavg = 0.5 * (pL + pR);
     for (int m = 0; m < d; ++m) vv += VL[m] * VR[m];
-    double C = 0.5 * vv + igm1 * inv_logmean(uL[0] / pL, uR[0] / pR);
+    sse_real C = 0.5 * vv + igm1 * inv_logmean(uL[0] / pL, uR[0] / pR);
     for (int n = 0; n < d; ++n) {
-      double frho = rho_avg * Vavg[n];
+      sse_real frho = rho_avg * Vavg[n];
       F[0 + MAXC * n] = frho;
       for (int m = 0; m < d; ++m)
         F[m + 1 + MAXC * n] = rho_avg * Vavg[m] * Vavg[n] + (m == n ? pavg : 0.0);
@@ -230,16 +239,16 @@ static void two_point_flux(const sse_config *c, int ec, const double *uL, const 
     return;
   }
   /* ConservativeFlux: average of physical fluxes (euler_navierstokes.jl:58-68) */
-  const double *us[2] = {uL, uR};
+  const sse_real *us[2] = {uL, uR};
   for (int n = 0; n < d; ++n)
     for (int e = 0; e < d + 2; ++e) F[e + MAXC * n] = 0.0;
   for (int s = 0; s < 2; ++s) {
-    const double *u = us[s];
-    double V[MAXD], sum = 0.0;
+    const sse_real *u = us[s];
+    sse_real V[MAXD], sum = 0.0;
     for (int m = 0; m < d; ++m) V[m] = u[m + 1] / u[0];
     for (int m = 0; m < d; ++m) sum += u[m + 1] * V[m];
-    double p = gm1 * (u[E] - 0.5 * sum);
-    double ht = u[E] + p;
+    sse_real p = gm1 * (u[E] - 0.5 * sum);
+    sse_real ht = u[E] + p;
     for (int n = 0; n < d; ++n) {
       F[0 + MAXC * n] += u[n + 1];
       for (int m = 0; m < d; ++m) F[m + 1 + MAXC * n] += u[m + 1] * V[n] + (m == n ? p : 0.0);
@@ -251,7 +260,7 @@ static void two_point_flux(const sse_config *c, int ec, const double *uL, const 
 }
 
 /* physical flux f[e + MAXC*n] (euler_navierstokes.jl:58-68; advection :54-61) */
-static void physical_flux(const sse_config *c, const double *u, double *F) {
+static void physical_flux(const sse_config *c, const sse_real *u, sse_real *F) {
   const int d = c->d;
   if (c->law == SSE_LINEAR_ADVECTION) {
     for (int m = 0; m < d; ++m) F[MAXC * m] = c->a[m] * u[0];
@@ -259,11 +268,11 @@ static void physical_flux(const sse_config *c, const double *u, double *F) {
   }
   const double gm1 = c->gamma - 1.0;
   const int E = d + 1;
-  double V[MAXD], sum = 0.0;
+  sse_real V[MAXD], sum = 0.0;
   for (int m = 0; m < d; ++m) V[m] = u[m + 1] / u[0];
   for (int m = 0; m < d; ++m) sum += u[m + 1] * V[m];
-  double p = gm1 * (u[E] - 0.5 * sum);
-  double ht = u[E] + p;
+  sse_real p = gm1 * (u[E] - 0.5 * sum);
+  sse_real ht = u[E] + p;
   for (int n = 0; n < d; ++n) {
     F[0 + MAXC * n] = u[n + 1];
     for (int m = 0; m < d; ++m) F[m + 1 + MAXC * n] = u[m + 1] * V[n] + (m == n ? p : 0.0);
@@ -272,7 +281,7 @@ static void physical_flux(const sse_config *c, const double *u, double *F) {
 }
 
 /* euler_navierstokes.jl:133-150; linear_advection_diffusion.jl:106-111 */
-static double wave_speed(const sse_config *c, const double *ui, const double *uo, const double *n) {
+static sse_real wave_speed(const sse_config *c, const sse_real *ui, const sse_real *uo, const double *n) {
   const int d = c->d;
   if (c->law == SSE_LINEAR_ADVECTION) {
     double s = 0.0;
@@ -281,55 +290,55 @@ static double wave_speed(const sse_config *c, const double *ui, const double *uo
   }
   const double gm1 = c->gamma - 1.0;
   const int E = d + 1;
-  double si = 0.0, so = 0.0, vni = 0.0, vno = 0.0;
+  sse_real si = 0.0, so = 0.0, vni = 0.0, vno = 0.0;
   for (int m = 0; m < d; ++m) { si += ui[m + 1] * ui[m + 1]; so += uo[m + 1] * uo[m + 1]; }
-  double pi_ = gm1 * (ui[E] - (0.5 / ui[0]) * si);
-  double po = gm1 * (uo[E] - (0.5 / uo[0]) * so);
+  sse_real pi_ = gm1 * (ui[E] - (0.5 / ui[0]) * si);
+  sse_real po = gm1 * (uo[E] - (0.5 / uo[0]) * so);
   for (int m = 0; m < d; ++m) { vni += (ui[m + 1] / ui[0]) * n[m]; vno += (uo[m + 1] / uo[0]) * n[m]; }
-  double ci = sqrt(c->gamma * pi_ / ui[0]);
-  double co = sqrt(c->gamma * po / uo[0]);
+  sse_real ci = sqrt(c->gamma * pi_ / ui[0]);
+  sse_real co = sqrt(c->gamma * po / uo[0]);
   return fmax(fabs(vni), fabs(vno)) + fmax(ci, co);
 }
 
 /* euler_navierstokes.jl:100-113 */
-static void cons_to_entropy(const sse_config *c, const double *u, double *w) {
+static void cons_to_entropy(const sse_config *c, const sse_real *u, sse_real *w) {
   const int d = c->d, E = d + 1;
   const double g = c->gamma, gm1 = g - 1.0, igm1 = 1.0 / (g - 1.0);
-  double s = 0.0;
+  sse_real s = 0.0;
   for (int m = 0; m < d; ++m) s += u[m + 1] * u[m + 1];
-  double k = (0.5 / u[0]) * s;
-  double p = gm1 * (u[E] - k);
-  double ip = 1.0 / p;
+  sse_real k = (0.5 / u[0]) * s;
+  sse_real p = gm1 * (u[E] - k);
+  sse_real ip = 1.0 / p;
   w[0] = igm1 * (g - log(p / pow(u[0], g))) - k * ip;
   for (int m = 0; m < d; ++m) w[m + 1] = u[m + 1] * ip;
   w[E] = -u[0] * ip;
 }
 
 /* euler_navierstokes.jl:115-131 */
-static void entropy_to_cons(const sse_config *c, const double *w_in, double *u) {
+static void entropy_to_cons(const sse_config *c, const sse_real *w_in, sse_real *u) {
   const int d = c->d, E = d + 1;
   const double g = c->gamma, gm1 = g - 1.0, igm1 = 1.0 / (g - 1.0);
-  double w[MAXC];
+  sse_real w[MAXC];
   for (int e = 0; e < d + 2; ++e) w[e] = w_in[e] * gm1;
-  double s = 0.0;
+  sse_real s = 0.0;
   for (int m = 0; m < d; ++m) s += w[m + 1] * w[m + 1];
-  double k = s / (2 * w[E]);
-  double sv = g - w[0] + k;
-  double rhoe = pow(gm1 / pow(-w[E], g), igm1) * exp(-sv * igm1);
+  sse_real k = s / (2 * w[E]);
+  sse_real sv = g - w[0] + k;
+  sse_real rhoe = pow(gm1 / pow(-w[E], g), igm1) * exp(-sv * igm1);
   u[0] = -w[E] * rhoe;
   for (int m = 0; m < d; ++m) u[m + 1] = w[m + 1] * rhoe;
   u[E] = rhoe * (1 - k);
 }
 
 /* numerical_flux! (ConservationLaws.jl:75-128) at facet node i: fstar[e] */
-static void numerical_flux(const sse_config *c, int two_point_ec, const double *ui,
-                           const double *uo, const double *n, double *fstar) {
-  double F[MAXC * MAXD];
+static void numerical_flux(const sse_config *c, int two_point_ec, const sse_real *ui,
+                           const sse_real *uo, const double *n, sse_real *fstar) {
+  sse_real F[MAXC * MAXD];
   two_point_flux(c, two_point_ec, ui, uo, F);
-  double a = 0.0;
+  sse_real a = 0.0;
   if (c->numerical_flux == SSE_LAX_FRIEDRICHS) a = c->half_lambda * wave_speed(c, ui, uo, n);
   for (int e = 0; e < c->n_c; ++e) {
-    double fn = 0.0;
+    sse_real fn = 0.0;
     for (int m = 0; m < c->d; ++m) fn = fma(F[e + MAXC * m], n[m], fn);
     fstar[e] = (c->numerical_flux == SSE_LAX_FRIEDRICHS) ? fma(a, ui[e] - uo[e], fn) : fn;
   }
@@ -340,17 +349,17 @@ static void numerical_flux(const sse_config *c, int two_point_ec, const double *
 /* ------------------------------------------------------------------ */
 
 typedef struct {
-  double *a, *b, *c, *w, *fq, *ff, *fn, *rq;
+  sse_real *a, *b, *c, *w, *fq, *ff, *fn, *rq;
 } scratch_t;
 
-static size_t scratch_doubles(const sse_config *c) {
+static size_t scratch_len(const sse_config *c) {
   size_t nq = c->n_q, nf = c->n_f, nc = c->n_c, np = c->n_p, d = c->d;
   size_t big = nq > nf ? nq : nf;
   if (np > big) big = np;
   return 4 * big * nc + nq * nc * d + 3 * nf * nc + nq * nc + 64;
 }
 
-static void scratch_carve(const sse_config *c, double *base, scratch_t *s) {
+static void scratch_carve(const sse_config *c, sse_real *base, scratch_t *s) {
   size_t nq = c->n_q, nf = c->n_f, nc = c->n_c, np = c->n_p, d = c->d;
   size_t big = nq > nf ? nq : nf;
   if (np > big) big = np;
@@ -366,7 +375,7 @@ static void scratch_carve(const sse_config *c, double *base, scratch_t *s) {
 
 /* WeightAdjustedSolver (M^-1 = I) / DiagonalSolver solve on one element,
  * rhs (N_p x N_c) in place; mass_matrix.jl:177-196 */
-static void mass_solve(const oracle_t *o, int k, double *rhs, double *tmp) {
+static void mass_solve(const oracle_t *o, int k, sse_real *rhs, sse_real *tmp) {
   const sse_config *c = &o->cfg;
   const int nq = c->n_q, np = c->n_p;
   if (c->mass_solver == SSE_DIAGONAL) {
@@ -383,11 +392,11 @@ static void mass_solve(const oracle_t *o, int k, double *rhs, double *tmp) {
   }
 }
 
-static void nodal_values_elem(oracle_t *o, const double *u, int k, scratch_t *s) {
+static void nodal_values_elem(oracle_t *o, const sse_real *u, int k, scratch_t *s) {
   const sse_config *c = &o->cfg;
   const int nq = c->n_q, nf = c->n_f, nc = c->n_c, np = c->n_p, ne = c->n_e;
-  const double *uk = u + (size_t)np * nc * k;
-  double *uq = o->u_q + (size_t)nq * nc * k;
+  const sse_real *uk = u + (size_t)np * nc * k;
+  sse_real *uq = o->u_q + (size_t)nq * nc * k;
   const int project = (c->form == SSE_FLUX_DIFFERENCING_FORM && c->law == SSE_EULER);
   if (!project) {
     /* u_q = V u; u_f = R u_q */
@@ -398,11 +407,11 @@ static void nodal_values_elem(oracle_t *o, const double *u, int k, scratch_t *s)
     }
     return;
   }
-  double ui[MAXC], wi[MAXC];
+  sse_real ui[MAXC], wi[MAXC];
   if (!o->ops.vdm_A) {
     /* nodal entropy projection (flux_differencing_form.jl:190-211) */
-    for (int e = 0; e < nc; ++e) memcpy(uq + nq * e, uk + np * e, sizeof(double) * nq);
-    double *wq = s->a, *wf = s->b;
+    for (int e = 0; e < nc; ++e) memcpy(uq + nq * e, uk + np * e, sizeof(sse_real) * nq);
+    sse_real *wq = s->a, *wf = s->b;
     for (int i = 0; i < nq; ++i) {
       for (int e = 0; e < nc; ++e) ui[e] = uq[i + nq * e];
       cons_to_entropy(c, ui, wi);
@@ -417,7 +426,7 @@ static void nodal_values_elem(oracle_t *o, const double *u, int k, scratch_t *s)
     return;
   }
   /* modal entropy projection (flux_differencing_form.jl:214-250) */
-  double *wq = s->a, *wf = s->b, *w = s->c, *tmp = s->w;
+  sse_real *wq = s->a, *wf = s->b, *w = s->c, *tmp = s->w;
   const double *WJ = o->geo.WJ + (size_t)nq * k;
   for (int e = 0; e < nc; ++e) vdm_mul(o, uk + np * e, uq + nq * e);
   for (int i = 0; i < nq; ++i) {
@@ -446,10 +455,11 @@ static void nodal_values_elem(oracle_t *o, const double *u, int k, scratch_t *s)
   }
 }
 
-static void numerical_flux_elem(oracle_t *o, int k, int two_point_ec, double *ff) {
+static void numerical_flux_elem(oracle_t *o, int k, int two_point_ec, sse_real *ff) {
   const sse_config *c = &o->cfg;
   const int nf = c->n_f, nc = c->n_c, ne = c->n_e, d = c->d;
-  double ui[MAXC], uo[MAXC], nn[MAXD], fs[MAXC];
+  sse_real ui[MAXC], uo[MAXC], fs[MAXC];
+  double nn[MAXD];
   for (int i = 0; i < nf; ++i) {
     int64_t P = o->geo.mapP[i + (size_t)nf * k] - 1;
     for (int e = 0; e < nc; ++e) {
@@ -463,11 +473,11 @@ static void numerical_flux_elem(oracle_t *o, int k, int two_point_ec, double *ff
 }
 
 /* StandardForm, ReferenceOperators: standard_form_first_order.jl:16-63 */
-static void time_derivative_standard(oracle_t *o, double *dudt, int k, scratch_t *s) {
+static void time_derivative_standard(oracle_t *o, sse_real *dudt, int k, scratch_t *s) {
   const sse_config *c = &o->cfg;
   const int nq = c->n_q, nf = c->n_f, nc = c->n_c, np = c->n_p, d = c->d;
-  double *uq = o->u_q + (size_t)nq * nc * k;
-  double F[MAXC * MAXD], ui[MAXC];
+  sse_real *uq = o->u_q + (size_t)nq * nc * k;
+  sse_real F[MAXC * MAXD], ui[MAXC];
   /* f_q[i, e, n] */
   for (int i = 0; i < nq; ++i) {
     for (int e = 0; e < nc; ++e) ui[e] = uq[i + nq * e];
@@ -481,7 +491,7 @@ static void time_derivative_standard(oracle_t *o, double *dudt, int k, scratch_t
     for (int m = 0; m < d; ++m) {
       const double *hw = o->geo.halfWLambda + (size_t)nq * (m + d * (n + d * (size_t)k));
       for (int e = 0; e < nc; ++e) {
-        const double *fqn = s->fq + nq * (e + nc * n);
+        const sse_real *fqn = s->fq + nq * (e + nc * n);
         for (int i = 0; i < nq; ++i) s->a[i] = hw[i] * fqn[i];
         csc_tmul(&o->ops.D[m], s->a, s->b);
         for (int i = 0; i < nq; ++i) s->rq[i + nq * e] += s->b[i];
@@ -504,18 +514,18 @@ static void time_derivative_standard(oracle_t *o, double *dudt, int k, scratch_t
     csc_tmul(&o->ops.R, s->ff + nf * e, s->a);
     for (int i = 0; i < nq; ++i) s->rq[i + nq * e] -= s->a[i];
   }
-  double *dk = dudt + (size_t)np * nc * k;
+  sse_real *dk = dudt + (size_t)np * nc * k;
   for (int e = 0; e < nc; ++e) vdm_tmul(o, s->rq + nq * e, dk + np * e);
   mass_solve(o, k, dk, s->a);
 }
 
 /* FluxDifferencingForm: flux_differencing_form.jl:294-347 */
-static void time_derivative_fd(oracle_t *o, double *dudt, int k, scratch_t *s) {
+static void time_derivative_fd(oracle_t *o, sse_real *dudt, int k, scratch_t *s) {
   const sse_config *c = &o->cfg;
   const int nq = c->n_q, nf = c->n_f, nc = c->n_c, np = c->n_p, d = c->d, ne = c->n_e;
   const int ec = (c->two_point_flux == SSE_EC_FLUX);
-  double *uq = o->u_q + (size_t)nq * nc * k;
-  double F[MAXC * MAXD], ui[MAXC], uj[MAXC];
+  sse_real *uq = o->u_q + (size_t)nq * nc * k;
+  sse_real F[MAXC * MAXD], ui[MAXC], uj[MAXC];
   numerical_flux_elem(o, k, ec, s->ff);
   const double *bjf = o->geo.BJf + (size_t)nf * k;
   for (int e = 0; e < nc; ++e)
@@ -533,12 +543,12 @@ static void time_derivative_fd(oracle_t *o, double *dudt, int k, scratch_t *s) {
           two_point_flux(c, ec, ui, uj, F);
           double Sij = S->nzval[ii];
           for (int e = 0; e < nc; ++e) {
-            double Fm = 0.0;
+            sse_real Fm = 0.0;
             for (int n = 0; n < d; ++n) {
               double Lij = Lq[i + nq * (m + d * n)] + Lq[j + nq * (m + d * n)];
               Fm = fma(Lij, F[e + MAXC * n], Fm);
             }
-            double diff = Sij * Fm;
+            sse_real diff = Sij * Fm;
             s->rq[i + nq * e] -= diff;
             s->rq[j + nq * e] += diff;
           }
@@ -560,12 +570,12 @@ static void time_derivative_fd(oracle_t *o, double *dudt, int k, scratch_t *s) {
         two_point_flux(c, ec, ui, uj, F);
         double Cij = C->nzval[ii];
         for (int e = 0; e < nc; ++e) {
-          double Fn = 0.0;
+          sse_real Fn = 0.0;
           for (int m = 0; m < d; ++m) {
             double nJ = hnf[m + d * j] + hnq[m + d * (f + c->num_faces * i)];
             Fn = fma(nJ, F[e + MAXC * m], Fn);
           }
-          double diff = Cij * Fn;
+          sse_real diff = Cij * Fn;
           s->rq[i + nq * e] -= diff;
           s->ff[j + nf * e] -= diff;
         }
@@ -576,7 +586,7 @@ static void time_derivative_fd(oracle_t *o, double *dudt, int k, scratch_t *s) {
     csc_tmul(&o->ops.R, s->ff + nf * e, s->a);
     for (int i = 0; i < nq; ++i) s->rq[i + nq * e] -= s->a[i];
   }
-  double *dk = dudt + (size_t)np * nc * k;
+  sse_real *dk = dudt + (size_t)np * nc * k;
   for (int e = 0; e < nc; ++e) vdm_tmul(o, s->rq + nq * e, dk + np * e);
   mass_solve(o, k, dk, s->a);
 }
@@ -591,8 +601,8 @@ void *oracle_create(const sse_config *cfg, const sse_operators *ops, const sse_g
   o->cfg = *cfg;
   o->ops = *ops;
   o->geo = *geo;
-  o->u_q = (double *)malloc(sizeof(double) * (size_t)cfg->n_q * cfg->n_c * cfg->n_e);
-  o->u_f = (double *)malloc(sizeof(double) * (size_t)cfg->n_f * cfg->n_c * cfg->n_e);
+  o->u_q = (sse_real *)malloc(sizeof(sse_real) * (size_t)cfg->n_q * cfg->n_c * cfg->n_e);
+  o->u_f = (sse_real *)malloc(sizeof(sse_real) * (size_t)cfg->n_f * cfg->n_c * cfg->n_e);
   o->nthreads = nthreads > 0 ? nthreads : 1;
   return o;
 }
@@ -613,12 +623,12 @@ int oracle_threads(void) {
 #endif
 }
 
-static void run_nodal_values(oracle_t *o, const double *u) {
+static void run_nodal_values(oracle_t *o, const sse_real *u) {
   const sse_config *c = &o->cfg;
-  size_t sd = scratch_doubles(c);
+  size_t sd = scratch_len(c);
 #pragma omp parallel num_threads(o->nthreads)
   {
-    double *buf = (double *)malloc(sizeof(double) * sd);
+    sse_real *buf = (sse_real *)malloc(sizeof(sse_real) * sd);
     scratch_t s;
     scratch_carve(c, buf, &s);
 #pragma omp for schedule(static)
@@ -627,22 +637,22 @@ static void run_nodal_values(oracle_t *o, const double *u) {
   }
 }
 
-void oracle_nodal_values(void *h, const double *u, double *u_q, double *u_f) {
+void oracle_nodal_values(void *h, const sse_real *u, sse_real *u_q, sse_real *u_f) {
   oracle_t *o = (oracle_t *)h;
   run_nodal_values(o, u);
-  if (u_q) memcpy(u_q, o->u_q, sizeof(double) * (size_t)o->cfg.n_q * o->cfg.n_c * o->cfg.n_e);
-  if (u_f) memcpy(u_f, o->u_f, sizeof(double) * (size_t)o->cfg.n_f * o->cfg.n_c * o->cfg.n_e);
+  if (u_q) memcpy(u_q, o->u_q, sizeof(sse_real) * (size_t)o->cfg.n_q * o->cfg.n_c * o->cfg.n_e);
+  if (u_f) memcpy(u_f, o->u_f, sizeof(sse_real) * (size_t)o->cfg.n_f * o->cfg.n_c * o->cfg.n_e);
 }
 
 /* semi_discrete_residual! (Threaded), Solvers.jl:495-514 */
-void oracle_residual(void *h, const double *u, double *dudt) {
+void oracle_residual(void *h, const sse_real *u, sse_real *dudt) {
   oracle_t *o = (oracle_t *)h;
   const sse_config *c = &o->cfg;
   run_nodal_values(o, u);
-  size_t sd = scratch_doubles(c);
+  size_t sd = scratch_len(c);
 #pragma omp parallel num_threads(o->nthreads)
   {
-    double *buf = (double *)malloc(sizeof(double) * sd);
+    sse_real *buf = (sse_real *)malloc(sizeof(sse_real) * sd);
     scratch_t s;
     scratch_carve(c, buf, &s);
 #pragma omp for schedule(static)
@@ -667,14 +677,14 @@ static const double CK_B[5] = {1432997174477.0 / 9575080441755.0,
 
 /* fixed-step time integration; scheme 0 = CK2N54 (tmp = A tmp + dt k;
  * u = u + B tmp), scheme 1 = classic RK4 */
-void oracle_rk_steps(void *h, double *u, int n_steps, double dt, int scheme) {
+void oracle_rk_steps(void *h, sse_real *u, int n_steps, double dt, int scheme) {
   oracle_t *o = (oracle_t *)h;
   const sse_config *c = &o->cfg;
   size_t n = (size_t)c->n_p * c->n_c * c->n_e;
-  double *k = (double *)malloc(sizeof(double) * n);
-  double *tmp = (double *)malloc(sizeof(double) * n);
-  double *acc = scheme == 1 ? (double *)malloc(sizeof(double) * n) : NULL;
-  double *ust = scheme == 1 ? (double *)malloc(sizeof(double) * n) : NULL;
+  sse_real *k = (sse_real *)malloc(sizeof(sse_real) * n);
+  sse_real *tmp = (sse_real *)malloc(sizeof(sse_real) * n);
+  sse_real *acc = scheme == 1 ? (sse_real *)malloc(sizeof(sse_real) * n) : NULL;
+  sse_real *ust = scheme == 1 ? (sse_real *)malloc(sizeof(sse_real) * n) : NULL;
   for (int step = 0; step < n_steps; ++step) {
     if (scheme == 0) {
       for (int s = 0; s < 5; ++s) {
@@ -708,29 +718,29 @@ void oracle_rk_steps(void *h, double *u, int n_steps, double dt, int scheme) {
  * out[N_c] = sum_k w_q' WJ V dudt with w_q the entropy variables of V u
  * (u itself for advection), which equals the reference's
  * (M^-1 V' WJ w_q)' M dudt for both mass solvers. */
-void oracle_conservation_residual(void *h, const double *u, const double *dudt, double *out) {
+void oracle_conservation_residual(void *h, const sse_real *u, const sse_real *dudt, sse_real *out) {
   oracle_t *o = (oracle_t *)h;
   const sse_config *c = &o->cfg;
   const int nq = c->n_q, nc = c->n_c, np = c->n_p;
   for (int e = 0; e <= nc; ++e) out[e] = 0.0;
-  double *uq = (double *)malloc(sizeof(double) * nq * nc);
-  double *vd = (double *)malloc(sizeof(double) * nq * nc);
-  double ui[MAXC], wi[MAXC];
+  sse_real *uq = (sse_real *)malloc(sizeof(sse_real) * nq * nc);
+  sse_real *vd = (sse_real *)malloc(sizeof(sse_real) * nq * nc);
+  sse_real ui[MAXC], wi[MAXC];
   for (int k = 0; k < c->n_e; ++k) {
     const double *WJ = o->geo.WJ + (size_t)nq * k;
     for (int e = 0; e < nc; ++e) {
       vdm_mul(o, u + (size_t)np * nc * k + np * e, uq + nq * e);
       vdm_mul(o, dudt + (size_t)np * nc * k + np * e, vd + nq * e);
-      double s = 0.0;
+      sse_real s = 0.0;
       for (int i = 0; i < nq; ++i) s += WJ[i] * vd[i + nq * e];
       out[e] += s;
     }
-    double s = 0.0;
+    sse_real s = 0.0;
     for (int i = 0; i < nq; ++i) {
       for (int e = 0; e < nc; ++e) ui[e] = uq[i + nq * e];
       if (c->law == SSE_EULER) cons_to_entropy(c, ui, wi);
-      else memcpy(wi, ui, sizeof(double) * nc);
-      double t = 0.0;
+      else memcpy(wi, ui, sizeof(sse_real) * nc);
+      sse_real t = 0.0;
       for (int e = 0; e < nc; ++e) t += wi[e] * vd[i + nq * e];
       s += WJ[i] * t;
     }

@@ -160,15 +160,107 @@ static void check_mixed(std::mt19937_64 &rng, double *worst) {
   }
 }
 
+// Reverse-mode functions against central differences of the forward ones
+// (relative errors of O(h^2) + O(eps/h), h = 1e-6 relative).
+template <int D>
+static void check_adjoint(std::mt19937_64 &rng, double *worst) {
+  const double g = 1.4, gm1 = g - 1, igm1 = 1 / gm1;
+  std::uniform_real_distribution<double> U(-1, 1);
+  for (int trial = 0; trial < 2000; ++trial) {
+    double pscale = (trial % 2) ? 71.4 : 1.0;
+    double uL[D + 2], uR[D + 2];
+    random_state<D>(rng, g, pscale, uL);
+    if (trial % 3) {
+      for (int e = 0; e < D + 2; ++e) uR[e] = uL[e] * (1.0 + 1e-3 * U(rng));
+    } else {
+      random_state<D>(rng, g, pscale, uR);
+    }
+    double G[D], ob[D + 2], du[D + 2];
+    for (int m = 0; m < D; ++m) G[m] = U(rng);
+    for (int e = 0; e < D + 2; ++e) { ob[e] = U(rng); du[e] = U(rng); }
+    // flux: d/du_L of ob . ECdot(prim(uL), prim(uR), G) via prims
+    double PL[3 + D], PR[3 + D], PbL[3 + D], PbR[3 + D], ubL[D + 2] = {0}, ubR[D + 2] = {0};
+    euler_prim_fast<D>(gm1, uL, PL);
+    euler_prim_fast<D>(gm1, uR, PR);
+    ec_flux_dot_bwd<D>(igm1, PL, PR, G, ob, PbL, PbR);
+    euler_prim_bwd<D>(gm1, uL, PL, PbL, ubL);
+    euler_prim_bwd<D>(gm1, uR, PR, PbR, ubR);
+    auto J = [&](const double *a, const double *b) {
+      double Pa[3 + D], Pb_[3 + D], o[D + 2], s = 0;
+      euler_prim_fast<D>(gm1, a, Pa);
+      euler_prim_fast<D>(gm1, b, Pb_);
+      ec_flux_dot<D>(igm1, Pa, Pb_, G, o);
+      for (int e = 0; e < D + 2; ++e) s += ob[e] * o[e];
+      return s;
+    };
+    double sL = 0, sR = 0, dirL = 0, dirR = 0;
+    double h = 1e-6;
+    double a1[D + 2], a2[D + 2], b1[D + 2], b2[D + 2];
+    for (int e = 0; e < D + 2; ++e) {
+      double he = h * std::fabs(uL[e]) + 1e-9;
+      a1[e] = uL[e] + he * du[e]; a2[e] = uL[e] - he * du[e];
+      sL += ubL[e] * du[e] * he;
+      double hr = h * std::fabs(uR[e]) + 1e-9;
+      b1[e] = uR[e] + hr * du[e]; b2[e] = uR[e] - hr * du[e];
+      sR += ubR[e] * du[e] * hr;
+    }
+    dirL = 0.5 * (J(a1, uR) - J(a2, uR));
+    dirR = 0.5 * (J(uL, b1) - J(uL, b2));
+    // floor: the round-off of the central difference itself, |J| eps / h
+    double scaleL = std::fabs(sL) + 1e-10 * std::fabs(J(uL, uR)) * h;
+    double scaleR = std::fabs(sR) + 1e-10 * std::fabs(J(uL, uR)) * h;
+    worst[6] = std::fmax(worst[6], std::fabs(dirL - sL) / scaleL);
+    worst[6] = std::fmax(worst[6], std::fabs(dirR - sR) / scaleR);
+    // entropy maps: JVP against central differences, and Jacobian symmetry
+    double w[D + 2], jw[D + 2], wp[D + 2], wm[D + 2], up[D + 2], um[D + 2];
+    cons_to_entropy_fast<D>(g, gm1, igm1, uL, w);
+    cons_to_entropy_jvp<D>(g, gm1, igm1, uL, du, jw);
+    for (int e = 0; e < D + 2; ++e) { up[e] = uL[e] + h * du[e]; um[e] = uL[e] - h * du[e]; }
+    cons_to_entropy_fast<D>(g, gm1, igm1, up, wp);
+    cons_to_entropy_fast<D>(g, gm1, igm1, um, wm);
+    double nrm = 0;
+    for (int e = 0; e < D + 2; ++e) nrm = std::fmax(nrm, std::fabs(jw[e]));
+    for (int e = 0; e < D + 2; ++e)
+      worst[7] = std::fmax(worst[7], std::fabs((wp[e] - wm[e]) / (2 * h) - jw[e]) / nrm);
+    double ju[D + 2];
+    entropy_to_cons_jvp<D>(g, gm1, igm1, std::log(gm1), w, du, ju);
+    double wpp[D + 2], wmm[D + 2], uu1[D + 2], uu2[D + 2];
+    double hw = 1e-7;
+    for (int e = 0; e < D + 2; ++e) { wpp[e] = w[e] + hw * du[e]; wmm[e] = w[e] - hw * du[e]; }
+    entropy_to_cons_fast<D>(g, gm1, igm1, std::log(gm1), wpp, uu1);
+    entropy_to_cons_fast<D>(g, gm1, igm1, std::log(gm1), wmm, uu2);
+    nrm = 0;
+    for (int e = 0; e < D + 2; ++e) nrm = std::fmax(nrm, std::fabs(ju[e]));
+    for (int e = 0; e < D + 2; ++e)
+      worst[7] = std::fmax(worst[7], std::fabs((uu1[e] - uu2[e]) / (2 * hw) - ju[e]) / nrm);
+    // symmetry: a . J b == b . J a
+    double a[D + 2], b[D + 2], Ja[D + 2], Jb[D + 2];
+    for (int e = 0; e < D + 2; ++e) { a[e] = U(rng); b[e] = U(rng); }
+    cons_to_entropy_jvp<D>(g, gm1, igm1, uL, a, Ja);
+    cons_to_entropy_jvp<D>(g, gm1, igm1, uL, b, Jb);
+    double x1 = 0, x2 = 0, sc = 0;
+    for (int e = 0; e < D + 2; ++e) { x1 += b[e] * Ja[e]; x2 += a[e] * Jb[e]; sc += std::fabs(b[e] * Ja[e]); }
+    worst[8] = std::fmax(worst[8], std::fabs(x1 - x2) / sc);
+    entropy_to_cons_jvp<D>(g, gm1, igm1, std::log(gm1), w, a, Ja);
+    entropy_to_cons_jvp<D>(g, gm1, igm1, std::log(gm1), w, b, Jb);
+    x1 = x2 = sc = 0;
+    for (int e = 0; e < D + 2; ++e) { x1 += b[e] * Ja[e]; x2 += a[e] * Jb[e]; sc += std::fabs(b[e] * Ja[e]); }
+    worst[8] = std::fmax(worst[8], std::fabs(x1 - x2) / sc);
+  }
+}
+
 int main() {
   std::mt19937_64 rng(20261203);
-  double worst[6] = {0, 0, 0, 0, 0, 0};
+  double worst[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   check<2>(rng, worst);
   check<3>(rng, worst);
   check_mixed<2>(rng, worst);
   check_mixed<3>(rng, worst);
+  check_adjoint<2>(rng, worst);
+  check_adjoint<3>(rng, worst);
   std::printf("{\"logmean\": %.3e, \"inv_logmean\": %.3e, \"ec_flux_dot\": %.3e, "
-              "\"cons_to_entropy\": %.3e, \"entropy_to_cons\": %.3e, \"mixed_reduced_flux\": %.3e}\n",
-              worst[0], worst[1], worst[2], worst[3], worst[4], worst[5]);
+              "\"cons_to_entropy\": %.3e, \"entropy_to_cons\": %.3e, \"mixed_reduced_flux\": %.3e, "
+              "\"flux_vjp_vs_fd\": %.3e, \"entropy_jvp_vs_fd\": %.3e, \"entropy_jacobian_symmetry\": %.3e}\n",
+              worst[0], worst[1], worst[2], worst[3], worst[4], worst[5], worst[6], worst[7], worst[8]);
   return 0;
 }

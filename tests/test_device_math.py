@@ -40,6 +40,16 @@ def test_mixed_reduced_flux(results):
     assert results["mixed_reduced_flux"] < 1e-4
 
 
+def test_adjoint_derivatives(results):
+    # hand-written transposes against central differences (h = 1e-6); the
+    # worst cases are directional derivatives ~1e-8 of fluxes ~1e2, where the
+    # difference quotient's own round-off is ~1e-6 relative
+    assert results["flux_vjp_vs_fd"] < 1e-5
+    assert results["entropy_jvp_vs_fd"] < 1e-6
+    # the entropy maps are gradients / inverse gradients: symmetric Jacobians
+    assert results["entropy_jacobian_symmetry"] < 1e-13
+
+
 def test_entropy_variable_maps(results):
     assert results["cons_to_entropy"] < 5e-14
     assert results["entropy_to_cons"] < 5e-14

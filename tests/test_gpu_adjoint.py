@@ -1,0 +1,173 @@
+"""Discrete adjoint on the GPU (sse_residual_vjp, sse_rk_record /
+sse_rk_adjoint) against the dual-number oracle: the dot-product identity
+<lam, J v> = <J^T lam, v> to round-off, the full transposed Jacobian on a
+small mesh, the adjoint Runge-Kutta sweep against the tangent of the whole
+oracle trajectory, checkpoint-interval invariance, the mixed-form
+recording, and central differences of an objective through the GPU
+forward."""
+import numpy as np
+import pytest
+
+import cases
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ADJ_NAMES = ["vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec", "tgv_tet_modal", "tgv_tet_ec",
+             "tgv_tet_nodal", "tgv_tet_p5"]
+
+
+def _dot_rel(a, b, c, d):
+    """|<a, b> - <c, d>| relative to the magnitude of the summands."""
+    lhs, rhs = float(np.vdot(a, b)), float(np.vdot(c, d))
+    scale = max(float(np.sum(np.abs(a * b))), float(np.sum(np.abs(c * d))), 1e-300)
+    return abs(lhs - rhs) / scale
+
+
+@pytest.mark.parametrize("name", ADJ_NAMES)
+def test_vjp_dot_product(name, gpu_lib, pkg):
+    host, u = cases.make(name)
+    G = pkg.GB300Solver(host)
+    T = O.TangentOracle(host)
+    rng = np.random.default_rng(11)
+    for _ in range(3):
+        lam = rng.standard_normal(u.shape)
+        v = rng.standard_normal(u.shape)
+        mu = G.residual_vjp(u, lam)
+        _, jv = T.jvp(u, v)
+        assert _dot_rel(lam, jv, mu, v) < 1e-12
+
+
+def test_vjp_full_transpose(gpu_lib, pkg):
+    """Every entry of J^T lam against lam . (J e_i) from the tangent oracle."""
+    pb = pkg.setups.vortex_tri(cells=8, p=2)
+    host = pkg.solver.HostArrays(pb.law, pb.sd, pb.form)
+    u = pkg.setups.perturbed(pb.u0, 7, 1e-3)
+    G = pkg.GB300Solver(host)
+    T = O.TangentOracle(host)
+    lam = np.random.default_rng(12).standard_normal(u.shape)
+    mu = G.residual_vjp(u, lam).ravel()
+    want = np.empty(u.size)
+    e = np.zeros(u.size)
+    for i in range(u.size):
+        e[i] = 1.0
+        want[i] = float(np.vdot(lam.ravel(), T.jvp(u, e.reshape(u.shape))[1].ravel()))
+        e[i] = 0.0
+    scale = np.abs(want).max()
+    assert np.abs(mu - want).max() < 1e-12 * scale
+
+
+def test_vjp_device_pointers_and_determinism(gpu_lib, pkg):
+    import torch
+    host, u = cases.make("tgv_tet_modal")
+    G = pkg.GB300Solver(host)
+    lam = np.random.default_rng(13).standard_normal(u.shape)
+    ud = torch.from_numpy(u).cuda()
+    ld = torch.from_numpy(lam).cuda()
+    m1 = G.residual_vjp(ud, ld)
+    m2 = G.residual_vjp(ud, ld)
+    torch.cuda.synchronize()
+    assert torch.equal(m1, m2)
+    assert np.array_equal(m1.cpu().numpy(), G.residual_vjp(u, lam))
+
+
+def _vortex(pkg, cells=8, p=3):
+    pb = pkg.setups.vortex_tri(cells=cells, p=p)
+    host = pkg.solver.HostArrays(pb.law, pb.sd, pb.form)
+    return pb, host
+
+
+@pytest.mark.parametrize("scheme,every", [(0, 3), (0, 0), (1, 2), (1, 7)])
+def test_rk_adjoint_against_trajectory_tangent(scheme, every, gpu_lib, pkg):
+    pb, host = _vortex(pkg)
+    u0 = pkg.setups.perturbed(pb.u0, 21, 1e-3)
+    n_steps = 7
+    G = pkg.GB300Solver(host)
+    uT = u0.copy()
+    G.rk_record(uT, n_steps, pb.dt, scheme, every)
+    rng = np.random.default_rng(22)
+    lamT = rng.standard_normal(u0.shape)
+    info = G.rk_adjoint(lamT)
+    lam0 = info["lam_0"]
+    assert info["segments"] * info["checkpoint_every"] >= n_steps
+    T = O.TangentOracle(host)
+    for _ in range(2):
+        v = rng.standard_normal(u0.shape)
+        uT_o, w = T.rk_jvp(u0, v, n_steps, pb.dt, scheme)
+        assert _dot_rel(lamT, w, lam0, v) < 1e-11
+    assert O.rel2(uT, uT_o) < 1e-12
+
+
+def test_rk_adjoint_checkpoint_interval_invariance(gpu_lib, pkg):
+    pb, host = _vortex(pkg)
+    u0 = pkg.setups.perturbed(pb.u0, 23, 1e-3)
+    G = pkg.GB300Solver(host)
+    lamT = np.random.default_rng(24).standard_normal(u0.shape)
+    grads = []
+    for every in (1, 2, 5, 6, 0):
+        u = u0.copy()
+        G.rk_record(u, 6, pb.dt, 0, every)
+        grads.append(G.rk_adjoint(lamT)["lam_0"])
+        # the recording stays valid for a second pullback
+        assert np.array_equal(G.rk_adjoint(lamT)["lam_0"], grads[-1])
+    for g in grads[1:]:
+        assert np.array_equal(g, grads[0])
+
+
+def test_rk_adjoint_mixed_recording(gpu_lib, pkg):
+    pb, host = _vortex(pkg)
+    u0 = pkg.setups.perturbed(pb.u0, 25, 1e-3)
+    G = pkg.GB300Solver(host)
+    lamT = np.random.default_rng(26).standard_normal(u0.shape)
+    u = u0.copy()
+    G.rk_record(u, 6, pb.dt, 0, 2)
+    g64 = G.rk_adjoint(lamT)["lam_0"]
+    G.set_precision(pkg.abi.SSE_MIXED)
+    um = u0.copy()
+    G.rk_record(um, 6, pb.dt, 0, 2)
+    gm = G.rk_adjoint(lamT)["lam_0"]
+    # the pullback linearises the FP64 residual along the mixed trajectory
+    assert O.rel2(um, u) < 1e-6
+    assert O.rel2(gm, g64) < 1e-5
+
+
+def test_gradient_against_central_differences(gpu_lib, pkg):
+    """dJ/du0 for J = 1/2 ||u(T) - u_target||^2_M against central
+    differences of J through the GPU forward along seeded directions."""
+    pb, host = _vortex(pkg)
+    tgt = pkg.setups.vortex_tri(cells=8, p=3, strength=5.5, shift=0.3)
+    obj = pkg.objectives
+    G = pkg.GB300Solver(host)
+    u0 = pb.u0.copy()
+    n_steps = 10
+
+    def J(u):
+        u = u.copy()
+        G.rk_steps(u, n_steps, pb.dt, 0)
+        return obj.mass_misfit(host, u, tgt.u0)
+
+    uT = u0.copy()
+    G.rk_record(uT, n_steps, pb.dt, 0, 4)
+    _, dJdu = obj.mass_misfit(host, uT, tgt.u0)
+    grad = G.rk_adjoint(dJdu)["lam_0"]
+    rng = np.random.default_rng(27)
+    for _ in range(4):
+        v = rng.standard_normal(u0.shape)
+        v /= np.linalg.norm(v)
+        h = 1e-6
+        fd = (J(u0 + h * v)[0] - J(u0 - h * v)[0]) / (2 * h)
+        ad = float(np.vdot(grad, v))
+        assert abs(fd - ad) <= 1e-5 * max(abs(ad), 1e-3 * np.linalg.norm(grad)), (fd, ad)
+
+
+def test_adjoint_rejections(gpu_lib, pkg):
+    host, u = cases.make("adv_tri_modal")
+    G = pkg.GB300Solver(host)
+    with pytest.raises(pkg.SSEError) as e:
+        G.residual_vjp(u, u)
+    assert e.value.code == pkg.abi.SSE_ERR_UNSUPPORTED
+    host, u = cases.make("vortex_tri_modal")
+    G = pkg.GB300Solver(host)
+    with pytest.raises(pkg.SSEError) as e:
+        G.rk_adjoint(u)
+    assert e.value.code == pkg.abi.SSE_ERR_INVALID_ARGUMENT
