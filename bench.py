@@ -143,6 +143,102 @@ def cpu_baseline(pb, host, budget_s: float):
                       f"reference restated in C with OpenMP over elements"}
 
 
+def timed(stream, fn):
+    """Device milliseconds of fn() by CUDA events on the launching stream."""
+    import torch
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    out = fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b), out
+
+
+def adjoint_workload(pkg, gpu, host, u0_np, dt, steps, fwd_ms, stream):
+    """Pullback of the volume-averaged kinetic energy after `steps`
+    CarpenterKennedy2N54 steps of the benchmark workload, w.r.t. the initial
+    state (the initial-momentum block is the gradient w.r.t. the velocity
+    field).  Cost relative to the plain forward of the same steps."""
+    import torch
+    out = {"objective": "volume-averaged kinetic energy at T, gradient w.r.t. the initial state",
+           "steps": steps, "stages": 5 * steps, "forward_ms": fwd_ms}
+    grads = {}
+    # every = 0: segments sized from free HBM (here the whole trajectory, no
+    # recomputation); every = 2: five segments, four recomputed
+    for every, key in ((0, "memory_sized"), (2, "every_2_steps")):
+        gpu.rk_record(torch.from_numpy(u0_np).cuda(), steps, dt, 0, every)   # warm-up / allocation
+        u = torch.from_numpy(u0_np).cuda()
+        rec_ms, _ = timed(stream, lambda: gpu.rk_record(u, steps, dt, 0, every))
+        ke, dke = pkg.objectives.kinetic_energy(host, u.cpu().numpy())
+        lamT = torch.from_numpy(dke).cuda()
+        lam0 = torch.empty_like(lamT)
+        adj_ms, info = timed(stream, lambda: gpu.rk_adjoint(lamT, lam0))
+        grads[key] = lam0.cpu().numpy()
+        out[key] = {"record_ms": rec_ms, "adjoint_ms": adj_ms,
+                    "adjoint_over_forward": adj_ms / fwd_ms, "record_over_forward": rec_ms / fwd_ms,
+                    "gradient_over_forward": (rec_ms + adj_ms) / fwd_ms,
+                    "checkpoint_every_steps": info["checkpoint_every"], "segments": info["segments"],
+                    "segments_recomputed": info["recomputed"], "recording_bytes": info["bytes"]}
+        out["kinetic_energy_T"] = ke
+    g = grads["memory_sized"]
+    out["grad_norm_momentum"] = float(np.linalg.norm(g[:, 1:-1]))
+    out["gradients_identical_across_intervals"] = bool(np.array_equal(g, grads["every_2_steps"]))
+    out["adjoint_over_forward"] = out["every_2_steps"]["adjoint_over_forward"]
+    return out
+
+
+def adjoint_gradient_check(pkg, stream, n_dirs: int = 8):
+    """2-D Euler vortex (64^2 x 2 = 8192 curved triangles, ModalTensor(4),
+    FD + LF): J = 1/2 ||u(T) - u_target||^2_M after 400 CarpenterKennedy2N54
+    stages, checkpoints every 20 stages; the adjoint gradient against
+    central differences (step 1e-6) of J through the GPU forward along
+    seeded unit directions."""
+    import torch
+    setups, obj = pkg.setups, pkg.objectives
+    pb = setups.vortex_tri(cells=64, p=4)
+    host = pb.host_arrays()
+    tgt = setups.perturbed(setups.vortex_tri(cells=64, p=4, strength=5.5, shift=0.3).u0, 20261207, 1e-3)
+    g = pkg.GB300Solver(host)
+    g.set_stream(stream.cuda_stream)
+    n_steps = 80
+    u0 = torch.from_numpy(pb.u0).cuda()
+
+    def J(x):
+        x = x.clone()
+        g.rk_steps(x, n_steps, pb.dt)
+        return obj.mass_misfit(host, x.cpu().numpy(), tgt)[0]
+
+    u = u0.clone()
+    fwd_ms, _ = timed(stream, lambda: g.rk_steps(u.clone(), n_steps, pb.dt))
+    g.rk_record(u0.clone(), n_steps, pb.dt, 0, 4)   # warm-up / allocation
+    u = u0.clone()
+    rec_ms, _ = timed(stream, lambda: g.rk_record(u, n_steps, pb.dt, 0, 4))
+    Jv, dJ = obj.mass_misfit(host, u.cpu().numpy(), tgt)
+    lamT = torch.from_numpy(dJ).cuda()
+    lam0 = torch.empty_like(lamT)
+    adj_ms, info = timed(stream, lambda: g.rk_adjoint(lamT, lam0))
+    grad = lam0.cpu().numpy()
+    rng = np.random.default_rng(20261204)
+    errs = []
+    for _ in range(n_dirs):
+        v = rng.standard_normal(grad.shape)
+        v /= np.linalg.norm(v)
+        vd = torch.from_numpy(v).cuda()
+        fd = (J(u0 + 1e-6 * vd) - J(u0 - 1e-6 * vd)) / 2e-6
+        ad = float(np.vdot(grad, v))
+        errs.append(abs(fd - ad) / max(abs(ad), 1e-300))
+    return {"workload": "2-D Euler isentropic vortex, 8192 curved tris, ModalTensor(4), FD + LF, "
+                        "400 CarpenterKennedy2N54 stages, checkpoints every 20 stages",
+            "objective": "1/2 ||u(T) - u_target||^2_M, u_target = perturbed vortex (strength 5.5, "
+                         "centre shifted by 0.3)",
+            "J": Jv, "forward_ms": fwd_ms, "record_ms": rec_ms, "adjoint_ms": adj_ms,
+            "adjoint_over_forward": adj_ms / fwd_ms, "segments": info["segments"],
+            "segments_recomputed": info["recomputed"],
+            "fd_directions": n_dirs, "fd_step": 1e-6,
+            "fd_rel_err_max": max(errs), "fd_rel_err_median": float(np.median(errs))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -152,6 +248,7 @@ def main():
     ap.add_argument("--cells", type=int, default=16)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -265,6 +362,13 @@ def main():
         mixed = {"unavailable": str(ex)}
         gpu.set_precision(abi.SSE_FP64)
 
+    # ---- discrete adjoint: cost against the plain forward of the same steps
+    # on this workload, and the gradient check on the 2-D vortex
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_workload(pkg, gpu, host, pb.u0, dt, args.steps, ms, stream)
+        adjoint["gradient_check"] = adjoint_gradient_check(pkg, stream)
+
     # ---- end to end through the C-ABI with host (pinned) buffers
     u_host = torch.from_numpy(pb.u0.copy()).pin_memory()
     gpu.rk_steps(u_host, 1, dt)
@@ -285,7 +389,7 @@ def main():
             "config": dict(WORKLOAD, dof=host.dof, form_precision="FP64 (drop-in form)",
                            parallelism="replicas only" if world > 1 else "1 GPU"),
             "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-            "mixed": mixed}
+            "mixed": mixed, "adjoint": adjoint}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pb, host, args.cpu_budget)
     if rank == 0:

@@ -74,11 +74,13 @@ struct sse_solver {
   struct Tape {
     bool valid = false;
     int n_steps = 0, every = 0, scheme = 0, stages = 0, nseg = 0;
+    int slots_seg = -1;  // segment whose stage data the slots hold
     bool mixed = false;  // recorded (and recomputed) in SSE_MIXED
     bool nodal = false;  // FP64 phase-A outputs kept per stage (FP64 recordings)
     double dt = 0.0;
     size_t bytes = 0;
-    std::vector<void *> bufs;  // freed when re-recorded and by sse_destroy
+    void *block = nullptr;     // one device allocation holding every buffer below;
+    size_t capacity = 0;       // kept across recordings that fit, freed by sse_destroy
     double *ckpt = nullptr, *ckpt_comp = nullptr;  // nseg states (+ compensation)
     double *seg_y = nullptr, *seg_uq = nullptr, *seg_uf = nullptr;  // every*stages slots
     double *w_u = nullptr, *w_tmp = nullptr, *w_comp = nullptr, *w_dudt = nullptr;
@@ -691,12 +693,6 @@ cudaError_t vjp_device(sse_solver *s, const double *u, const double *lam, double
   return launch_residual_vjp_kernels(ka, s->stream);
 }
 
-void free_tape(sse_solver *s) {
-  if (s->stream) cudaStreamSynchronize(s->stream);
-  for (void *p : s->tape.bufs) cudaFree(p);
-  s->tape = sse_solver::Tape{};
-}
-
 // one Runge-Kutta step of u (device) using the tape's work buffers; with
 // slot >= 0 every stage's input state (and, for FP64 recordings, its nodal
 // states) is stored in the segment slots slot*stages + stage
@@ -812,7 +808,7 @@ int32_t sse_create(const sse_config *cfg, const sse_operators *ops, const sse_ge
 int32_t sse_destroy(sse_solver *s) {
   if (!s) return SSE_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
-  for (void *p : s->tape.bufs) cudaFree(p);
+  if (s->tape.block) cudaFree(s->tape.block);
   for (void *p : s->allocations) cudaFree(p);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -997,11 +993,12 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
   int rc = enable_adjoint(s);
   if (rc != SSE_OK) return rc;
-  free_tape(s);
   const sse_config &c = s->cfg;
   const size_t n = (size_t)c.n_p * c.n_c * c.n_e;
   const size_t nqs = (size_t)c.n_q * c.n_c * c.n_e, nfs = (size_t)c.n_f * c.n_c * c.n_e;
   sse_solver::Tape &T = s->tape;
+  T.valid = false;
+  T.slots_seg = -1;
   T.n_steps = n_steps;
   T.scheme = scheme;
   T.stages = scheme == SSE_RK4 ? 4 : 5;
@@ -1011,42 +1008,60 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
   const size_t ckpt_state = (T.mixed ? 2 : 1) * n * 8;
   const size_t stage_bytes = (n + (T.nodal ? nqs + nfs : 0)) * 8;
   // fixed work buffers: u, tmp, comp, dudt, acc, ust, ybar, qbar, ybar'
-  const size_t fixed = 9 * n * 8;
+  // (every buffer padded to 256 bytes)
+  const size_t fixed = 9 * (n * 8 + 256);
   auto need = [&](int every) {
     const size_t nseg = (n_steps + every - 1) / every;
-    return nseg * ckpt_state + (size_t)every * T.stages * stage_bytes + fixed;
+    return nseg * ckpt_state + (size_t)every * T.stages * stage_bytes + fixed + 8 * 256;
   };
+  cudaError_t e;
   int every = checkpoint_every > 0 ? std::min(checkpoint_every, (int)n_steps) : 1;
-  if (checkpoint_every == 0)
-    for (int c2 = 2; c2 <= n_steps; ++c2)
-      if (need(c2) < need(every)) every = c2;
-  size_t free_b = 0, total_b = 0;
-  cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
-  if (e != cudaSuccess) return cuda_fail(s, e, "cudaMemGetInfo");
+  if (checkpoint_every == 0) {
+    // the longest segments that fit in 3/4 of the free device memory (less
+    // 512 MiB): fewest segments to recompute in the reverse sweep
+    size_t free_b = 0, total_b = 0;
+    if ((e = cudaMemGetInfo(&free_b, &total_b))) return cuda_fail(s, e, "cudaMemGetInfo");
+    const double budget = 0.75 * (double)(free_b + T.capacity) - (double)((size_t)512 << 20);
+    for (int c2 = n_steps; c2 >= 1; --c2)
+      if ((double)need(c2) <= budget) { every = c2; break; }
+  }
   const size_t bytes = need(every);
-  if (bytes + ((size_t)256 << 20) > free_b)
-    return fail(s, SSE_ERR_OUT_OF_MEMORY,
-                "recording needs " + std::to_string(bytes >> 20) + " MiB of device memory, " +
-                    std::to_string(free_b >> 20) + " MiB free (choose another checkpoint_every)");
+  if (bytes > T.capacity) {
+    // grow: release the old block first, then check what is free
+    if (s->stream && (e = cudaStreamSynchronize(s->stream))) return cuda_fail(s, e, "sync");
+    if (T.block) cudaFree(T.block);
+    T.block = nullptr;
+    T.capacity = 0;
+    size_t free_b = 0, total_b = 0;
+    if ((e = cudaMemGetInfo(&free_b, &total_b))) return cuda_fail(s, e, "cudaMemGetInfo");
+    if (bytes + ((size_t)256 << 20) > free_b)
+      return fail(s, SSE_ERR_OUT_OF_MEMORY,
+                  "recording needs " + std::to_string(bytes >> 20) + " MiB of device memory, " +
+                      std::to_string(free_b >> 20) + " MiB free (choose another checkpoint_every)");
+    if ((e = cudaMalloc(&T.block, bytes))) {
+      T.block = nullptr;
+      return fail(s, SSE_ERR_OUT_OF_MEMORY, std::string("recording: ") + cudaGetErrorString(e));
+    }
+    T.capacity = bytes;
+  }
   T.every = every;
   T.nseg = (n_steps + every - 1) / every;
   T.bytes = bytes;
-  auto get = [&](size_t count, double **out) -> cudaError_t {
-    void *p = nullptr;
-    cudaError_t err = cudaMalloc(&p, std::max<size_t>(count, 1) * 8);
-    if (err != cudaSuccess) return err;
-    T.bufs.push_back(p);
-    *out = (double *)p;
-    return cudaSuccess;
-  };
-  const size_t slots = (size_t)every * T.stages;
-  if ((e = get(T.nseg * n, &T.ckpt)) || (T.mixed && (e = get(T.nseg * n, &T.ckpt_comp))) ||
-      (e = get(slots * n, &T.seg_y)) || (T.nodal && (e = get(slots * nqs, &T.seg_uq))) ||
-      (T.nodal && (e = get(slots * nfs, &T.seg_uf))) || (e = get(n, &T.w_u)) || (e = get(n, &T.w_tmp)) ||
-      (e = get(n, &T.w_comp)) || (e = get(n, &T.w_dudt)) || (e = get(n, &T.w_acc)) ||
-      (e = get(n, &T.w_ust)) || (e = get(n, &T.ybar)) || (e = get(n, &T.qbar)) || (e = get(n, &T.yp))) {
-    free_tape(s);
-    return fail(s, SSE_ERR_OUT_OF_MEMORY, std::string("recording: ") + cudaGetErrorString(e));
+  {
+    char *cur = (char *)T.block;
+    auto carve = [&](size_t count) {
+      double *p = (double *)cur;
+      cur += (count * 8 + 255) / 256 * 256;
+      return p;
+    };
+    const size_t slots = (size_t)every * T.stages;
+    T.ckpt = carve(T.nseg * n);
+    T.ckpt_comp = T.mixed ? carve(T.nseg * n) : nullptr;
+    T.seg_y = carve(slots * n);
+    T.seg_uq = T.nodal ? carve(slots * nqs) : nullptr;
+    T.seg_uf = T.nodal ? carve(slots * nfs) : nullptr;
+    T.w_u = carve(n); T.w_tmp = carve(n); T.w_comp = carve(n); T.w_dudt = carve(n);
+    T.w_acc = carve(n); T.w_ust = carve(n); T.ybar = carve(n); T.qbar = carve(n); T.yp = carve(n);
   }
   double *du = u;
   if (memory == SSE_HOST) {
@@ -1063,13 +1078,17 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
                                           s->stream)))
         return cuda_fail(s, e, "checkpoint");
     }
-    if ((e = tape_step(s, du, -1))) return cuda_fail(s, e, "step");
+    // the last segment's stage data is kept from this run: the reverse
+    // sweep starts without recomputing it
+    const int last0 = (T.nseg - 1) * every;
+    if ((e = tape_step(s, du, step >= last0 ? step - last0 : -1))) return cuda_fail(s, e, "step");
   }
   if (memory == SSE_HOST && (e = cudaMemcpyAsync(u, s->d_u, n * 8, cudaMemcpyDeviceToHost, s->stream)))
     return cuda_fail(s, e, "D2H");
   if (t) *t += n_steps * dt;
   rc = check_flag(s);
   T.valid = rc == SSE_OK;
+  T.slots_seg = T.nseg - 1;
   return rc;
 }
 
@@ -1095,12 +1114,20 @@ int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double
     const double *uf = T.nodal ? T.seg_uf + q * nfs : nullptr;
     return vjp_device(s, T.seg_y + q * n, lam, s->d_mu, uq, uf);
   };
+  int recomputed = 0;
   for (int seg = T.nseg - 1; seg >= 0 && e == cudaSuccess; --seg) {
     const int s0 = seg * T.every, m = std::min(T.n_steps, s0 + T.every) - s0;
-    e = cudaMemcpyAsync(T.w_u, T.ckpt + (size_t)seg * n, n * 8, cudaMemcpyDeviceToDevice, s->stream);
-    if (e == cudaSuccess && T.mixed)
-      e = cudaMemcpyAsync(T.w_comp, T.ckpt_comp + (size_t)seg * n, n * 8, cudaMemcpyDeviceToDevice, s->stream);
-    for (int i = 0; i < m && e == cudaSuccess; ++i) e = tape_step(s, T.w_u, i);
+    if (T.slots_seg != seg) {
+      // recompute the segment from its checkpoint, storing its stage data
+      T.slots_seg = -1;
+      e = cudaMemcpyAsync(T.w_u, T.ckpt + (size_t)seg * n, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+      if (e == cudaSuccess && T.mixed)
+        e = cudaMemcpyAsync(T.w_comp, T.ckpt_comp + (size_t)seg * n, n * 8, cudaMemcpyDeviceToDevice,
+                            s->stream);
+      for (int i = 0; i < m && e == cudaSuccess; ++i) e = tape_step(s, T.w_u, i);
+      if (e == cudaSuccess) T.slots_seg = seg;
+      ++recomputed;
+    }
     for (int i = m - 1; i >= 0 && e == cudaSuccess; --i) {
       const size_t q0 = (size_t)i * T.stages;
       if (T.scheme == SSE_CARPENTER_KENNEDY_2N54) {
@@ -1134,6 +1161,7 @@ int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double
     out_info[0] = T.nseg;
     out_info[1] = T.every;
     out_info[2] = (double)T.bytes;
+    out_info[3] = recomputed;
   }
   return check_flag(s);
 }

@@ -172,16 +172,16 @@ class GB300Solver:
 
     def rk_adjoint(self, lam_T, lam_0=None) -> dict:
         """(du(T)/du(0))^T lam_T for the last ``rk_record``; returns
-        {"lam_0", "segments", "checkpoint_every", "bytes"}."""
+        {"lam_0", "segments", "checkpoint_every", "bytes", "recomputed"}."""
         if lam_0 is None:
             lam_0 = np.empty_like(lam_T) if isinstance(lam_T, np.ndarray) else lam_T.new_empty(lam_T.shape)
         pl, ml = _addr(lam_T)
         p0, m0 = _addr(lam_0)
         assert ml == m0
-        info = np.zeros(3)
+        info = np.zeros(4)
         self._check(self.L.sse_rk_adjoint(self.h, pl, p0, C.c_void_p(info.ctypes.data), ml))
         return {"lam_0": lam_0, "segments": int(info[0]), "checkpoint_every": int(info[1]),
-                "bytes": int(info[2])}
+                "bytes": int(info[2]), "recomputed": int(info[3])}
 
     def conservation_residual(self, u, dudt) -> np.ndarray:
         out = np.zeros(self.host.N_c + 1)

@@ -193,12 +193,14 @@ int32_t sse_residual_vjp(sse_solver *s, const double *u, const double *lam, doub
 
 /* sse_rk_steps that also records the trajectory for sse_rk_adjoint: the
  * state at every checkpoint_every-th step (and the compensation term in
- * SSE_MIXED) is kept in device memory owned by the handle, replacing the
- * previous recording.  checkpoint_every = 0 picks the interval that
- * minimises checkpoint plus one segment's stage storage.  Fails with
- * SSE_ERR_OUT_OF_MEMORY (nothing advanced) when the recording does not fit
- * in free device memory.  The forward half of the stepper's rrule; no
- * counterpart in the reference. */
+ * SSE_MIXED) plus the stage data of the last segment are kept in device
+ * memory owned by the handle, replacing the previous recording (the memory
+ * is reused when it suffices).  checkpoint_every = 0 picks the longest
+ * segments whose recording fits in 3/4 of the free device memory less
+ * 512 MiB, i.e. the fewest segments to recompute (none when the whole
+ * trajectory fits).  Fails with SSE_ERR_OUT_OF_MEMORY (nothing advanced)
+ * when the recording does not fit.  The forward half of the stepper's
+ * rrule; no counterpart in the reference. */
 int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme,
                       int32_t checkpoint_every, double *t, int32_t memory);
 
@@ -207,9 +209,11 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
  * (both N_p x N_c x N_e, host or device).  Each checkpoint segment is
  * recomputed once, in the precision it was recorded in, storing its RK
  * stage states; the stage adjoints use sse_residual_vjp's kernels at those
- * states.  The recording stays valid for further calls.  out_info, if not
- * NULL, receives {segments, checkpoint_every, stored stage bytes}.  The
- * pullback half of the stepper's rrule; no counterpart in the reference. */
+ * states.  The segment whose stage data is still held (the last one, after
+ * sse_rk_record) is not recomputed.  The recording stays valid for further
+ * calls.  out_info, if not NULL, receives {segments, checkpoint_every,
+ * recording bytes, segments recomputed by this call}.  The pullback half of
+ * the stepper's rrule; no counterpart in the reference. */
 int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double *out_info,
                        int32_t memory);
 

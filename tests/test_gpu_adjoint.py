@@ -107,9 +107,16 @@ def test_rk_adjoint_checkpoint_interval_invariance(gpu_lib, pkg):
     for every in (1, 2, 5, 6, 0):
         u = u0.copy()
         G.rk_record(u, 6, pb.dt, 0, every)
-        grads.append(G.rk_adjoint(lamT)["lam_0"])
-        # the recording stays valid for a second pullback
-        assert np.array_equal(G.rk_adjoint(lamT)["lam_0"], grads[-1])
+        first = G.rk_adjoint(lamT)
+        grads.append(first["lam_0"])
+        nseg = first["segments"]
+        # the recording run kept the last segment's stage data
+        assert first["recomputed"] == nseg - 1
+        # the recording stays valid for a second pullback, which recomputes
+        # the last segment too when there are several
+        second = G.rk_adjoint(lamT)
+        assert second["recomputed"] == (nseg if nseg > 1 else 0)
+        assert np.array_equal(second["lam_0"], grads[-1])
     for g in grads[1:]:
         assert np.array_equal(g, grads[0])
 
