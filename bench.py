@@ -1,12 +1,21 @@
-"""Benchmark: DOF-stage updates per second of the semi-discrete residual on
-the 3-D Euler Taylor-Green workload (16^3 x 6 = 24,576 curved tetrahedra,
-ModalTensor(4), FluxDifferencingForm with the entropy-conservative volume
-flux and Lax-Friedrichs interface dissipation, CarpenterKennedy2N54).
+"""Benchmark: DOF-stage updates per second of the semi-discrete residual.
 
-One step = one CarpenterKennedy2N54 time step = 5 residual evaluations and
-stage updates on the whole mesh; DOF = N_p * N_c * N_e (get_dof).
+Default workload (the headline line): 3-D Euler Taylor-Green, 16^3 x 6 =
+24,576 curved tetrahedra, ModalTensor(4), FluxDifferencingForm with the
+entropy-conservative volume flux and Lax-Friedrichs interface dissipation,
+CarpenterKennedy2N54.  The line also carries the mixed FP32/FP64 form on the
+same handle, the discrete adjoint (cost against the forward) and the 2-D
+vortex gradient check.  ``--workload`` selects the other configurations:
+``advection_tri`` (512 triangles, StandardForm, RK4), ``vortex_tri`` (8,192
+triangles, FD + LF), ``tgv_p5`` (82,944 tets at p = 5, mixed forward plus the
+adjoint of the kinetic energy over 200 stages).
+
+One step = one Runge-Kutta time step (5 residual evaluations and stage
+updates for CarpenterKennedy2N54, 4 for RK4) on the whole mesh; DOF =
+N_p * N_c * N_e (get_dof).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload tgv_p4|advection_tri|vortex_tri|tgv_p5]
 
 ``--impl reference`` times the reference's residual restated in C (OpenMP
 over elements on all host cores, the reference's ``Threaded()`` strategy)
@@ -31,14 +40,47 @@ import __graft_entry__  # noqa: E402
 
 METRIC = "DOF-stage updates/s, 3D Euler p4 tets, FP64 vs mixed at fixed err; adj/fwd cost"
 UNIT = "DOF-stage updates/s"
-WORKLOAD = {"workload": "3-D Euler Taylor-Green vortex, Mach 0.1, periodic [0,2pi]^3",
-            "mesh": "16^3 hexahedra x 6 = 24576 curved tetrahedra (Chan warp 0.05)",
-            "approximation": "ModalTensor(4) on Tet, N_p=35, N_q=125, N_f=100",
-            "form": "FluxDifferencingForm, entropy-conservative (Ranocha) volume flux + Lax-Friedrichs",
-            "metrics": "ChanWilcox (conservative curl)",
-            "time_integrator": "CarpenterKennedy2N54 (5 stages per step)",
-            "dof": None,
-            "l2_policy": "inputs larger than L2: metric terms and states ~0.7 GB read per stage"}
+
+WORKLOADS = {
+    "tgv_p4": {
+        "workload": "3-D Euler Taylor-Green vortex, Mach 0.1, periodic [0,2pi]^3",
+        "mesh": "16^3 hexahedra x 6 = 24576 curved tetrahedra (Chan warp 0.05)",
+        "approximation": "ModalTensor(4) on Tet, N_p=35, N_q=125, N_f=100",
+        "form": "FluxDifferencingForm, entropy-conservative (Ranocha) volume flux + Lax-Friedrichs",
+        "metrics": "ChanWilcox (conservative curl)",
+        "time_integrator": "CarpenterKennedy2N54 (5 stages per step)",
+        "l2_policy": "inputs larger than L2: metric terms and states ~0.7 GB read per stage"},
+    "advection_tri": {
+        "workload": "2-D linear advection, velocity (1,1), sine initial data, periodic [0,1]^2",
+        "mesh": "16^2 quadrilaterals x 2 = 512 curved triangles (Chan warp 0.1)",
+        "approximation": "ModalTensor(4) on Tri, N_p=15, N_q=25, N_f=15",
+        "form": "StandardForm, Lax-Friedrichs",
+        "metrics": "exact",
+        "time_integrator": "RK4 (4 stages per step)",
+        "l2_policy": "working set (~2 MB) is L2-resident: launch-latency bound, reported as is"},
+    "vortex_tri": {
+        "workload": "2-D Euler isentropic vortex (strength 5, free stream (1,1)), periodic [0,10]^2",
+        "mesh": "64^2 quadrilaterals x 2 = 8192 curved triangles (Chan warp 0.1)",
+        "approximation": "ModalTensor(4) on Tri, N_p=15, N_q=25, N_f=15",
+        "form": "FluxDifferencingForm, entropy-conservative volume flux + Lax-Friedrichs",
+        "metrics": "ChanWilcox (conservative curl)",
+        "time_integrator": "CarpenterKennedy2N54 (5 stages per step)",
+        "l2_policy": "working set ~40 MB fits in L2; reported as is"},
+    "tgv_p5": {
+        "workload": "3-D Euler Taylor-Green vortex, Mach 0.1, periodic [0,2pi]^3",
+        "mesh": "24^3 hexahedra x 6 = 82944 curved tetrahedra (Chan warp 0.05)",
+        "approximation": "ModalTensor(5) on Tet, N_p=56, N_q=216, N_f=144",
+        "form": "FluxDifferencingForm, entropy-conservative (Ranocha) volume flux + Lax-Friedrichs",
+        "metrics": "ChanWilcox (conservative curl)",
+        "time_integrator": "CarpenterKennedy2N54 (5 stages per step)",
+        "l2_policy": "inputs larger than L2: ~4 GB read per stage"},
+}
+
+# DRAM bytes (read + write) per element of one fd_time_derivative_kernel<3,5>
+# / nodal_values_kernel<3,5> launch at p = 4, from ncu captures of the same
+# kernels on the 8^3 x 6 = 3,072-tet case (118.2 MB and 10.6 MB per launch);
+# reads scale with the element count
+TRAFFIC_PER_ELEMENT = {"tgv_p4": {"B": 38_483, "A": 3_450}}
 
 
 def env_rank():
@@ -92,10 +134,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_problem(cells: int):
+def build_problem(workload: str, cells: int | None):
     pkg = __graft_entry__.load_package()
-    pb = pkg.setups.tgv_tet(cells=cells, p=4, lf=True)
+    s = pkg.setups
+    if workload == "tgv_p4":
+        pb = s.tgv_tet(cells=cells or 16, p=4, lf=True)
+    elif workload == "tgv_p5":
+        pb = s.tgv_tet(cells=cells or 24, p=5, lf=True)
+    elif workload == "vortex_tri":
+        pb = s.vortex_tri(cells=cells or 64, p=4)
+    elif workload == "advection_tri":
+        pb = s.advection_tri(cells=cells or 16, p=4)
+    else:
+        raise KeyError(workload)
     return pkg, pb, pb.host_arrays()
+
+
+def workload_config(args, host, world):
+    cfg = dict(WORKLOADS[args.workload], dof=host.dof, elements=host.N_e,
+               form_precision="FP64 (drop-in form)",
+               parallelism="replicas only" if world > 1 else "1 GPU")
+    if args.cells:
+        cfg["mesh"] = f"{args.cells}^d cells (--cells override)"
+    return cfg
 
 
 def run_reference(args):
@@ -103,25 +164,23 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle.oracle import Oracle
-    pkg, pb, host = build_problem(args.cells)
+    pkg, pb, host = build_problem(args.workload, args.cells)
     o = Oracle(host)
     u = pb.u0.copy()
     for _ in range(args.warmup):
-        u = o.rk_steps(u, 1, pb.dt, 0)
+        u = o.rk_steps(u, 1, pb.dt, pb.scheme)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        u = o.rk_steps(u, 1, pb.dt, 0)
+        u = o.rk_steps(u, 1, pb.dt, pb.scheme)
     dt = time.perf_counter() - t0
-    value = host.dof * 5 * args.steps / dt
-    cfg = dict(WORKLOAD, dof=host.dof)
+    value = host.dof * pb.stages_per_step * args.steps / dt
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": cfg, "impl": "reference",
+            "config": workload_config(args, host, world), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": o.nthreads, "kind": "port",
-                             "sample": f"{args.steps} full CarpenterKennedy2N54 steps on the whole "
-                                       f"mesh; reference restated in C (OpenMP), not the Julia "
-                                       f"reference itself"},
+                             "sample": f"{args.steps} full time steps on the whole mesh; reference "
+                                       f"restated in C (OpenMP), not the Julia reference itself"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -139,8 +198,8 @@ def cpu_baseline(pb, host, budget_s: float):
             break
     t = (time.perf_counter() - t0) / n
     return {"value": host.dof / t, "unit": UNIT, "cores": o.nthreads, "kind": "port",
-            "sample": f"{n} residual evaluations (one stage each) on the whole 24576-tet mesh; "
-                      f"reference restated in C with OpenMP over elements"}
+            "sample": f"{n} residual evaluations (one stage each) on the whole {host.N_e}-element "
+                      f"mesh; reference restated in C with OpenMP over elements"}
 
 
 def timed(stream, fn):
@@ -157,9 +216,9 @@ def timed(stream, fn):
 
 def adjoint_workload(pkg, gpu, host, u0_np, dt, steps, fwd_ms, stream):
     """Pullback of the volume-averaged kinetic energy after `steps`
-    CarpenterKennedy2N54 steps of the benchmark workload, w.r.t. the initial
-    state (the initial-momentum block is the gradient w.r.t. the velocity
-    field).  Cost relative to the plain forward of the same steps."""
+    CarpenterKennedy2N54 steps, w.r.t. the initial state (its momentum block
+    is the gradient w.r.t. the initial velocity field), at two checkpoint
+    intervals.  Cost relative to the plain forward of the same steps."""
     import torch
     out = {"objective": "volume-averaged kinetic energy at T, gradient w.r.t. the initial state",
            "steps": steps, "stages": 5 * steps, "forward_ms": fwd_ms}
@@ -185,6 +244,39 @@ def adjoint_workload(pkg, gpu, host, u0_np, dt, steps, fwd_ms, stream):
     out["grad_norm_momentum"] = float(np.linalg.norm(g[:, 1:-1]))
     out["gradients_identical_across_intervals"] = bool(np.array_equal(g, grads["every_2_steps"]))
     out["adjoint_over_forward"] = out["every_2_steps"]["adjoint_over_forward"]
+    return out
+
+
+def adjoint_mixed_workload(pkg, gpu, host, u0_np, dt, steps, stream):
+    """Mixed-form forward plus the adjoint of the volume-averaged kinetic
+    energy over `steps` CarpenterKennedy2N54 steps (checkpoints sized from
+    free HBM), against the same pullback of an FP64 recording."""
+    import torch
+    abi = pkg.abi
+    out = {"objective": "volume-averaged kinetic energy at T, gradient w.r.t. the initial velocity "
+                        "(momentum block of the initial-state gradient)",
+           "steps": steps, "stages": 5 * steps}
+    grads = {}
+    for prec, key in ((abi.SSE_MIXED, "mixed"), (abi.SSE_FP64, "fp64")):
+        gpu.set_precision(prec)
+        fwd_ms, _ = timed(stream, lambda: gpu.rk_steps(torch.from_numpy(u0_np).cuda(), steps, dt))
+        u = torch.from_numpy(u0_np).cuda()
+        rec_ms, _ = timed(stream, lambda: gpu.rk_record(u, steps, dt, 0, 0))
+        ke, dke = pkg.objectives.kinetic_energy(host, u.cpu().numpy())
+        lamT = torch.from_numpy(dke).cuda()
+        lam0 = torch.empty_like(lamT)
+        adj_ms, info = timed(stream, lambda: gpu.rk_adjoint(lamT, lam0))
+        grads[key] = lam0.cpu().numpy()
+        out[key] = {"forward_ms": fwd_ms, "forward_value": host.dof * 5 * steps / (fwd_ms * 1e-3),
+                    "record_ms": rec_ms, "adjoint_ms": adj_ms,
+                    "adjoint_over_forward": adj_ms / fwd_ms,
+                    "checkpoint_every_steps": info["checkpoint_every"], "segments": info["segments"],
+                    "segments_recomputed": info["recomputed"], "recording_bytes": info["bytes"],
+                    "kinetic_energy_T": ke}
+    gpu.set_precision(abi.SSE_FP64)
+    gm, g64 = grads["mixed"][:, 1:-1], grads["fp64"][:, 1:-1]
+    out["gradient_rel_err_mixed_vs_fp64_adjoint"] = float(np.linalg.norm(gm - g64) / np.linalg.norm(g64))
+    out["adjoint_over_forward"] = out["mixed"]["adjoint_over_forward"]
     return out
 
 
@@ -245,10 +337,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cells", type=int, default=16)
+    ap.add_argument("--workload", default="tgv_p4", choices=sorted(WORKLOADS))
+    ap.add_argument("--cells", type=int, default=None, help="override the mesh resolution")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=40,
+                    help="time steps of the tgv_p5 adjoint leg (40 = 200 stages)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -259,17 +354,18 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    pkg, pb, host = build_problem(args.cells)
+    pkg, pb, host = build_problem(args.workload, args.cells)
     pkg.build.build()
     gpu = pkg.GB300Solver(host)
     stream = torch.cuda.current_stream()
     gpu.set_stream(stream.cuda_stream)
     u = torch.from_numpy(pb.u0).cuda()
-    dt = pb.dt
+    dt, scheme, stages = pb.dt, pb.scheme, pb.stages_per_step
+    fd = pkg.abi.SSE_FLUX_DIFFERENCING_FORM == host.cfg.form
 
     # ---- device-resident throughput (value)
     for _ in range(args.warmup):
-        gpu.rk_steps(u, 1, dt)
+        gpu.rk_steps(u, 1, dt, scheme)
     sampler = ClockSampler(local)
     sampler.start()
     if world > 1:
@@ -278,7 +374,7 @@ def main():
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for _ in range(args.steps):
-        gpu.rk_steps(u, 1, dt)
+        gpu.rk_steps(u, 1, dt, scheme)
     ev1.record(stream)
     torch.cuda.synchronize()
     if world > 1:
@@ -289,7 +385,7 @@ def main():
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * host.dof * 5 * args.steps / (ms * 1e-3)
+    value = world * host.dof * stages * args.steps / (ms * 1e-3)
 
     # ---- per-kernel timings (CUDA events on the launching stream) and roofline
     phases = gpu.phase_timings(u, 5)
@@ -304,13 +400,18 @@ def main():
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    kernel_B = "fd_time_derivative_kernel" if fd else "std_time_derivative_kernel"
+    traffic = TRAFFIC_PER_ELEMENT.get(args.workload) if not args.cells else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak,
-                "kernel": "fd_time_derivative_kernel" if dom == "B" else "nodal_values_kernel",
+                "kernel": kernel_B if dom == "B" else "nodal_values_kernel",
                 "peak_source": "measured live: FP64 FMA-chain microbenchmark on this GPU",
                 "hbm_achieved_gbs": dom_bytes / (dom_ms * 1e-3) / 1e9,
                 "hbm_frac_of_measured": dom_bytes / (dom_ms * 1e-3) / 1e9 / hbm_peak,
-                "traffic": None,
+                "traffic": traffic[dom] * ne if traffic else None,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on "
+                                   "the 3,072-tet case, scaled by the element count") if traffic
+                else "no ncu capture of this workload",
                 "phase_ms": {"nodal_values": phases[0], "time_derivative": phases[1],
                              "rk_stage_update": phases[2]},
                 "algorithmic_flops_per_element": {"nodal_values": work.flops_A,
@@ -327,12 +428,12 @@ def main():
         um = torch.from_numpy(pb.u0).cuda()
         torch.cuda.synchronize()
         for _ in range(args.warmup):
-            gpu.rk_steps(um, 1, dt)
+            gpu.rk_steps(um, 1, dt, scheme)
         torch.cuda.synchronize()
         m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         m0.record(stream)
         for _ in range(args.steps):
-            gpu.rk_steps(um, 1, dt)
+            gpu.rk_steps(um, 1, dt, scheme)
         m1.record(stream)
         torch.cuda.synchronize()
         mms = m0.elapsed_time(m1)
@@ -345,7 +446,7 @@ def main():
         state_err = float(torch.linalg.norm(um - u) / torch.linalg.norm(u))
         res_err = float(np.linalg.norm(r_mixed - r_fp64) / np.linalg.norm(r_fp64))
         cons = gpu.conservation_residual(u0d, torch.from_numpy(r_mixed).cuda())
-        mvalue = world * host.dof * 5 * args.steps / (mms * 1e-3)
+        mvalue = world * host.dof * stages * args.steps / (mms * 1e-3)
         mixed = {"value": mvalue, "unit": UNIT, "ms_per_step": mms / args.steps,
                  "speedup_vs_fp64": mvalue / value,
                  "state_rel_err_vs_fp64": state_err,
@@ -362,32 +463,34 @@ def main():
         mixed = {"unavailable": str(ex)}
         gpu.set_precision(abi.SSE_FP64)
 
-    # ---- discrete adjoint: cost against the plain forward of the same steps
-    # on this workload, and the gradient check on the 2-D vortex
+    # ---- discrete adjoint
     adjoint = None
     if not args.no_adjoint:
-        adjoint = adjoint_workload(pkg, gpu, host, pb.u0, dt, args.steps, ms, stream)
-        adjoint["gradient_check"] = adjoint_gradient_check(pkg, stream)
+        if args.workload == "tgv_p4":
+            adjoint = adjoint_workload(pkg, gpu, host, pb.u0, dt, args.steps, ms, stream)
+            adjoint["gradient_check"] = adjoint_gradient_check(pkg, stream)
+        elif args.workload == "tgv_p5":
+            adjoint = adjoint_mixed_workload(pkg, gpu, host, pb.u0, dt, args.adjoint_steps, stream)
 
     # ---- end to end through the C-ABI with host (pinned) buffers
     u_host = torch.from_numpy(pb.u0.copy()).pin_memory()
-    gpu.rk_steps(u_host, 1, dt)
+    gpu.rk_steps(u_host, 1, dt, scheme)
     torch.cuda.synchronize()
     e2e_steps = max(2, args.steps // 2)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        gpu.rk_steps(u_host, 1, dt)           # H2D copy, 5 stages, D2H copy
+        gpu.rk_steps(u_host, 1, dt, scheme)   # H2D copy, all stages, D2H copy
     e2e_s = time.perf_counter() - t0
     nbytes = host.dof * 8
-    e2e = {"value": world * host.dof * 5 * e2e_steps / e2e_s, "unit": UNIT,
+    e2e = {"value": world * host.dof * stages * e2e_steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
 
-    launches = args.steps * 5 * 3
+    # per stage: phase A, phase B and one stage-update kernel
+    launches = args.steps * stages * 3
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(WORKLOAD, dof=host.dof, form_precision="FP64 (drop-in form)",
-                           parallelism="replicas only" if world > 1 else "1 GPU"),
+            "config": workload_config(args, host, world),
             "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "mixed": mixed, "adjoint": adjoint}
     if rank == 0 and not args.no_cpu_baseline:

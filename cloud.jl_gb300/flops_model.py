@@ -72,7 +72,6 @@ def model(host) -> Work:
     # ---- phase B
     nV_B = 3 if ra.V is not None else 0
     if fd:
-        npair = sum(1 for _ in range(0))
         S_inc = sum(s.nnz for s in host.S) // 2          # (pair, m) incidences with i < j
         pairs = _unique_pairs(host)
         nfp = host.C.nnz if host.C is not None else 0
@@ -90,7 +89,6 @@ def model(host) -> Work:
             flops_B = (nf * (pair_flux + 2 * d + 4) + pairs * pair_flux
                        + S_inc * (d + 2 * d + 2 + 2) + nfp * (pair_flux + d + 2 * d + 3)
                        + 2 * nnzR + nq + nV_B * vf + nq)
-        del npair
         bytes_B = f8 * (nq * nc + 2 * nf * nc + d * d * nq + d * ra.reference_element.num_faces * nq
                         + 2 * d * nf + nf + nq + np_ * nc) + 4.0 * nf
     else:

@@ -195,15 +195,16 @@ def initialize(initial_data, sd: SpatialDiscretization) -> np.ndarray:
     V = ra.V
     WJ = ra.W[None, :] * sd.geometric_factors.J_q       # (N_e, N_q)
     out = np.empty((sd.N_e, uq.shape[2], ra.N_p))
-    chunk = 4096
+    Np = ra.N_p
+    # M_k[a, b] = sum_q WJ[k, q] V[q, a] V[q, b]: one GEMM against the
+    # products of Vandermonde columns
+    VV = (V[:, :, None] * V[:, None, :]).reshape(V.shape[0], Np * Np)
+    chunk = 8192
     for s in range(0, sd.N_e, chunk):
         e = min(sd.N_e, s + chunk)
-        M = np.einsum("qa,kq,qb->kab", V, WJ[s:e], V)
-        rhs = np.einsum("qa,kq,kqc->kac", V, WJ[s:e], uq[s:e])
-        L = np.linalg.cholesky(M)
-        y = np.linalg.solve(L, rhs)
-        sol = np.linalg.solve(np.swapaxes(L, 1, 2), y)
-        out[s:e] = sol.transpose(0, 2, 1)
+        M = (WJ[s:e] @ VV).reshape(e - s, Np, Np)
+        rhs = np.stack([(WJ[s:e] * uq[s:e, :, c]) @ V for c in range(uq.shape[2])], axis=-1)
+        out[s:e] = np.linalg.solve(M, rhs).transpose(0, 2, 1)
     return out
 
 
