@@ -432,6 +432,14 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   // ---- team geometry and shared-memory layouts
   const int nc = c.n_c, np = c.n_p, nq = c.n_q, nf = c.n_f, d = c.d;
   int tpe = nq >= 64 ? 128 : 32;
+  // doubles of shared memory per element team that keep two blocks per SM
+  auto team_budget = [](int tpe_) {
+    const int epb_ = (tpe_ == 32) ? 4 : 1;
+    return (int)((size_t)110 * 1024 / 8 / epb_);
+  };
+  if (tpe == 128 && nq + nf > kMaxNodeSlots * tpe) tpe = 256;
+  if (nq + nf > kMaxNodeSlots * tpe)
+    return fail(s, SSE_ERR_UNSUPPORTED, "n_q + n_f too large for one element team");
   int zsz = 0, wsz = 0;
   if (has_vdm) {
     if (d == 2) zsz = nc * op.p1 * op.M2;
@@ -447,10 +455,33 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   // N_f) (modal scratch, facet values, or V dudt in the conservation kernel)
   finish(ka.layA, {nc * std::max(np, nq), nc * nq, zsz, wsz, nc * std::max({np, nq, nf}), tpe * (nc + 1)});
   if (fd) {
-    int diff = std::max({op.nvp * nc, op.nfp * nc, nc * (np + nq)});
-    int prim = (c.law == SSE_EULER) ? (nq + nf) * (3 + d) : 0;
-    finish(ka.layB, {nc * nq, nc * nf, nc * nf, nc * nq, diff, d * d * nq,
-                     op.nfp > 0 ? d * c.num_faces * nq : 0, prim, zsz, wsz});
+    // the pair buffer holds one chunk of per-pair contributions, and after
+    // the pair passes the modal / nodal buffers and the sum-factorisation
+    // scratch of the lift: chunks as large as that region (at least 256
+    // pairs when there are that many)
+    const int zsz_e = (zsz + 1) & ~1;
+    const int final_scratch = nc * (np + nq) + zsz_e + wsz;
+    const int max_pairs = std::max(op.nvp, op.nfp);
+    const int prim = (c.law == SSE_EULER) ? (nq + nf) * (3 + d) : 0;
+    auto layout = [&](int chunk) {
+      finish(ka.layB, {nc * nq, nc * nf, nc * nf, nc * nq, std::max(chunk * nc, final_scratch),
+                       d * d * nq, op.nfp > 0 ? d * c.num_faces * nq : 0, prim});
+      return ka.layB.team_doubles;
+    };
+    // all pairs at once when two blocks still fit on an SM (measured faster
+    // than more, smaller blocks with chunked passes); otherwise the largest
+    // chunk, a whole number of passes of the element's threads, that does
+    const int budget = team_budget(tpe);
+    int chunk = max_pairs;
+    if (layout(chunk) > budget) {
+      const int fixed = layout(0) - ((std::max(0, final_scratch) + 1) & ~1);
+      chunk = std::max(1, (budget - fixed) / nc);
+      if (chunk >= tpe) chunk = chunk / tpe * tpe;
+      chunk = std::max(1, std::min(chunk, max_pairs));
+    }
+    ka.fd_chunk = chunk;
+    ka.vdm_zsz = zsz_e;
+    layout(chunk);
   } else {
     finish(ka.layB, {nc * nq, nc * nf, nc * nf, nc * nq, d * nc * nq, nc * nq, nc * nq, 0, zsz, wsz});
   }
@@ -556,6 +587,46 @@ int enable_mixed(sse_solver *s) {
   size_t smm = (size_t)ka.epb * off * sizeof(float);
   if (smm > 220 * 1024) return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed kernel");
   if ((e = sse_set_smem_limit_mixed(ka, smm))) return cuda_fail(s, e, "cudaFuncSetAttribute");
+  if (op.has_vdm) {
+    // phase A with FP32 projection arithmetic: layouts, and the FP64
+    // projection of the constant function on every element
+    auto ev = [](int n) { return (n + 1) & ~1; };
+    const int big = nc * std::max(np, (int)nq), bigf = nc * std::max({np, (int)nq, (int)nf});
+    Layout &A = ka.layAm;
+    A.off[0] = 0;
+    A.off[1] = A.off[0] + ev(big);
+    A.off[2] = A.off[1] + ev(nc * (int)nq);
+    A.off[3] = A.off[2] + ev(zsz);
+    A.off[4] = A.off[3] + ev(wsz);                 // float region (doubles offset)
+    A.off[5] = 0;                                  // floats from here on
+    A.off[6] = A.off[5] + ev(bigf);
+    A.off[7] = A.off[6] + ev(nc * (int)nq);
+    A.off[8] = A.off[7] + ev(big);
+    A.off[9] = A.off[8] + ev(zsz);
+    const int nfloats = A.off[9] + ev(wsz);
+    for (int i = 10; i < 12; ++i) A.off[i] = 0;
+    A.team_doubles = A.off[4] + nfloats / 2;
+    int zsz1 = 0, wsz1 = 0;
+    if (c.d == 2) zsz1 = op.p1 * op.M2;
+    else { zsz1 = op.nb12 * op.M3; wsz1 = op.p1 * op.M2 * op.M3; }
+    Layout &P = ka.layP1;
+    const int big1 = std::max({np, (int)nq, (int)nf});
+    const int sizes1[5] = {big1, (int)nq, zsz1, wsz1, big1};
+    int o1 = 0;
+    for (int i = 0; i < 5; ++i) { P.off[i] = o1; o1 += ev(sizes1[i]); }
+    for (int i = 5; i < 12; ++i) P.off[i] = o1;
+    P.team_doubles = o1;
+    if ((size_t)ka.epb * std::max(A.team_doubles, P.team_doubles) * 8 > 220 * 1024)
+      return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed projection kernel");
+    if ((e = sse_set_smem_limits_mixed_a(ka))) return cuda_fail(s, e, "cudaFuncSetAttribute");
+    if ((e = alloc(s, nq * ne * sizeof(double), &p))) return cuda_fail(s, e, "alloc");
+    double *P1 = (double *)p;
+    if ((e = alloc(s, nf * ne * sizeof(double), &p))) return cuda_fail(s, e, "alloc");
+    double *RP1 = (double *)p;
+    if ((e = launch_projection_of_one(ka, P1, RP1, s->stream))) return cuda_fail(s, e, "projection of 1");
+    g.P1 = P1;
+    g.RP1 = RP1;
+  }
   if ((e = cudaStreamSynchronize(s->stream))) return cuda_fail(s, e, "sync");
   s->mixed_ready = true;
   return SSE_OK;
@@ -585,6 +656,12 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
   ph.p_ref = ph.gm1 * ph.E_ref;
   ph.theta_ref = ph.p_ref / ph.rho_ref;
   ph.H_ref = ph.gamma / ph.gm1 * ph.theta_ref;
+  {
+    double uref[5] = {ph.rho_ref, 0.0, 0.0, 0.0, 0.0};
+    uref[c.n_c - 1] = ph.E_ref;
+    if (c.d == 2) cons_to_entropy_fast<2>(ph.gamma, ph.gm1, ph.igm1, uref, ph.w_ref);
+    else cons_to_entropy_fast<3>(ph.gamma, ph.gm1, ph.igm1, uref, ph.w_ref);
+  }
   if (!(ph.rho_ref > 0.0) || !(ph.p_ref > 0.0))
     return fail(s, SSE_ERR_NONPHYSICAL, "mixed form: mean density or energy not positive");
   s->ref_ready = true;
@@ -640,6 +717,7 @@ int enable_adjoint(sse_solver *s) {
     L.team_doubles = off;
   };
   const size_t cap = (size_t)220 * 1024 / 8 / ka.epb;  // doubles per team
+  const int tpe_adj = ka.tpb / ka.epb;
   // lift: X, Y, Z, W, F as in phase A
   ka.layAdjB1 = ka.layA;
   // projection transpose: X, Y, Z, W, F, u_q0, w_q, w_f, ubar_q, ubar_f
@@ -650,11 +728,12 @@ int enable_adjoint(sse_solver *s) {
   Layout base{};
   finish(base, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf, d * d * nq, hsz});
   const int max_pairs = std::max(op.nvp, op.nfp);
-  // chunk: keep the team no larger than the forward flux-differencing team
-  // when that leaves room for at least 64 pairs, else as large as fits
-  long room = (long)std::max<size_t>(ka.layB.team_doubles, base.team_doubles + 64 * 2 * ps) - base.team_doubles;
+  // chunk: as large as keeps two blocks per SM (at least 128 pairs), all
+  // pairs when they fit
+  long room = std::max<long>((long)(110 * 1024 / 8 / ka.epb) - base.team_doubles, 128 * 2 * ps);
   room = std::min<long>(room, (long)cap - base.team_doubles);
   int chunk = (int)std::min<long>(max_pairs, room / (2 * ps));
+  if (chunk >= tpe_adj) chunk = chunk / tpe_adj * tpe_adj;
   if (chunk < 1 || ka.layAdjA.team_doubles > (int)cap)
     return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the adjoint kernels' shared memory");
   ka.pair_chunk = chunk;

@@ -172,8 +172,15 @@ __global__ void __launch_bounds__(256) adj_flux_kernel(KernelArgs ka) {
   }
   __syncthreads();
 
-  // volume pairs: dbar_p = rbar[j] - rbar[i]
+  // volume pairs: dbar_p = rbar[j] - rbar[i]; each node keeps a cursor into
+  // its (ascending) incidence list across the chunks
   const int CH = ka.pair_chunk;
+  int cur[kMaxNodeSlots];
+#pragma unroll
+  for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+    const int i = lane + sl * tpe;
+    cur[sl] = i < nq ? op.vp_inc_ptr[i] : 0;
+  }
   for (int c0 = 0; c0 < op.nvp; c0 += CH) {
     const int c1 = min(op.nvp, c0 + CH);
     for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
@@ -196,19 +203,24 @@ __global__ void __launch_bounds__(256) adj_flux_kernel(KernelArgs ka) {
       ec_flux_dot_bwd<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, db, slot, slot + PS);
     }
     __syncthreads();
-    for (int i = lane; i < nq; i += tpe) {
+#pragma unroll
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int i = lane + sl * tpe;
+      if (i >= nq) continue;
       double acc[3 + D];
 #pragma unroll
       for (int c = 0; c < PS; ++c) acc[c] = 0.0;
-      for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
+      int q = cur[sl];
+      const int qe = op.vp_inc_ptr[i + 1];
+      for (; q < qe; ++q) {
         const int inc = op.vp_inc[q];
         const int pidx = inc >> 1;
-        if (pidx < c0) continue;
         if (pidx >= c1) break;
         const double *slot = buf + (size_t)(pidx - c0) * 2 * PS + ((inc & 1) ? 0 : PS);
 #pragma unroll
         for (int c = 0; c < PS; ++c) acc[c] += slot[c];
       }
+      cur[sl] = q;
 #pragma unroll
       for (int c = 0; c < PS; ++c) Pb[(size_t)i * PS + c] += acc[c];
     }
@@ -218,6 +230,11 @@ __global__ void __launch_bounds__(256) adj_flux_kernel(KernelArgs ka) {
   // facet correction pairs: dbar_p = -rbar[i] - fbar_f[j]
   if (op.nfp > 0) {
     const double *hnf = g.halfnJf + (size_t)kk * D * nf;
+#pragma unroll
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int t = lane + sl * tpe;
+      cur[sl] = t < nq ? op.fp_q_ptr[t] : (t < nq + nf ? op.fp_f_ptr[t - nq] : 0);
+    }
     for (int c0 = 0; c0 < op.nfp; c0 += CH) {
       const int c1 = min(op.nfp, c0 + CH);
       for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
@@ -235,22 +252,26 @@ __global__ void __launch_bounds__(256) adj_flux_kernel(KernelArgs ka) {
                            slot + PS);
       }
       __syncthreads();
-      for (int t = lane; t < nq + nf; t += tpe) {
+#pragma unroll
+      for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+        const int t = lane + sl * tpe;
+        if (t >= nq + nf) continue;
         const bool vol = t < nq;
         const int r = vol ? t : t - nq;
-        const int *ptr = vol ? op.fp_q_ptr : op.fp_f_ptr;
         const int *lst = vol ? op.fp_q : op.fp_f;
+        const int qe = vol ? op.fp_q_ptr[r + 1] : op.fp_f_ptr[r + 1];
         double acc[3 + D];
 #pragma unroll
         for (int c = 0; c < PS; ++c) acc[c] = 0.0;
-        for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+        int q = cur[sl];
+        for (; q < qe; ++q) {
           const int pidx = lst[q];
-          if (pidx < c0) continue;
           if (pidx >= c1) break;
           const double *slot = buf + (size_t)(pidx - c0) * 2 * PS + (vol ? 0 : PS);
 #pragma unroll
           for (int c = 0; c < PS; ++c) acc[c] += slot[c];
         }
+        cur[sl] = q;
 #pragma unroll
         for (int c = 0; c < PS; ++c) Pb[(size_t)t * PS + c] += acc[c];
       }

@@ -93,6 +93,9 @@ struct DevGeo {
   const double *WJinv;        // nq x ne
   // FP32 roundings of the FP64 metric terms for the mixed form
   const float *BJff, *n_ff, *Lambda_qf, *halfnJff, *halfnJqf, *JinvWf, *WJinvf;
+  // mixed form: the entropy projection of the constant function 1 at the
+  // volume nodes (V M^-1 V^T (W J), nq x ne) and its facet values (R P1, nf x ne)
+  const double *P1, *RP1;
 };
 
 struct Physics {
@@ -107,6 +110,7 @@ struct Physics {
   double rho_ref, E_ref, p_ref;
   double theta_ref;  // p_ref / rho_ref
   double H_ref;      // gamma/(gamma-1) theta_ref: enthalpy removed from the energy fluxes
+  double w_ref[5];   // entropy variables of the reference state
 };
 
 // ---------------------------------------------------------------------------
@@ -259,8 +263,8 @@ SSE_HD void entropy_to_cons_fast(double gamma, double gm1, double igm1, double l
 // central differences.
 // ---------------------------------------------------------------------------
 
-// partial derivatives of logmean_fast(x, y)
-SSE_HD void logmean_fast_grad(double x, double y, double *dx, double *dy) {
+// logmean_fast(x, y) and its partial derivatives, sharing one reciprocal
+SSE_HD double logmean_fast_vgrad(double x, double y, double *dx, double *dy) {
   const double s = x + y;
   const double r = sse_rcp(s);
   const double f = (x - y) * r;
@@ -268,19 +272,21 @@ SSE_HD void logmean_fast_grad(double x, double y, double *dx, double *dy) {
   if (z < 1.0e-4) {
     const double P = fma(z, fma(z, fma(z, kInvQ3, kInvQ2), kInvQ1), 1.0);
     const double dP = fma(z, fma(z, 3.0 * kInvQ3, 2.0 * kInvQ2), kInvQ1);
-    const double c = 0.5 * s * dP * 4.0 * f * r * r;  // (s/2) P'(z) * 4 f / s^2
-    *dx = 0.5 * P + c * y;
-    *dy = 0.5 * P - c * x;
-    return;
+    const double c = 2.0 * s * dP * f * r * r;  // (s/2) P'(z) dz/dx with dz/dx = 4 f y / s^2
+    *dx = fma(c, y, 0.5 * P);
+    *dy = fma(-c, x, 0.5 * P);
+    return 0.5 * s * P;
   }
   const double N = y - x, Dl = log(y / x);
-  const double iD2 = 1.0 / (Dl * Dl);
+  const double iD = 1.0 / Dl;
+  const double iD2 = iD * iD;
   *dx = (-Dl + N / x) * iD2;
   *dy = (Dl - N / y) * iD2;
+  return N * iD;
 }
 
-// partial derivatives of inv_logmean_fast(x, y)
-SSE_HD void inv_logmean_fast_grad(double x, double y, double *dx, double *dy) {
+// inv_logmean_fast(x, y) and its partial derivatives
+SSE_HD double inv_logmean_fast_vgrad(double x, double y, double *dx, double *dy) {
   const double s = x + y;
   const double r = sse_rcp(s);
   const double f = (x - y) * r;
@@ -288,16 +294,19 @@ SSE_HD void inv_logmean_fast_grad(double x, double y, double *dx, double *dy) {
   if (z < 1.0e-4) {
     const double Q = fma(z, fma(z, fma(z, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
     const double dQ = fma(z, fma(z, 3.0 / 7.0, 0.4), 1.0 / 3.0);
-    const double base = -2.0 * r * r * Q;
-    const double c = 2.0 * r * dQ * 4.0 * f * r * r;
-    *dx = base + c * y;
-    *dy = base - c * x;
-    return;
+    const double r2 = r * r;
+    const double base = -2.0 * r2 * Q;
+    const double c = 8.0 * r * dQ * f * r2;  // 2 r Q'(z) dz/dx with dz/dx = 4 f y / s^2
+    *dx = fma(c, y, base);
+    *dy = fma(-c, x, base);
+    return 2.0 * r * Q;
   }
   const double N = y - x, Dl = log(y / x);
-  const double iN2 = 1.0 / (N * N);
+  const double iN = 1.0 / N;
+  const double iN2 = iN * iN;
   *dx = (Dl - N / x) * iN2;
   *dy = (N / y - Dl) * iN2;
+  return Dl * iN;
 }
 
 // Transpose of ec_flux_dot with respect to the two primitive vectors:
@@ -305,8 +314,9 @@ SSE_HD void inv_logmean_fast_grad(double x, double y, double *dx, double *dy) {
 template <int D>
 SSE_HD void ec_flux_dot_bwd(double igm1, const double *Pi, const double *Pj, const double *G,
                             const double *ob, double *Pbi, double *Pbj) {
-  const double rho_hat = logmean_fast(Pi[0], Pj[0]);
-  const double ilm = inv_logmean_fast(Pi[2], Pj[2]);
+  double dlx, dly, dix, diy;
+  const double rho_hat = logmean_fast_vgrad(Pi[0], Pj[0], &dlx, &dly);
+  const double ilm = inv_logmean_fast_vgrad(Pi[2], Pj[2], &dix, &diy);
   double vs[D];
   double vv = 0.0, gvs = 0.0, gvi = 0.0, gvj = 0.0;
 #pragma unroll
@@ -336,9 +346,6 @@ SSE_HD void ec_flux_dot_bwd(double igm1, const double *Pi, const double *Pj, con
   const double rhob = 0.5 * gvs * f0b;
   const double ilmb = igm1 * Cb;
   const double vvb = 0.5 * Cb;
-  double dlx, dly, dix, diy;
-  logmean_fast_grad(Pi[0], Pj[0], &dlx, &dly);
-  inv_logmean_fast_grad(Pi[2], Pj[2], &dix, &diy);
   Pbi[0] = rhob * dlx;
   Pbj[0] = rhob * dly;
   Pbi[1] = 0.5 * pbar_b + 0.5 * oE * gvj;

@@ -174,6 +174,105 @@ __device__ void facet_flux(const KernelArgs &ka, int kk, const double *uf, doubl
 }
 
 // ---------------------------------------------------------------------------
+// Mixed-form phase A (modal V): the entropy projection with its operator
+// arithmetic in FP32.  With w_ref the entropy variables of the constant
+// reference state, the projection P = V M^-1 V^T diag(W J) is linear, so
+//   P w = w_ref P(1) + P(w - w_ref):
+// P(1) and R P(1) are precomputed per element in FP64, and P is applied in
+// FP32 only to the perturbation w - w_ref, which is small where the flow is
+// near the reference state.  V u and the entropy-variable maps stay FP64.
+// ---------------------------------------------------------------------------
+template <int D, int NC>
+__global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) {
+  static_assert(NC == D + 2, "mixed form of the Euler entropy projection");
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const Layout &L = ka.layAm;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wd = base + L.off[3];
+  float *fb = reinterpret_cast<float *>(base + L.off[4]);
+  float *Af = fb + L.off[5], *Bf = fb + L.off[6], *Cf = fb + L.off[7], *Zf = fb + L.off[8],
+        *Wf = fb + L.off[9];
+  const double *WJ = ka.geo.WJ + (size_t)kk * nq;
+
+  const double *uk = ka.u + (size_t)kk * NC * np;
+  for (int t = lane; t < NC * np; t += tpe) X[t] = uk[t];
+  __syncthreads();
+  vdm_mul<double, D, NC>(op, X, Y, Z, Wd, lane, tpe);  // Y = u_q = V u (FP64)
+  // x' = W J (c2e(u_q) - w_ref), rounded to FP32
+  for (int i = lane; i < nq; i += tpe) {
+    double ui[NC], wi[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) ui[e] = Y[e * nq + i];
+    if (!(ui[0] > 0.0)) ka.flag_nonphysical();
+    cons_to_entropy_fast<D>(ph.gamma, ph.gm1, ph.igm1, ui, wi);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) Af[e * nq + i] = (float)(WJ[i] * (wi[e] - ph.w_ref[e]));
+  }
+  __syncthreads();
+  vdm_tmul<float, D, NC>(op, Af, Cf, Zf, Wf, lane, tpe);                               // V^T x'
+  mass_solve<float, D, NC>(op, ka.geo.JinvWf + (size_t)kk * nq, nullptr, 1, Cf, Af, Zf, Wf, lane, tpe);
+  vdm_mul<float, D, NC>(op, Cf, Bf, Zf, Wf, lane, tpe);                                // w'_q
+  csr_mul<float, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_valf, Bf, Af, lane, tpe);        // w'_f
+  __syncthreads();
+  const double *P1 = ka.geo.P1 + (size_t)kk * nq, *RP1 = ka.geo.RP1 + (size_t)kk * nf;
+  for (int t = lane; t < nq + nf; t += tpe) {
+    const bool vol = t < nq;
+    const int r = vol ? t : t - nq;
+    const double p1 = vol ? P1[r] : RP1[r];
+    const float *src = vol ? Bf + r : Af + r;
+    const int stride = vol ? nq : nf;
+    double wi[NC], ui[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) wi[e] = fma(ph.w_ref[e], p1, (double)src[e * stride]);
+    entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui);
+    const size_t o = (size_t)kk * NC * (vol ? nq : nf) + r;
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      if (live)
+        store_state<NC>(ka, vol ? ka.u_q : ka.u_f, vol ? ka.u_qf : ka.u_ff, o + (size_t)e * stride, e, ui[e]);
+      if (!(ui[0] > 0.0) || !isfinite(ui[e])) ka.flag_nonphysical();
+    }
+  }
+}
+
+// The entropy projection of the constant function 1 on every element,
+// P(1) = V M^-1 V^T (W J) with the weight-adjusted inverse, and R P(1).
+template <int D>
+__global__ void __launch_bounds__(256) projection_of_one_kernel(KernelArgs ka, double *P1, double *RP1) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Layout &L = ka.layP1;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int nq = op.nq, nf = op.nf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3],
+         *F = base + L.off[4];
+  for (int t = lane; t < nq; t += tpe) X[t] = ka.geo.WJ[(size_t)kk * nq + t];
+  __syncthreads();
+  vdm_tmul<double, D, 1>(op, X, F, Z, Wb, lane, tpe);
+  mass_solve<double, D, 1>(op, ka.geo.JinvW + (size_t)kk * nq, nullptr, 1, F, X, Z, Wb, lane, tpe);
+  vdm_mul<double, D, 1>(op, F, Y, Z, Wb, lane, tpe);
+  csr_mul<double, 1>(nf, nq, op.R_ptr, op.R_idx, op.R_val, Y, F, lane, tpe);
+  __syncthreads();
+  if (live) {
+    for (int t = lane; t < nq; t += tpe) P1[(size_t)kk * nq + t] = Y[t];
+    for (int t = lane; t < nf; t += tpe) RP1[(size_t)kk * nf + t] = F[t];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Phase B, FluxDifferencingForm
 // ---------------------------------------------------------------------------
 template <int D, int NC>
@@ -191,7 +290,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
   double *base = smem + (size_t)team * L.team_doubles;
   double *uq = base + L.off[0], *uf = base + L.off[1], *ff = base + L.off[2], *rq = base + L.off[3],
          *diff = base + L.off[4], *Lam = base + L.off[5], *hnq = base + L.off[6],
-         *prim = base + L.off[7], *Z = base + L.off[8], *Wb = base + L.off[9];
+         *prim = base + L.off[7];
 
   // stage the element's data
   const double *uqg = ka.u_q + (size_t)kk * NC * nq;
@@ -221,100 +320,42 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
   }
   facet_flux<D, NC>(ka, kk, uf, ff, ec, lane, tpe, (NC > 1 && ec) ? prim + (size_t)nq * PS : nullptr);
 
-  // volume flux differencing, pass 1: per-pair contributions
-  // (flux_difference!, flux_differencing_form.jl:37-75, one flux per unique
-  // pair).  For the EC flux the metric vector G[n] = sum_m S_m (Lambda_i +
-  // Lambda_j)[m, n] is formed first and contracted inside the flux.
-  for (int pidx = lane; pidx < op.nvp; pidx += tpe) {
-    int ij = op.vp_ij[pidx];
-    int i = ij & 0xffff, j = ij >> 16;
-    if constexpr (NC > 1) {
-      if (ec) {
-        double G[D];
+  // volume flux differencing (flux_difference!, flux_differencing_form.jl:
+  // 37-75), one flux per unique pair, over chunks of at most CH pairs so the
+  // per-pair buffer stays small: pass 1 writes each pair's contribution,
+  // pass 2 adds them to r_q at both nodes in ascending pair order
+  // (deterministic; each node keeps a cursor into its incidence list).  For
+  // the EC flux the metric vector G[n] = sum_m S_m (Lambda_i + Lambda_j)[m, n]
+  // is formed first and contracted inside the flux.
+  const int CH = ka.fd_chunk;
+  int cur[kMaxNodeSlots];
 #pragma unroll
-        for (int n = 0; n < D; ++n) G[n] = 0.0;
-#pragma unroll
-        for (int m = 0; m < D; ++m) {
-          const double Sm = op.vp_S[pidx * D + m];
-          if (Sm == 0.0) continue;
-#pragma unroll
-          for (int n = 0; n < D; ++n)
-            G[n] = fma(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
-        }
-        double out[NC];
-        ec_flux_dot<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, out);
-#pragma unroll
-        for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
-        continue;
-      }
-    }
-    double F[NC][D];
-    if constexpr (NC > 1) {
-      {
-        double ui[NC], uj[NC];
-#pragma unroll
-        for (int e = 0; e < NC; ++e) { ui[e] = uq[e * nq + i]; uj[e] = uq[e * nq + j]; }
-        two_point<D, NC>(ph, ui, uj, F);
-      }
-    } else {
-      double ui[1] = {uq[i]}, uj[1] = {uq[j]};
-      two_point<D, NC>(ph, ui, uj, F);
-    }
-    double out[NC];
-#pragma unroll
-    for (int e = 0; e < NC; ++e) out[e] = 0.0;
-#pragma unroll
-    for (int m = 0; m < D; ++m) {
-      double Sm = op.vp_S[pidx * D + m];
-      if (Sm == 0.0) continue;
-      double Lij[D];
-#pragma unroll
-      for (int n = 0; n < D; ++n) Lij[n] = Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)];
-#pragma unroll
-      for (int e = 0; e < NC; ++e) {
-        double Fm = 0.0;
-#pragma unroll
-        for (int n = 0; n < D; ++n) Fm = fma(Lij[n], F[e][n], Fm);
-        out[e] = fma(Sm, Fm, out[e]);
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+  for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+    const int i = lane + sl * tpe;
+    cur[sl] = i < nq ? op.vp_inc_ptr[i] : 0;
+    if (i < nq)
+      for (int e = 0; e < NC; ++e) rq[e * nq + i] = 0.0;
   }
-  __syncthreads();
-  // pass 2: r_q[i] = sum over incident pairs (-diff if i is the first node, +diff otherwise)
-  for (int i = lane; i < nq; i += tpe) {
-    double acc[NC];
-#pragma unroll
-    for (int e = 0; e < NC; ++e) acc[e] = 0.0;
-    for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
-      int inc = op.vp_inc[q];
-      int pidx = inc >> 1;
-      double sgn = (inc & 1) ? -1.0 : 1.0;
-#pragma unroll
-      for (int e = 0; e < NC; ++e) acc[e] = fma(sgn, diff[(size_t)pidx * NC + e], acc[e]);
-    }
-#pragma unroll
-    for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
-  }
-  __syncthreads();
-
-  // facet correction (facet_correction!, flux_differencing_form.jl:126-168)
-  if (op.nfp > 0) {
-    const double *hnf = ka.geo.halfnJf + (size_t)kk * D * nf;
-    for (int pidx = lane; pidx < op.nfp; pidx += tpe) {
-      int ij = op.fp_ij[pidx];
+  for (int c0 = 0; c0 < op.nvp; c0 += CH) {
+    const int c1 = min(op.nvp, c0 + CH);
+    for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+      int ij = op.vp_ij[pidx];
       int i = ij & 0xffff, j = ij >> 16;
-      int f = j / npf;
+      double *dp = diff + (size_t)(pidx - c0) * NC;
       if constexpr (NC > 1) {
         if (ec) {
-          const double Cij = op.fp_C[pidx];
-          double G[D], out[NC];
+          double G[D];
 #pragma unroll
-          for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
-          ec_flux_dot<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, out);
+          for (int n = 0; n < D; ++n) G[n] = 0.0;
 #pragma unroll
-          for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+          for (int m = 0; m < D; ++m) {
+            const double Sm = op.vp_S[pidx * D + m];
+            if (Sm == 0.0) continue;
+#pragma unroll
+            for (int n = 0; n < D; ++n)
+              G[n] = fma(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
+          }
+          ec_flux_dot<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, dp);
           continue;
         }
       }
@@ -323,47 +364,139 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
         {
           double ui[NC], uj[NC];
 #pragma unroll
-          for (int e = 0; e < NC; ++e) { ui[e] = uq[e * nq + i]; uj[e] = uf[e * nf + j]; }
+          for (int e = 0; e < NC; ++e) { ui[e] = uq[e * nq + i]; uj[e] = uq[e * nq + j]; }
           two_point<D, NC>(ph, ui, uj, F);
         }
       } else {
-        double ui[1] = {uq[i]}, uj[1] = {uf[j]};
+        double ui[1] = {uq[i]}, uj[1] = {uq[j]};
         two_point<D, NC>(ph, ui, uj, F);
       }
-      double nJ[D];
+      double out[NC];
 #pragma unroll
-      for (int m = 0; m < D; ++m) nJ[m] = hnf[m + D * j] + hnq[m + D * (f + nfac * i)];
-      double Cij = op.fp_C[pidx];
+      for (int e = 0; e < NC; ++e) out[e] = 0.0;
 #pragma unroll
-      for (int e = 0; e < NC; ++e) {
-        double Fn = 0.0;
+      for (int m = 0; m < D; ++m) {
+        double Sm = op.vp_S[pidx * D + m];
+        if (Sm == 0.0) continue;
+        double Lij[D];
 #pragma unroll
-        for (int m = 0; m < D; ++m) Fn = fma(nJ[m], F[e][m], Fn);
-        diff[(size_t)pidx * NC + e] = Cij * Fn;
+        for (int n = 0; n < D; ++n) Lij[n] = Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) {
+          double Fm = 0.0;
+#pragma unroll
+          for (int n = 0; n < D; ++n) Fm = fma(Lij[n], F[e][n], Fm);
+          out[e] = fma(Sm, Fm, out[e]);
+        }
       }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) dp[e] = out[e];
     }
     __syncthreads();
-    for (int t = lane; t < nq + nf; t += tpe) {
+    // r_q[i] += -diff if i is the pair's first node, +diff otherwise
+#pragma unroll
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int i = lane + sl * tpe;
+      if (i >= nq) continue;
       double acc[NC];
 #pragma unroll
-      for (int e = 0; e < NC; ++e) acc[e] = 0.0;
-      const int *ptr = (t < nq) ? op.fp_q_ptr : op.fp_f_ptr;
-      const int *lst = (t < nq) ? op.fp_q : op.fp_f;
-      int r = (t < nq) ? t : t - nq;
-      for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
-        int pidx = lst[q];
+      for (int e = 0; e < NC; ++e) acc[e] = rq[e * nq + i];
+      int q = cur[sl];
+      const int qe = op.vp_inc_ptr[i + 1];
+      for (; q < qe; ++q) {
+        const int inc = op.vp_inc[q];
+        const int pidx = inc >> 1;
+        if (pidx >= c1) break;
+        const double sgn = (inc & 1) ? -1.0 : 1.0;
+        const double *dp = diff + (size_t)(pidx - c0) * NC;
 #pragma unroll
-        for (int e = 0; e < NC; ++e) acc[e] += diff[(size_t)pidx * NC + e];
+        for (int e = 0; e < NC; ++e) acc[e] = fma(sgn, dp[e], acc[e]);
       }
-      if (t < nq) {
+      cur[sl] = q;
 #pragma unroll
-        for (int e = 0; e < NC; ++e) rq[e * nq + r] -= acc[e];
-      } else {
-#pragma unroll
-        for (int e = 0; e < NC; ++e) ff[e * nf + r] -= acc[e];
-      }
+      for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
     }
     __syncthreads();
+  }
+
+  // facet correction (facet_correction!, flux_differencing_form.jl:126-168),
+  // chunked the same way; each chunk's sum is subtracted from r_q / f_f
+  if (op.nfp > 0) {
+    const double *hnf = ka.geo.halfnJf + (size_t)kk * D * nf;
+#pragma unroll
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int t = lane + sl * tpe;
+      cur[sl] = t < nq ? op.fp_q_ptr[t] : (t < nq + nf ? op.fp_f_ptr[t - nq] : 0);
+    }
+    for (int c0 = 0; c0 < op.nfp; c0 += CH) {
+      const int c1 = min(op.nfp, c0 + CH);
+      for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+        int ij = op.fp_ij[pidx];
+        int i = ij & 0xffff, j = ij >> 16;
+        int f = j / npf;
+        double *dp = diff + (size_t)(pidx - c0) * NC;
+        if constexpr (NC > 1) {
+          if (ec) {
+            const double Cij = op.fp_C[pidx];
+            double G[D];
+#pragma unroll
+            for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+            ec_flux_dot<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, dp);
+            continue;
+          }
+        }
+        double F[NC][D];
+        if constexpr (NC > 1) {
+          {
+            double ui[NC], uj[NC];
+#pragma unroll
+            for (int e = 0; e < NC; ++e) { ui[e] = uq[e * nq + i]; uj[e] = uf[e * nf + j]; }
+            two_point<D, NC>(ph, ui, uj, F);
+          }
+        } else {
+          double ui[1] = {uq[i]}, uj[1] = {uf[j]};
+          two_point<D, NC>(ph, ui, uj, F);
+        }
+        double nJ[D];
+#pragma unroll
+        for (int m = 0; m < D; ++m) nJ[m] = hnf[m + D * j] + hnq[m + D * (f + nfac * i)];
+        double Cij = op.fp_C[pidx];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) {
+          double Fn = 0.0;
+#pragma unroll
+          for (int m = 0; m < D; ++m) Fn = fma(nJ[m], F[e][m], Fn);
+          dp[e] = Cij * Fn;
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+        const int t = lane + sl * tpe;
+        if (t >= nq + nf) continue;
+        double acc[NC];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = 0.0;
+        const bool vol = t < nq;
+        const int r = vol ? t : t - nq;
+        const int *lst = vol ? op.fp_q : op.fp_f;
+        const int qe = vol ? op.fp_q_ptr[r + 1] : op.fp_f_ptr[r + 1];
+        int q = cur[sl];
+        for (; q < qe; ++q) {
+          const int pidx = lst[q];
+          if (pidx >= c1) break;
+          const double *dp = diff + (size_t)(pidx - c0) * NC;
+#pragma unroll
+          for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+        }
+        cur[sl] = q;
+        double *dst = vol ? rq + r : ff + r;
+        const int stride = vol ? nq : nf;
+#pragma unroll
+        for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+      }
+      __syncthreads();
+    }
   }
 
   // r_q -= R^T f_f
@@ -375,8 +508,11 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
   }
   __syncthreads();
 
-  // dudt = V^T r_q ; mass solve  (scratch: diff region reused for modal / nodal buffers)
+  // dudt = V^T r_q ; mass solve  (the pair buffer is free now: it holds the
+  // modal and nodal buffers and the sum-factorisation scratch)
   double *Xm = diff, *Yq = diff + (size_t)NC * np;
+  double *Z = Yq + (size_t)NC * nq;
+  double *Wb = Z + ka.vdm_zsz;
   vdm_tmul<double, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
   mass_solve<double, D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
                     ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq,
@@ -843,9 +979,44 @@ cudaError_t sse_set_smem_limits(const KernelArgs &ka, size_t smA, size_t smB) {
 
 cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st) {
   int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  if (ka.mixed && ka.op.has_vdm && ka.geo.P1) {
+    size_t sm = (size_t)ka.epb * ka.layAm.team_doubles * sizeof(double);
+    if (ka.op.d == 2 && ka.op.nc == 4) nodal_values_mixed_kernel<2, 4><<<grid, ka.tpb, sm, st>>>(ka);
+    else if (ka.op.d == 3 && ka.op.nc == 5) nodal_values_mixed_kernel<3, 5><<<grid, ka.tpb, sm, st>>>(ka);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+  }
   size_t sm = (size_t)ka.epb * ka.layA.team_doubles * sizeof(double);
   SSE_DISPATCH(D, NC, (nodal_values_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka)));
   return cudaGetLastError();
+}
+
+cudaError_t launch_projection_of_one(const KernelArgs &ka, double *P1, double *RP1, cudaStream_t st) {
+  int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  size_t sm = (size_t)ka.epb * ka.layP1.team_doubles * sizeof(double);
+  if (ka.op.d == 2) projection_of_one_kernel<2><<<grid, ka.tpb, sm, st>>>(ka, P1, RP1);
+  else projection_of_one_kernel<3><<<grid, ka.tpb, sm, st>>>(ka, P1, RP1);
+  return cudaGetLastError();
+}
+
+cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka) {
+  cudaError_t e = cudaSuccess;
+  const int am = (int)((size_t)ka.epb * ka.layAm.team_doubles * sizeof(double));
+  const int p1 = (int)((size_t)ka.epb * ka.layP1.team_doubles * sizeof(double));
+  if (ka.op.d == 2 && ka.op.nc == 4) {
+    e = cudaFuncSetAttribute((const void *)nodal_values_mixed_kernel<2, 4>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, am);
+  } else if (ka.op.d == 3 && ka.op.nc == 5) {
+    e = cudaFuncSetAttribute((const void *)nodal_values_mixed_kernel<3, 5>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, am);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(ka.op.d == 2 ? (const void *)projection_of_one_kernel<2>
+                                          : (const void *)projection_of_one_kernel<3>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, p1);
+  return e;
 }
 
 cudaError_t sse_set_smem_limit_mixed(const KernelArgs &ka, size_t smBm) {

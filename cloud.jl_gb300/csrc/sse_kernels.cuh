@@ -8,6 +8,10 @@
 
 namespace sse {
 
+// Nodes (volume plus facet) a thread of an element team handles in the
+// chunked pair passes: n_q + n_f <= kMaxNodeSlots * threads per element.
+constexpr int kMaxNodeSlots = 4;
+
 // Per-team shared-memory layout (offsets in doubles) computed on the host.
 struct Layout {
   int off[12];
@@ -20,6 +24,8 @@ struct KernelArgs {
   Physics ph;
   Layout layA, layB;
   Layout layBm;      // mixed-form phase B layout, offsets and team size in floats
+  Layout layAm;      // mixed-form phase A layout (doubles; FP32 arrays from off[4], in floats)
+  Layout layP1;      // projection of the constant function (NC = 1), doubles
   int ne, epb, tpb;
   int fd, project_entropy, mass_wa;
   const double *u;   // modal state (np x nc x ne)
@@ -39,6 +45,8 @@ struct KernelArgs {
   double *ubar_f;    // adjoint of u_f                (nf x nc x ne, element-major)
   Layout layAdjB1, layAdjB2, layAdjA;
   int pair_chunk;    // pairs per shared-memory chunk in the pair-adjoint passes
+  int fd_chunk;      // pairs per chunk in the FP64 flux-differencing passes
+  int vdm_zsz;       // doubles of the first sum-factorisation scratch (even)
 
   __device__ __forceinline__ void flag_nonphysical() const { atomicOr(flag, 1); }
 };
@@ -50,6 +58,8 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
                                         cudaStream_t st);
 cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st);
 cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st);
+cudaError_t launch_projection_of_one(const KernelArgs &ka, double *P1, double *RP1, cudaStream_t st);
+cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka);
 cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_conservation(const KernelArgs &ka, const double *u, const double *dudt,
                                 double *partial, cudaStream_t st);
