@@ -66,6 +66,15 @@ struct sse_solver {
   bool mixed_ready = false; // FP32 copies allocated
   bool ref_ready = false;   // reference state of the mixed form chosen
   double *d_comp = nullptr; // compensation of the mixed form's stage accumulation
+  // one Runge-Kutta step captured as a CUDA graph, replayed by sse_rk_steps;
+  // rebuilt when any of the values it was captured with changes
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    double *u = nullptr;
+    double dt = 0.0;
+    int scheme = -1, mixed = -1;
+    cudaStream_t stream = nullptr;
+  } step_graph;
   // discrete adjoint: VJP scratch (allocated on first use)
   bool adj_ready = false;
   bool mapP_involution = false;  // mapP(mapP(x)) == x: each interface seen from both sides
@@ -888,6 +897,7 @@ int32_t sse_destroy(sse_solver *s) {
   if (!s) return SSE_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->tape.block) cudaFree(s->tape.block);
+  if (s->step_graph.exec) cudaGraphExecDestroy(s->step_graph.exec);
   for (void *p : s->allocations) cudaFree(p);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -1013,26 +1023,62 @@ int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt, int32
   }
   const bool mixed = s->ka.mixed;
   if (mixed && (e = cudaMemsetAsync(s->d_comp, 0, n * 8, s->stream))) return cuda_fail(s, e, "memset");
-  for (int step = 0; step < n_steps; ++step) {
+  // the mixed form picks its reference state (a synchronising reduction)
+  // before any step is launched or captured
+  if (mixed && n_steps > 0) {
+    int rc = ensure_reference(s, du);
+    if (rc != SSE_OK) return rc;
+  }
+  auto step_once = [&]() -> cudaError_t {
+    cudaError_t err;
     if (scheme == SSE_CARPENTER_KENNEDY_2N54) {
       for (int st = 0; st < 5; ++st) {
-        if ((e = residual_device(s, du, s->d_dudt))) return cuda_fail(s, e, "residual");
-        e = mixed ? launch_ck_stage_compensated(du, s->d_comp, s->d_tmp, s->d_dudt, kCKA[st], kCKB[st],
-                                                dt, st == 0, n, s->stream)
-                  : launch_ck_stage(du, s->d_tmp, s->d_dudt, kCKA[st], kCKB[st], dt, st == 0, n, s->stream);
-        if (e) return cuda_fail(s, e, "stage");
+        if ((err = residual_device(s, du, s->d_dudt))) return err;
+        err = mixed ? launch_ck_stage_compensated(du, s->d_comp, s->d_tmp, s->d_dudt, kCKA[st], kCKB[st],
+                                                  dt, st == 0, n, s->stream)
+                    : launch_ck_stage(du, s->d_tmp, s->d_dudt, kCKA[st], kCKB[st], dt, st == 0, n, s->stream);
+        if (err) return err;
       }
-    } else {
-      const double half = dt / 2;
-      if ((e = residual_device(s, du, s->d_dudt))) return cuda_fail(s, e, "residual");
-      if ((e = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 0.0, half, 1, n, s->stream))) return cuda_fail(s, e, "stage");
-      if ((e = residual_device(s, s->d_ust, s->d_dudt))) return cuda_fail(s, e, "residual");
-      if ((e = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 2.0, half, 0, n, s->stream))) return cuda_fail(s, e, "stage");
-      if ((e = residual_device(s, s->d_ust, s->d_dudt))) return cuda_fail(s, e, "residual");
-      if ((e = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 2.0, dt, 0, n, s->stream))) return cuda_fail(s, e, "stage");
-      if ((e = residual_device(s, s->d_ust, s->d_dudt))) return cuda_fail(s, e, "residual");
-      if ((e = launch_rk4_final(du, s->d_acc, s->d_dudt, dt / 6, n, s->stream))) return cuda_fail(s, e, "stage");
+      return cudaSuccess;
     }
+    const double half = dt / 2;
+    if ((err = residual_device(s, du, s->d_dudt))) return err;
+    if ((err = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 0.0, half, 1, n, s->stream))) return err;
+    if ((err = residual_device(s, s->d_ust, s->d_dudt))) return err;
+    if ((err = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 2.0, half, 0, n, s->stream))) return err;
+    if ((err = residual_device(s, s->d_ust, s->d_dudt))) return err;
+    if ((err = launch_rk4_stage(du, s->d_ust, s->d_acc, s->d_dudt, 2.0, dt, 0, n, s->stream))) return err;
+    if ((err = residual_device(s, s->d_ust, s->d_dudt))) return err;
+    return launch_rk4_final(du, s->d_acc, s->d_dudt, dt / 6, n, s->stream);
+  };
+  // several steps: replay one captured step (one graph launch per step
+  // instead of three kernel launches per stage); direct launches when the
+  // stream cannot be captured (the legacy default stream)
+  sse_solver::StepGraph &G = s->step_graph;
+  if (n_steps >= 2) {
+    const bool same = G.exec && G.u == du && G.dt == dt && G.scheme == scheme && G.mixed == (int)mixed &&
+                      G.stream == s->stream;
+    if (!same) {
+      if (G.exec) cudaGraphExecDestroy(G.exec);
+      G = sse_solver::StepGraph{};
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        cudaError_t ec = step_once();
+        cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
+        if (ec == cudaSuccess && ee == cudaSuccess && graph &&
+            cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess) {
+          G.u = du; G.dt = dt; G.scheme = scheme; G.mixed = (int)mixed; G.stream = s->stream;
+        } else {
+          G.exec = nullptr;
+        }
+        if (graph) cudaGraphDestroy(graph);
+      }
+      cudaGetLastError();  // a refused capture leaves no sticky error; clear the last one
+    }
+  }
+  for (int step = 0; step < n_steps; ++step) {
+    e = (n_steps >= 2 && G.exec) ? cudaGraphLaunch(G.exec, s->stream) : step_once();
+    if (e) return cuda_fail(s, e, "step");
   }
   if (memory == SSE_HOST && (e = cudaMemcpyAsync(u, s->d_u, n * 8, cudaMemcpyDeviceToHost, s->stream)))
     return cuda_fail(s, e, "D2H");
