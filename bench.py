@@ -134,6 +134,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_time_ms(ms: float, world: int, device: str = "cuda") -> float:
+    """Timed region of the slowest rank (replicas only: one independent
+    solver per GPU, no exchange; the job's time is the maximum over ranks)."""
+    if world == 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(dof: int, stages: int, steps: int, ms_max: float, world: int) -> float:
+    """Whole-job DOF-stage updates per second: every rank advances its own
+    copy of the workload (weak scaling)."""
+    return world * dof * stages * steps / (ms_max * 1e-3)
+
+
 def build_problem(workload: str, cells: int | None):
     pkg = __graft_entry__.load_package()
     s = pkg.setups
@@ -379,12 +397,8 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * host.dof * stages * args.steps / (ms * 1e-3)
+    ms = replica_time_ms(ev0.elapsed_time(ev1), world)
+    value = replica_value(host.dof, stages, args.steps, ms, world)
 
     # ---- per-kernel timings (CUDA events on the launching stream) and roofline
     phases = gpu.phase_timings(u, 5)

@@ -737,10 +737,10 @@ int enable_adjoint(sse_solver *s) {
   Layout base{};
   finish(base, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf, d * d * nq, hsz});
   const int max_pairs = std::max(op.nvp, op.nfp);
-  // chunk: as large as keeps two blocks per SM (at least 128 pairs), all
-  // pairs when they fit
-  long room = std::max<long>((long)(110 * 1024 / 8 / ka.epb) - base.team_doubles, 128 * 2 * ps);
-  room = std::min<long>(room, (long)cap - base.team_doubles);
+  // chunk: as large as keeps two blocks per SM when that leaves at least
+  // 128 pairs; otherwise one block per SM with chunks as large as fit
+  long room = (long)(110 * 1024 / 8 / ka.epb) - base.team_doubles;
+  if (room < 128 * 2 * ps) room = (long)cap - base.team_doubles;
   int chunk = (int)std::min<long>(max_pairs, room / (2 * ps));
   if (chunk >= tpe_adj) chunk = chunk / tpe_adj * tpe_adj;
   if (chunk < 1 || ka.layAdjA.team_doubles > (int)cap)
