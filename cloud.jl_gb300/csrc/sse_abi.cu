@@ -78,6 +78,8 @@ struct sse_solver {
   // discrete adjoint: VJP scratch (allocated on first use)
   bool adj_ready = false;
   bool mapP_involution = false;  // mapP(mapP(x)) == x: each interface seen from both sides
+  int mode0 = -1;                // modal index of the constant basis function (modal V)
+  double phi0 = 0.0;             // its (constant) value at the quadrature nodes
   double *d_lam = nullptr, *d_mu = nullptr;
   // trajectory recorded by sse_rk_record for sse_rk_adjoint
   struct Tape {
@@ -279,6 +281,12 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
         b12_index[b1 + p1 * b2] = (int)b12.size();
         b12.push_back(b1 | (b2 << 8));
       }
+    // the constant mode (b1, b2, b3) = 0: its value is the product of the
+    // first entries of the 1-D factors (each constant in its node index)
+    s->mode0 = sigma[0];
+    s->phi0 = ops->vdm_A[0] * ops->vdm_B[0] * (c.d == 3 ? ops->vdm_C[0] : 1.0);
+    if (s->mode0 < 0 || !(std::fabs(s->phi0) > 0.0))
+      return fail(s, SSE_ERR_INVALID_ARGUMENT, "the modal basis has no constant mode");
   }
   // ---- connectivity (validated before any device work)
   std::vector<int> mapP((size_t)c.n_f * c.n_e);
@@ -602,11 +610,7 @@ int enable_mixed(sse_solver *s) {
     auto ev = [](int n) { return (n + 1) & ~1; };
     const int big = nc * std::max(np, (int)nq), bigf = nc * std::max({np, (int)nq, (int)nf});
     Layout &A = ka.layAm;
-    A.off[0] = 0;
-    A.off[1] = A.off[0] + ev(big);
-    A.off[2] = A.off[1] + ev(nc * (int)nq);
-    A.off[3] = A.off[2] + ev(zsz);
-    A.off[4] = A.off[3] + ev(wsz);                 // float region (doubles offset)
+    for (int i = 0; i < 5; ++i) A.off[i] = 0;      // no FP64 arrays: the float region starts at 0
     A.off[5] = 0;                                  // floats from here on
     A.off[6] = A.off[5] + ev(bigf);
     A.off[7] = A.off[6] + ev(nc * (int)nq);
@@ -670,6 +674,16 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
     uref[c.n_c - 1] = ph.E_ref;
     if (c.d == 2) cons_to_entropy_fast<2>(ph.gamma, ph.gm1, ph.igm1, uref, ph.w_ref);
     else cons_to_entropy_fast<3>(ph.gamma, ph.gm1, ph.igm1, uref, ph.w_ref);
+    // constants of the mixed-form entropy maps around the reference state
+    ph.mode0 = s->mode0;
+    for (int e = 0; e < 5; ++e) ph.u_ref_modal[e] = s->phi0 != 0.0 ? uref[e] / s->phi0 : 0.0;
+    ph.ip_ref = 1.0 / ph.p_ref;
+    ph.irho_ref = 1.0 / ph.rho_ref;
+    ph.s_ref = std::log(ph.p_ref) - ph.gamma * std::log(ph.rho_ref);
+    ph.a_ref = -ph.gm1 * ph.w_ref[c.n_c - 1];
+    ph.ia_ref = 1.0 / ph.a_ref;
+    ph.sv_ref = ph.gamma - ph.gm1 * ph.w_ref[0];
+    ph.rhoe_ref = ph.E_ref;  // internal energy p_ref / (gamma - 1) at zero velocity
   }
   if (!(ph.rho_ref > 0.0) || !(ph.p_ref > 0.0))
     return fail(s, SSE_ERR_NONPHYSICAL, "mixed form: mean density or energy not positive");

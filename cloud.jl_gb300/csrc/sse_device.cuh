@@ -111,6 +111,15 @@ struct Physics {
   double theta_ref;  // p_ref / rho_ref
   double H_ref;      // gamma/(gamma-1) theta_ref: enthalpy removed from the energy fluxes
   double w_ref[5];   // entropy variables of the reference state
+  // mixed-form phase A: the reference state's modal coefficient (mode0) and
+  // the constants of the entropy-variable maps around it
+  int mode0;         // modal index of the constant basis function
+  double u_ref_modal[5];
+  double ip_ref, irho_ref;  // 1 / p_ref, 1 / rho_ref
+  double s_ref;             // log(p_ref) - gamma log(rho_ref)
+  double a_ref, ia_ref;     // a_ref and 1 / a_ref with a = -(gamma-1) w_E
+  double sv_ref;            // gamma - (gamma-1) w_0 of the reference state
+  double rhoe_ref;          // (rho e) of the reference state: p_ref / (gamma-1)
 };
 
 // ---------------------------------------------------------------------------
@@ -431,6 +440,51 @@ SSE_HD void entropy_to_cons_jvp(double gamma, double gm1, double igm1, double lo
 #pragma unroll
   for (int m = 0; m < D; ++m) du[m + 1] = dw[m + 1] * rhoe + w[m + 1] * drhoe;
   du[D + 1] = drhoe * (1 - k) - rhoe * dk;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-form entropy-variable maps: the algebra in FP64, the logarithms and
+// the exponential of the small relative deviations from the reference state
+// in FP32 (log1pf / expm1f), so their error is relative to the deviation:
+//   log p - gamma log rho = s_ref + log1p(dp/p_ref) - gamma log1p(drho/rho_ref)
+//   rho e = rhoe_ref exp(dX),  dX = (-gamma log(a/a_ref) - (sv - sv_ref))/(gamma-1)
+// (euler_navierstokes.jl:100-131).
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void cons_to_entropy_mixed(const Physics &ph, const double *u, double *w) {
+  double s2 = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) s2 = fma(u[m + 1], u[m + 1], s2);
+  const double k = 0.5 * s2 * sse_rcp(u[0]);
+  const double p = ph.gm1 * (u[D + 1] - k);
+  const double ip = sse_rcp(p);
+  const float lp = log1pf((float)((p - ph.p_ref) * ph.ip_ref));
+  const float lr = log1pf((float)((u[0] - ph.rho_ref) * ph.irho_ref));
+  const double ls = ph.s_ref + (double)lp - ph.gamma * (double)lr;
+  w[0] = fma(ph.igm1, ph.gamma - ls, -k * ip);
+#pragma unroll
+  for (int m = 0; m < D; ++m) w[m + 1] = u[m + 1] * ip;
+  w[D + 1] = -u[0] * ip;
+}
+
+template <int D>
+__device__ __forceinline__ void entropy_to_cons_mixed(const Physics &ph, const double *w_in, double *u) {
+  double wg[D + 2];
+#pragma unroll
+  for (int e = 0; e < D + 2; ++e) wg[e] = w_in[e] * ph.gm1;
+  double s2 = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) s2 = fma(wg[m + 1], wg[m + 1], s2);
+  const double k = 0.5 * s2 * sse_rcp(wg[D + 1]);
+  const double sv = ph.gamma - wg[0] + k;
+  const double a = -wg[D + 1];
+  const float la = log1pf((float)((a - ph.a_ref) * ph.ia_ref));
+  const double dX = ph.igm1 * (-ph.gamma * (double)la - (sv - ph.sv_ref));
+  const double rhoe = fma(ph.rhoe_ref, (double)expm1f((float)dX), ph.rhoe_ref);
+  u[0] = a * rhoe;
+#pragma unroll
+  for (int m = 0; m < D; ++m) u[m + 1] = wg[m + 1] * rhoe;
+  u[D + 1] = rhoe * (1.0 - k);
 }
 
 // ---------------------------------------------------------------------------

@@ -196,23 +196,30 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
   const int kk = live ? k : 0;
   const int np = op.np, nq = op.nq, nf = op.nf;
   double *base = smem + (size_t)team * L.team_doubles;
-  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wd = base + L.off[3];
   float *fb = reinterpret_cast<float *>(base + L.off[4]);
   float *Af = fb + L.off[5], *Bf = fb + L.off[6], *Cf = fb + L.off[7], *Zf = fb + L.off[8],
         *Wf = fb + L.off[9];
   const double *WJ = ka.geo.WJ + (size_t)kk * nq;
 
+  // u - u_ref in modal coefficients (only the constant mode changes), FP32;
+  // u_q = u_ref + V (u - u_ref) with V applied in FP32
   const double *uk = ka.u + (size_t)kk * NC * np;
-  for (int t = lane; t < NC * np; t += tpe) X[t] = uk[t];
+  for (int t = lane; t < NC * np; t += tpe) {
+    const int e = t / np, l = t - e * np;
+    Cf[t] = (float)(l == ph.mode0 ? uk[t] - ph.u_ref_modal[e] : uk[t]);
+  }
   __syncthreads();
-  vdm_mul<double, D, NC>(op, X, Y, Z, Wd, lane, tpe);  // Y = u_q = V u (FP64)
+  vdm_mul<float, D, NC>(op, Cf, Bf, Zf, Wf, lane, tpe);
   // x' = W J (c2e(u_q) - w_ref), rounded to FP32
   for (int i = lane; i < nq; i += tpe) {
     double ui[NC], wi[NC];
 #pragma unroll
-    for (int e = 0; e < NC; ++e) ui[e] = Y[e * nq + i];
+    for (int e = 0; e < NC; ++e) {
+      const double ref = (e == 0) ? ph.rho_ref : ((e == NC - 1) ? ph.E_ref : 0.0);
+      ui[e] = ref + (double)Bf[e * nq + i];
+    }
     if (!(ui[0] > 0.0)) ka.flag_nonphysical();
-    cons_to_entropy_fast<D>(ph.gamma, ph.gm1, ph.igm1, ui, wi);
+    cons_to_entropy_mixed<D>(ph, ui, wi);
 #pragma unroll
     for (int e = 0; e < NC; ++e) Af[e * nq + i] = (float)(WJ[i] * (wi[e] - ph.w_ref[e]));
   }
@@ -232,7 +239,7 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
     double wi[NC], ui[NC];
 #pragma unroll
     for (int e = 0; e < NC; ++e) wi[e] = fma(ph.w_ref[e], p1, (double)src[e * stride]);
-    entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui);
+    entropy_to_cons_mixed<D>(ph, wi, ui);
     const size_t o = (size_t)kk * NC * (vol ? nq : nf) + r;
 #pragma unroll
     for (int e = 0; e < NC; ++e) {
