@@ -594,13 +594,36 @@ int enable_mixed(sse_solver *s) {
     if (c.d == 2) zsz = nc * op.p1 * op.M2;
     else { zsz = nc * op.nb12 * op.M3; wsz = nc * op.p1 * op.M2 * op.M3; }
   }
-  const int sizes[10] = {nc * (int)nq, nc * (int)nf, nc * (int)nf, nc * (int)nq,
-                         std::max({op.nvp * nc, op.nfp * nc, nc * (np + (int)nq)}), (int)(d * d * nq),
-                         op.nfp > 0 ? (int)(d * c.num_faces * nq) : 0, (int)((nq + nf) * (4 + d)), zsz, wsz};
-  int off = 0, i = 0;
-  for (int sz : sizes) { ka.layBm.off[i++] = off; off += (sz + 3) & ~3; }
-  for (; i < 12; ++i) ka.layBm.off[i] = off;
-  ka.layBm.team_doubles = off;  // counted in floats for this layout
+  // the pair buffer holds one chunk of pair contributions, then the modal /
+  // nodal buffers and the sum-factorisation scratch of the lift; all pairs
+  // at once when four blocks fit on an SM, else chunks (a whole number of
+  // passes of the element's threads) that keep four
+  auto r4 = [](int n) { return (n + 3) & ~3; };
+  const int zsz4 = r4(zsz);
+  const int final_m = nc * (np + (int)nq) + zsz4 + wsz;
+  const int max_pairs = std::max(op.nvp, op.nfp);
+  const int tpe_m = ka.tpb / ka.epb;
+  auto layout_m = [&](int chunk) {
+    const int sizes[8] = {nc * (int)nq, nc * (int)nf, nc * (int)nf, nc * (int)nq,
+                          std::max(chunk * nc, final_m), (int)(d * d * nq),
+                          op.nfp > 0 ? (int)(d * c.num_faces * nq) : 0, (int)((nq + nf) * (4 + d))};
+    int off = 0, i = 0;
+    for (int sz : sizes) { ka.layBm.off[i++] = off; off += r4(sz); }
+    for (; i < 12; ++i) ka.layBm.off[i] = off;
+    ka.layBm.team_doubles = off;  // counted in floats for this layout
+    return off;
+  };
+  const int budget_m = (int)((size_t)55 * 1024 / 4 / ka.epb);
+  int chunk_m = max_pairs;
+  if (layout_m(chunk_m) > budget_m) {
+    const int fixed = layout_m(0) - r4(final_m);
+    chunk_m = std::max(1, (budget_m - fixed) / nc);
+    if (chunk_m >= tpe_m) chunk_m = chunk_m / tpe_m * tpe_m;
+    chunk_m = std::max(1, std::min(chunk_m, max_pairs));
+  }
+  ka.fd_chunk_mixed = chunk_m;
+  ka.vdm_zsz_mixed = zsz4;
+  const int off = layout_m(chunk_m);
   size_t smm = (size_t)ka.epb * off * sizeof(float);
   if (smm > 220 * 1024) return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed kernel");
   if ((e = sse_set_smem_limit_mixed(ka, smm))) return cuda_fail(s, e, "cudaFuncSetAttribute");

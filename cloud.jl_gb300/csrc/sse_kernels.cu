@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
   for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
     const int i = lane + sl * tpe;
     cur[sl] = i < nq ? op.vp_inc_ptr[i] : 0;
-    if (i < nq)
+    if (i < nq && CH < op.nvp)
       for (int e = 0; e < NC; ++e) rq[e * nq + i] = 0.0;
   }
   for (int c0 = 0; c0 < op.nvp; c0 += CH) {
@@ -401,6 +401,25 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
     }
     __syncthreads();
     // r_q[i] += -diff if i is the pair's first node, +diff otherwise
+    if (CH >= op.nvp) {
+      // one chunk: each node sums its whole incidence list
+      for (int i = lane; i < nq; i += tpe) {
+        double acc[NC];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = 0.0;
+        for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
+          const int inc = op.vp_inc[q];
+          const double sgn = (inc & 1) ? -1.0 : 1.0;
+          const double *dp = diff + (size_t)(inc >> 1) * NC;
+#pragma unroll
+          for (int e = 0; e < NC; ++e) acc[e] = fma(sgn, dp[e], acc[e]);
+        }
+#pragma unroll
+        for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
+      }
+      __syncthreads();
+      continue;
+    }
 #pragma unroll
     for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
       const int i = lane + sl * tpe;
@@ -477,6 +496,29 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
         }
       }
       __syncthreads();
+      if (CH >= op.nfp) {
+        // one chunk: each node sums its whole incidence list
+        for (int t = lane; t < nq + nf; t += tpe) {
+          double acc[NC];
+#pragma unroll
+          for (int e = 0; e < NC; ++e) acc[e] = 0.0;
+          const bool vol = t < nq;
+          const int r = vol ? t : t - nq;
+          const int *ptr = vol ? op.fp_q_ptr : op.fp_f_ptr;
+          const int *lst = vol ? op.fp_q : op.fp_f;
+          for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+            const double *dp = diff + (size_t)lst[q] * NC;
+#pragma unroll
+            for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+          }
+          double *dst = vol ? rq + r : ff + r;
+          const int stride = vol ? nq : nf;
+#pragma unroll
+          for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+        }
+        __syncthreads();
+        continue;
+      }
 #pragma unroll
       for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
         const int t = lane + sl * tpe;
@@ -680,7 +722,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   float *base = smem + (size_t)team * L.team_doubles;  // team size in floats for this layout
   float *uq = base + L.off[0], *uf = base + L.off[1], *ff = base + L.off[2], *rq = base + L.off[3],
         *diff = base + L.off[4], *Lam = base + L.off[5], *hnq = base + L.off[6],
-        *prim = base + L.off[7], *Z = base + L.off[8], *Wb = base + L.off[9];
+        *prim = base + L.off[7];
   const int PS = 4 + D;
   const float gm1 = (float)ph.gm1, igm1 = (float)ph.igm1, gam = (float)ph.gamma;
   const float rho_ref = (float)ph.rho_ref, p_ref = (float)ph.p_ref, hl = (float)ph.half_lambda;
@@ -736,81 +778,164 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
     }
   }
 
-  // volume flux differencing: one contracted EC flux per unique pair
+  // volume flux differencing: one contracted EC flux per unique pair, in
+  // chunks of at most CH pairs with per-node cursors (ascending pair order)
   const float *vpS = OpVals<float>::vpS(op);
-  for (int pidx = lane; pidx < op.nvp; pidx += tpe) {
-    int ij = op.vp_ij[pidx];
-    int i = ij & 0xffff, j = ij >> 16;
-    float G[D], out[NC];
+  const int CH = ka.fd_chunk_mixed;
+  int cur[kMaxNodeSlots];
 #pragma unroll
-    for (int n = 0; n < D; ++n) G[n] = 0.f;
-#pragma unroll
-    for (int m = 0; m < D; ++m) {
-      const float Sm = vpS[pidx * D + m];
-      if (Sm == 0.f) continue;
-#pragma unroll
-      for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
-    }
-    ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)j * PS, G, out);
-#pragma unroll
-    for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+  for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+    const int i = lane + sl * tpe;
+    cur[sl] = i < nq ? op.vp_inc_ptr[i] : 0;
+    if (i < nq && CH < op.nvp)
+      for (int e = 0; e < NC; ++e) rq[e * nq + i] = 0.f;
   }
-  __syncthreads();
-  for (int i = lane; i < nq; i += tpe) {
-    float acc[NC];
+  for (int c0 = 0; c0 < op.nvp; c0 += CH) {
+    const int c1 = min(op.nvp, c0 + CH);
+    for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+      int ij = op.vp_ij[pidx];
+      int i = ij & 0xffff, j = ij >> 16;
+      float G[D], out[NC];
 #pragma unroll
-    for (int e = 0; e < NC; ++e) acc[e] = 0.f;
-    for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
-      int inc = op.vp_inc[q];
-      const float *dp = diff + (size_t)(inc >> 1) * NC;
-      if (inc & 1) {
+      for (int n = 0; n < D; ++n) G[n] = 0.f;
 #pragma unroll
-        for (int e = 0; e < NC; ++e) acc[e] -= dp[e];
-      } else {
+      for (int m = 0; m < D; ++m) {
+        const float Sm = vpS[pidx * D + m];
+        if (Sm == 0.f) continue;
 #pragma unroll
-        for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+        for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
       }
+      ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)j * PS, G, out);
+#pragma unroll
+      for (int e = 0; e < NC; ++e) diff[(size_t)(pidx - c0) * NC + e] = out[e];
+    }
+    __syncthreads();
+    if (CH >= op.nvp) {
+      // one chunk: each node sums its whole incidence list
+      for (int i = lane; i < nq; i += tpe) {
+        float acc[NC];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = 0.f;
+        for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
+          const int inc = op.vp_inc[q];
+          const float *dp = diff + (size_t)(inc >> 1) * NC;
+          if (inc & 1) {
+#pragma unroll
+            for (int e = 0; e < NC; ++e) acc[e] -= dp[e];
+          } else {
+#pragma unroll
+            for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
+      }
+      __syncthreads();
+      continue;
     }
 #pragma unroll
-    for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int i = lane + sl * tpe;
+      if (i >= nq) continue;
+      float acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = rq[e * nq + i];
+      int q = cur[sl];
+      const int qe = op.vp_inc_ptr[i + 1];
+      for (; q < qe; ++q) {
+        const int inc = op.vp_inc[q];
+        const int pidx = inc >> 1;
+        if (pidx >= c1) break;
+        const float *dp = diff + (size_t)(pidx - c0) * NC;
+        if (inc & 1) {
+#pragma unroll
+          for (int e = 0; e < NC; ++e) acc[e] -= dp[e];
+        } else {
+#pragma unroll
+          for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+        }
+      }
+      cur[sl] = q;
+#pragma unroll
+      for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
+    }
+    __syncthreads();
   }
-  __syncthreads();
 
-  // facet correction
+  // facet correction, chunked the same way
   if (op.nfp > 0) {
     const float *hnf = g.halfnJff + (size_t)kk * D * nf;
     const float *fpC = OpVals<float>::fpC(op);
-    for (int pidx = lane; pidx < op.nfp; pidx += tpe) {
-      int ij = op.fp_ij[pidx];
-      int i = ij & 0xffff, j = ij >> 16;
-      int f = j / npf;
-      const float Cij = fpC[pidx];
-      float G[D], out[NC];
 #pragma unroll
-      for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
-      ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, out);
-#pragma unroll
-      for (int e = 0; e < NC; ++e) diff[(size_t)pidx * NC + e] = out[e];
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int t = lane + sl * tpe;
+      cur[sl] = t < nq ? op.fp_q_ptr[t] : (t < nq + nf ? op.fp_f_ptr[t - nq] : 0);
     }
-    __syncthreads();
-    for (int t = lane; t < nq + nf; t += tpe) {
-      float acc[NC];
+    for (int c0 = 0; c0 < op.nfp; c0 += CH) {
+      const int c1 = min(op.nfp, c0 + CH);
+      for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+        int ij = op.fp_ij[pidx];
+        int i = ij & 0xffff, j = ij >> 16;
+        int f = j / npf;
+        const float Cij = fpC[pidx];
+        float G[D], out[NC];
 #pragma unroll
-      for (int e = 0; e < NC; ++e) acc[e] = 0.f;
-      const int *ptr = (t < nq) ? op.fp_q_ptr : op.fp_f_ptr;
-      const int *lst = (t < nq) ? op.fp_q : op.fp_f;
-      int r = (t < nq) ? t : t - nq;
-      for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
-        const float *dp = diff + (size_t)lst[q] * NC;
+        for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+        ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, out);
 #pragma unroll
-        for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+        for (int e = 0; e < NC; ++e) diff[(size_t)(pidx - c0) * NC + e] = out[e];
       }
-      float *dst = (t < nq) ? rq + r : ff + r;
-      const int stride = (t < nq) ? nq : nf;
+      __syncthreads();
+      if (CH >= op.nfp) {
+        // one chunk: each node sums its whole incidence list
+        for (int t = lane; t < nq + nf; t += tpe) {
+          float acc[NC];
 #pragma unroll
-      for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+          for (int e = 0; e < NC; ++e) acc[e] = 0.f;
+          const bool vol = t < nq;
+          const int r = vol ? t : t - nq;
+          const int *ptr = vol ? op.fp_q_ptr : op.fp_f_ptr;
+          const int *lst = vol ? op.fp_q : op.fp_f;
+          for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+            const float *dp = diff + (size_t)lst[q] * NC;
+#pragma unroll
+            for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+          }
+          float *dst = vol ? rq + r : ff + r;
+          const int stride = vol ? nq : nf;
+#pragma unroll
+          for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+        }
+        __syncthreads();
+        continue;
+      }
+#pragma unroll
+      for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+        const int t = lane + sl * tpe;
+        if (t >= nq + nf) continue;
+        float acc[NC];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = 0.f;
+        const bool vol = t < nq;
+        const int r = vol ? t : t - nq;
+        const int *lst = vol ? op.fp_q : op.fp_f;
+        const int qe = vol ? op.fp_q_ptr[r + 1] : op.fp_f_ptr[r + 1];
+        int q = cur[sl];
+        for (; q < qe; ++q) {
+          const int pidx = lst[q];
+          if (pidx >= c1) break;
+          const float *dp = diff + (size_t)(pidx - c0) * NC;
+#pragma unroll
+          for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+        }
+        cur[sl] = q;
+        float *dst = vol ? rq + r : ff + r;
+        const int stride = vol ? nq : nf;
+#pragma unroll
+        for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 
   // r_q -= R^T f_f
@@ -823,7 +948,10 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   }
   __syncthreads();
 
+  // the pair buffer holds the modal / nodal buffers and the scratch now
   float *Xm = diff, *Yq = diff + (size_t)NC * np;
+  float *Z = Yq + (size_t)NC * nq;
+  float *Wb = Z + ka.vdm_zsz_mixed;
   vdm_tmul<float, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
   mass_solve<float, D, NC>(op, g.JinvWf ? g.JinvWf + (size_t)kk * nq : nullptr,
                            g.WJinvf ? g.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq, Z,

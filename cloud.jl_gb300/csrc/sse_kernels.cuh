@@ -47,6 +47,8 @@ struct KernelArgs {
   int pair_chunk;    // pairs per shared-memory chunk in the pair-adjoint passes
   int fd_chunk;      // pairs per chunk in the FP64 flux-differencing passes
   int vdm_zsz;       // doubles of the first sum-factorisation scratch (even)
+  int fd_chunk_mixed;  // pairs per chunk in the mixed-form FP32 passes
+  int vdm_zsz_mixed;   // floats of the first sum-factorisation scratch (multiple of 4)
 
   __device__ __forceinline__ void flag_nonphysical() const { atomicOr(flag, 1); }
 };
