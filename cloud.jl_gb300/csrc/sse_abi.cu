@@ -77,6 +77,7 @@ struct sse_solver {
   } step_graph;
   // discrete adjoint: VJP scratch (allocated on first use)
   bool adj_ready = false;
+  bool adj_mixed_ready = false;
   bool mapP_involution = false;  // mapP(mapP(x)) == x: each interface seen from both sides
   int mode0 = -1;                // modal index of the constant basis function (modal V)
   double phi0 = 0.0;             // its (constant) value at the quadrature nodes
@@ -799,6 +800,64 @@ int enable_adjoint(sse_solver *s) {
   return SSE_OK;
 }
 
+// Layouts (in floats) of the mixed-form VJP kernels; needs enable_adjoint
+// and enable_mixed first.
+int enable_adjoint_mixed(sse_solver *s) {
+  if (s->adj_mixed_ready) return SSE_OK;
+  const sse_config &c = s->cfg;
+  KernelArgs &ka = s->ka;
+  const DevOps &op = ka.op;
+  if (!op.has_vdm)
+    return fail(s, SSE_ERR_UNSUPPORTED, "the mixed-form adjoint covers modal (ModalTensor) bases");
+  const int nc = c.n_c, np = c.n_p, nq = c.n_q, nf = c.n_f, d = c.d, ps = 4 + d;
+  int zsz = 0, wsz = 0;
+  if (d == 2) zsz = nc * op.p1 * op.M2;
+  else { zsz = nc * op.nb12 * op.M3; wsz = nc * op.p1 * op.M2 * op.M3; }
+  auto r4 = [](int n) { return (n + 3) & ~3; };
+  auto finish = [&](Layout &L, std::initializer_list<int> sizes) {
+    int off = 0, i = 0;
+    for (int sz : sizes) { L.off[i++] = off; off += r4(sz); }
+    for (; i < 12; ++i) L.off[i] = off;
+    L.team_doubles = off;  // counted in floats for these layouts
+  };
+  const int big = nc * std::max(np, nq), bigf = nc * std::max({np, nq, nf});
+  finish(ka.layAdjB1m, {big, nc * nq, zsz, wsz, bigf});
+  finish(ka.layAdjAm, {big, nc * nq, nc * nq, nc * nq, nc * nf, big, nc * nq, zsz, wsz, nc * nf});
+  const int hsz = op.nfp > 0 ? d * c.num_faces * nq : 0;
+  Layout base{};
+  finish(base, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf, d * d * nq, hsz});
+  const int max_pairs = std::max(op.nvp, op.nfp);
+  const int tpe_adj = ka.tpb / ka.epb;
+  const long cap = (long)(220 * 1024 / 4 / ka.epb);          // floats per team
+  long room = (long)(55 * 1024 / 4 / ka.epb) - base.team_doubles;  // four blocks per SM
+  if (room < 128 * 2 * ps) room = (long)(110 * 1024 / 4 / ka.epb) - base.team_doubles;  // two
+  if (room < 128 * 2 * ps) room = cap - base.team_doubles;
+  int chunk = (int)std::min<long>(max_pairs, room / (2 * ps));
+  if (chunk >= tpe_adj) chunk = chunk / tpe_adj * tpe_adj;
+  if (chunk < 1 || (long)ka.layAdjAm.team_doubles > cap)
+    return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed-form adjoint kernels");
+  ka.pair_chunk_mixed = chunk;
+  finish(ka.layAdjB2m, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf,
+                        d * d * nq, hsz, chunk * 2 * ps});
+  cudaError_t e;
+  if ((e = sse_set_smem_limits_adjoint_mixed(ka))) return cuda_fail(s, e, "cudaFuncSetAttribute (mixed adjoint)");
+  s->adj_mixed_ready = true;
+  return SSE_OK;
+}
+
+// mu = (dR/du)^T lam for the mixed form at u: its phase A writes the FP32
+// perturbation states, then the FP32 transposes run with lam~.
+cudaError_t vjp_device_mixed(sse_solver *s, const double *u, const double *lam, double *mu) {
+  KernelArgs ka = s->ka;
+  ka.mixed = 1;
+  ka.u = u;
+  ka.lam = lam;
+  ka.mu = mu;
+  cudaError_t e = launch_nodal_values(ka, s->stream);
+  if (e != cudaSuccess) return e;
+  return launch_residual_vjp_mixed_kernels(ka, s->stream);
+}
+
 // mu = (dR/du)^T lam on device buffers.  u_q / u_f: the FP64 nodal states of
 // u when already computed (a recorded stage), else phase A runs first.
 cudaError_t vjp_device(sse_solver *s, const double *u, const double *lam, double *mu,
@@ -1130,15 +1189,23 @@ int32_t sse_residual_vjp(sse_solver *s, const double *u, const double *lam, doub
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
   int rc = enable_adjoint(s);
   if (rc != SSE_OK) return rc;
+  const bool mixed = s->ka.mixed != 0;
+  if (mixed && (rc = enable_adjoint_mixed(s)) != SSE_OK) return rc;
   const size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
   cudaError_t e;
+  auto run = [&](const double *du, const double *dl, double *dm) -> cudaError_t {
+    return mixed ? vjp_device_mixed(s, du, dl, dm) : vjp_device(s, du, dl, dm);
+  };
   if (memory == SSE_DEVICE) {
-    if ((e = vjp_device(s, u, lam, mu))) return cuda_fail(s, e, "residual vjp");
+    // the mixed form picks its reference state on its first call
+    if (mixed && (rc = ensure_reference(s, u)) != SSE_OK) return rc;
+    if ((e = run(u, lam, mu))) return cuda_fail(s, e, "residual vjp");
   } else {
     if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream)) ||
         (e = cudaMemcpyAsync(s->d_lam, lam, n * 8, cudaMemcpyHostToDevice, s->stream)))
       return cuda_fail(s, e, "H2D");
-    if ((e = vjp_device(s, s->d_u, s->d_lam, s->d_mu))) return cuda_fail(s, e, "residual vjp");
+    if (mixed && (rc = ensure_reference(s, s->d_u)) != SSE_OK) return rc;
+    if ((e = run(s->d_u, s->d_lam, s->d_mu))) return cuda_fail(s, e, "residual vjp");
     if ((e = cudaMemcpyAsync(mu, s->d_mu, n * 8, cudaMemcpyDeviceToHost, s->stream))) return cuda_fail(s, e, "D2H");
   }
   return check_flag(s);
@@ -1271,7 +1338,12 @@ int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double
   // the recomputation runs in the recorded precision; the stage adjoints in FP64
   const int saved_mixed = s->ka.mixed;
   s->ka.mixed = T.mixed ? 1 : 0;
+  if (T.mixed) {
+    int rc = enable_adjoint_mixed(s);
+    if (rc != SSE_OK) return rc;
+  }
   auto stage_vjp = [&](size_t q, const double *lam) -> cudaError_t {
+    if (T.mixed) return vjp_device_mixed(s, T.seg_y + q * n, lam, s->d_mu);
     const double *uq = T.nodal ? T.seg_uq + q * nqs : nullptr;
     const double *uf = T.nodal ? T.seg_uf + q * nfs : nullptr;
     return vjp_device(s, T.seg_y + q * n, lam, s->d_mu, uq, uf);

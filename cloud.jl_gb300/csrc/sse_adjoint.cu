@@ -401,6 +401,399 @@ __global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
     for (int t = lane; t < NC * np; t += tpe) ka.mu[(size_t)kk * NC * np + t] = F[t];
 }
 
+// ===========================================================================
+// Mixed-form vector-Jacobian product: the transposes of the mixed residual
+// (FP32 fluxes on perturbations, FP32 projection arithmetic), with the
+// cotangent of the reduced residual lam~ = (lam_rho + H_ref lam_E, lam_m,
+// lam_E).  The FP32 buffers live in the FP64 VJP scratch (reinterpreted).
+// ===========================================================================
+
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_lift_mixed_kernel(KernelArgs ka) {
+  extern __shared__ double smem_raw[];
+  float *smem = reinterpret_cast<float *>(smem_raw);
+  const DevOps &op = ka.op;
+  const Layout &L = ka.layAdjB1m;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  float *base = smem + (size_t)team * L.team_doubles;  // floats
+  float *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3],
+        *F = base + L.off[4];
+  const double *lk = ka.lam + (size_t)kk * NC * np;
+  for (int t = lane; t < NC * np; t += tpe) {
+    const int e = t / np;
+    const double v = (e == 0) ? fma(ka.ph.H_ref, lk[t + (NC - 1) * np], lk[t]) : lk[t];
+    X[t] = (float)v;
+  }
+  __syncthreads();
+  mass_solve<float, D, NC>(op, ka.geo.JinvWf ? ka.geo.JinvWf + (size_t)kk * nq : nullptr,
+                           ka.geo.WJinvf ? ka.geo.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, X, Y, Z,
+                           Wb, lane, tpe);
+  vdm_mul<float, D, NC>(op, X, Y, Z, Wb, lane, tpe);
+  float *rbq = reinterpret_cast<float *>(ka.rbar_q);
+  float *gbf = reinterpret_cast<float *>(ka.gbar_f);
+  if (live)
+    for (int t = lane; t < NC * nq; t += tpe) rbq[(size_t)kk * NC * nq + t] = Y[t];
+  csr_mul<float, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_valf, Y, F, lane, tpe);
+  __syncthreads();
+  if (live)
+    for (int t = lane; t < NC * nf; t += tpe)
+      gbf[(size_t)kk * NC * nf + t] = -F[t] * ka.geo.BJff[(size_t)kk * nf + t % nf];
+}
+
+// transpose of the mixed-form Lax-Friedrichs interface flux w.r.t. one side
+// (reduced energy: the jump's energy component is E' - H_ref rho')
+template <int D, int NC>
+__device__ void lf_flux_mixed_bwd(const Physics &ph, float igm1, float rho_ref, float theta_ref, float H_ref,
+                                  const float *uin, const float *uout, const float *Pin, const float *Pout,
+                                  const float *n, const float *g, int side, float *Pb, float *ub_direct) {
+  float Pbi[4 + D], Pbo[4 + D];
+  ec_flux_dot_mixed_bwd<D>(igm1, rho_ref, theta_ref, Pin, Pout, n, g, Pbi, Pbo);
+  const float *Pself = side ? Pbo : Pbi;
+#pragma unroll
+  for (int c = 0; c < 4 + D; ++c) Pb[c] += Pself[c];
+  if (ph.nflux != 0) return;
+  const float hl = (float)ph.half_lambda, gam = (float)ph.gamma;
+  float vni = 0.f, vno = 0.f;
+#pragma unroll
+  for (int m = 0; m < D; ++m) { vni = fmaf(Pin[3 + m], n[m], vni); vno = fmaf(Pout[3 + m], n[m], vno); }
+  const float ci = sqrtf(gam * (theta_ref + Pin[2])), co = sqrtf(gam * (theta_ref + Pout[2]));
+  const float a = hl * (fmaxf(fabsf(vni), fabsf(vno)) + fmaxf(ci, co));
+  float abar = 0.f;
+#pragma unroll
+  for (int e = 0; e < NC; ++e) abar = fmaf(g[e], uin[e] - uout[e], abar);
+  abar = fmaf(-H_ref * g[NC - 1], uin[0] - uout[0], abar);
+  const float sg_side = side ? -1.f : 1.f;
+#pragma unroll
+  for (int e = 0; e < NC; ++e) ub_direct[e] += sg_side * a * g[e];
+  ub_direct[0] -= sg_side * a * H_ref * g[NC - 1];
+  const float hb = hl * abar;
+  const bool v_in = fabsf(vni) >= fabsf(vno);
+  const bool c_in = ci >= co;
+  if (v_in == (side == 0)) {
+    const float vn = side ? vno : vni;
+    const float sg = vn >= 0.f ? 1.f : -1.f;
+#pragma unroll
+    for (int m = 0; m < D; ++m) Pb[3 + m] += hb * sg * n[m];
+  }
+  if (c_in == (side == 0)) {
+    const float c = side ? co : ci;
+    Pb[2] += hb * gam / (2.f * c);
+  }
+}
+
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_flux_mixed_kernel(KernelArgs ka) {
+  static_assert(NC == D + 2, "adjoint of the Euler flux-differencing residual");
+  extern __shared__ double smem_raw[];
+  float *smem = reinterpret_cast<float *>(smem_raw);
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const DevGeo &g = ka.geo;
+  const Layout &L = ka.layAdjB2m;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  const int PS = 4 + D;
+  const float gm1 = (float)ph.gm1, igm1 = (float)ph.igm1;
+  const float rho_ref = (float)ph.rho_ref, p_ref = (float)ph.p_ref;
+  const float theta_ref = (float)ph.theta_ref, H_ref = (float)ph.H_ref;
+  float *base = smem + (size_t)team * L.team_doubles;
+  float *uq = base + L.off[0], *uf = base + L.off[1], *rb = base + L.off[2], *fb = base + L.off[3],
+        *prim = base + L.off[4], *Pb = base + L.off[5], *ubd = base + L.off[6], *Lam = base + L.off[7],
+        *hnq = base + L.off[8], *buf = base + L.off[9];
+  const float *rbq = reinterpret_cast<const float *>(ka.rbar_q);
+  const float *gbf = reinterpret_cast<const float *>(ka.gbar_f);
+
+  for (int t = lane; t < NC * nq; t += tpe) {
+    uq[t] = ka.u_qf[(size_t)kk * NC * nq + t];
+    rb[t] = rbq[(size_t)kk * NC * nq + t];
+  }
+  for (int t = lane; t < NC * nf; t += tpe) {
+    uf[t] = ka.u_ff[(size_t)kk * NC * nf + t];
+    ubd[t] = 0.f;
+  }
+  for (int t = lane; t < nq * D * D; t += tpe) Lam[t] = g.Lambda_qf[(size_t)kk * nq * D * D + t];
+  if (op.nfp > 0)
+    for (int t = lane; t < D * nfac * nq; t += tpe) hnq[t] = g.halfnJqf[(size_t)kk * D * nfac * nq + t];
+  for (int t = lane; t < (nq + nf) * PS; t += tpe) Pb[t] = 0.f;
+  __syncthreads();
+  for (int i = lane; i < nq + nf; i += tpe) {
+    float du[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) du[e] = (i < nq) ? uq[e * nq + i] : uf[e * nf + (i - nq)];
+    euler_prim_mixed<D>(gm1, rho_ref, p_ref, du, prim + (size_t)i * PS);
+  }
+  csr_mul<float, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_valf, rb, fb, lane, tpe);
+  __syncthreads();
+  for (int t = lane; t < NC * nf; t += tpe) fb[t] = -fb[t];
+
+  // interface flux: own flux w.r.t. the inner state, neighbour's w.r.t. its outer state
+  for (int j = lane; j < nf; j += tpe) {
+    const int P = g.mapP[(size_t)kk * nf + j];
+    const int jn = P % nf, kn = P / nf;
+    float ui[NC], uo[NC], Po[4 + D], n[D], nn[D], gown[NC], gnb[NC], ub[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      ui[e] = uf[e * nf + j];
+      uo[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
+      gown[e] = gbf[((size_t)kk * NC + e) * nf + j];
+      gnb[e] = gbf[((size_t)kn * NC + e) * nf + jn];
+      ub[e] = 0.f;
+    }
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      n[m] = g.n_ff[m + D * (j + (size_t)nf * kk)];
+      nn[m] = g.n_ff[m + D * (jn + (size_t)nf * kn)];
+    }
+    euler_prim_mixed<D>(gm1, rho_ref, p_ref, uo, Po);
+    float *Pself = Pb + (size_t)(nq + j) * PS;
+    const float *Pi = prim + (size_t)(nq + j) * PS;
+    lf_flux_mixed_bwd<D, NC>(ph, igm1, rho_ref, theta_ref, H_ref, ui, uo, Pi, Po, n, gown, 0, Pself, ub);
+    lf_flux_mixed_bwd<D, NC>(ph, igm1, rho_ref, theta_ref, H_ref, uo, ui, Po, Pi, nn, gnb, 1, Pself, ub);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) ubd[e * nf + j] += ub[e];
+  }
+  __syncthreads();
+
+  // volume pairs: dbar_p = rbar[j] - rbar[i]
+  const int CH = ka.pair_chunk_mixed;
+  const float *vpS = op.vp_Sf;
+  int cur[kMaxNodeSlots];
+#pragma unroll
+  for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+    const int i = lane + sl * tpe;
+    cur[sl] = i < nq ? op.vp_inc_ptr[i] : 0;
+  }
+  for (int c0 = 0; c0 < op.nvp; c0 += CH) {
+    const int c1 = min(op.nvp, c0 + CH);
+    for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+      const int ij = op.vp_ij[pidx];
+      const int i = ij & 0xffff, j = ij >> 16;
+      float G[D], db[NC];
+#pragma unroll
+      for (int n_ = 0; n_ < D; ++n_) G[n_] = 0.f;
+#pragma unroll
+      for (int m = 0; m < D; ++m) {
+        const float Sm = vpS[pidx * D + m];
+        if (Sm == 0.f) continue;
+#pragma unroll
+        for (int n_ = 0; n_ < D; ++n_)
+          G[n_] = fmaf(Sm, Lam[i + nq * (m + D * n_)] + Lam[j + nq * (m + D * n_)], G[n_]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) db[e] = rb[e * nq + j] - rb[e * nq + i];
+      float *slot = buf + (size_t)(pidx - c0) * 2 * PS;
+      ec_flux_dot_mixed_bwd<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)j * PS, G, db,
+                               slot, slot + PS);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int i = lane + sl * tpe;
+      if (i >= nq) continue;
+      float acc[4 + D];
+#pragma unroll
+      for (int c = 0; c < PS; ++c) acc[c] = 0.f;
+      int q = cur[sl];
+      const int qe = op.vp_inc_ptr[i + 1];
+      for (; q < qe; ++q) {
+        const int inc = op.vp_inc[q];
+        const int pidx = inc >> 1;
+        if (pidx >= c1) break;
+        const float *slot = buf + (size_t)(pidx - c0) * 2 * PS + ((inc & 1) ? 0 : PS);
+#pragma unroll
+        for (int c = 0; c < PS; ++c) acc[c] += slot[c];
+      }
+      cur[sl] = q;
+#pragma unroll
+      for (int c = 0; c < PS; ++c) Pb[(size_t)i * PS + c] += acc[c];
+    }
+    __syncthreads();
+  }
+
+  // facet correction pairs: dbar_p = -rbar[i] - fbar_f[j]
+  if (op.nfp > 0) {
+    const float *hnf = g.halfnJff + (size_t)kk * D * nf;
+    const float *fpC = op.fp_Cf;
+#pragma unroll
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int t = lane + sl * tpe;
+      cur[sl] = t < nq ? op.fp_q_ptr[t] : (t < nq + nf ? op.fp_f_ptr[t - nq] : 0);
+    }
+    for (int c0 = 0; c0 < op.nfp; c0 += CH) {
+      const int c1 = min(op.nfp, c0 + CH);
+      for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+        const int ij = op.fp_ij[pidx];
+        const int i = ij & 0xffff, j = ij >> 16;
+        const int f = j / npf;
+        const float Cij = fpC[pidx];
+        float G[D], db[NC];
+#pragma unroll
+        for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+#pragma unroll
+        for (int e = 0; e < NC; ++e) db[e] = -rb[e * nq + i] - fb[e * nf + j];
+        float *slot = buf + (size_t)(pidx - c0) * 2 * PS;
+        ec_flux_dot_mixed_bwd<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS,
+                                 G, db, slot, slot + PS);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+        const int t = lane + sl * tpe;
+        if (t >= nq + nf) continue;
+        const bool vol = t < nq;
+        const int r = vol ? t : t - nq;
+        const int *lst = vol ? op.fp_q : op.fp_f;
+        const int qe = vol ? op.fp_q_ptr[r + 1] : op.fp_f_ptr[r + 1];
+        float acc[4 + D];
+#pragma unroll
+        for (int c = 0; c < PS; ++c) acc[c] = 0.f;
+        int q = cur[sl];
+        for (; q < qe; ++q) {
+          const int pidx = lst[q];
+          if (pidx >= c1) break;
+          const float *slot = buf + (size_t)(pidx - c0) * 2 * PS + (vol ? 0 : PS);
+#pragma unroll
+          for (int c = 0; c < PS; ++c) acc[c] += slot[c];
+        }
+        cur[sl] = q;
+#pragma unroll
+        for (int c = 0; c < PS; ++c) Pb[(size_t)t * PS + c] += acc[c];
+      }
+      __syncthreads();
+    }
+  }
+
+  // primitive cotangents -> cotangents of the stored perturbations u_q', u_f'
+  float *ubq = reinterpret_cast<float *>(ka.ubar_q);
+  float *ubf = reinterpret_cast<float *>(ka.ubar_f);
+  if (live) {
+    for (int t = lane; t < nq + nf; t += tpe) {
+      const bool vol = t < nq;
+      const int r = vol ? t : t - nq;
+      float ub[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) ub[e] = vol ? 0.f : ubd[e * nf + r];
+      euler_prim_mixed_bwd<D>(gm1, theta_ref, prim + (size_t)t * PS, Pb + (size_t)t * PS, ub);
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        if (vol) ubq[(size_t)kk * NC * nq + e * nq + r] = ub[e];
+        else ubf[((size_t)kk * NC + e) * nf + r] = ub[e];
+      }
+    }
+  }
+}
+
+// transpose of the mixed-form entropy projection (nodal_values_mixed_kernel)
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka) {
+  static_assert(NC == D + 2, "mixed form of the Euler entropy projection");
+  extern __shared__ double smem_raw[];
+  float *smem = reinterpret_cast<float *>(smem_raw);
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const Layout &L = ka.layAdjAm;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  float *base = smem + (size_t)team * L.team_doubles;
+  float *U1 = base + L.off[0], *Q0 = base + L.off[1], *XQ = base + L.off[2], *WQ = base + L.off[3],
+        *WF = base + L.off[4], *T1 = base + L.off[5], *S1 = base + L.off[6], *Zf = base + L.off[7],
+        *Wf = base + L.off[8], *BF = base + L.off[9];
+  const double *WJ = ka.geo.WJ + (size_t)kk * nq;
+  const float *JinvWf = ka.geo.JinvWf + (size_t)kk * nq;
+  const double *P1 = ka.geo.P1 + (size_t)kk * nq, *RP1 = ka.geo.RP1 + (size_t)kk * nf;
+
+  // ---- forward recompute (as nodal_values_mixed_kernel)
+  const double *uk = ka.u + (size_t)kk * NC * np;
+  for (int t = lane; t < NC * np; t += tpe) {
+    const int e = t / np, l = t - e * np;
+    U1[t] = (float)(l == ph.mode0 ? uk[t] - ph.u_ref_modal[e] : uk[t]);
+  }
+  __syncthreads();
+  vdm_mul<float, D, NC>(op, U1, Q0, Zf, Wf, lane, tpe);  // u_q0'
+  for (int i = lane; i < nq; i += tpe) {
+    double ui[NC], wi[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      const double ref = (e == 0) ? ph.rho_ref : ((e == NC - 1) ? ph.E_ref : 0.0);
+      ui[e] = ref + (double)Q0[e * nq + i];
+    }
+    cons_to_entropy_mixed<D>(ph, ui, wi);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) XQ[e * nq + i] = (float)(WJ[i] * (wi[e] - ph.w_ref[e]));
+  }
+  __syncthreads();
+  vdm_tmul<float, D, NC>(op, XQ, T1, Zf, Wf, lane, tpe);
+  mass_solve<float, D, NC>(op, JinvWf, nullptr, 1, T1, S1, Zf, Wf, lane, tpe);
+  vdm_mul<float, D, NC>(op, T1, WQ, Zf, Wf, lane, tpe);                      // w'_q
+  csr_mul<float, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_valf, WQ, WF, lane, tpe);  // w'_f
+  __syncthreads();
+
+  // ---- backward: facet then volume entropy-to-conservative transposes
+  const float *ubq = reinterpret_cast<const float *>(ka.ubar_q);
+  const float *ubf = reinterpret_cast<const float *>(ka.ubar_f);
+  for (int t = lane; t < nq + nf; t += tpe) {
+    const bool vol = t < nq;
+    const int r = vol ? t : t - nq;
+    const double p1 = vol ? P1[r] : RP1[r];
+    const float *src = vol ? WQ + r : WF + r;
+    const int stride = vol ? nq : nf;
+    double wi[NC], bi[NC], ri[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      wi[e] = fma(ph.w_ref[e], p1, (double)src[e * stride]);
+      bi[e] = vol ? (double)ubq[(size_t)kk * NC * nq + e * nq + r] : (double)ubf[((size_t)kk * NC + e) * nf + r];
+    }
+    const double rhoe = entropy_to_cons_mixed_rhoe<D>(ph, wi);
+    entropy_to_cons_jvp_rhoe<D>(ph.gm1, ph.igm1, ph.gamma, wi, rhoe, bi, ri);
+    float *dst = vol ? S1 + r : BF + r;
+#pragma unroll
+    for (int e = 0; e < NC; ++e) dst[e * stride] = (float)ri[e];
+  }
+  __syncthreads();
+  // wbar_q += R^T wbar_f
+  for (int t = lane; t < NC * nq; t += tpe) {
+    const int i = t % nq, e = t / nq;
+    float acc = 0.f;
+    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc = fmaf(op.Rt_valf[q], BF[e * nf + op.Rt_idx[q]], acc);
+    XQ[t] = S1[t] + acc;
+  }
+  __syncthreads();
+  // projection transpose (V M V^T is symmetric): the same operators
+  vdm_tmul<float, D, NC>(op, XQ, T1, Zf, Wf, lane, tpe);
+  mass_solve<float, D, NC>(op, JinvWf, nullptr, 1, T1, S1, Zf, Wf, lane, tpe);
+  vdm_mul<float, D, NC>(op, T1, XQ, Zf, Wf, lane, tpe);
+  // ubar_q0 = J_c2e(u_q0)^T (W J x), symmetric Jacobian
+  for (int i = lane; i < nq; i += tpe) {
+    double ui[NC], bi[NC], ri[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      const double ref = (e == 0) ? ph.rho_ref : ((e == NC - 1) ? ph.E_ref : 0.0);
+      ui[e] = ref + (double)Q0[e * nq + i];
+      bi[e] = WJ[i] * (double)XQ[e * nq + i];
+    }
+    cons_to_entropy_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ui, bi, ri);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) XQ[e * nq + i] = (float)ri[e];
+  }
+  __syncthreads();
+  vdm_tmul<float, D, NC>(op, XQ, T1, Zf, Wf, lane, tpe);  // mu = V^T ubar_q0
+  if (live)
+    for (int t = lane; t < NC * np; t += tpe) ka.mu[(size_t)kk * NC * np + t] = (double)T1[t];
+}
+
 // ---------------------------------------------------------------------------
 // elementwise pieces of the adjoint Runge-Kutta sweep
 //
@@ -480,6 +873,46 @@ cudaError_t sse_set_smem_limits_adjoint(const KernelArgs &ka) {
     return cudaErrorInvalidValue;
   }
   return e;
+}
+
+cudaError_t sse_set_smem_limits_adjoint_mixed(const KernelArgs &ka) {
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void *f, const Layout &L) {
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)((size_t)ka.epb * L.team_doubles * sizeof(float)));
+  };
+  if (ka.op.d == 2 && ka.op.nc == 4) {
+    set((const void *)adj_lift_mixed_kernel<2, 4>, ka.layAdjB1m);
+    set((const void *)adj_flux_mixed_kernel<2, 4>, ka.layAdjB2m);
+    set((const void *)adj_projection_mixed_kernel<2, 4>, ka.layAdjAm);
+  } else if (ka.op.d == 3 && ka.op.nc == 5) {
+    set((const void *)adj_lift_mixed_kernel<3, 5>, ka.layAdjB1m);
+    set((const void *)adj_flux_mixed_kernel<3, 5>, ka.layAdjB2m);
+    set((const void *)adj_projection_mixed_kernel<3, 5>, ka.layAdjAm);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  return e;
+}
+
+cudaError_t launch_residual_vjp_mixed_kernels(const KernelArgs &ka, cudaStream_t st) {
+  const int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  const size_t s1 = (size_t)ka.epb * ka.layAdjB1m.team_doubles * sizeof(float);
+  const size_t s2 = (size_t)ka.epb * ka.layAdjB2m.team_doubles * sizeof(float);
+  const size_t s3 = (size_t)ka.epb * ka.layAdjAm.team_doubles * sizeof(float);
+  if (ka.op.d == 2 && ka.op.nc == 4) {
+    adj_lift_mixed_kernel<2, 4><<<grid, ka.tpb, s1, st>>>(ka);
+    adj_flux_mixed_kernel<2, 4><<<grid, ka.tpb, s2, st>>>(ka);
+    adj_projection_mixed_kernel<2, 4><<<grid, ka.tpb, s3, st>>>(ka);
+  } else if (ka.op.d == 3 && ka.op.nc == 5) {
+    adj_lift_mixed_kernel<3, 5><<<grid, ka.tpb, s1, st>>>(ka);
+    adj_flux_mixed_kernel<3, 5><<<grid, ka.tpb, s2, st>>>(ka);
+    adj_projection_mixed_kernel<3, 5><<<grid, ka.tpb, s3, st>>>(ka);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_residual_vjp_kernels(const KernelArgs &ka, cudaStream_t st) {

@@ -614,6 +614,179 @@ SSE_HD void ec_flux_dot_mixed(float igm1, float rho_ref, float theta_ref, const 
                                  0.5f * fmaf(Pi[3 + D], gvj, Pj[3 + D] * gvi)));
 }
 
+// ---------------------------------------------------------------------------
+// Reverse mode of the mixed form (FP32): transposes of euler_prim_mixed and
+// ec_flux_dot_mixed.  The residual's energy component is H_ref times the
+// density residual plus the reduced-flux residual, so for a cotangent lam of
+// the residual the reduced fluxes see lam~ = (lam_rho + H_ref lam_E, lam_m,
+// lam_E); their Jacobians carry no enthalpy-sized terms, which keeps FP32
+// accurate at low Mach.  Checked against the FP64 transposes in
+// tests/device_math_check.cu.
+// ---------------------------------------------------------------------------
+
+// q'(z) for q = 1 + z/3 + z^2/5 + ... (the FP32 series)
+SSE_HD float q_series_f_deriv(float z) {
+  return fmaf(z, fmaf(z, fmaf(z, fmaf(z, 5.f / 11.f, 4.f / 9.f), 3.f / 7.f), 0.4f), 1.f / 3.f);
+}
+
+// partial derivatives of logmean(x, y) (the value of the mixed form comes
+// from logmean_minus_ref)
+SSE_HD void logmean_f_grad(float x, float y, float *dx, float *dy) {
+  const float s = x + y;
+  const float f = (x - y) / s;
+  const float z = f * f;
+  if (z < 0.05f) {
+    const float q = q_series_f(z), iq = 1.f / q;
+    const float c = 2.f * q_series_f_deriv(z) * f * iq * iq / s;
+    *dx = fmaf(-c, y, 0.5f * iq);
+    *dy = fmaf(c, x, 0.5f * iq);
+    return;
+  }
+  const float L = logf(y / x), iL = 1.f / L, N = y - x;
+  *dx = (N / x - L) * iL * iL;
+  *dy = (L - N / y) * iL * iL;
+}
+
+// partial derivatives of inv_logmean(1/theta_i, 1/theta_j) w.r.t. the
+// temperatures theta_i, theta_j: q(z) hm with hm = 2 ti tj/(ti + tj),
+// f = (tj - ti)/(ti + tj) on the series branch
+SSE_HD void inv_logmean_theta_grad(float ti, float tj, float *di, float *dj) {
+  const float sg = ti + tj;
+  const float f = (tj - ti) / sg;
+  const float z = f * f;
+  if (z < 0.05f) {
+    const float q = q_series_f(z), qp = q_series_f_deriv(z);
+    const float is2 = 1.f / (sg * sg);
+    const float hm = 2.f * ti * tj / sg;
+    *di = fmaf(qp * hm, -4.f * f * tj * is2, q * 2.f * tj * tj * is2);
+    *dj = fmaf(qp * hm, 4.f * f * ti * is2, q * 2.f * ti * ti * is2);
+    return;
+  }
+  const float L = logf(ti / tj), N = ti - tj, iN = 1.f / N;
+  const float w = ti * tj * L * iN * iN;
+  *di = fmaf(tj, (L + 1.f) * iN, -w);
+  *dj = fmaf(ti, (L - 1.f) * iN, w);
+}
+
+// Transpose of ec_flux_dot_mixed w.r.t. the two primitive vectors (layout
+// [rho, rho', theta', V_1..V_D, p']); the density cotangent is returned in
+// slot 1 (rho' and rho are the same variable), slot 0 is zero.
+template <int D>
+SSE_HD void ec_flux_dot_mixed_bwd(float igm1, float rho_ref, float theta_ref, const float *Pi,
+                                  const float *Pj, const float *G, const float *ob, float *Pbi,
+                                  float *Pbj) {
+  const float drho_hat = logmean_minus_ref(rho_ref, Pi[0], Pj[0], Pi[1], Pj[1]);
+  const float dilm = inv_logmean_beta_minus_ref(theta_ref, Pi[2], Pj[2]);
+  float vs[D];
+  float vv = 0.f, gvs = 0.f, gvi = 0.f, gvj = 0.f;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    vs[m] = Pi[3 + m] + Pj[3 + m];
+    vv = fmaf(Pi[3 + m], Pj[3 + m], vv);
+    gvs = fmaf(G[m], vs[m], gvs);
+    gvi = fmaf(G[m], Pi[3 + m], gvi);
+    gvj = fmaf(G[m], Pj[3 + m], gvj);
+  }
+  const float rho_hat = rho_ref + drho_hat;
+  const float f0 = 0.5f * rho_hat * gvs;
+  const float dC = fmaf(igm1, dilm, 0.5f * vv);
+  const float t = 0.5f * f0;
+  const float oE = ob[D + 1];
+  float ovs = 0.f, pbar_b = 0.f;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    ovs = fmaf(ob[1 + m], vs[m], ovs);
+    pbar_b = fmaf(ob[1 + m], G[m], pbar_b);
+  }
+  const float f0b = fmaf(0.5f, ovs, fmaf(dC, oE, ob[0]));
+  const float gvsb = fmaf(0.5f * rho_hat, f0b, -0.5f * theta_ref * drho_hat * oE);
+  const float drb = fmaf(0.5f * gvs, f0b, -0.5f * gvs * theta_ref * oE);
+  const float dCb = f0 * oE;
+  const float vvb = 0.5f * dCb;
+  const float gvjb = 0.5f * oE * Pi[3 + D];
+  const float gvib = 0.5f * oE * Pj[3 + D];
+  float lx, ly, ti, tj;
+  logmean_f_grad(Pi[0], Pj[0], &lx, &ly);
+  inv_logmean_theta_grad(theta_ref + Pi[2], theta_ref + Pj[2], &ti, &tj);
+  Pbi[0] = 0.f;
+  Pbj[0] = 0.f;
+  Pbi[1] = drb * lx;
+  Pbj[1] = drb * ly;
+  Pbi[2] = igm1 * dCb * ti;
+  Pbj[2] = igm1 * dCb * tj;
+  Pbi[3 + D] = fmaf(0.5f * oE, gvj, 0.5f * pbar_b);
+  Pbj[3 + D] = fmaf(0.5f * oE, gvi, 0.5f * pbar_b);
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    const float vsb = fmaf(t, ob[1 + m], G[m] * gvsb);
+    Pbi[3 + m] = fmaf(G[m], gvib, fmaf(Pj[3 + m], vvb, vsb));
+    Pbj[3 + m] = fmaf(G[m], gvjb, fmaf(Pi[3 + m], vvb, vsb));
+  }
+}
+
+// Transpose of euler_prim_mixed: accumulate ub += (dP/du')^T Pb.
+template <int D>
+SSE_HD void euler_prim_mixed_bwd(float gm1, float theta_ref, const float *P, const float *Pb, float *ub) {
+  const float rho = P[0], rr = 1.f / rho;
+  const float theta = theta_ref + P[2];
+  const float pb = fmaf(Pb[2], rr, Pb[3 + D]);  // p' cotangent, including theta' = (p_ref + p')/rho - theta_ref
+  float v2 = 0.f, vvb = 0.f;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    v2 = fmaf(P[3 + m], P[3 + m], v2);
+    vvb = fmaf(Pb[3 + m], P[3 + m], vvb);
+  }
+  ub[0] += Pb[0] + Pb[1] - Pb[2] * theta * rr + 0.5f * gm1 * pb * v2 - vvb * rr;
+#pragma unroll
+  for (int m = 0; m < D; ++m) ub[m + 1] += fmaf(-gm1 * pb, P[3 + m], Pb[3 + m] * rr);
+  ub[D + 1] += gm1 * pb;
+}
+
+// (rho e) of entropy_to_cons_mixed(w) alone
+template <int D>
+__device__ __forceinline__ double entropy_to_cons_mixed_rhoe(const Physics &ph, const double *w_in) {
+  double wg[D + 2];
+#pragma unroll
+  for (int e = 0; e < D + 2; ++e) wg[e] = w_in[e] * ph.gm1;
+  double s2 = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) s2 = fma(wg[m + 1], wg[m + 1], s2);
+  const double k = 0.5 * s2 * sse_rcp(wg[D + 1]);
+  const double sv = ph.gamma - wg[0] + k;
+  const double a = -wg[D + 1];
+  const float la = log1pf((float)((a - ph.a_ref) * ph.ia_ref));
+  const double dX = ph.igm1 * (-ph.gamma * (double)la - (sv - ph.sv_ref));
+  return fma(ph.rhoe_ref, (double)expm1f((float)dX), ph.rhoe_ref);
+}
+
+// Directional derivative of entropy_to_cons at w along dw given rhoe
+// (the internal energy rho e of the state, from entropy_to_cons_mixed)
+template <int D>
+SSE_HD void entropy_to_cons_jvp_rhoe(double gm1, double igm1, double gamma, const double *w_in,
+                                     double rhoe, const double *dw_in, double *du) {
+  double w[D + 2], dw[D + 2];
+#pragma unroll
+  for (int e = 0; e < D + 2; ++e) {
+    w[e] = w_in[e] * gm1;
+    dw[e] = dw_in[e] * gm1;
+  }
+  double s = 0.0, ds = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    s = fma(w[m + 1], w[m + 1], s);
+    ds = fma(w[m + 1], dw[m + 1], ds);
+  }
+  const double iwE = sse_rcp(w[D + 1]);
+  const double k = 0.5 * s * iwE;
+  const double dk = ds * iwE - k * dw[D + 1] * iwE;
+  const double dsv = -dw[0] + dk;
+  const double drhoe = rhoe * igm1 * (-gamma * dw[D + 1] * iwE - dsv);
+  du[0] = -dw[D + 1] * rhoe - w[D + 1] * drhoe;
+#pragma unroll
+  for (int m = 0; m < D; ++m) du[m + 1] = dw[m + 1] * rhoe + w[m + 1] * drhoe;
+  du[D + 1] = drhoe * (1 - k) - rhoe * dk;
+}
+
 // Primitive quantities of one Euler state, computed once per node so that
 // the pairwise loops do no per-pair divisions for them.
 template <int D>

@@ -48,6 +48,8 @@ struct KernelArgs {
   int fd_chunk;      // pairs per chunk in the FP64 flux-differencing passes
   int vdm_zsz;       // doubles of the first sum-factorisation scratch (even)
   int fd_chunk_mixed;  // pairs per chunk in the mixed-form FP32 passes
+  Layout layAdjB1m, layAdjB2m, layAdjAm;  // mixed-form VJP layouts (floats)
+  int pair_chunk_mixed;  // pairs per chunk in the mixed-form pair-adjoint passes
   int vdm_zsz_mixed;   // floats of the first sum-factorisation scratch (multiple of 4)
 
   __device__ __forceinline__ void flag_nonphysical() const { atomicOr(flag, 1); }
@@ -77,6 +79,8 @@ cudaError_t launch_facet_layout(const double *in, double *out, int nf, int ne, i
 // discrete adjoint (sse_adjoint.cu)
 cudaError_t sse_set_smem_limits_adjoint(const KernelArgs &ka);
 cudaError_t launch_residual_vjp_kernels(const KernelArgs &ka, cudaStream_t st);
+cudaError_t sse_set_smem_limits_adjoint_mixed(const KernelArgs &ka);
+cudaError_t launch_residual_vjp_mixed_kernels(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_adj_ck_stage(double *ybar, double *qbar, const double *mu, double dt, double a,
                                 double b_prev, size_t n, cudaStream_t st);
 cudaError_t launch_adj_lincomb(double *y, const double *x, double alpha, double beta, size_t n,

@@ -184,10 +184,12 @@ int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt,
 /* Discrete adjoint of the FP64 residual: mu <- (dR/du)^T lam at the state u
  * (all three N_p x N_c x N_e, host or device).  Covers FluxDifferencingForm
  * with the entropy-conservative two-point flux (Euler) and any of the three
- * interface fluxes; other configurations return SSE_ERR_UNSUPPORTED.  The
- * vector-Jacobian product of semi_discrete_residual!; no counterpart in the
- * reference, whose residual is typed Float64 throughout and has no AD or
- * adjoint code (Solvers.jl:474-514). */
+ * interface fluxes; other configurations return SSE_ERR_UNSUPPORTED.  With
+ * the handle in SSE_MIXED the product is that of the mixed form (FP32
+ * transposes of its reduced fluxes and projection arithmetic, ModalTensor
+ * bases).  The vector-Jacobian product of semi_discrete_residual!; no
+ * counterpart in the reference, whose residual is typed Float64 throughout
+ * and has no AD or adjoint code (Solvers.jl:474-514). */
 int32_t sse_residual_vjp(sse_solver *s, const double *u, const double *lam, double *mu,
                          int32_t memory);
 
@@ -209,7 +211,7 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
  * (both N_p x N_c x N_e, host or device).  Each checkpoint segment is
  * recomputed once, in the precision it was recorded in, storing its RK
  * stage states; the stage adjoints use sse_residual_vjp's kernels at those
- * states.  The segment whose stage data is still held (the last one, after
+ * states, in the recorded precision.  The segment whose stage data is still held (the last one, after
  * sse_rk_record) is not recomputed.  The recording stays valid for further
  * calls.  out_info, if not NULL, receives {segments, checkpoint_every,
  * recording bytes, segments recomputed by this call}.  The pullback half of

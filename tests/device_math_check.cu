@@ -249,18 +249,75 @@ static void check_adjoint(std::mt19937_64 &rng, double *worst) {
   }
 }
 
+// Mixed-form reverse mode: the FP32 transpose of the reduced flux with the
+// transformed cotangent (ob_rho + H_ref ob_E, ob_m, ob_E), mapped to
+// conservative-perturbation cotangents, against the FP64 transpose of the
+// full flux mapped to conservative cotangents (the same quantity); errors
+// relative to the largest FP64 cotangent of the pair.
+template <int D>
+static void check_mixed_adjoint(std::mt19937_64 &rng, double *worst) {
+  const double g = 1.4, gm1 = g - 1;
+  std::uniform_real_distribution<double> U(-1, 1);
+  const double rho_ref = 1.0, E_ref = 71.4 / gm1 + 0.3, p_ref = gm1 * E_ref;
+  const double theta_ref = p_ref / rho_ref, H_ref = g / gm1 * theta_ref;
+  for (int trial = 0; trial < 20000; ++trial) {
+    double uL[D + 2], uR[D + 2];
+    {
+      double rho = 1.0 + 0.3 * U(rng), p = 71.4 * (1.0 + 0.01 * U(rng)), ke = 0;
+      uL[0] = rho;
+      for (int m = 0; m < D; ++m) { double v = U(rng); uL[m + 1] = rho * v; ke += 0.5 * rho * v * v; }
+      uL[D + 1] = p / gm1 + ke;
+    }
+    for (int e = 0; e < D + 2; ++e) uR[e] = uL[e] * (1.0 + ((trial % 4) ? 1e-3 : 2e-1) * U(rng));
+    double PL[3 + D], PR[3 + D], G[D], ob[D + 2], PbL[3 + D], PbR[3 + D];
+    euler_prim_fast<D>(gm1, uL, PL);
+    euler_prim_fast<D>(gm1, uR, PR);
+    for (int m = 0; m < D; ++m) G[m] = U(rng);
+    for (int e = 0; e < D + 2; ++e) ob[e] = U(rng);
+    ec_flux_dot_bwd<D>(1 / gm1, PL, PR, G, ob, PbL, PbR);
+    double ubL[D + 2] = {0}, ubR[D + 2] = {0};
+    euler_prim_bwd<D>(gm1, uL, PL, PbL, ubL);
+    euler_prim_bwd<D>(gm1, uR, PR, PbR, ubR);
+    float dL[D + 2], dR[D + 2], QL[4 + D], QR[4 + D], Gf[D], obf[D + 2], QbL[4 + D], QbR[4 + D];
+    for (int e = 0; e < D + 2; ++e) {
+      double ref = (e == 0) ? rho_ref : (e == D + 1 ? E_ref : 0.0);
+      dL[e] = (float)(uL[e] - ref);
+      dR[e] = (float)(uR[e] - ref);
+      obf[e] = (float)ob[e];
+    }
+    obf[0] = (float)(ob[0] + H_ref * ob[D + 1]);
+    for (int m = 0; m < D; ++m) Gf[m] = (float)G[m];
+    euler_prim_mixed<D>((float)gm1, (float)rho_ref, (float)p_ref, dL, QL);
+    euler_prim_mixed<D>((float)gm1, (float)rho_ref, (float)p_ref, dR, QR);
+    ec_flux_dot_mixed_bwd<D>((float)(1 / gm1), (float)rho_ref, (float)theta_ref, QL, QR, Gf, obf, QbL, QbR);
+    float vbL[D + 2] = {0}, vbR[D + 2] = {0};
+    euler_prim_mixed_bwd<D>((float)gm1, (float)theta_ref, QL, QbL, vbL);
+    euler_prim_mixed_bwd<D>((float)gm1, (float)theta_ref, QR, QbR, vbR);
+    double scale = 0;
+    for (int e = 0; e < D + 2; ++e) scale = std::fmax(scale, std::fmax(std::fabs(ubL[e]), std::fabs(ubR[e])));
+    for (int e = 0; e < D + 2; ++e) {
+      worst[9] = std::fmax(worst[9], std::fabs(vbL[e] - ubL[e]) / scale);
+      worst[9] = std::fmax(worst[9], std::fabs(vbR[e] - ubR[e]) / scale);
+    }
+  }
+}
+
 int main() {
   std::mt19937_64 rng(20261203);
-  double worst[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double worst[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   check<2>(rng, worst);
   check<3>(rng, worst);
   check_mixed<2>(rng, worst);
   check_mixed<3>(rng, worst);
   check_adjoint<2>(rng, worst);
   check_adjoint<3>(rng, worst);
+  check_mixed_adjoint<2>(rng, worst);
+  check_mixed_adjoint<3>(rng, worst);
   std::printf("{\"logmean\": %.3e, \"inv_logmean\": %.3e, \"ec_flux_dot\": %.3e, "
               "\"cons_to_entropy\": %.3e, \"entropy_to_cons\": %.3e, \"mixed_reduced_flux\": %.3e, "
-              "\"flux_vjp_vs_fd\": %.3e, \"entropy_jvp_vs_fd\": %.3e, \"entropy_jacobian_symmetry\": %.3e}\n",
-              worst[0], worst[1], worst[2], worst[3], worst[4], worst[5], worst[6], worst[7], worst[8]);
+              "\"flux_vjp_vs_fd\": %.3e, \"entropy_jvp_vs_fd\": %.3e, \"entropy_jacobian_symmetry\": %.3e, "
+              "\"mixed_flux_vjp\": %.3e}\n",
+              worst[0], worst[1], worst[2], worst[3], worst[4], worst[5], worst[6], worst[7], worst[8],
+              worst[9]);
   return 0;
 }

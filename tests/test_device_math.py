@@ -50,6 +50,13 @@ def test_adjoint_derivatives(results):
     assert results["entropy_jacobian_symmetry"] < 1e-13
 
 
+def test_mixed_adjoint_derivatives(results):
+    # FP32 transpose of the reduced flux (cotangent ob_rho + H_ref ob_E, ...)
+    # mapped to conservative cotangents vs the FP64 transpose of the full
+    # flux, relative to the largest cotangent, low-Mach states
+    assert results["mixed_flux_vjp"] < 1e-5
+
+
 def test_entropy_variable_maps(results):
     assert results["cons_to_entropy"] < 5e-14
     assert results["entropy_to_cons"] < 5e-14
