@@ -186,6 +186,30 @@ def test_gradient_against_central_differences(gpu_lib, pkg):
         assert abs(fd - ad) <= 1e-5 * max(abs(ad), 1e-3 * np.linalg.norm(grad)), (fd, ad)
 
 
+def test_recording_larger_than_memory_is_refused(gpu_lib, pkg):
+    """A recording that cannot fit is refused on the host before any step
+    runs (the state is left as it was)."""
+    host, u = cases.make("vortex_tri_modal")
+    G = pkg.GB300Solver(host)
+    u0 = u.copy()
+    n = 2_000_000
+    with pytest.raises(pkg.SSEError) as e:
+        G.rk_record(u, n, 1e-6, 0, n)        # one segment of every stage: far above HBM
+    assert e.value.code == pkg.abi.SSE_ERR_OUT_OF_MEMORY
+    assert np.array_equal(u, u0)
+    with pytest.raises(pkg.SSEError):
+        G.rk_adjoint(u)                      # nothing recorded
+
+
+def test_mixed_vjp_needs_a_modal_basis(gpu_lib, pkg):
+    host, u = cases.make("vortex_tri_nodal")
+    G = pkg.GB300Solver(host)
+    G.set_precision(pkg.abi.SSE_MIXED)
+    with pytest.raises(pkg.SSEError) as e:
+        G.residual_vjp(u, u)
+    assert e.value.code == pkg.abi.SSE_ERR_UNSUPPORTED
+
+
 def test_adjoint_rejections(gpu_lib, pkg):
     host, u = cases.make("adv_tri_modal")
     G = pkg.GB300Solver(host)
