@@ -91,6 +91,9 @@ def test_rejects_invalid_arguments_on_host(pkg, lib):
 def test_null_handle_calls(pkg, lib):
     abi = pkg.abi
     assert lib.sse_residual(None, None, None, 0.0, 0) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert lib.sse_residual_vjp(None, None, None, None, 0) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert lib.sse_rk_record(None, None, 1, 1e-3, 0, 0, None, 0) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert lib.sse_rk_adjoint(None, None, None, None, 0) == abi.SSE_ERR_INVALID_ARGUMENT
     assert lib.sse_destroy(None) == abi.SSE_OK
     assert lib.sse_last_error(None) == b"null handle"
 
