@@ -266,6 +266,29 @@ def adjoint_workload(pkg, gpu, host, u0_np, dt, steps, fwd_ms, stream):
     out["grad_norm_momentum"] = float(np.linalg.norm(g[:, 1:-1]))
     out["gradients_identical_across_intervals"] = bool(np.array_equal(g, grads["every_2_steps"]))
     out["adjoint_over_forward"] = out["every_2_steps"]["adjoint_over_forward"]
+    # the same pullback of a mixed-form recording (mixed-form VJP), against
+    # the mixed forward of the same steps
+    abi = pkg.abi
+    try:
+        gpu.set_precision(abi.SSE_MIXED)
+        gpu.rk_steps(torch.from_numpy(u0_np).cuda(), 2, dt)                   # warm-up / graph capture
+        mfwd_ms, _ = timed(stream, lambda: gpu.rk_steps(torch.from_numpy(u0_np).cuda(), steps, dt))
+        gpu.rk_record(torch.from_numpy(u0_np).cuda(), steps, dt, 0, 0)        # warm-up / allocation
+        u = torch.from_numpy(u0_np).cuda()
+        rec_ms, _ = timed(stream, lambda: gpu.rk_record(u, steps, dt, 0, 0))
+        ke, dke = pkg.objectives.kinetic_energy(host, u.cpu().numpy())
+        lamT = torch.from_numpy(dke).cuda()
+        lam0 = torch.empty_like(lamT)
+        adj_ms, info = timed(stream, lambda: gpu.rk_adjoint(lamT, lam0))
+        gm = lam0.cpu().numpy()
+        out["mixed"] = {"forward_ms": mfwd_ms, "record_ms": rec_ms, "adjoint_ms": adj_ms,
+                        "adjoint_over_forward": adj_ms / mfwd_ms,
+                        "segments": info["segments"], "segments_recomputed": info["recomputed"],
+                        "gradient_rel_err_vs_fp64_adjoint": float(np.linalg.norm(gm - g) / np.linalg.norm(g))}
+    except pkg.SSEError as ex:
+        out["mixed"] = {"unavailable": str(ex)}
+    finally:
+        gpu.set_precision(abi.SSE_FP64)
     return out
 
 

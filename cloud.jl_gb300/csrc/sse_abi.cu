@@ -823,13 +823,19 @@ int enable_adjoint_mixed(sse_solver *s) {
   const int big = nc * std::max(np, nq), bigf = nc * std::max({np, nq, nf});
   finish(ka.layAdjB1m, {big, nc * nq, zsz, wsz, bigf});
   finish(ka.layAdjAm, {big, nc * nq, nc * nq, nc * nq, nc * nf, big, nc * nq, zsz, wsz, nc * nf});
-  const int hsz = op.nfp > 0 ? d * c.num_faces * nq : 0;
+  int hsz = op.nfp > 0 ? d * c.num_faces * nq : 0;
   Layout base{};
   finish(base, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf, d * d * nq, hsz});
   const int max_pairs = std::max(op.nvp, op.nfp);
   const int tpe_adj = ka.tpb / ka.epb;
   const long cap = (long)(220 * 1024 / 4 / ka.epb);          // floats per team
-  long room = (long)(55 * 1024 / 4 / ka.epb) - base.team_doubles;  // four blocks per SM
+  const long four = (long)(55 * 1024 / 4 / ka.epb);          // team size for four blocks per SM
+  if (four - base.team_doubles < 128 * 2 * ps && four - (base.team_doubles - r4(hsz)) >= 128 * 2 * ps) {
+    // halfnJq read from global memory keeps four blocks per SM
+    hsz = 0;
+    finish(base, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf, d * d * nq, 0});
+  }
+  long room = four - base.team_doubles;
   if (room < 128 * 2 * ps) room = (long)(110 * 1024 / 4 / ka.epb) - base.team_doubles;  // two
   if (room < 128 * 2 * ps) room = cap - base.team_doubles;
   int chunk = (int)std::min<long>(max_pairs, room / (2 * ps));

@@ -521,8 +521,16 @@ __global__ void __launch_bounds__(256) adj_flux_mixed_kernel(KernelArgs ka) {
     ubd[t] = 0.f;
   }
   for (int t = lane; t < nq * D * D; t += tpe) Lam[t] = g.Lambda_qf[(size_t)kk * nq * D * D + t];
-  if (op.nfp > 0)
-    for (int t = lane; t < D * nfac * nq; t += tpe) hnq[t] = g.halfnJqf[(size_t)kk * D * nfac * nq + t];
+  // halfnJq is staged when the layout has room for it, else read from global
+  // memory (the host drops it from the layout to keep more blocks per SM)
+  const float *hnq_src = hnq;
+  if (op.nfp > 0) {
+    if (L.off[9] > L.off[8]) {
+      for (int t = lane; t < D * nfac * nq; t += tpe) hnq[t] = g.halfnJqf[(size_t)kk * D * nfac * nq + t];
+    } else {
+      hnq_src = g.halfnJqf + (size_t)kk * D * nfac * nq;
+    }
+  }
   for (int t = lane; t < (nq + nf) * PS; t += tpe) Pb[t] = 0.f;
   __syncthreads();
   for (int i = lane; i < nq + nf; i += tpe) {
@@ -637,7 +645,7 @@ __global__ void __launch_bounds__(256) adj_flux_mixed_kernel(KernelArgs ka) {
         const float Cij = fpC[pidx];
         float G[D], db[NC];
 #pragma unroll
-        for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+        for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq_src[m + D * (f + nfac * i)]);
 #pragma unroll
         for (int e = 0; e < NC; ++e) db[e] = -rb[e * nq + i] - fb[e * nf + j];
         float *slot = buf + (size_t)(pidx - c0) * 2 * PS;
