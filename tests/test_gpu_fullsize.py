@@ -1,7 +1,9 @@
 """Size-independent properties at the full benchmark sizes, where the CPU
-oracle would take too long: the 2-D Euler vortex mesh (64x64 cells = 8192
-curved triangles, p = 4) and the 3-D Taylor-Green mesh (16^3 x 6 = 24,576
-curved tetrahedra, p = 4).
+oracle would take too long to step: the 2-D advection mesh (16x16 cells =
+512 curved triangles, RK4), the 2-D Euler vortex mesh (64x64 cells = 8192
+curved triangles, p = 4), the 3-D Taylor-Green mesh (16^3 x 6 = 24,576
+curved tetrahedra, p = 4) and the p = 5 Taylor-Green mesh (24^3 x 6 =
+82,944 curved tetrahedra).
 
 * discrete conservation: sum_k 1' WJ V dudt = 0 to round-off
   (the reference asserts it at 1e-10, test/runtests.jl:120);
@@ -91,3 +93,66 @@ def test_vortex_8192_matches_oracle_and_conserves(gpu_lib, pkg, vortex):
     assert err < 1e-12
     out = gpu.conservation_residual(u, got)
     assert np.abs(out[:host.N_c]).max() < 1e-12 * _scale(host, got)
+
+
+def test_advection_512_rk4_trajectory_matches_oracle(gpu_lib, pkg):
+    """100 classic RK4 steps (400 stages) of the 2-D advection workload."""
+    pb = pkg.setups.advection_tri(cells=16, p=4)
+    host = pb.host_arrays()
+    gpu = pkg.GB300Solver(host)
+    u = pb.u0.copy()
+    gpu.rk_steps(u, 100, pb.dt, 1)
+    want = Oracle(host).rk_steps(pb.u0, 100, pb.dt, 1)
+    assert np.linalg.norm(u - want) / np.linalg.norm(want) < 1e-12
+
+
+@pytest.fixture(scope="module")
+def tgv5(pkg):
+    pb = pkg.setups.tgv_tet(cells=24, p=5, lf=True)
+    return pb, pb.host_arrays()
+
+
+def test_tgv5_82944_matches_oracle_and_conserves(gpu_lib, pkg, tgv5):
+    from oracle.oracle import rel2, roundoff_floor
+    pb, host = tgv5
+    gpu = pkg.GB300Solver(host)
+    u = pkg.setups.perturbed(pb.u0, 13, 1e-3)
+    got = gpu.residual(u)
+    want = Oracle(host).residual(u)
+    floor = roundoff_floor(host, u)
+    assert rel2(got, want) <= max(1e-12, 4 * floor)
+    out = gpu.conservation_residual(u, got)
+    assert np.abs(out[:host.N_c]).max() < 1e-12 * _scale(host, got)
+    assert np.array_equal(gpu.residual(u), got)
+
+
+def test_tgv5_82944_adjoint_dot_product(gpu_lib, pkg, tgv5):
+    """<lam, J v> from the dual-number oracle against <J^T lam, v> from the
+    GPU at the full p = 5 size, FP64 and mixed-form VJPs."""
+    from oracle.oracle import TangentOracle
+    pb, host = tgv5
+    gpu = pkg.GB300Solver(host)
+    u = pkg.setups.perturbed(pb.u0, 17, 1e-3)
+    rng = np.random.default_rng(19)
+    lam, v = rng.standard_normal(u.shape), rng.standard_normal(u.shape)
+    _, jv = TangentOracle(host).jvp(u, v)
+    lhs, scale = float(np.vdot(lam, jv)), float(np.sum(np.abs(lam * jv)))
+    mu = gpu.residual_vjp(u, lam)
+    assert abs(lhs - float(np.vdot(mu, v))) < 1e-12 * scale
+    gpu.set_precision(pkg.abi.SSE_MIXED)
+    mu32 = gpu.residual_vjp(u, lam)
+    assert abs(lhs - float(np.vdot(mu32, v))) < 1e-4 * scale
+    assert np.linalg.norm(mu32 - mu) / np.linalg.norm(mu) < 1e-4
+
+
+def test_tgv5_82944_mixed_trajectory(gpu_lib, pkg, tgv5):
+    import torch
+    pb, host = tgv5
+    gpu = pkg.GB300Solver(host)
+    u64 = torch.from_numpy(pb.u0.copy()).cuda()
+    gpu.rk_steps(u64, 3, pb.dt)
+    gpu.set_precision(pkg.abi.SSE_MIXED)
+    u32 = torch.from_numpy(pb.u0.copy()).cuda()
+    gpu.rk_steps(u32, 3, pb.dt)
+    torch.cuda.synchronize()
+    assert float(torch.linalg.norm(u32 - u64) / torch.linalg.norm(u64)) < 1e-6
