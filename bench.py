@@ -485,7 +485,18 @@ def main():
         res_err = float(np.linalg.norm(r_mixed - r_fp64) / np.linalg.norm(r_fp64))
         cons = gpu.conservation_residual(u0d, torch.from_numpy(r_mixed).cuda())
         mvalue = world * host.dof * stages * args.steps / (mms * 1e-3)
-        mixed = {"value": mvalue, "unit": UNIT, "ms_per_step": mms / args.steps,
+        # roofline of the FP32 phase B: max(FP32 pipe, HBM) with the
+        # algorithmic flops and the FP32 bytes (half the FP64 bytes)
+        mB = mphases[1] * 1e-3
+        m_fp32 = work.flops_B * ne / mB / 1e12
+        m_hbm = 0.5 * work.bytes_B * ne / mB / 1e9
+        mixed_roofline = {"kernel": "fd_time_derivative_mixed_kernel", "bound": "max(fp32, hbm)",
+                          "fp32_achieved_tflops": m_fp32, "fp32_peak_tflops": fp32_peak,
+                          "fp32_frac": m_fp32 / fp32_peak, "hbm_achieved_gbs": m_hbm,
+                          "hbm_peak_gbs": hbm_peak, "hbm_frac": m_hbm / hbm_peak,
+                          "frac": max(m_fp32 / fp32_peak, m_hbm / hbm_peak),
+                          "note": "neither roof binds: latency (dependent FP32 chains, table loads)"}
+        mixed = {"value": mvalue, "unit": UNIT, "ms_per_step": mms / args.steps, "roofline": mixed_roofline,
                  "speedup_vs_fp64": mvalue / value,
                  "state_rel_err_vs_fp64": state_err,
                  "state_err_after_steps": args.warmup + args.steps,
