@@ -499,6 +499,17 @@ __device__ __forceinline__ void entropy_to_cons_mixed(const Physics &ph, const d
 // conservative-curl metrics), so the dropped terms sum to zero exactly.
 // ---------------------------------------------------------------------------
 
+// FP32 quotient for the mixed form: the fast reciprocal-based division
+// (2 ulp) on the device, where the form's error budget is set by the FP32
+// rounding of the perturbations anyway; exact division on the host.
+SSE_HD float sse_fdiv(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
 // 1 + z/3 + z^2/5 + z^3/7 + z^4/9 + z^5/11 (= atanh(f)/f, z = f^2)
 SSE_HD float q_series_f(float z) {
   return fmaf(z, fmaf(z, fmaf(z, fmaf(z, fmaf(z, 1.f / 11.f, 1.f / 9.f), 1.f / 7.f), 0.2f), 1.f / 3.f), 1.f);
@@ -539,7 +550,7 @@ SSE_HD float inv_logmean_mixed(float x, float y) {
 template <int D>
 SSE_HD void euler_prim_mixed(float gm1, float rho_ref, float p_ref, const float *du, float *P) {
   const float rho = rho_ref + du[0];
-  const float rr = 1.f / rho;
+  const float rr = sse_fdiv(1.f, rho);
   float s = 0.f;
 #pragma unroll
   for (int m = 0; m < D; ++m) {
@@ -549,7 +560,7 @@ SSE_HD void euler_prim_mixed(float gm1, float rho_ref, float p_ref, const float 
   const float pp = gm1 * (du[D + 1] - 0.5f * rho * s);
   P[0] = rho;
   P[1] = du[0];
-  P[2] = (pp * rho_ref - p_ref * du[0]) * rr / rho_ref;  // p/rho - p_ref/rho_ref
+  P[2] = sse_fdiv((pp * rho_ref - p_ref * du[0]) * rr, rho_ref);  // p/rho - p_ref/rho_ref
   P[3 + D] = pp;
 }
 
@@ -561,13 +572,13 @@ SSE_HD float q_minus_one_f(float z) {
 // logmean(rho_i, rho_j) - rho_ref from density perturbations
 SSE_HD float logmean_minus_ref(float rho_ref, float ri, float rj, float dri, float drj) {
   const float s = 2.f * rho_ref + (dri + drj);
-  const float f = (dri - drj) / s;
+  const float f = sse_fdiv(dri - drj, s);
   const float z = f * f;
   if (z < 0.05f) {
     const float qm1 = q_minus_one_f(z);
-    return (0.5f * (dri + drj) - rho_ref * qm1) / (1.f + qm1);
+    return sse_fdiv(0.5f * (dri + drj) - rho_ref * qm1, 1.f + qm1);
   }
-  return (rj - ri) / logf(rj / ri) - rho_ref;
+  return sse_fdiv(rj - ri, logf(sse_fdiv(rj, ri))) - rho_ref;
 }
 
 // inv_logmean(beta_i, beta_j) - theta_ref with beta = 1/theta, from
@@ -576,14 +587,15 @@ SSE_HD float inv_logmean_beta_minus_ref(float theta_ref, float dti, float dtj) {
   const float ti = theta_ref + dti, tj = theta_ref + dtj;
   const float sig = dti + dtj;
   const float den = 2.f * theta_ref + sig;
-  const float f = (dtj - dti) / den;
+  const float rden = sse_fdiv(1.f, den);
+  const float f = (dtj - dti) * rden;
   const float z = f * f;
   if (z < 0.05f) {
-    const float hm_minus = (theta_ref * sig + 2.f * dti * dtj) / den;  // 2 ti tj/(ti+tj) - theta_ref
+    const float hm_minus = (theta_ref * sig + 2.f * dti * dtj) * rden;  // 2 ti tj/(ti+tj) - theta_ref
     const float hm = theta_ref + hm_minus;
     return fmaf(q_minus_one_f(z), hm, hm_minus);
   }
-  return ti * tj * logf(ti / tj) / (ti - tj) - theta_ref;
+  return sse_fdiv(ti * tj * logf(sse_fdiv(ti, tj)), ti - tj) - theta_ref;
 }
 
 // ec_flux_dot in FP32: momentum with pbar - p_ref, energy reduced by H_ref f_rho.
@@ -633,18 +645,19 @@ SSE_HD float q_series_f_deriv(float z) {
 // from logmean_minus_ref)
 SSE_HD void logmean_f_grad(float x, float y, float *dx, float *dy) {
   const float s = x + y;
-  const float f = (x - y) / s;
+  const float is = sse_fdiv(1.f, s);
+  const float f = (x - y) * is;
   const float z = f * f;
   if (z < 0.05f) {
-    const float q = q_series_f(z), iq = 1.f / q;
-    const float c = 2.f * q_series_f_deriv(z) * f * iq * iq / s;
+    const float iq = sse_fdiv(1.f, q_series_f(z));
+    const float c = 2.f * q_series_f_deriv(z) * f * iq * iq * is;
     *dx = fmaf(-c, y, 0.5f * iq);
     *dy = fmaf(c, x, 0.5f * iq);
     return;
   }
-  const float L = logf(y / x), iL = 1.f / L, N = y - x;
-  *dx = (N / x - L) * iL * iL;
-  *dy = (L - N / y) * iL * iL;
+  const float L = logf(sse_fdiv(y, x)), iL = sse_fdiv(1.f, L), N = y - x;
+  *dx = (sse_fdiv(N, x) - L) * iL * iL;
+  *dy = (L - sse_fdiv(N, y)) * iL * iL;
 }
 
 // partial derivatives of inv_logmean(1/theta_i, 1/theta_j) w.r.t. the
@@ -652,17 +665,18 @@ SSE_HD void logmean_f_grad(float x, float y, float *dx, float *dy) {
 // f = (tj - ti)/(ti + tj) on the series branch
 SSE_HD void inv_logmean_theta_grad(float ti, float tj, float *di, float *dj) {
   const float sg = ti + tj;
-  const float f = (tj - ti) / sg;
+  const float isg = sse_fdiv(1.f, sg);
+  const float f = (tj - ti) * isg;
   const float z = f * f;
   if (z < 0.05f) {
     const float q = q_series_f(z), qp = q_series_f_deriv(z);
-    const float is2 = 1.f / (sg * sg);
-    const float hm = 2.f * ti * tj / sg;
+    const float is2 = isg * isg;
+    const float hm = 2.f * ti * tj * isg;
     *di = fmaf(qp * hm, -4.f * f * tj * is2, q * 2.f * tj * tj * is2);
     *dj = fmaf(qp * hm, 4.f * f * ti * is2, q * 2.f * ti * ti * is2);
     return;
   }
-  const float L = logf(ti / tj), N = ti - tj, iN = 1.f / N;
+  const float L = logf(sse_fdiv(ti, tj)), N = ti - tj, iN = sse_fdiv(1.f, N);
   const float w = ti * tj * L * iN * iN;
   *di = fmaf(tj, (L + 1.f) * iN, -w);
   *dj = fmaf(ti, (L - 1.f) * iN, w);
@@ -727,7 +741,7 @@ SSE_HD void ec_flux_dot_mixed_bwd(float igm1, float rho_ref, float theta_ref, co
 // Transpose of euler_prim_mixed: accumulate ub += (dP/du')^T Pb.
 template <int D>
 SSE_HD void euler_prim_mixed_bwd(float gm1, float theta_ref, const float *P, const float *Pb, float *ub) {
-  const float rho = P[0], rr = 1.f / rho;
+  const float rho = P[0], rr = sse_fdiv(1.f, rho);
   const float theta = theta_ref + P[2];
   const float pb = fmaf(Pb[2], rr, Pb[3 + D]);  // p' cotangent, including theta' = (p_ref + p')/rho - theta_ref
   float v2 = 0.f, vvb = 0.f;
