@@ -1103,10 +1103,15 @@ int32_t sse_nodal_values(sse_solver *s, const double *u, double *u_q, double *u_
   return check_flag(s);
 }
 
-int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme, double *t,
-                     int32_t memory) {
+// fixed-step time loop of sse_rk_steps / sse_rk_steps_snapshots: every > 0
+// copies the state (and, with residuals, its residual) after every
+// every-th step into the caller's buffers, in the memory kind of u
+static int32_t rk_run(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme, double *t,
+                      int32_t memory, int32_t every, double *snapshots, double *residuals) {
   if (!s) return SSE_ERR_INVALID_ARGUMENT;
   if (!u || n_steps < 0) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u or negative n_steps");
+  if (every < 0 || (every > 0 && !snapshots))
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "snapshots need every >= 1 and a snapshot buffer");
   if (scheme != SSE_CARPENTER_KENNEDY_2N54 && scheme != SSE_RK4) return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown scheme");
   const sse_config &c = s->cfg;
   size_t n = (size_t)c.n_p * c.n_c * c.n_e;
@@ -1178,14 +1183,37 @@ int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt, int32
       cudaGetLastError();  // a refused capture leaves no sticky error; clear the last one
     }
   }
+  const cudaMemcpyKind out_kind = memory == SSE_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   for (int step = 0; step < n_steps; ++step) {
     e = (n_steps >= 2 && G.exec) ? cudaGraphLaunch(G.exec, s->stream) : step_once();
     if (e) return cuda_fail(s, e, "step");
+    if (every > 0 && (step + 1) % every == 0) {
+      const size_t i = (size_t)((step + 1) / every - 1);
+      if ((e = cudaMemcpyAsync(snapshots + i * n, du, n * 8, out_kind, s->stream)))
+        return cuda_fail(s, e, "snapshot");
+      if (residuals) {
+        if ((e = residual_device(s, du, s->d_dudt))) return cuda_fail(s, e, "snapshot residual");
+        if ((e = cudaMemcpyAsync(residuals + i * n, s->d_dudt, n * 8, out_kind, s->stream)))
+          return cuda_fail(s, e, "snapshot residual");
+      }
+    }
   }
   if (memory == SSE_HOST && (e = cudaMemcpyAsync(u, s->d_u, n * 8, cudaMemcpyDeviceToHost, s->stream)))
     return cuda_fail(s, e, "D2H");
   if (t) *t += n_steps * dt;
   return check_flag(s);
+}
+
+int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme, double *t,
+                     int32_t memory) {
+  return rk_run(s, u, n_steps, dt, scheme, t, memory, 0, nullptr, nullptr);
+}
+
+int32_t sse_rk_steps_snapshots(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme,
+                               int32_t every, double *snapshots, double *residuals, double *t,
+                               int32_t memory) {
+  if (every < 1) return s ? fail(s, SSE_ERR_INVALID_ARGUMENT, "every must be >= 1") : SSE_ERR_INVALID_ARGUMENT;
+  return rk_run(s, u, n_steps, dt, scheme, t, memory, every, snapshots, residuals);
 }
 
 int32_t sse_residual_vjp(sse_solver *s, const double *u, const double *lam, double *mu, int32_t memory) {

@@ -23,7 +23,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "libsse_gb300.so")
 
 EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual",
             "sse_residual_static_scratch", "sse_nodal_values",
-            "sse_rk_steps", "sse_residual_vjp", "sse_rk_record", "sse_rk_adjoint",
+            "sse_rk_steps", "sse_rk_steps_snapshots", "sse_residual_vjp", "sse_rk_record",
+            "sse_rk_adjoint",
             "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
             "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
             "sse_create_error"]
@@ -60,6 +61,8 @@ def load_library(path: str | None = None):
     L.sse_nodal_values.restype = i32
     L.sse_rk_steps.argtypes = [vp, vp, i32, dp, i32, C.POINTER(dp), i32]
     L.sse_rk_steps.restype = i32
+    L.sse_rk_steps_snapshots.argtypes = [vp, vp, i32, dp, i32, i32, vp, vp, C.POINTER(dp), i32]
+    L.sse_rk_steps_snapshots.restype = i32
     L.sse_residual_vjp.argtypes = [vp, vp, vp, vp, i32]
     L.sse_residual_vjp.restype = i32
     L.sse_rk_record.argtypes = [vp, vp, i32, dp, i32, i32, C.POINTER(dp), i32]
@@ -149,6 +152,32 @@ class GB300Solver:
         tt = C.c_double(t)
         self._check(self.L.sse_rk_steps(self.h, pu, n_steps, dt, scheme, C.byref(tt), mu))
         return tt.value
+
+    def rk_steps_snapshots(self, u, n_steps: int, dt: float, every: int,
+                           scheme: int = abi.SSE_CARPENTER_KENNEDY_2N54, with_residuals: bool = False,
+                           t: float = 0.0):
+        """``rk_steps`` with the ``save_callback`` hook: returns (t, snapshots,
+        residuals) with the state (and its residual) after every ``every``-th
+        step, in the memory kind of ``u``."""
+        k = n_steps // every
+        if k == 0:
+            t = self.rk_steps(u, n_steps, dt, scheme, t)
+            shape = (0,) + tuple(u.shape)
+            empty = np.empty(shape) if isinstance(u, np.ndarray) else u.new_empty(shape)
+            return t, empty, (empty if with_residuals else None)
+        if isinstance(u, np.ndarray):
+            snaps = np.empty((k,) + u.shape)
+            res = np.empty((k,) + u.shape) if with_residuals else None
+        else:
+            snaps = u.new_empty((k,) + tuple(u.shape))
+            res = u.new_empty((k,) + tuple(u.shape)) if with_residuals else None
+        pu, mu = _addr(u)
+        ps = _addr(snaps)[0]
+        pr = _addr(res)[0] if res is not None else C.c_void_p(0)
+        tt = C.c_double(t)
+        self._check(self.L.sse_rk_steps_snapshots(self.h, pu, n_steps, dt, scheme, every, ps, pr,
+                                                  C.byref(tt), mu))
+        return tt.value, snaps, res
 
     def residual_vjp(self, u, lam, mu=None):
         """(dR/du)^T lam at u: the discrete adjoint of ``residual``."""

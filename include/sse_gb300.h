@@ -219,6 +219,17 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
 int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double *out_info,
                        int32_t memory);
 
+/* sse_rk_steps with the snapshot hook of the reference's save_callback /
+ * save_solution (File/save.jl:44-89): after every `every`-th step the state
+ * is copied to snapshots[i] and, when residuals is not NULL, its residual
+ * R(u) (the saved "du") to residuals[i], i = 0 .. n_steps/every - 1, each
+ * N_p x N_c x N_e, in the memory kind of u (copies are ordered on the
+ * handle's stream; the call returns after the last one).  The state at
+ * snapshot i belongs to t0 + (i + 1) every dt. */
+int32_t sse_rk_steps_snapshots(sse_solver *s, double *u, int32_t n_steps, double dt,
+                               int32_t scheme, int32_t every, double *snapshots,
+                               double *residuals, double *t, int32_t memory);
+
 /* FP64 reductions of Analysis/conservation.jl:145-189 for one (u, dudt):
  * out[0..N_c-1] = sum_k 1' WJ V dudt[:, e, k]       (primary conservation)
  * out[N_c]      = sum_k (P w)' M dudt               (entropy production, Euler)

@@ -47,3 +47,27 @@ def test_replayed_steps_match_single_steps(name, scheme, mixed, gpu_lib, pkg):
     h = u0.copy()
     G.rk_steps(h, 6, dt, scheme)
     assert np.array_equal(h, a.cpu().numpy()) or mixed
+
+
+@pytest.mark.parametrize("scheme,device", [(0, True), (1, False)])
+def test_snapshot_hook(scheme, device, gpu_lib, pkg):
+    """sse_rk_steps_snapshots (the save_callback hook): the states after every
+    k-th step and their residuals, bitwise those of stepping k at a time."""
+    import torch
+    host, u0 = cases.make("vortex_tri_modal")
+    G = pkg.GB300Solver(host)
+    dt = 1e-3
+    u = torch.from_numpy(u0.copy()).cuda() if device else u0.copy()
+    t, snaps, res = G.rk_steps_snapshots(u, 7, dt, every=3, scheme=scheme, with_residuals=True)
+    assert t == pytest.approx(7 * dt)
+    assert snaps.shape[0] == 2 and res.shape[0] == 2
+    if device:
+        torch.cuda.synchronize()
+        snaps, res, u = snaps.cpu().numpy(), res.cpu().numpy(), u.cpu().numpy()
+    w = u0.copy()
+    for i in range(2):
+        G.rk_steps(w, 3, dt, scheme)
+        assert np.array_equal(snaps[i], w)
+        assert np.array_equal(res[i], G.residual(w))
+    G.rk_steps(w, 1, dt, scheme)
+    assert np.array_equal(u, w)
