@@ -156,17 +156,17 @@ def replica_value(dof: int, stages: int, steps: int, ms_max: float, world: int) 
     return world * dof * stages * steps / (ms_max * 1e-3)
 
 
-def build_problem(workload: str, cells: int | None):
+def build_problem(workload: str, cells: int | None, p: int | None = None):
     pkg = __graft_entry__.load_package()
     s = pkg.setups
     if workload == "tgv_p4":
-        pb = s.tgv_tet(cells=cells or 16, p=4, lf=True)
+        pb = s.tgv_tet(cells=cells or 16, p=p or 4, lf=True)
     elif workload == "tgv_p5":
-        pb = s.tgv_tet(cells=cells or 24, p=5, lf=True)
+        pb = s.tgv_tet(cells=cells or 24, p=p or 5, lf=True)
     elif workload == "vortex_tri":
-        pb = s.vortex_tri(cells=cells or 64, p=4)
+        pb = s.vortex_tri(cells=cells or 64, p=p or 4)
     elif workload == "advection_tri":
-        pb = s.advection_tri(cells=cells or 16, p=4)
+        pb = s.advection_tri(cells=cells or 16, p=p or 4)
     else:
         raise KeyError(workload)
     return pkg, pb, pb.host_arrays()
@@ -178,6 +178,8 @@ def workload_config(args, host, world):
                parallelism="replicas only" if world > 1 else "1 GPU")
     if args.cells:
         cfg["mesh"] = f"{args.cells}^d cells (--cells override)"
+    if args.p:
+        cfg["approximation"] = f"degree {args.p} (--p override), N_p={host.N_p}, N_q={host.N_q}, N_f={host.N_f}"
     return cfg
 
 
@@ -186,7 +188,7 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle.oracle import Oracle
-    pkg, pb, host = build_problem(args.workload, args.cells)
+    pkg, pb, host = build_problem(args.workload, args.cells, args.p)
     o = Oracle(host)
     u = pb.u0.copy()
     for _ in range(args.warmup):
@@ -384,6 +386,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tgv_p4", choices=sorted(WORKLOADS))
     ap.add_argument("--cells", type=int, default=None, help="override the mesh resolution")
+    ap.add_argument("--p", type=int, default=None, help="override the polynomial degree")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
@@ -399,7 +402,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    pkg, pb, host = build_problem(args.workload, args.cells)
+    pkg, pb, host = build_problem(args.workload, args.cells, args.p)
     pkg.build.build()
     gpu = pkg.GB300Solver(host)
     stream = torch.cuda.current_stream()
@@ -441,7 +444,7 @@ def main():
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     kernel_B = "fd_time_derivative_kernel" if fd else "std_time_derivative_kernel"
-    traffic = TRAFFIC_PER_ELEMENT.get(args.workload) if not args.cells else None
+    traffic = TRAFFIC_PER_ELEMENT.get(args.workload) if not (args.cells or args.p) else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak,
                 "kernel": kernel_B if dom == "B" else "nodal_values_kernel",

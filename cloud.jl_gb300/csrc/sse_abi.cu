@@ -492,8 +492,13 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
     const int budget = team_budget(tpe);
     int chunk = max_pairs;
     if (layout(chunk) > budget) {
+      // chunks of at least one pass of the element's threads: two blocks per
+      // SM when that leaves room for them, else one block per SM
       const int fixed = layout(0) - ((std::max(0, final_scratch) + 1) & ~1);
-      chunk = std::max(1, (budget - fixed) / nc);
+      const int cap1 = (int)((size_t)220 * 1024 / 8 / ((tpe == 32) ? 4 : 1));
+      int room = budget - fixed;
+      if (room / nc < std::min(tpe, max_pairs)) room = cap1 - fixed;
+      chunk = std::max(1, room / nc);
       if (chunk >= tpe) chunk = chunk / tpe * tpe;
       chunk = std::max(1, std::min(chunk, max_pairs));
     }
@@ -617,8 +622,14 @@ int enable_mixed(sse_solver *s) {
   const int budget_m = (int)((size_t)55 * 1024 / 4 / ka.epb);
   int chunk_m = max_pairs;
   if (layout_m(chunk_m) > budget_m) {
+    // four blocks per SM when chunks of at least one pass of the element's
+    // threads fit, else two, else one
     const int fixed = layout_m(0) - r4(final_m);
-    chunk_m = std::max(1, (budget_m - fixed) / nc);
+    const int need = std::min(tpe_m, max_pairs) * nc;
+    int room = budget_m - fixed;
+    if (room < need) room = 2 * budget_m - fixed;
+    if (room < need) room = (int)((size_t)220 * 1024 / 4 / ka.epb) - fixed;
+    chunk_m = std::max(1, room / nc);
     if (chunk_m >= tpe_m) chunk_m = chunk_m / tpe_m * tpe_m;
     chunk_m = std::max(1, std::min(chunk_m, max_pairs));
   }
