@@ -139,3 +139,25 @@ def test_nonphysical_state_is_reported(built, pkg):
     # the handle stays usable afterwards
     good = gpu.residual(u)
     assert np.isfinite(good).all()
+
+
+@pytest.mark.parametrize("name", ["vortex_tri_modal", "tgv_tet_modal"])
+def test_dense_operators_match_oracle(name, gpu_lib, pkg):
+    """flux_difference! / facet_correction! with dense S_m and C (the
+    reference's dense variants, flux_differencing_form.jl:1-35, 91-124):
+    every pair of volume nodes and every (volume, facet) pair is a flux
+    evaluation, so the pair passes run in many chunks.  The operators are
+    random (antisymmetric S_m), so only parity with the oracle is meaningful."""
+    host, u = cases.make(name)
+    rng = np.random.default_rng(41)
+    nq, nf, d = host.N_q, host.N_f, host.cfg.d
+    for m in range(d):
+        a = rng.standard_normal((nq, nq)) * 0.1
+        host.S[m] = pkg.abi.CscArrays(a - a.T)
+        host.ops.S[m] = host.S[m].struct()
+    host.C = pkg.abi.CscArrays(rng.standard_normal((nq, nf)) * 0.1)
+    host.ops.C = host.C.struct()
+    got = pkg.GB300Solver(host).residual(u)
+    want = Oracle(host).residual(u)
+    floor = roundoff_floor(host, u)
+    assert rel2(got, want) <= max(1e-12, 4 * floor), (rel2(got, want), floor)
