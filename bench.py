@@ -378,6 +378,53 @@ def adjoint_gradient_check(pkg, stream, n_dirs: int = 8):
             "fd_rel_err_max": max(errs), "fd_rel_err_median": float(np.median(errs))}
 
 
+def geometry_workload(pkg, pb, fp64_peak):
+    """GeometricFactors + project_jacobian! of the workload's mesh
+    (mesh.jl:229-506, SpatialDiscretizations.jl:310-317): the host numpy
+    restatement against sse_geometric_factors, whose FP64 kernel builds every
+    element's metric terms in shared memory.  Device buffers: CUDA events
+    around the whole call (operator upload, kernel, synchronisation); host
+    buffers: wall clock including the copies of coordinates and results."""
+    import torch
+    sd = pb.sd
+    mesh, ra, metrics = sd.mesh, sd.reference_approximation, sd.metrics
+    project = metrics == "Exact"
+    t0 = time.perf_counter()
+    want = pkg.mesh.spatial_discretization(mesh, ra, metrics=metrics, project_jac=project).geometric_factors
+    host_s = time.perf_counter() - t0
+    xyz = [torch.from_numpy(x).cuda() for x in mesh.xyz]
+    pkg.gb300.geometric_factors(mesh, ra, metrics, project, xyz=xyz)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        pkg.gb300.geometric_factors(mesh, ra, metrics, project, xyz=xyz)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    dev_ms = float(np.median(times))
+    t0 = time.perf_counter()
+    got = pkg.gb300.geometric_factors(mesh, ra, metrics, project)
+    hostbuf_s = time.perf_counter() - t0
+    err = max(float(np.abs(getattr(got, f) - getattr(want, f)).max() / np.abs(getattr(want, f)).max())
+              for f in ("J_q", "Lambda_q", "J_f", "nJf", "nJq"))
+    mo = pkg.mesh.metric_operators(ra, metrics, project)
+    flops = pkg.flops_model.geometric_factors_flops(
+        ra.d, metrics, mesh.xyz[0].shape[1], mo.Vq.shape[0], mo.Vf.shape[0], mo.num_faces,
+        0 if mo.N_to_N1 is None else mo.N_to_N1.shape[0], project) * sd.N_e
+    tflops = flops / (dev_ms * 1e-3) / 1e12
+    kernel = ("curl_metrics_3d_kernel" if ra.d == 3 else "curl_metrics_2d_kernel") \
+        if metrics != "Exact" else "exact_metrics_kernel"
+    return {"metrics": metrics, "project_jacobian": project, "elements": sd.N_e,
+            "host_numpy_s": host_s, "gpu_device_buffers_ms": dev_ms,
+            "gpu_host_buffers_ms": hostbuf_s * 1e3, "speedup_device_buffers": host_s / (dev_ms * 1e-3),
+            "max_field_rel_err_vs_host": err,
+            "roofline": {"kernel": kernel, "bound": "fp64", "achieved": tflops, "peak": fp64_peak,
+                         "unit": "TFLOP/s", "frac": tflops / fp64_peak,
+                         "algorithmic_flops_per_element": flops / sd.N_e}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -390,6 +437,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-geometry", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=40,
                     help="time steps of the tgv_p5 adjoint leg (40 = 200 stages)")
     args = ap.parse_args()
@@ -524,6 +572,8 @@ def main():
         elif args.workload == "tgv_p5":
             adjoint = adjoint_mixed_workload(pkg, gpu, host, pb.u0, dt, args.adjoint_steps, stream)
 
+    geometry = None if args.no_geometry else geometry_workload(pkg, pb, fp64_peak)
+
     # ---- end to end through the C-ABI with host (pinned) buffers
     u_host = torch.from_numpy(pb.u0.copy()).pin_memory()
     gpu.rk_steps(u_host, 1, dt, scheme)
@@ -544,7 +594,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args, host, world),
             "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-            "mixed": mixed, "adjoint": adjoint}
+            "mixed": mixed, "adjoint": adjoint, "geometric_factors": geometry}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pb, host, args.cpu_budget)
     if rank == 0:

@@ -33,6 +33,8 @@ SSE_HOST = 0
 SSE_DEVICE = 1
 SSE_CARPENTER_KENNEDY_2N54 = 0
 SSE_RK4 = 1
+SSE_EXACT_METRICS = 0
+SSE_CONSERVATIVE_CURL_METRICS = 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int64)
@@ -63,6 +65,20 @@ class SseGeometry(C.Structure):
     _fields_ = [("BJf", _dp), ("n_f", _dp), ("mapP", _ip), ("halfWLambda", _dp),
                 ("WJ", _dp), ("Lambda_q", _dp), ("halfnJf", _dp), ("halfnJq", _dp),
                 ("JinvW", _dp), ("WJinv", _dp)]
+
+
+class SseMetricOperators(C.Structure):
+    _fields_ = [("d", C.c_int32), ("metrics", C.c_int32), ("n_map", C.c_int32),
+                ("n_q", C.c_int32), ("n_f", C.c_int32), ("num_faces", C.c_int32),
+                ("n_curl", C.c_int32), ("project_jacobian", C.c_int32),
+                ("Drst", _dp * 3), ("Vq", _dp), ("Vf", _dp), ("nrstJ", _dp * 3),
+                ("N_to_Nplus1", _dp), ("Drst_Nplus1", _dp * 3), ("Vq_Nplus1", _dp),
+                ("Vf_Nplus1", _dp), ("project", _dp)]
+
+
+class SseGeometricFactorsOut(C.Structure):
+    _fields_ = [("J_q", C.c_void_p), ("Lambda_q", C.c_void_p), ("J_f", C.c_void_p),
+                ("nJf", C.c_void_p), ("nJq", C.c_void_p)]
 
 
 def dptr(a: np.ndarray | None):

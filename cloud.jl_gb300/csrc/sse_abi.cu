@@ -1520,7 +1520,21 @@ int32_t sse_struct_sizes(int32_t *out) {
   out[1] = (int32_t)sizeof(sse_csc);
   out[2] = (int32_t)sizeof(sse_operators);
   out[3] = (int32_t)sizeof(sse_geometry);
-  return 4;
+  out[4] = (int32_t)sizeof(sse_metric_operators);
+  out[5] = (int32_t)sizeof(sse_geometric_factors_out);
+  return 6;
+}
+
+int32_t sse_geometric_factors(const sse_metric_operators *ops, int64_t n_e,
+                              const double *const *xyz,
+                              const sse_geometric_factors_out *out, int32_t memory) {
+  g_create_error.clear();
+  try {
+    return geometric_factors_run(ops, n_e, xyz, out, memory, &g_create_error);
+  } catch (const std::exception &ex) {
+    g_create_error = ex.what();
+    return SSE_ERR_OUT_OF_MEMORY;
+  }
 }
 
 }  // extern "C"

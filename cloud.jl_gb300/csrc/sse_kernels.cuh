@@ -2,8 +2,10 @@
 #pragma once
 
 #include <cstddef>
+#include <string>
 #include <cuda_runtime.h>
 
+#include "../../include/sse_gb300.h"
 #include "sse_device.cuh"
 
 namespace sse {
@@ -87,5 +89,10 @@ cudaError_t launch_adj_lincomb(double *y, const double *x, double alpha, double 
                                cudaStream_t st);
 cudaError_t launch_adj_rk4_stage(double *ybar, double *kbar, const double *mu, const double *yp,
                                  double cy, double cm, int last, size_t n, cudaStream_t st);
+
+// GeometricFactors on the device (sse_geometry.cu); returns an sse_status
+// and leaves a message in *err on failure.
+int geometric_factors_run(const sse_metric_operators *ops, int64_t n_e, const double *const *xyz,
+                          const sse_geometric_factors_out *out, int memory, std::string *err);
 
 }  // namespace sse

@@ -112,3 +112,26 @@ def _unique_pairs(host) -> int:
                 if i < j:
                     seen.add((i, j))
     return len(seen)
+
+
+def geometric_factors_flops(d: int, metrics: str, n_map: int, n_q: int, n_f: int,
+                            num_faces: int, n_curl: int = 0, project: bool = False) -> float:
+    """FP64 flops per element of GeometricFactors as sse_geometric_factors
+    evaluates it (mesh.jl:229-282, 284-339, 410-506): dense matrix-vector
+    products at 2 flops per entry, the per-node metric algebra and the
+    normals (3 products and 2 sums per component, one square root)."""
+    normals = n_q * num_faces * d * (2 * d - 1) + n_f * (d * (2 * d - 1) + 2 * d)
+    if metrics == "Exact":
+        adj = 12 * 3 + 5 if d == 3 else 3
+        work = (2.0 * d * d * n_map * n_map + 2.0 * d * d * n_map * (n_q + n_f)
+                + adj * (n_q + n_f))
+        if project:
+            work += 2.0 * n_q * n_q
+        return work + normals
+    if d == 2:
+        return (2.0 * 4 * n_map * n_map + 7 * n_map + 2.0 * 5 * n_q * n_map
+                + 2.0 * 4 * n_f * n_map + normals)
+    n1 = n_curl
+    return (2.0 * 9 * n_map * n_map + 17 * n_map + 2.0 * 3 * n1 * n_map + 2.0 * 9 * n1 * n1
+            + 9 * n1 + 2.0 * 18 * n1 * n1 + 9 * n1 + 2.0 * n_q * n_map
+            + 2.0 * 9 * (n_q + n_f) * n1 + normals)

@@ -27,7 +27,7 @@ EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual",
             "sse_rk_adjoint",
             "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
             "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
-            "sse_create_error"]
+            "sse_create_error", "sse_geometric_factors"]
 
 _lib = None
 
@@ -84,6 +84,8 @@ def load_library(path: str | None = None):
     L.sse_last_error.argtypes = [vp]
     L.sse_last_error.restype = C.c_char_p
     L.sse_create_error.restype = C.c_char_p
+    L.sse_geometric_factors.argtypes = [vp, C.c_int64, vp, vp, i32]
+    L.sse_geometric_factors.restype = i32
     _lib = L
     return L
 
@@ -240,6 +242,79 @@ def measure_fma_peaks():
     if rc != abi.SSE_OK:
         raise SSEError(rc, "peak measurement failed")
     return float(out[0]), float(out[1])
+
+
+def _fortran(a):
+    """Column-major FP64 copy of a reference matrix (Julia Matrix layout)."""
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+def geometric_factors(mesh, ra, metrics: str = "Exact", project_jac: bool = True, xyz=None):
+    """``GeometricFactors(mesh, reference_element, metric_type)`` plus
+    ``project_jacobian!`` computed on the GPU in FP64 (sse_geometric_factors).
+
+    ``xyz`` defaults to ``mesh.xyz`` (numpy (N_e, N_map) per coordinate, the
+    layout of Julia's (N_map, N_e)): the result is then a host
+    ``GeometricFactors`` of numpy arrays, as the host path returns.  CUDA
+    float64 tensors in ``xyz`` keep everything on the device and return the
+    fields as CUDA tensors of the same shapes."""
+    from .mesh import GeometricFactors, metric_operators
+    L = load_library()
+    mo = metric_operators(ra, metrics, project_jac)
+    d = ra.d
+    xyz = mesh.xyz if xyz is None else xyz
+    N_e, n_map = xyz[0].shape
+    keep = []
+
+    def mat(a):
+        if a is None:
+            return None
+        f = _fortran(a)
+        keep.append(f)
+        return f.ctypes.data_as(C.POINTER(C.c_double))
+
+    ops = abi.SseMetricOperators()
+    ops.d = d
+    ops.metrics = abi.SSE_EXACT_METRICS if metrics == "Exact" else abi.SSE_CONSERVATIVE_CURL_METRICS
+    ops.n_map = n_map
+    ops.n_q = mo.Vq.shape[0]
+    ops.n_f = mo.Vf.shape[0]
+    ops.num_faces = mo.num_faces
+    ops.n_curl = 0 if mo.N_to_N1 is None else mo.N_to_N1.shape[0]
+    ops.project_jacobian = 1 if mo.project is not None else 0
+    for m in range(d):
+        ops.Drst[m] = mat(mo.Drst[m])
+        ops.nrstJ[m] = mat(mo.nrstJ[m])
+    ops.Vq = mat(mo.Vq)
+    ops.Vf = mat(mo.Vf)
+    if mo.N_to_N1 is not None:
+        ops.N_to_Nplus1 = mat(mo.N_to_N1)
+        for m in range(3):
+            ops.Drst_Nplus1[m] = mat(mo.D1[m])
+        ops.Vq_Nplus1 = mat(mo.Vq1)
+        ops.Vf_Nplus1 = mat(mo.Vf1)
+    ops.project = mat(mo.project)
+
+    nq, nf, nfac = ops.n_q, ops.n_f, mo.num_faces
+    shapes = [(N_e, nq), (N_e, d, d, nq), (N_e, nf), (N_e, nf, d), (N_e, nq, nfac, d)]
+    on_device = not isinstance(xyz[0], np.ndarray)
+    if on_device:
+        import torch
+        outs = [torch.empty(sh, dtype=torch.float64, device=xyz[0].device) for sh in shapes]
+        memory = abi.SSE_DEVICE
+        xs = [x.contiguous() for x in xyz]
+        ptrs = (C.c_void_p * 3)(*[x.data_ptr() for x in xs], *([None] * (3 - d)))
+    else:
+        outs = [np.empty(sh) for sh in shapes]
+        memory = abi.SSE_HOST
+        xs = [np.ascontiguousarray(x, dtype=np.float64) for x in xyz]
+        ptrs = (C.c_void_p * 3)(*[x.ctypes.data for x in xs], *([None] * (3 - d)))
+    addr = (lambda t: t.data_ptr()) if on_device else (lambda a: a.ctypes.data)
+    res = abi.SseGeometricFactorsOut(*[addr(o) for o in outs])
+    rc = L.sse_geometric_factors(C.byref(ops), N_e, ptrs, C.byref(res), memory)
+    if rc != abi.SSE_OK:
+        raise SSEError(rc, L.sse_create_error().decode())
+    return GeometricFactors(*outs)
 
 
 @dataclass

@@ -341,6 +341,59 @@ def _curl_metrics_3d(x, y, z, Dr, Ds, Dt):
     return rxJ, sxJ, txJ, ryJ, syJ, tyJ, rzJ, szJ, tzJ
 
 
+@dataclass
+class MetricOperators:
+    """Reference-element matrices the geometric factors are built from (the
+    fields of ``sse_metric_operators``): derivative matrices at the mapping
+    nodes, interpolation to the volume / facet quadrature nodes, the scaled
+    reference normals, and for the tetrahedral curl metrics the degree N+1
+    element of mesh.jl:414-433."""
+    d: int
+    metrics: str                 # "Exact" or "ChanWilcox"
+    Drst: tuple
+    Vq: np.ndarray
+    Vf: np.ndarray
+    nrstJ: tuple
+    num_faces: int
+    N_to_N1: np.ndarray | None = None
+    D1: tuple | None = None
+    Vq1: np.ndarray | None = None
+    Vf1: np.ndarray | None = None
+    project: np.ndarray | None = None
+
+
+def metric_operators(ra: ReferenceApproximation, metrics: str = "Exact",
+                     project_jac: bool = True) -> MetricOperators:
+    """The matrices of ``metrics`` for ``ra``, built once per reference
+    approximation and kept on it."""
+    cache = ra.__dict__.setdefault("_metric_operators", {})
+    key = (metrics, bool(project_jac))
+    if key not in cache:
+        cache[key] = _build_metric_operators(ra, metrics, project_jac)
+    return cache[key]
+
+
+def _build_metric_operators(ra: ReferenceApproximation, metrics: str,
+                            project_jac: bool) -> MetricOperators:
+    ref = ra.reference_element
+    ops = MetricOperators(ra.d, metrics, tuple(ref.Drst), ref.Vq, ref.Vf, tuple(ref.nrstJ),
+                          ref.num_faces)
+    if metrics == "ChanWilcox" and ra.d == 3:
+        N = ref.N
+        r1, s1, t1 = simplex_nodes("Tet", N + 1)
+        V1, G1 = _simplex_basis("Tet", N + 1, r1, s1, t1)
+        ops.D1 = tuple(np.linalg.solve(V1.T, G.T).T for G in G1)
+        ops.N_to_N1 = np.linalg.solve(ref.VDM.T, _simplex_basis("Tet", N, r1, s1, t1)[0].T).T
+        N1_to_N = np.linalg.solve(V1.T, _simplex_basis("Tet", N + 1, *ref.rst)[0].T).T
+        ops.Vq1 = ref.Vq @ N1_to_N
+        ops.Vf1 = ref.Vf @ N1_to_N
+    if metrics == "Exact" and project_jac:
+        V = ra.V_dense
+        W = np.diag(ra.W)
+        ops.project = V @ np.linalg.inv(V.T @ W @ V) @ V.T @ W
+    return ops
+
+
 def geometric_factors_curl(mesh: MeshData, ra: ReferenceApproximation) -> GeometricFactors:
     """``GeometricFactors(..., ConservativeCurlMetrics())`` = ChanWilcoxMetrics
     (mesh.jl:284-339 for triangles, :410-506 for tetrahedra)."""
@@ -354,14 +407,8 @@ def geometric_factors_curl(mesh: MeshData, ra: ReferenceApproximation) -> Geomet
         comp = {(0, 0): rxJ, (1, 0): sxJ, (0, 1): ryJ, (1, 1): syJ}
         J_q = J @ Vq.T
     else:
-        N = ref.N
-        r1, s1, t1 = simplex_nodes("Tet", N + 1)
-        V1, G1 = _simplex_basis("Tet", N + 1, r1, s1, t1)
-        D1 = tuple(np.linalg.solve(V1.T, G.T).T for G in G1)
-        N_to_N1 = np.linalg.solve(ref.VDM.T, _simplex_basis("Tet", N, r1, s1, t1)[0].T).T
-        N1_to_N = np.linalg.solve(V1.T, _simplex_basis("Tet", N + 1, *ref.rst)[0].T).T
-        Vq = ref.Vq @ N1_to_N
-        Vf = ref.Vf @ N1_to_N
+        mo = metric_operators(ra, "ChanWilcox")
+        Vq, Vf = mo.Vq1, mo.Vf1
         x, y, z = mesh.xyz
         Dr, Ds, Dt = ref.Drst
         xr, xs, xt = x @ Dr.T, x @ Ds.T, x @ Dt.T
@@ -369,7 +416,8 @@ def geometric_factors_curl(mesh: MeshData, ra: ReferenceApproximation) -> Geomet
         zr, zs, zt = z @ Dr.T, z @ Ds.T, z @ Dt.T
         J = xr * (ys * zt - zs * yt) - yr * (xs * zt - zs * xt) + zr * (xs * yt - ys * xt)
         J_q = J @ ref.Vq.T
-        terms = _curl_metrics_3d(x @ N_to_N1.T, y @ N_to_N1.T, z @ N_to_N1.T, *D1)
+        N_to_N1 = mo.N_to_N1
+        terms = _curl_metrics_3d(x @ N_to_N1.T, y @ N_to_N1.T, z @ N_to_N1.T, *mo.D1)
         rxJ, sxJ, txJ, ryJ, syJ, tyJ, rzJ, szJ, tzJ = terms
         comp = {(0, 0): rxJ, (1, 0): sxJ, (2, 0): txJ,
                 (0, 1): ryJ, (1, 1): syJ, (2, 1): tyJ,
@@ -388,10 +436,7 @@ def geometric_factors_curl(mesh: MeshData, ra: ReferenceApproximation) -> Geomet
 def project_jacobian(J_q: np.ndarray, ra: ReferenceApproximation) -> np.ndarray:
     """project_jacobian! (SpatialDiscretizations.jl:310-317):
     J_q <- V (V^T W V)^{-1} V^T W J_q for every element."""
-    V = ra.V_dense
-    W = np.diag(ra.W)
-    proj = V @ np.linalg.inv(V.T @ W @ V) @ V.T @ W
-    return J_q @ proj.T
+    return J_q @ metric_operators(ra, "Exact", True).project.T
 
 
 @dataclass
@@ -408,7 +453,20 @@ class SpatialDiscretization:
 
 
 def spatial_discretization(mesh: MeshData, ra: ReferenceApproximation,
-                           metrics: str = "Exact", project_jac: bool = True) -> SpatialDiscretization:
+                           metrics: str = "Exact", project_jac: bool = True,
+                           geometry: str = "host") -> SpatialDiscretization:
+    """``SpatialDiscretization(mesh, reference_approximation, metric_type;
+    project_jacobian)``.  ``geometry="gpu"`` builds the geometric factors
+    with the library's ``sse_geometric_factors`` (FP64, on the current CUDA
+    device) instead of numpy."""
+    if metrics == "ConservativeCurl":
+        metrics = "ChanWilcox"
+    if geometry == "gpu":
+        from . import gb300
+        gf = gb300.geometric_factors(mesh, ra, metrics, project_jac)
+        return SpatialDiscretization(mesh, ra, gf, metrics)
+    if geometry != "host":
+        raise ValueError(geometry)
     if metrics == "Exact":
         gf = geometric_factors_exact(mesh, ra)
         if project_jac:

@@ -254,13 +254,69 @@ int32_t sse_set_stream(sse_solver *s, void *stream);
  * sections of Solvers.jl:474-489. */
 int32_t sse_phase_timings(sse_solver *s, const double *u_dev, int32_t n_iter, double *out);
 
+/* ---- Geometric factors on the device -------------------------------------
+ *
+ * Drop-in for the constructor GeometricFactors(mesh, reference_element,
+ * metric_type) (src/SpatialDiscretizations/mesh.jl:229-282 ExactMetrics,
+ * :284-339 ConservativeCurlMetrics on Tri, :410-506 on Tet) followed by
+ * project_jacobian! (SpatialDiscretizations.jl:310-317), which
+ * SpatialDiscretization(...) calls (SpatialDiscretizations.jl:333-392).  All
+ * arithmetic is FP64; each element's metric terms come from its own
+ * mapping-node coordinates, one CTA per element. */
+enum sse_metrics { SSE_EXACT_METRICS = 0, SSE_CONSERVATIVE_CURL_METRICS = 1 };
+
+/* Reference-element matrices, column-major (Julia Matrix{Float64}). */
+typedef struct sse_metric_operators {
+  int32_t d;                /* 2 (Tri) or 3 (Tet) */
+  int32_t metrics;          /* enum sse_metrics (ChanWilcoxMetrics = curl) */
+  int32_t n_map;            /* mapping nodes per element: size(mesh.xyz[1], 1) */
+  int32_t n_q;              /* size(reference_element.Vq, 1) */
+  int32_t n_f;              /* size(reference_element.Vf, 1) */
+  int32_t num_faces;        /* 3 (Tri) or 4 (Tet) */
+  int32_t n_curl;           /* Tet curl: nodes of the degree N+1 basis; else 0 */
+  int32_t project_jacobian; /* 1: J_q <- project J_q (exact metrics only) */
+  const double *Drst[3];    /* reference_element.Dr, Ds, Dt: n_map x n_map */
+  const double *Vq;         /* reference_element.Vq: n_q x n_map */
+  const double *Vf;         /* reference_element.Vf: n_f x n_map */
+  const double *nrstJ[3];   /* reference_element.nrstJ: n_f each */
+  /* Tet with ConservativeCurlMetrics (mesh.jl:410-464) */
+  const double *N_to_Nplus1;     /* n_curl x n_map */
+  const double *Drst_Nplus1[3];  /* Vr_Nplus1 / V_Nplus1, ...: n_curl x n_curl */
+  const double *Vq_Nplus1;       /* reference_element.Vq * Nplus1_to_N: n_q x n_curl */
+  const double *Vf_Nplus1;       /* reference_element.Vf * Nplus1_to_N: n_f x n_curl */
+  /* project_jacobian!: VDM inv(VDM' W VDM) VDM' W, n_q x n_q */
+  const double *project;
+} sse_metric_operators;
+
+/* GeometricFactors fields (SpatialDiscretizations.jl:283-289), written in
+ * the reference's layouts. */
+typedef struct sse_geometric_factors_out {
+  double *J_q;      /* n_q x N_e */
+  double *Lambda_q; /* n_q x d x d x N_e : Λ_q[i, m, n, k] = J ∂ξ_m/∂x_n */
+  double *J_f;      /* n_f x N_e */
+  double *nJf;      /* d x n_f x N_e */
+  double *nJq;      /* d x num_faces x n_q x N_e */
+} sse_geometric_factors_out;
+
+/* Compute the geometric factors of n_e elements from the mapping-node
+ * coordinates xyz[m] (mesh.xyz[m], n_map x n_e each).  memory = SSE_HOST:
+ * xyz and the outputs are host arrays (staged through temporary device
+ * buffers); SSE_DEVICE: all are device pointers.  The operator matrices are
+ * host arrays in both cases.  Errors leave their message for
+ * sse_create_error(). */
+int32_t sse_geometric_factors(const sse_metric_operators *ops, int64_t n_e,
+                              const double *const *xyz,
+                              const sse_geometric_factors_out *out, int32_t memory);
+
 /* Measured FMA throughput of the current device in TFLOP/s (2 flops per
  * FMA): out[0] FP64, out[1] FP32 CUDA-core pipes.  The roofline
  * denominators of the residual kernels; no counterpart in the reference. */
 int32_t sse_measure_fma_peaks(double *out);
 
 /* sizeof(sse_config), sizeof(sse_csc), sizeof(sse_operators),
- * sizeof(sse_geometry) into out[0..3], for checking foreign bindings. */
+ * sizeof(sse_geometry), sizeof(sse_metric_operators),
+ * sizeof(sse_geometric_factors_out) into out[0..5], for checking foreign
+ * bindings; returns the count. */
 int32_t sse_struct_sizes(int32_t *out);
 
 /* Message of the last failing call on this handle ("" if none). */

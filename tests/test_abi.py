@@ -38,10 +38,11 @@ def test_exports_every_declared_symbol(pkg, lib):
 
 def test_struct_layouts(pkg, lib):
     abi = pkg.abi
-    sizes = (C.c_int32 * 4)()
-    assert lib.sse_struct_sizes(sizes) == 4
+    sizes = (C.c_int32 * 6)()
+    assert lib.sse_struct_sizes(sizes) == 6
     assert list(sizes) == [C.sizeof(abi.SseConfig), C.sizeof(abi.SseCsc),
-                           C.sizeof(abi.SseOperators), C.sizeof(abi.SseGeometry)]
+                           C.sizeof(abi.SseOperators), C.sizeof(abi.SseGeometry),
+                           C.sizeof(abi.SseMetricOperators), C.sizeof(abi.SseGeometricFactorsOut)]
     assert lib.sse_abi_version() == 1
 
 
@@ -111,3 +112,43 @@ def test_product_has_no_cpu_fallback(pkg):
             pkg.gb300.load_library(os.path.join(ROOT, "does-not-exist.so"))
     finally:
         pkg.gb300._lib = saved
+
+
+def test_geometric_factors_rejects_invalid_arguments(pkg, lib):
+    """sse_geometric_factors validates its operators and sizes before it
+    touches the device."""
+    abi = pkg.abi
+    ops = abi.SseMetricOperators()
+    res = abi.SseGeometricFactorsOut()
+    xyz = (C.c_void_p * 3)()
+    assert lib.sse_geometric_factors(None, 4, xyz, C.byref(res), abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    ops.d = 4
+    assert lib.sse_geometric_factors(C.byref(ops), 4, xyz, C.byref(res), abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert "d must be" in lib.sse_create_error().decode()
+    ops.d, ops.metrics = 3, 7
+    assert lib.sse_geometric_factors(C.byref(ops), 4, xyz, C.byref(res), abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    ops.metrics = abi.SSE_CONSERVATIVE_CURL_METRICS
+    ops.n_map, ops.n_q, ops.n_f, ops.num_faces = 10, 27, 30, 4    # 30 facet nodes on 4 faces
+    assert lib.sse_geometric_factors(C.byref(ops), 4, xyz, C.byref(res), abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert "sizes" in lib.sse_create_error().decode()
+    # a complete set of matrices but no degree N+1 element for the Tet curl form
+    ra = pkg.reference.reference_approximation("ModalTensor", "Tet", 2, mapping_degree=2)
+    mo = pkg.mesh.metric_operators(ra, "Exact", False)
+    keep = [np.asfortranarray(a) for a in (*mo.Drst, mo.Vq, mo.Vf, *mo.nrstJ)]
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    ops.n_map, ops.n_q, ops.n_f = mo.Vq.shape[1], mo.Vq.shape[0], mo.Vf.shape[0]
+    for m in range(3):
+        ops.Drst[m], ops.nrstJ[m] = dp(keep[m]), dp(keep[5 + m])
+    ops.Vq, ops.Vf = dp(keep[3]), dp(keep[4])
+    x = np.zeros((4, ops.n_map))
+    xyz = (C.c_void_p * 3)(x.ctypes.data, x.ctypes.data, x.ctypes.data)
+    assert lib.sse_geometric_factors(C.byref(ops), 4, xyz, C.byref(res), abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert "n_curl" in lib.sse_create_error().decode()
+    # projection is defined for exact metrics only
+    ops.metrics, ops.project_jacobian = abi.SSE_EXACT_METRICS, 1
+    assert lib.sse_geometric_factors(C.byref(ops), 4, xyz, C.byref(res), abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert "project" in lib.sse_create_error().decode()
+    # outputs are required
+    ops.project_jacobian = 0
+    assert lib.sse_geometric_factors(C.byref(ops), 4, xyz, C.byref(res), abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert "output" in lib.sse_create_error().decode()
