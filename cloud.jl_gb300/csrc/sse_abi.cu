@@ -449,13 +449,16 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
 
   // ---- team geometry and shared-memory layouts
   const int nc = c.n_c, np = c.n_p, nq = c.n_q, nf = c.n_f, d = c.d;
-  int tpe = nq >= 64 ? 128 : 32;
+  // Tets: one element per 256-thread block (measured against 128 threads at
+  // p = 4 and 5: phase B 7.6 % and 5.4 % faster, mixed phase A 1.75x; the
+  // FP64 pipe idles less with eight warps per element).  Tris: four
+  // elements of 32 threads per block (measured against 64 x 4 and 32 x 8).
+  const int tpe = nq >= 64 ? 256 : 32;
   // doubles of shared memory per element team that keep two blocks per SM
   auto team_budget = [](int tpe_) {
     const int epb_ = (tpe_ == 32) ? 4 : 1;
     return (int)((size_t)110 * 1024 / 8 / epb_);
   };
-  if (tpe == 128 && nq + nf > kMaxNodeSlots * tpe) tpe = 256;
   if (nq + nf > kMaxNodeSlots * tpe)
     return fail(s, SSE_ERR_UNSUPPORTED, "n_q + n_f too large for one element team");
   int zsz = 0, wsz = 0;
