@@ -449,11 +449,13 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
 
   // ---- team geometry and shared-memory layouts
   const int nc = c.n_c, np = c.n_p, nq = c.n_q, nf = c.n_f, d = c.d;
-  // Tets: one element per 256-thread block (measured against 128 threads at
-  // p = 4 and 5: phase B 7.6 % and 5.4 % faster, mixed phase A 1.75x; the
-  // FP64 pipe idles less with eight warps per element).  Tris: four
-  // elements of 32 threads per block (measured against 64 x 4 and 32 x 8).
-  const int tpe = nq >= 64 ? 256 : 32;
+  // Tets: one element per block, 256 threads once the element has more than
+  // 192 volume and facet nodes (measured against 128 threads: phase B 7.6 %
+  // and 5.4 % faster at p = 4 and 5, mixed phase A 1.75x -- the FP64 pipe
+  // idles less with eight warps per element -- but 15 % slower at p = 3,
+  // whose 128 nodes leave half the threads idle).  Tris: four elements of 32
+  // threads per block (measured against 64 x 4 and 32 x 8).
+  const int tpe = nq < 64 ? 32 : (nq + nf > 192 ? 256 : 128);
   // doubles of shared memory per element team that keep two blocks per SM
   auto team_budget = [](int tpe_) {
     const int epb_ = (tpe_ == 32) ? 4 : 1;
@@ -757,9 +759,11 @@ cudaError_t residual_device(sse_solver *s, const double *u, double *dudt, double
 // VJP scratch and shared-memory layouts of the three adjoint kernels.
 int enable_adjoint(sse_solver *s) {
   const sse_config &c = s->cfg;
-  if (!(c.form == SSE_FLUX_DIFFERENCING_FORM && c.law == SSE_EULER && c.two_point_flux == SSE_EC_FLUX))
-    return fail(s, SSE_ERR_UNSUPPORTED,
-                "the discrete adjoint covers FluxDifferencingForm with the entropy-conservative flux (Euler)");
+  const bool fd = c.form == SSE_FLUX_DIFFERENCING_FORM;
+  // FluxDifferencingForm pair transposes: the contracted entropy-conservative
+  // flux (Euler) or the conservative two-point flux (advection, Euler with
+  // ConservativeFlux)
+  const bool ec_pairs = c.law == SSE_EULER && c.two_point_flux == SSE_EC_FLUX;
   if (!s->mapP_involution)
     return fail(s, SSE_ERR_UNSUPPORTED, "the discrete adjoint needs mapP to pair facet nodes (mapP(mapP(x)) == x)");
   if (s->adj_ready) return SSE_OK;
@@ -779,39 +783,68 @@ int enable_adjoint(sse_solver *s) {
   };
   const size_t cap = (size_t)220 * 1024 / 8 / ka.epb;  // doubles per team
   const int tpe_adj = ka.tpb / ka.epb;
-  // lift: X, Y, Z, W, F as in phase A
+  // lift (and the plain nodal-values transpose): X, Y, Z, W, F as in phase A
   ka.layAdjB1 = ka.layA;
+  cudaError_t e;
+  void *p;
+  const size_t ne = c.n_e, n = (size_t)np * nc * ne;
+  auto alloc_vjp = [&]() -> int {
+    if ((e = alloc(s, (size_t)nq * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.rbar_q = (double *)p;
+    if ((e = alloc(s, (size_t)nf * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.gbar_f = (double *)p;
+    if ((e = alloc(s, (size_t)nq * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.ubar_q = (double *)p;
+    if ((e = alloc(s, (size_t)nf * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.ubar_f = (double *)p;
+    if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_lam = (double *)p;
+    if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_mu = (double *)p;
+    if ((e = sse_set_smem_limits_adjoint(ka))) return cuda_fail(s, e, "cudaFuncSetAttribute (adjoint)");
+    s->adj_ready = true;
+    return SSE_OK;
+  };
+  if (!fd) {
+    // StandardForm flux transposes: u_q, u_f, rbar_q, gbar_f, fbar_n (d of
+    // them), two volume temporaries, one facet temporary
+    finish(ka.layAdjS, {nc * nq, nc * nf, nc * nq, nc * nf, d * nc * nq, nc * nq, nc * nq, nc * nf});
+    if (ka.layAdjS.team_doubles > (int)cap)
+      return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the adjoint kernels' shared memory");
+    return alloc_vjp();
+  }
   // projection transpose: X, Y, Z, W, F, u_q0, w_q, w_f, ubar_q, ubar_f
   finish(ka.layAdjA, {nc * std::max(np, nq), nc * nq, zsz, wsz, nc * std::max({np, nq, nf}), nc * nq,
                       nc * nq, nc * nf, nc * nq, nc * nf});
-  // pair transposes: fixed arrays, then a chunk of per-pair primitive cotangents
+  if (ka.layAdjA.team_doubles > (int)cap)
+    return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the adjoint kernels' shared memory");
   const int hsz = op.nfp > 0 ? d * c.num_faces * nq : 0;
+  const int max_pairs = std::max(op.nvp, op.nfp);
+  if (!ec_pairs) {
+    // conservative two-point flux: u_q, u_f, rbar_q, fbar_f, ubar_q, ubar_f,
+    // Lambda_q, halfnJq, then a chunk of per-pair state cotangents (2 NC each)
+    Layout gbase{};
+    finish(gbase, {nc * nq, nc * nf, nc * nq, nc * nf, nc * nq, nc * nf, d * d * nq, hsz});
+    long room = (long)(110 * 1024 / 8 / ka.epb) - gbase.team_doubles;
+    if (room < 128 * 2 * nc) room = (long)cap - gbase.team_doubles;
+    int chunk = (int)std::min<long>(max_pairs, room / (2 * nc));
+    if (chunk >= tpe_adj) chunk = chunk / tpe_adj * tpe_adj;
+    if (chunk < 1)
+      return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the adjoint kernels' shared memory");
+    ka.pair_chunk_generic = chunk;
+    finish(ka.layAdjG, {nc * nq, nc * nf, nc * nq, nc * nf, nc * nq, nc * nf, d * d * nq, hsz,
+                        chunk * 2 * nc});
+    return alloc_vjp();
+  }
+  // pair transposes: fixed arrays, then a chunk of per-pair primitive cotangents
   Layout base{};
   finish(base, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf, d * d * nq, hsz});
-  const int max_pairs = std::max(op.nvp, op.nfp);
   // chunk: as large as keeps two blocks per SM when that leaves at least
   // 128 pairs; otherwise one block per SM with chunks as large as fit
   long room = (long)(110 * 1024 / 8 / ka.epb) - base.team_doubles;
   if (room < 128 * 2 * ps) room = (long)cap - base.team_doubles;
   int chunk = (int)std::min<long>(max_pairs, room / (2 * ps));
   if (chunk >= tpe_adj) chunk = chunk / tpe_adj * tpe_adj;
-  if (chunk < 1 || ka.layAdjA.team_doubles > (int)cap)
+  if (chunk < 1)
     return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the adjoint kernels' shared memory");
   ka.pair_chunk = chunk;
   finish(ka.layAdjB2, {nc * nq, nc * nf, nc * nq, nc * nf, (nq + nf) * ps, (nq + nf) * ps, nc * nf,
                        d * d * nq, hsz, chunk * 2 * ps});
-  cudaError_t e;
-  void *p;
-  const size_t ne = c.n_e, n = (size_t)np * nc * ne;
-  if ((e = alloc(s, (size_t)nq * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.rbar_q = (double *)p;
-  if ((e = alloc(s, (size_t)nf * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.gbar_f = (double *)p;
-  if ((e = alloc(s, (size_t)nq * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.ubar_q = (double *)p;
-  if ((e = alloc(s, (size_t)nf * nc * ne * 8, &p))) return cuda_fail(s, e, "alloc"); ka.ubar_f = (double *)p;
-  if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_lam = (double *)p;
-  if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_mu = (double *)p;
-  if ((e = sse_set_smem_limits_adjoint(ka))) return cuda_fail(s, e, "cudaFuncSetAttribute (adjoint)");
-  s->adj_ready = true;
-  return SSE_OK;
+  return alloc_vjp();
 }
 
 // Layouts (in floats) of the mixed-form VJP kernels; needs enable_adjoint

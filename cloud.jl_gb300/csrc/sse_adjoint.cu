@@ -1,19 +1,26 @@
-// sse_adjoint.cu -- discrete adjoint of the FP64 flux-differencing residual
-// (Euler, entropy-conservative volume flux, Lax-Friedrichs or EC interface
-// flux): mu = (dR/du)^T lam for the residual of flux_differencing_form.jl:
-// 253-347, with no counterpart in the reference (which has no AD).
+// sse_adjoint.cu -- discrete adjoint of the FP64 residual: mu = (dR/du)^T lam
+// for every configuration of the forward -- FluxDifferencingForm
+// (flux_differencing_form.jl:253-347) with the entropy-conservative or the
+// conservative two-point flux, and StandardForm
+// (standard_form_first_order.jl:1-63), for the Euler equations and linear
+// advection, with any interface flux -- with no counterpart in the
+// reference (which has no AD).
 //
 // Three kernels per vector-Jacobian product, after the forward phase A has
 // written u_q, u_f for the state:
 //   adj_lift_kernel     rbar_q = V M lam, interface cotangent gbar = -BJf R rbar_q
-//   adj_flux_kernel     per-pair transposes of the contracted EC flux, the
-//                       interface flux seen from both sides (no cross-element
-//                       atomics: each element differentiates its own flux
-//                       w.r.t. its inner state and its neighbour's flux w.r.t.
-//                       the neighbour's outer state), deterministic chunked
-//                       two-pass accumulation -> ubar_q, ubar_f
-//   adj_projection_kernel  recomputes the entropy projection and applies its
-//                       transpose (symmetric Jacobians of the entropy maps) -> mu
+//   adj_flux_kernel     (Euler, EC flux) per-pair transposes of the contracted
+//                       EC flux, the interface flux seen from both sides (no
+//                       cross-element atomics: each element differentiates its
+//                       own flux w.r.t. its inner state and its neighbour's
+//                       flux w.r.t. the neighbour's outer state), deterministic
+//                       chunked two-pass accumulation -> ubar_q, ubar_f
+//   adj_flux_generic_kernel  the same for the conservative two-point flux
+//   adj_std_flux_kernel      StandardForm volume, facet and interface transposes
+//   adj_projection_kernel  (Euler FD) recomputes the entropy projection and
+//                       applies its transpose (symmetric Jacobians of the
+//                       entropy maps) -> mu
+//   adj_nodal_kernel    (no projection) mu = V^T (ubar_q + R^T ubar_f)
 #include "sse_device.cuh"
 #include "sse_kernels.cuh"
 #include "sse_ops.cuh"
@@ -399,6 +406,458 @@ __global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
   vdm_tmul<double, D, NC>(op, Y, F, Z, Wb, lane, tpe);  // mu = V^T ubar_q0
   if (live)
     for (int t = lane; t < NC * np; t += tpe) ka.mu[(size_t)kk * NC * np + t] = F[t];
+}
+
+// ===========================================================================
+// StandardForm (standard_form_first_order.jl:1-63) and plain nodal values:
+// after adj_lift_kernel,
+//   adj_std_flux_kernel  transposes of the skew-symmetric volume terms
+//                        (halfWΛ, D_m), the facet term -halfN R f_n, the
+//                        physical flux and the interface numerical flux seen
+//                        from both sides -> ubar_q, ubar_f
+//   adj_nodal_kernel     u_q = V u, u_f = R u_q  =>  mu = V^T (ubar_q + R^T ubar_f)
+// The same adj_nodal_kernel closes the FluxDifferencingForm VJP of scalar
+// laws, which have no entropy projection.
+// ===========================================================================
+
+// Transpose of the physical flux F[e][n](u) (euler_navierstokes.jl:85-91;
+// linear advection F[0][n] = a_n u) applied to Fb[e][n]; adds to ub.
+template <int D, int NC>
+__device__ __forceinline__ void physical_flux_vjp(const Physics &ph, const double *u,
+                                                  const double (&Fb)[NC][D], double *ub) {
+  if constexpr (NC == 1) {
+#pragma unroll
+    for (int n = 0; n < D; ++n) ub[0] = fma(ph.a[n], Fb[0][n], ub[0]);
+  } else {
+    const double ir = 1.0 / u[0];
+    double V[D], vv = 0.0;
+#pragma unroll
+    for (int m = 0; m < D; ++m) { V[m] = u[m + 1] * ir; vv = fma(u[m + 1], V[m], vv); }
+    const double p = ph.gm1 * (u[D + 1] - 0.5 * vv);
+    const double ht = u[D + 1] + p;
+    double Vb[D], pb = 0.0, htb = 0.0;
+#pragma unroll
+    for (int n = 0; n < D; ++n) {
+      // F[0][n] = m_n ; F[m+1][n] = m_m V_n + delta_mn p ; F[D+1][n] = ht V_n
+      ub[n + 1] += Fb[0][n];
+      Vb[n] = Fb[D + 1][n] * ht;
+      htb = fma(Fb[D + 1][n], V[n], htb);
+      pb += Fb[n + 1][n];
+#pragma unroll
+      for (int m = 0; m < D; ++m) {
+        ub[m + 1] = fma(Fb[m + 1][n], V[n], ub[m + 1]);
+        Vb[n] = fma(Fb[m + 1][n], u[m + 1], Vb[n]);
+      }
+    }
+    // ht = E + p ; p = gm1 (E - |m|^2 / (2 rho)) ; V = m / rho
+    pb += htb;
+    ub[D + 1] += htb + ph.gm1 * pb;
+    double rb = 0.5 * ph.gm1 * pb * vv * ir;
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      ub[m + 1] += Vb[m] * ir - ph.gm1 * pb * V[m];
+      rb -= Vb[m] * V[m] * ir;
+    }
+    ub[0] += rb;
+  }
+}
+
+// Transpose, with respect to one side (0 inner, 1 outer), of the StandardForm
+// interface flux f* = (F(u_in) + F(u_out))/2 . n + a (u_in - u_out) with
+// a = halfλ wave_speed (LF; ConservationLaws.jl:75-128) or a = 0, applied to
+// the cotangent g; adds to ub (that side's conservative cotangent).
+template <int D, int NC>
+__device__ void std_iface_bwd(const Physics &ph, const double *uin, const double *uout,
+                              const double *n, const double *g, int side, double *ub) {
+  const double *us = side ? uout : uin;
+  double Fb[NC][D];
+#pragma unroll
+  for (int e = 0; e < NC; ++e)
+#pragma unroll
+    for (int m = 0; m < D; ++m) Fb[e][m] = 0.5 * g[e] * n[m];
+  physical_flux_vjp<D, NC>(ph, us, Fb, ub);
+  if (ph.nflux != 0) return;
+  const double a = ph.half_lambda * wave_speed<D, NC>(ph, uin, uout, n);
+  double abar = 0.0;
+#pragma unroll
+  for (int e = 0; e < NC; ++e) {
+    abar = fma(g[e], uin[e] - uout[e], abar);
+    ub[e] += side ? -a * g[e] : a * g[e];
+  }
+  if constexpr (NC > 1) {
+    // wave_speed = max(|V_in.n|, |V_out.n|) + max(c_in, c_out); the inner
+    // side owns ties (fmax returns its first argument's value)
+    const double hb = ph.half_lambda * abar;
+    double vn[2] = {0.0, 0.0}, c[2], p[2];
+    const double *uu[2] = {uin, uout};
+#pragma unroll
+    for (int sd = 0; sd < 2; ++sd) {
+      double s2 = 0.0;
+#pragma unroll
+      for (int m = 0; m < D; ++m) {
+        s2 += uu[sd][m + 1] * uu[sd][m + 1];
+        vn[sd] += (uu[sd][m + 1] / uu[sd][0]) * n[m];
+      }
+      p[sd] = ph.gm1 * (uu[sd][D + 1] - (0.5 / uu[sd][0]) * s2);
+      c[sd] = sqrt(ph.gamma * p[sd] / uu[sd][0]);
+    }
+    const double ir = 1.0 / us[0];
+    if ((fabs(vn[0]) >= fabs(vn[1])) == (side == 0)) {
+      // vn = sum_m (m_m / rho) n_m
+      const double vb = hb * (vn[side] >= 0.0 ? 1.0 : -1.0);
+#pragma unroll
+      for (int m = 0; m < D; ++m) ub[m + 1] += vb * n[m] * ir;
+      ub[0] -= vb * vn[side] * ir;
+    }
+    if ((c[0] >= c[1]) == (side == 0)) {
+      // c = sqrt(gamma p / rho), p = gm1 (E - |m|^2 / (2 rho))
+      const double cs = c[side];
+      const double pb = hb * ph.gamma * ir / (2.0 * cs);
+      double vv = 0.0;
+#pragma unroll
+      for (int m = 0; m < D; ++m) {
+        const double Vm = us[m + 1] * ir;
+        vv = fma(Vm, Vm, vv);
+        ub[m + 1] -= pb * ph.gm1 * Vm;
+      }
+      ub[D + 1] += pb * ph.gm1;
+      ub[0] += pb * 0.5 * ph.gm1 * vv - hb * cs * ir * 0.5;
+    }
+  }
+}
+
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_std_flux_kernel(KernelArgs ka) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const DevGeo &g = ka.geo;
+  const Layout &L = ka.layAdjS;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int nq = op.nq, nf = op.nf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *uq = base + L.off[0], *uf = base + L.off[1], *rb = base + L.off[2], *gb = base + L.off[3],
+         *fb = base + L.off[4], *t1 = base + L.off[5], *t2 = base + L.off[6], *tf = base + L.off[7];
+
+  for (int t = lane; t < NC * nq; t += tpe) {
+    uq[t] = ka.u_q[(size_t)kk * NC * nq + t];
+    rb[t] = ka.rbar_q[(size_t)kk * NC * nq + t];
+  }
+  for (int t = lane; t < NC * nf; t += tpe) {
+    uf[t] = ka.u_f[(size_t)kk * NC * nf + t];
+    gb[t] = ka.gbar_f[(size_t)kk * NC * nf + t];
+  }
+  for (int t = lane; t < D * NC * nq; t += tpe) fb[t] = 0.0;
+  __syncthreads();
+  // r_q += sum_{n,m} D_m^T (hw_mn .* f_n) - hw_mn .* (D_m f_n)
+  //   =>  fbar_n += hw_mn .* (D_m rbar_q) - D_m^T (hw_mn .* rbar_q)
+  const double *hwl = g.halfWLambda + (size_t)kk * nq * D * D;
+  for (int m = 0; m < D; ++m) {
+    csr_mul<double, NC>(nq, nq, op.D_ptr[m], op.D_idx[m], op.D_val[m], rb, t1, lane, tpe);
+    __syncthreads();
+    for (int n = 0; n < D; ++n) {
+      const double *hw = hwl + nq * (m + D * n);
+      for (int t = lane; t < NC * nq; t += tpe) t2[t] = hw[t % nq] * rb[t];
+      __syncthreads();
+      double *fn_ = fb + (size_t)n * NC * nq;
+      for (int t = lane; t < NC * nq; t += tpe) {
+        const int i = t % nq, e = t / nq;
+        double acc = 0.0;
+        for (int q = op.Dt_ptr[m][i]; q < op.Dt_ptr[m][i + 1]; ++q)
+          acc += op.Dt_val[m][q] * t2[e * nq + op.Dt_idx[m][q]];
+        fn_[t] += hw[i] * t1[t] - acc;
+      }
+      __syncthreads();
+    }
+  }
+  // f_f -= halfN_n .* (R f_n)  =>  fbar_n -= R^T (halfN_n .* gbar)
+  for (int n = 0; n < D; ++n) {
+    for (int t = lane; t < NC * nf; t += tpe) {
+      const int j = t % nf;
+      tf[t] = 0.5 * g.n_f[n + D * (j + (size_t)nf * kk)] * gb[t];
+    }
+    __syncthreads();
+    double *fn_ = fb + (size_t)n * NC * nq;
+    for (int t = lane; t < NC * nq; t += tpe) {
+      const int i = t % nq, e = t / nq;
+      double acc = 0.0;
+      for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * tf[e * nf + op.Rt_idx[q]];
+      fn_[t] -= acc;
+    }
+    __syncthreads();
+  }
+  // f_n = F_n(u_q)  =>  ubar_q = sum_n J_{F_n}^T fbar_n
+  for (int i = lane; i < nq; i += tpe) {
+    double u[NC], Fb[NC][D], ub[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      u[e] = uq[e * nq + i];
+      ub[e] = 0.0;
+#pragma unroll
+      for (int n = 0; n < D; ++n) Fb[e][n] = fb[(n * NC + e) * nq + i];
+    }
+    physical_flux_vjp<D, NC>(ph, u, Fb, ub);
+    if (live)
+#pragma unroll
+      for (int e = 0; e < NC; ++e) ka.ubar_q[((size_t)kk * NC + e) * nq + i] = ub[e];
+  }
+  // interface: own flux w.r.t. the inner state, neighbour's flux w.r.t. its outer state
+  for (int j = lane; j < nf; j += tpe) {
+    const int P = g.mapP[(size_t)kk * nf + j];
+    const int jn = P % nf, kn = P / nf;
+    double ui[NC], uo[NC], n[D], nn[D], gown[NC], gnb[NC], ub[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      ui[e] = uf[e * nf + j];
+      uo[e] = ka.u_f[((size_t)kn * NC + e) * nf + jn];
+      gown[e] = gb[e * nf + j];
+      gnb[e] = ka.gbar_f[((size_t)kn * NC + e) * nf + jn];
+      ub[e] = 0.0;
+    }
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      n[m] = g.n_f[m + D * (j + (size_t)nf * kk)];
+      nn[m] = g.n_f[m + D * (jn + (size_t)nf * kn)];
+    }
+    std_iface_bwd<D, NC>(ph, ui, uo, n, gown, 0, ub);
+    std_iface_bwd<D, NC>(ph, uo, ui, nn, gnb, 1, ub);
+    if (live)
+#pragma unroll
+      for (int e = 0; e < NC; ++e) ka.ubar_f[((size_t)kk * NC + e) * nf + j] = ub[e];
+  }
+}
+
+// Transpose of the conservative two-point flux F(uL, uR) = (F(uL) + F(uR))/2
+// (advection: a (uL + uR)/2), applied to Fb; adds to ubL and ubR.
+template <int D, int NC>
+__device__ __forceinline__ void two_point_cons_vjp(const Physics &ph, const double *uL,
+                                                   const double *uR, double (&Fb)[NC][D],
+                                                   double *ubL, double *ubR) {
+#pragma unroll
+  for (int e = 0; e < NC; ++e)
+#pragma unroll
+    for (int n = 0; n < D; ++n) Fb[e][n] *= 0.5;
+  physical_flux_vjp<D, NC>(ph, uL, Fb, ubL);
+  physical_flux_vjp<D, NC>(ph, uR, Fb, ubR);
+}
+
+// FluxDifferencingForm with the conservative two-point flux (scalar
+// advection, or Euler with ConservativeFlux): transposes of the volume pairs
+// (flux_difference!), the facet-correction pairs (facet_correction!) and
+// the interface flux, with the forward's chunked deterministic two-pass
+// accumulation -> ubar_q, ubar_f.  Each pair buffer entry holds the
+// cotangents of the pair's two states.
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_flux_generic_kernel(KernelArgs ka) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Physics &ph = ka.ph;
+  const DevGeo &g = ka.geo;
+  const Layout &L = ka.layAdjG;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *uq = base + L.off[0], *uf = base + L.off[1], *rb = base + L.off[2], *fb = base + L.off[3],
+         *ubq = base + L.off[4], *ubf = base + L.off[5], *Lam = base + L.off[6], *hnq = base + L.off[7],
+         *buf = base + L.off[8];
+  for (int t = lane; t < NC * nq; t += tpe) {
+    uq[t] = ka.u_q[(size_t)kk * NC * nq + t];
+    rb[t] = ka.rbar_q[(size_t)kk * NC * nq + t];
+    ubq[t] = 0.0;
+  }
+  for (int t = lane; t < NC * nf; t += tpe) uf[t] = ka.u_f[(size_t)kk * NC * nf + t];
+  for (int t = lane; t < nq * D * D; t += tpe) Lam[t] = g.Lambda_q[(size_t)kk * nq * D * D + t];
+  if (op.nfp > 0)
+    for (int t = lane; t < D * nfac * nq; t += tpe) hnq[t] = g.halfnJq[(size_t)kk * D * nfac * nq + t];
+  __syncthreads();
+  // fbar_f = -R rbar_q (cotangent of f_f after the BJf scaling)
+  csr_mul<double, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_val, rb, fb, lane, tpe);
+  __syncthreads();
+  for (int t = lane; t < NC * nf; t += tpe) fb[t] = -fb[t];
+  // interface: own flux w.r.t. the inner state, neighbour's flux w.r.t. its outer state
+  for (int j = lane; j < nf; j += tpe) {
+    const int P = g.mapP[(size_t)kk * nf + j];
+    const int jn = P % nf, kn = P / nf;
+    double ui[NC], uo[NC], n[D], nn[D], gown[NC], gnb[NC], ub[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) {
+      ui[e] = uf[e * nf + j];
+      uo[e] = ka.u_f[((size_t)kn * NC + e) * nf + jn];
+      gown[e] = ka.gbar_f[((size_t)kk * NC + e) * nf + j];
+      gnb[e] = ka.gbar_f[((size_t)kn * NC + e) * nf + jn];
+      ub[e] = 0.0;
+    }
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      n[m] = g.n_f[m + D * (j + (size_t)nf * kk)];
+      nn[m] = g.n_f[m + D * (jn + (size_t)nf * kn)];
+    }
+    std_iface_bwd<D, NC>(ph, ui, uo, n, gown, 0, ub);
+    std_iface_bwd<D, NC>(ph, uo, ui, nn, gnb, 1, ub);
+#pragma unroll
+    for (int e = 0; e < NC; ++e) ubf[e * nf + j] = ub[e];
+  }
+  __syncthreads();
+
+  // volume pairs: diff = sum_m S_m (Lambda_i + Lambda_j)[m, :] . F(u_i, u_j),
+  // r_i -= diff, r_j += diff  =>  diffbar = rbar_j - rbar_i
+  const int CH = ka.pair_chunk_generic;
+  int cur[kMaxNodeSlots];
+#pragma unroll
+  for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+    const int i = lane + sl * tpe;
+    cur[sl] = i < nq ? op.vp_inc_ptr[i] : 0;
+  }
+  for (int c0 = 0; c0 < op.nvp; c0 += CH) {
+    const int c1 = min(op.nvp, c0 + CH);
+    for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+      const int ij = op.vp_ij[pidx];
+      const int i = ij & 0xffff, j = ij >> 16;
+      double G[D];
+#pragma unroll
+      for (int n = 0; n < D; ++n) G[n] = 0.0;
+#pragma unroll
+      for (int m = 0; m < D; ++m) {
+        const double Sm = op.vp_S[pidx * D + m];
+        if (Sm == 0.0) continue;
+#pragma unroll
+        for (int n = 0; n < D; ++n)
+          G[n] = fma(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
+      }
+      double ui[NC], uj[NC], Fb[NC][D];
+      double *bi = buf + (size_t)(pidx - c0) * 2 * NC, *bj = bi + NC;
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        ui[e] = uq[e * nq + i];
+        uj[e] = uq[e * nq + j];
+        const double db = rb[e * nq + j] - rb[e * nq + i];
+#pragma unroll
+        for (int n = 0; n < D; ++n) Fb[e][n] = db * G[n];
+        bi[e] = 0.0;
+        bj[e] = 0.0;
+      }
+      two_point_cons_vjp<D, NC>(ph, ui, uj, Fb, bi, bj);
+    }
+    __syncthreads();
+    // node sums in ascending pair order (inc & 1: the node is the pair's first)
+#pragma unroll
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int i = lane + sl * tpe;
+      if (i >= nq) continue;
+      int q = cur[sl];
+      const int qe = op.vp_inc_ptr[i + 1];
+      for (; q < qe; ++q) {
+        const int inc = op.vp_inc[q];
+        const int pidx = inc >> 1;
+        if (pidx >= c1) break;
+        const double *src = buf + (size_t)(pidx - c0) * 2 * NC + ((inc & 1) ? 0 : NC);
+#pragma unroll
+        for (int e = 0; e < NC; ++e) ubq[e * nq + i] += src[e];
+      }
+      cur[sl] = q;
+    }
+    __syncthreads();
+  }
+
+  // facet-correction pairs: dp = C_ij nJ . F(u_q[i], u_f[j]), r_i -= dp,
+  // f_j -= dp  =>  dpbar = -(rbar_i + fbar_j)
+  if (op.nfp > 0) {
+    const double *hnf = g.halfnJf + (size_t)kk * D * nf;
+#pragma unroll
+    for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+      const int t = lane + sl * tpe;
+      cur[sl] = t < nq ? op.fp_q_ptr[t] : (t < nq + nf ? op.fp_f_ptr[t - nq] : 0);
+    }
+    for (int c0 = 0; c0 < op.nfp; c0 += CH) {
+      const int c1 = min(op.nfp, c0 + CH);
+      for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+        const int ij = op.fp_ij[pidx];
+        const int i = ij & 0xffff, j = ij >> 16;
+        const int f = j / npf;
+        const double Cij = op.fp_C[pidx];
+        double nJ[D], ui[NC], uj[NC], Fb[NC][D];
+#pragma unroll
+        for (int m = 0; m < D; ++m) nJ[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+        double *bi = buf + (size_t)(pidx - c0) * 2 * NC, *bj = bi + NC;
+#pragma unroll
+        for (int e = 0; e < NC; ++e) {
+          ui[e] = uq[e * nq + i];
+          uj[e] = uf[e * nf + j];
+          const double db = -(rb[e * nq + i] + fb[e * nf + j]);
+#pragma unroll
+          for (int m = 0; m < D; ++m) Fb[e][m] = db * nJ[m];
+          bi[e] = 0.0;
+          bj[e] = 0.0;
+        }
+        two_point_cons_vjp<D, NC>(ph, ui, uj, Fb, bi, bj);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
+        const int t = lane + sl * tpe;
+        if (t >= nq + nf) continue;
+        const bool vol = t < nq;
+        const int r = vol ? t : t - nq;
+        const int *lst = vol ? op.fp_q : op.fp_f;
+        const int qe = vol ? op.fp_q_ptr[r + 1] : op.fp_f_ptr[r + 1];
+        double *dst = vol ? ubq + r : ubf + r;
+        const int stride = vol ? nq : nf;
+        int q = cur[sl];
+        for (; q < qe; ++q) {
+          const int pidx = lst[q];
+          if (pidx >= c1) break;
+          const double *src = buf + (size_t)(pidx - c0) * 2 * NC + (vol ? 0 : NC);
+#pragma unroll
+          for (int e = 0; e < NC; ++e) dst[e * stride] += src[e];
+        }
+        cur[sl] = q;
+      }
+      __syncthreads();
+    }
+  }
+  if (live) {
+    for (int t = lane; t < NC * nq; t += tpe) ka.ubar_q[(size_t)kk * NC * nq + t] = ubq[t];
+    for (int t = lane; t < NC * nf; t += tpe) ka.ubar_f[(size_t)kk * NC * nf + t] = ubf[t];
+  }
+}
+
+// u_q = V u, u_f = R u_q (standard_form_first_order.jl:1-14, and
+// flux_differencing_form.jl:253-292 for scalar laws)  =>  mu = V^T (ubar_q + R^T ubar_f)
+template <int D, int NC>
+__global__ void __launch_bounds__(256) adj_nodal_kernel(KernelArgs ka) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Layout &L = ka.layAdjB1;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3],
+         *F = base + L.off[4];
+  for (int t = lane; t < NC * nf; t += tpe) F[t] = ka.ubar_f[(size_t)kk * NC * nf + t];
+  __syncthreads();
+  for (int t = lane; t < NC * nq; t += tpe) {
+    const int i = t % nq, e = t / nq;
+    double acc = 0.0;
+    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * F[e * nf + op.Rt_idx[q]];
+    Y[t] = ka.ubar_q[(size_t)kk * NC * nq + t] + acc;
+  }
+  __syncthreads();
+  vdm_tmul<double, D, NC>(op, Y, X, Z, Wb, lane, tpe);
+  __syncthreads();
+  if (live)
+    for (int t = lane; t < NC * np; t += tpe) ka.mu[(size_t)kk * NC * np + t] = X[t];
 }
 
 // ===========================================================================
@@ -869,6 +1328,36 @@ cudaError_t sse_set_smem_limits_adjoint(const KernelArgs &ka) {
       e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)((size_t)ka.epb * L.team_doubles * sizeof(double)));
   };
+  if (!ka.fd) {
+#define SSE_STD_ADJ_LIMITS(DD, NN)                                  \
+  set((const void *)adj_lift_kernel<DD, NN>, ka.layAdjB1);          \
+  set((const void *)adj_std_flux_kernel<DD, NN>, ka.layAdjS);       \
+  set((const void *)adj_nodal_kernel<DD, NN>, ka.layAdjB1);
+    if (ka.op.d == 2 && ka.op.nc == 1) { SSE_STD_ADJ_LIMITS(2, 1) }
+    else if (ka.op.d == 3 && ka.op.nc == 1) { SSE_STD_ADJ_LIMITS(3, 1) }
+    else if (ka.op.d == 2 && ka.op.nc == 4) { SSE_STD_ADJ_LIMITS(2, 4) }
+    else if (ka.op.d == 3 && ka.op.nc == 5) { SSE_STD_ADJ_LIMITS(3, 5) }
+    else return cudaErrorInvalidValue;
+#undef SSE_STD_ADJ_LIMITS
+    return e;
+  }
+  if (ka.op.nc == 1 || !ka.ph.ec) {
+#define SSE_GEN_ADJ_LIMITS(DD, NN)                                  \
+  set((const void *)adj_lift_kernel<DD, NN>, ka.layAdjB1);          \
+  set((const void *)adj_flux_generic_kernel<DD, NN>, ka.layAdjG);   \
+  set((const void *)adj_nodal_kernel<DD, NN>, ka.layAdjB1);
+    if (ka.op.d == 2 && ka.op.nc == 1) { SSE_GEN_ADJ_LIMITS(2, 1) }
+    else if (ka.op.d == 3 && ka.op.nc == 1) { SSE_GEN_ADJ_LIMITS(3, 1) }
+    else if (ka.op.d == 2 && ka.op.nc == 4) {
+      SSE_GEN_ADJ_LIMITS(2, 4)
+      set((const void *)adj_projection_kernel<2, 4>, ka.layAdjA);
+    } else if (ka.op.d == 3 && ka.op.nc == 5) {
+      SSE_GEN_ADJ_LIMITS(3, 5)
+      set((const void *)adj_projection_kernel<3, 5>, ka.layAdjA);
+    } else return cudaErrorInvalidValue;
+#undef SSE_GEN_ADJ_LIMITS
+    return e;
+  }
   if (ka.op.d == 2 && ka.op.nc == 4) {
     set((const void *)adj_lift_kernel<2, 4>, ka.layAdjB1);
     set((const void *)adj_flux_kernel<2, 4>, ka.layAdjB2);
@@ -926,6 +1415,44 @@ cudaError_t launch_residual_vjp_mixed_kernels(const KernelArgs &ka, cudaStream_t
 cudaError_t launch_residual_vjp_kernels(const KernelArgs &ka, cudaStream_t st) {
   const int grid = (ka.ne + ka.epb - 1) / ka.epb;
   const size_t s1 = (size_t)ka.epb * ka.layAdjB1.team_doubles * sizeof(double);
+  if (!ka.fd) {
+    const size_t ss = (size_t)ka.epb * ka.layAdjS.team_doubles * sizeof(double);
+#define SSE_STD_ADJ_LAUNCH(DD, NN)                                  \
+  adj_lift_kernel<DD, NN><<<grid, ka.tpb, s1, st>>>(ka);            \
+  adj_std_flux_kernel<DD, NN><<<grid, ka.tpb, ss, st>>>(ka);        \
+  adj_nodal_kernel<DD, NN><<<grid, ka.tpb, s1, st>>>(ka);
+    if (ka.op.d == 2 && ka.op.nc == 1) { SSE_STD_ADJ_LAUNCH(2, 1) }
+    else if (ka.op.d == 3 && ka.op.nc == 1) { SSE_STD_ADJ_LAUNCH(3, 1) }
+    else if (ka.op.d == 2 && ka.op.nc == 4) { SSE_STD_ADJ_LAUNCH(2, 4) }
+    else if (ka.op.d == 3 && ka.op.nc == 5) { SSE_STD_ADJ_LAUNCH(3, 5) }
+    else return cudaErrorInvalidValue;
+#undef SSE_STD_ADJ_LAUNCH
+    return cudaGetLastError();
+  }
+  if (ka.op.nc == 1 || !ka.ph.ec) {
+    const size_t sg = (size_t)ka.epb * ka.layAdjG.team_doubles * sizeof(double);
+    const size_t s3 = (size_t)ka.epb * ka.layAdjA.team_doubles * sizeof(double);
+    if (ka.op.d == 2 && ka.op.nc == 1) {
+      adj_lift_kernel<2, 1><<<grid, ka.tpb, s1, st>>>(ka);
+      adj_flux_generic_kernel<2, 1><<<grid, ka.tpb, sg, st>>>(ka);
+      adj_nodal_kernel<2, 1><<<grid, ka.tpb, s1, st>>>(ka);
+    } else if (ka.op.d == 3 && ka.op.nc == 1) {
+      adj_lift_kernel<3, 1><<<grid, ka.tpb, s1, st>>>(ka);
+      adj_flux_generic_kernel<3, 1><<<grid, ka.tpb, sg, st>>>(ka);
+      adj_nodal_kernel<3, 1><<<grid, ka.tpb, s1, st>>>(ka);
+    } else if (ka.op.d == 2 && ka.op.nc == 4) {
+      adj_lift_kernel<2, 4><<<grid, ka.tpb, s1, st>>>(ka);
+      adj_flux_generic_kernel<2, 4><<<grid, ka.tpb, sg, st>>>(ka);
+      adj_projection_kernel<2, 4><<<grid, ka.tpb, s3, st>>>(ka);
+    } else if (ka.op.d == 3 && ka.op.nc == 5) {
+      adj_lift_kernel<3, 5><<<grid, ka.tpb, s1, st>>>(ka);
+      adj_flux_generic_kernel<3, 5><<<grid, ka.tpb, sg, st>>>(ka);
+      adj_projection_kernel<3, 5><<<grid, ka.tpb, s3, st>>>(ka);
+    } else {
+      return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+  }
   const size_t s2 = (size_t)ka.epb * ka.layAdjB2.team_doubles * sizeof(double);
   const size_t s3 = (size_t)ka.epb * ka.layAdjA.team_doubles * sizeof(double);
   if (ka.op.d == 2 && ka.op.nc == 4) {

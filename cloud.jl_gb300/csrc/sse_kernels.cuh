@@ -46,7 +46,10 @@ struct KernelArgs {
   double *ubar_q;    // adjoint of u_q                (nq x nc x ne)
   double *ubar_f;    // adjoint of u_f                (nf x nc x ne, element-major)
   Layout layAdjB1, layAdjB2, layAdjA;
+  Layout layAdjS;                          // StandardForm flux-transpose layout
+  Layout layAdjG;                          // conservative-two-point pair-transpose layout
   int pair_chunk;    // pairs per shared-memory chunk in the pair-adjoint passes
+  int pair_chunk_generic;  // the same for the conservative two-point flux
   int fd_chunk;      // pairs per chunk in the FP64 flux-differencing passes
   int vdm_zsz;       // doubles of the first sum-factorisation scratch (even)
   int fd_chunk_mixed;  // pairs per chunk in the mixed-form FP32 passes

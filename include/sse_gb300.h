@@ -182,9 +182,10 @@ int32_t sse_rk_steps(sse_solver *s, double *u, int32_t n_steps, double dt,
                      int32_t scheme, double *t, int32_t memory);
 
 /* Discrete adjoint of the FP64 residual: mu <- (dR/du)^T lam at the state u
- * (all three N_p x N_c x N_e, host or device).  Covers FluxDifferencingForm
- * with the entropy-conservative two-point flux (Euler) and any of the three
- * interface fluxes; other configurations return SSE_ERR_UNSUPPORTED.  With
+ * (all three N_p x N_c x N_e, host or device).  Covers every configuration
+ * sse_create accepts: StandardForm and FluxDifferencingForm (entropy-
+ * conservative or conservative two-point flux), Euler and linear advection,
+ * any of the three interface fluxes.  With
  * the handle in SSE_MIXED the product is that of the mixed form (FP32
  * transposes of its reduced fluxes and projection arithmetic, ModalTensor
  * bases).  The vector-Jacobian product of semi_discrete_residual!; no
