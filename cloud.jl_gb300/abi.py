@@ -58,7 +58,7 @@ class SseCsc(C.Structure):
 class SseOperators(C.Structure):
     _fields_ = [("vdm_p", C.c_int32), ("vdm_m", C.c_int32 * 3), ("vdm_A", _dp),
                 ("vdm_B", _dp), ("vdm_C", _dp), ("vdm_sigma_in", _ip), ("R", SseCsc),
-                ("D", SseCsc * 3), ("S", SseCsc * 3), ("C", SseCsc)]
+                ("D", SseCsc * 3), ("S", SseCsc * 3), ("C", SseCsc), ("V_dense", _dp)]
 
 
 class SseGeometry(C.Structure):

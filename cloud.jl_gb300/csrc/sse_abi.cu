@@ -61,7 +61,7 @@ struct sse_solver {
   int precision = SSE_FP64;
   std::string last_error;
   // element counts of the device operator arrays (for the FP32 roundings)
-  size_t nA = 0, nB = 0, nC = 0, nnzR = 0, nvpS = 0, nfpC = 0;
+  size_t nA = 0, nB = 0, nC = 0, nnzR = 0, nvpS = 0, nfpC = 0, nVd = 0;
   double volume = 0.0;      // sum of W .* J_q over the mesh
   bool mixed_ready = false; // FP32 copies allocated
   bool ref_ready = false;   // reference state of the mixed form chosen
@@ -224,7 +224,10 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   if ((double)c.n_f * c.n_e > 2.0e9 || (double)c.n_q * c.n_c * c.n_e > 4.0e18)
     return fail(s, SSE_ERR_UNSUPPORTED, "mesh too large for 32-bit facet indices");
   const bool fd = c.form == SSE_FLUX_DIFFERENCING_FORM;
-  const bool has_vdm = ops->vdm_A != nullptr;
+  const bool dense_v = ops->V_dense != nullptr;
+  if (dense_v && (ops->vdm_A || ops->vdm_B || ops->vdm_C))
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "give V either as warped tensor-product factors or dense, not both");
+  const bool has_vdm = ops->vdm_A != nullptr || dense_v;
   if (!has_vdm && c.n_p != c.n_q) return fail(s, SSE_ERR_INVALID_ARGUMENT, "V = I requires n_p == n_q");
   if (c.mass_solver == SSE_WEIGHT_ADJUSTED && !has_vdm)
     return fail(s, SSE_ERR_UNSUPPORTED, "WeightAdjustedSolver requires a modal V");
@@ -254,7 +257,20 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   // ---- warped tensor-product factors (validated before any device work)
   int p1 = 0, M1 = 0, M2 = 0, M3 = 1;
   std::vector<int> sigma, modes, b12, b12_index;
-  if (has_vdm) {
+  if (dense_v) {
+    // the constant mode of a multidimensional orthonormal basis: the column
+    // of V that is the same at every volume node
+    M3 = 0;
+    for (int a = 0; a < c.n_p && s->mode0 < 0; ++a) {
+      const double *col = ops->V_dense + (size_t)c.n_q * a;
+      bool same = std::isfinite(col[0]) && std::fabs(col[0]) > 0.0;
+      for (int i = 1; i < c.n_q && same; ++i)
+        same = std::fabs(col[i] - col[0]) <= 1e-12 * std::fabs(col[0]);
+      if (same) { s->mode0 = a; s->phi0 = col[0]; }
+    }
+    for (size_t t = 0; t < (size_t)c.n_q * c.n_p; ++t)
+      if (!std::isfinite(ops->V_dense[t])) return fail(s, SSE_ERR_INVALID_ARGUMENT, "V_dense is not finite");
+  } else if (has_vdm) {
     p1 = ops->vdm_p + 1;
     M1 = ops->vdm_m[0]; M2 = ops->vdm_m[1]; M3 = c.d == 3 ? ops->vdm_m[2] : 1;
     if (p1 < 1 || p1 > 16 || M1 < 1 || M2 < 1 || M3 < 1 || M1 * M2 * M3 != c.n_q || !ops->vdm_B ||
@@ -311,7 +327,13 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   cudaError_t e;
 
   op.has_vdm = has_vdm;
-  if (has_vdm) {
+  op.dense_v = dense_v;
+  if (dense_v) {
+    op.p1 = 0; op.M1 = 0; op.M2 = 0; op.M3 = 0; op.nb12 = 0;
+    if ((e = upload(s, ops->V_dense, (size_t)c.n_q * c.n_p, &op.Vd)) != cudaSuccess)
+      return cuda_fail(s, e, "upload V_dense");
+    s->nVd = (size_t)c.n_q * c.n_p;
+  } else if (has_vdm) {
     op.p1 = p1; op.M1 = M1; op.M2 = M2; op.M3 = M3;
     op.nb12 = (int)b12.size();
     if ((e = upload(s, ops->vdm_A, (size_t)M1 * p1, &op.A)) != cudaSuccess) return cuda_fail(s, e, "upload A");
@@ -564,6 +586,8 @@ int enable_mixed(sse_solver *s) {
   if (!(c.form == SSE_FLUX_DIFFERENCING_FORM && c.law == SSE_EULER && c.two_point_flux == SSE_EC_FLUX))
     return fail(s, SSE_ERR_UNSUPPORTED,
                 "SSE_MIXED covers FluxDifferencingForm with the entropy-conservative flux (Euler)");
+  if (s->ka.op.has_vdm && s->mode0 < 0)
+    return fail(s, SSE_ERR_UNSUPPORTED, "SSE_MIXED needs a modal basis with a constant basis function");
   if (s->mixed_ready) return SSE_OK;
   KernelArgs &ka = s->ka;
   DevOps &op = ka.op;
@@ -583,7 +607,7 @@ int enable_mixed(sse_solver *s) {
   if ((e = rounded(op.A, s->nA, &op.Af)) || (e = rounded(op.B, s->nB, &op.Bf)) ||
       (e = rounded(op.C, s->nC, &op.Cf)) || (e = rounded(op.R_val, s->nnzR, &op.R_valf)) ||
       (e = rounded(op.Rt_val, s->nnzR, &op.Rt_valf)) || (e = rounded(op.vp_S, s->nvpS, &op.vp_Sf)) ||
-      (e = rounded(op.fp_C, s->nfpC, &op.fp_Cf)))
+      (e = rounded(op.fp_C, s->nfpC, &op.fp_Cf)) || (e = rounded(op.Vd, s->nVd, &op.Vdf)))
     return cuda_fail(s, e, "mixed operators");
   if ((e = rounded(g.BJf, nf * ne, &g.BJff)) || (e = rounded(g.n_f, d * nf * ne, &g.n_ff)) ||
       (e = rounded(g.Lambda_q, nq * d * d * ne, &g.Lambda_qf)) ||

@@ -49,6 +49,11 @@ struct DevOps {
   const int *fp_f_ptr, *fp_f;  // per facet node: incident pair ids
   // FP32 copies of the operator values for the mixed form (rounded from FP64)
   const float *Af, *Bf, *Cf, *R_valf, *Rt_valf, *vp_Sf, *fp_Cf;
+  // dense V (nq x np, column-major) of a multidimensional modal basis:
+  // has_vdm == 1 and dense_v == 1, the warped factors unused
+  int dense_v;
+  const double *Vd;
+  const float *Vdf;
 };
 
 // Operator values of scalar type T (FP64 form: the caller's values; mixed
@@ -62,6 +67,7 @@ template <> struct OpVals<double> {
   __device__ static const double *Rt(const DevOps &o) { return o.Rt_val; }
   __device__ static const double *vpS(const DevOps &o) { return o.vp_S; }
   __device__ static const double *fpC(const DevOps &o) { return o.fp_C; }
+  __device__ static const double *Vd(const DevOps &o) { return o.Vd; }
 };
 template <> struct OpVals<float> {
   __device__ static const float *A(const DevOps &o) { return o.Af; }
@@ -71,6 +77,7 @@ template <> struct OpVals<float> {
   __device__ static const float *Rt(const DevOps &o) { return o.Rt_valf; }
   __device__ static const float *vpS(const DevOps &o) { return o.vp_Sf; }
   __device__ static const float *fpC(const DevOps &o) { return o.fp_Cf; }
+  __device__ static const float *Vd(const DevOps &o) { return o.Vdf; }
 };
 
 __device__ __forceinline__ int modes_index2(const DevOps &op, int b1, int b2) {

@@ -21,6 +21,19 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
     __syncthreads();
     return;
   }
+  if (op.dense_v) {
+    // dense V (multidimensional.jl:1-41): one row of V per output node
+    const T *V = OpVals<T>::Vd(op);
+    const int nq = op.nq, np = op.np;
+    for (int t = lane; t < NC * nq; t += tpe) {
+      const int i = t % nq, e = t / nq;
+      T acc = 0;
+      for (int a = 0; a < np; ++a) acc = fma(V[i + (size_t)nq * a], x[e * np + a], acc);
+      y[t] = acc;
+    }
+    __syncthreads();
+    return;
+  }
   const T *A = OpVals<T>::A(op), *B = OpVals<T>::B(op);
   const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
   if constexpr (D == 2) {
@@ -82,6 +95,20 @@ template <typename T, int D, int NC>
 __device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lane, int tpe) {
   if (!op.has_vdm) {
     for (int t = lane; t < NC * op.nq; t += tpe) x[t] = y[t];
+    __syncthreads();
+    return;
+  }
+  if (op.dense_v) {
+    // V^T with the dense V: one column of V per output mode
+    const T *V = OpVals<T>::Vd(op);
+    const int nq = op.nq, np = op.np;
+    for (int t = lane; t < NC * np; t += tpe) {
+      const int a = t % np, e = t / np;
+      const T *col = V + (size_t)nq * a;
+      T acc = 0;
+      for (int i = 0; i < nq; ++i) acc = fma(col[i], y[e * nq + i], acc);
+      x[t] = acc;
+    }
     __syncthreads();
     return;
   }

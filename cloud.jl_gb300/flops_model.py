@@ -34,6 +34,8 @@ def vdm_flops(ra) -> float:
     """One sum-factorised application of V (or V^T) to one component."""
     if ra.V is None:
         return 0.0
+    if ra.warped is None:
+        return 2.0 * ra.N_q * ra.N_p          # dense V (ModalMulti)
     p1 = ra.p + 1
     if ra.d == 2:
         M1, M2 = ra.n1d

@@ -253,11 +253,114 @@ def _ref_elem(shape: str, N: int, rstq, wq, rstf, wf, nrstJ, num_faces) -> RefEl
     return RefElem(shape, N, rst, VDM, Drst, rstq, wq, Vq, rstf, wf, Vf, nrstJ, num_faces)
 
 
+def _collapsed_quadrature(shape: str, rules: tuple):
+    """``quadrature(::Tri|::Tet, NTuple of line rules)`` (quadrature_rules.jl:
+    131-166): the tensor grid of the 1-D rules (first rule slowest) mapped by
+    the collapsed-coordinate map, with the weights of the rules' Jacobi
+    parameters."""
+    eta = [r.nodes_weights() for r in rules]
+    ab = [(r.a, r.b) for r in rules]
+    if shape == "Tri":
+        g1, g2 = _meshgrid_flat(eta[0][0], eta[1][0])
+        w = np.multiply(*_meshgrid_flat(eta[0][1], eta[1][1]))
+        if ab == [(0, 0), (0, 0)]:
+            w = 0.5 * (1.0 - g2) * w
+        elif ab == [(0, 0), (1, 0)]:
+            w = 0.5 * w
+        else:
+            raise ValueError("Chosen Jacobi weight not supported")
+        return chi_tri(g1, g2), w
+    g1, g2, g3 = _meshgrid_flat(eta[0][0], eta[1][0], eta[2][0])
+    w = np.prod(_meshgrid_flat(eta[0][1], eta[1][1], eta[2][1]), axis=0)
+    if ab == [(0, 0), (0, 0), (0, 0)]:
+        w = 0.125 * (1.0 - g2) * (1.0 - g3) ** 2 * w
+    elif ab == [(0, 0), (0, 0), (1, 0)]:
+        w = 0.125 * (1.0 - g2) * (1.0 - g3) * w
+    else:
+        raise ValueError("Chosen Jacobi weight not supported")
+    return chi_tet(g1, g2, g3), w
+
+
+def _facet_nodes(shape: str, facet_rule):
+    """Facet quadrature nodes, weights and scaled reference normals of the
+    reference element (ref_elem_data.jl:22-27 for the triangle's edges; the
+    tetrahedron's four faces from a triangle rule)."""
+    if shape == "Tri":
+        eta_f, w_f1 = facet_rule.nodes_weights()
+        nf1 = len(eta_f)
+        rf = np.concatenate([eta_f, -eta_f, -np.ones(nf1)])
+        sf = np.concatenate([-np.ones(nf1), eta_f, eta_f])
+        nrJ = np.concatenate([np.zeros(nf1), np.ones(nf1), -np.ones(nf1)])
+        nsJ = np.concatenate([-np.ones(nf1), np.ones(nf1), np.zeros(nf1)])
+        return (rf, sf), np.concatenate([w_f1, w_f1, w_f1]), (nrJ, nsJ), 3
+    (r2, s2), w_2d = _collapsed_quadrature("Tri", facet_rule)
+    ee = np.ones_like(r2)
+    zz = np.zeros_like(r2)
+    rf = np.concatenate([r2, -(ee + r2 + s2), -ee, r2])
+    sf = np.concatenate([-ee, r2, r2, s2])
+    tf = np.concatenate([s2, s2, s2, -ee])
+    nrJ = np.concatenate([zz, ee, -ee, zz])
+    nsJ = np.concatenate([-ee, ee, zz, zz])
+    ntJ = np.concatenate([zz, ee, zz, -ee])
+    return (rf, sf, tf), np.concatenate([w_2d] * 4), (nrJ, nsJ, ntJ), 4
+
+
+def _multidimensional(approx_type: str, shape: str, p: int, mapping_degree: int,
+                      volume_quadrature_rule, facet_quadrature_rule) -> ReferenceApproximation:
+    """``ReferenceApproximation(ModalMulti(p)|NodalMulti(p), Tri()|Tet();
+    mapping_degree, volume_quadrature_rule, facet_quadrature_rule)``
+    (multidimensional.jl:1-76): the orthonormal simplex basis VDM and its
+    gradients at the volume nodes, the projection P = (VDM' W VDM)^-1 VDM' W,
+    D_m = grad_m VDM P, R = Vf P; V = VDM (ModalMulti, dense) or the identity
+    (NodalMulti).  No reference mapping (the metric terms apply directly).
+
+    The reference's default rules (``DefaultQuadrature(2p)``: tabulated
+    Xiao-Gimbutas / Jaskowiec-Sukumar nodes from third-party packages) are
+    not restated here; collapsed tensor-product rules (tuples of Gauss line
+    rules, quadrature_rules.jl:131-166) are, and the triangle's facet rule
+    defaults to the Gauss rule of DefaultQuadrature(2p) on a line (p + 1
+    points)."""
+    d = 2 if shape == "Tri" else 3
+    if volume_quadrature_rule is None:
+        raise ValueError(f"{approx_type}: pass volume_quadrature_rule as a tuple of {d} line rules "
+                         "(the tabulated default rules are not available)")
+    if facet_quadrature_rule is None:
+        if d == 3:
+            raise ValueError(f"{approx_type} on Tet: pass facet_quadrature_rule as a tuple of 2 line rules")
+        facet_quadrature_rule = LGQuadrature(p)
+    (rq, wq) = _collapsed_quadrature(shape, tuple(volume_quadrature_rule))
+    rstf, wf, nrstJ, nfaces = _facet_nodes(shape, facet_quadrature_rule)
+    ref = _ref_elem(shape, mapping_degree, rq, wq, rstf, wf, nrstJ, nfaces)
+    VDM, grads = _simplex_basis(shape, p, *rq)
+    Vf = _simplex_basis(shape, p, *rstf)[0]
+    Pq = np.linalg.solve(VDM.T @ (wq[:, None] * VDM), VDM.T * wq[None, :])
+    D = tuple(G @ Pq for G in grads)
+    R = Vf @ Pq
+    N_q = len(wq)
+    V = VDM if approx_type == "ModalMulti" else None
+    N_p = VDM.shape[1] if V is not None else N_q
+    L_ref = np.zeros((N_q, d, d))
+    for m in range(d):
+        L_ref[:, m, m] = 1.0
+    return ReferenceApproximation(
+        approx_type=approx_type, shape=shape, p=p, d=d, N_p=N_p, N_q=N_q, N_f=R.shape[0],
+        n1d=(), eta_1d=(), D_1d=(), R_L=(), R_R=(), facet_interp={}, D=D, V=V, warped=None,
+        R=R, W=ref.wq.copy(), B=ref.wf.copy(), J_ref=np.ones(N_q), Lambda_ref=L_ref,
+        reference_element=ref, nodes_per_face=R.shape[0] // nfaces)
+
+
 def reference_approximation(approx_type: str, shape: str, p: int,
-                            mapping_degree: int = 1) -> ReferenceApproximation:
+                            mapping_degree: int = 1, volume_quadrature_rule=None,
+                            facet_quadrature_rule=None) -> ReferenceApproximation:
     """``ReferenceApproximation(ModalTensor(p)|NodalTensor(p), Tri()|Tet();
     mapping_degree)`` with the default quadrature rules
-    (tensor_simplex.jl:158-306)."""
+    (tensor_simplex.jl:158-306), or ``ModalMulti(p)|NodalMulti(p)`` with
+    collapsed tensor-product rules (multidimensional.jl:1-76)."""
+    if approx_type in ("ModalMulti", "NodalMulti"):
+        if shape not in ("Tri", "Tet"):
+            raise ValueError(f"unsupported element {shape}")
+        return _multidimensional(approx_type, shape, p, mapping_degree, volume_quadrature_rule,
+                                 facet_quadrature_rule)
     if approx_type not in ("ModalTensor", "NodalTensor"):
         raise ValueError(f"unsupported approximation type {approx_type}")
     if shape == "Tri":

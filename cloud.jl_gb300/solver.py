@@ -269,6 +269,11 @@ class HostArrays:
             ops.vdm_B = abi.dptr(self.vdm_B)
             ops.vdm_C = abi.dptr(self.vdm_C)
             ops.vdm_sigma_in = abi.iptr(self.vdm_sigma)
+        elif ra.V is not None:
+            # ModalMulti: Matrix(V), N_q x N_p column-major
+            self.V_dense = np.ascontiguousarray(ra.V.T)
+            ops.vdm_p = ra.p
+            ops.V_dense = abi.dptr(self.V_dense)
         self.R = abi.CscArrays(ra.R)
         ops.R = self.R.struct()
         self.D = [abi.CscArrays(Dm) for Dm in ra.D]

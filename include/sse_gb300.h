@@ -107,6 +107,10 @@ typedef struct sse_operators {
   /* FluxDifferencingForm (FluxDifferencingOperators.S, C; operators.jl:192-200) */
   sse_csc S[3];              /* N_q x N_q each */
   sse_csc C;                 /* N_q x N_f; nnz = 0 means no facet correction */
+  /* Dense V, N_q x N_p: Matrix(V) of the multidimensional ModalMulti
+   * approximation (OctavianMap(VDM), multidimensional.jl:1-41), with vdm_*
+   * NULL; NULL for the tensor-product and nodal approximations. */
+  const double *V_dense;
 } sse_operators;
 
 typedef struct sse_geometry {

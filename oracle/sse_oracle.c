@@ -87,6 +87,16 @@ static void csc_tmul(const sse_csc *A, const sse_real *x, sse_real *y) {
  * warped_product_2d.jl:31-55, warped_product_3d.jl:47-84 */
 static void vdm_mul(const oracle_t *o, const sse_real *x, sse_real *y) {
   const sse_operators *op = &o->ops;
+  if (op->V_dense) {
+    /* dense V of a multidimensional basis (multidimensional.jl:1-41) */
+    const int nq = o->cfg.n_q, np = o->cfg.n_p;
+    for (int i = 0; i < nq; ++i) {
+      sse_real t = 0.0;
+      for (int a = 0; a < np; ++a) t = fma(op->V_dense[i + (size_t)nq * a], x[a], t);
+      y[i] = t;
+    }
+    return;
+  }
   if (!op->vdm_A) { memcpy(y, x, sizeof(sse_real) * o->cfg.n_q); return; }
   const int p1 = op->vdm_p + 1;
   const int M1 = op->vdm_m[0], M2 = op->vdm_m[1], M3 = op->vdm_m[2];
@@ -140,6 +150,15 @@ static void vdm_mul(const oracle_t *o, const sse_real *x, sse_real *y) {
 /* V^T x; warped_product_2d.jl:61-89, warped_product_3d.jl:94-136 */
 static void vdm_tmul(const oracle_t *o, const sse_real *x, sse_real *y) {
   const sse_operators *op = &o->ops;
+  if (op->V_dense) {
+    const int nq = o->cfg.n_q, np = o->cfg.n_p;
+    for (int a = 0; a < np; ++a) {
+      sse_real t = 0.0;
+      for (int i = 0; i < nq; ++i) t = fma(op->V_dense[i + (size_t)nq * a], x[i], t);
+      y[a] = t;
+    }
+    return;
+  }
   if (!op->vdm_A) { memcpy(y, x, sizeof(sse_real) * o->cfg.n_q); return; }
   const int p1 = op->vdm_p + 1;
   const int M1 = op->vdm_m[0], M2 = op->vdm_m[1], M3 = op->vdm_m[2];
@@ -408,7 +427,7 @@ static void nodal_values_elem(oracle_t *o, const sse_real *u, int k, scratch_t *
     return;
   }
   sse_real ui[MAXC], wi[MAXC];
-  if (!o->ops.vdm_A) {
+  if (!o->ops.vdm_A && !o->ops.V_dense) {
     /* nodal entropy projection (flux_differencing_form.jl:190-211) */
     for (int e = 0; e < nc; ++e) memcpy(uq + nq * e, uk + np * e, sizeof(sse_real) * nq);
     sse_real *wq = s->a, *wf = s->b;

@@ -25,8 +25,51 @@ def _disc(approx, shape, p, cells, L, warp, metrics):
     return M.spatial_discretization(mesh, ra, metrics=metrics)
 
 
+def _disc_multi(approx, shape, p, cells, L, warp, metrics):
+    """ModalMulti / NodalMulti with collapsed Gauss rules (Tri: LG x LG;
+    Tet: LG x LG x GJ(1,0), faces LG x GJ(1,0))."""
+    if shape == "Tri":
+        vol, fac = (R.LGQuadrature(p), R.LGQuadrature(p)), R.LGQuadrature(p)
+    else:
+        vol = (R.LGQuadrature(p), R.LGQuadrature(p), R.GaussRule(p, 1, 0))
+        fac = (R.LGQuadrature(p), R.GaussRule(p, 1, 0))
+    ra = R.reference_approximation(approx, shape, p, mapping_degree=p, volume_quadrature_rule=vol,
+                                   facet_quadrature_rule=fac)
+    d = 2 if shape == "Tri" else 3
+    mesh = M.uniform_periodic_mesh(ra, ((0.0, L),) * d, (cells,) * d)
+    mesh = M.warp_mesh(mesh, ra, "Chan", warp, (L,) * d)
+    return M.spatial_discretization(mesh, ra, metrics=metrics)
+
+
 def make(name):
     seed = SEED + sum(map(ord, name))
+    if name.startswith("multi_"):
+        # multidimensional (dense-operator) approximations
+        approx = "NodalMulti" if "nodal" in name else "ModalMulti"
+        if "_adv_" in name:
+            sd = _disc_multi(approx, "Tri", 4, 4, 1.0, 0.1, "Exact")
+            law = S.LinearAdvectionEquation((1.0, 1.0))
+            ic = S.InitialDataSine(1.0, (2 * math.pi, 2 * math.pi))
+            form = S.StandardForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux())
+            if "fd" in name:
+                form = S.FluxDifferencingForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux())
+        elif "_tri" in name:
+            vort = setups.vortex_tri(cells=2, p=2)
+            sd = _disc_multi(approx, "Tri", 3, 8, 10.0, 0.1, "ChanWilcox")
+            law, ic = vort.law, vort.initial_data
+            nflux = S.EntropyConservativeNumericalFlux() if "ec" in name else S.LaxFriedrichsNumericalFlux()
+            form = S.FluxDifferencingForm(inviscid_numerical_flux=nflux)
+            if "std" in name:
+                form = S.StandardForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux())
+        else:
+            tgv = setups.tgv_tet(cells=1, p=2)
+            sd = _disc_multi(approx, "Tet", 3, 2, 2 * math.pi, 0.05, "ChanWilcox")
+            law, ic = tgv.law, tgv.initial_data
+            nflux = S.EntropyConservativeNumericalFlux() if "ec" in name else S.LaxFriedrichsNumericalFlux()
+            form = S.FluxDifferencingForm(inviscid_numerical_flux=nflux)
+        host = S.HostArrays(law, sd, form)
+        u0 = S.initialize(ic, sd)
+        return host, setups.perturbed(u0, seed, 1.0e-3)
     if name.startswith("adv_tri"):
         approx = "NodalTensor" if "nodal" in name else "ModalTensor"
         sd = _disc(approx, "Tri", 4, 4, 1.0, 0.1, "Exact")
@@ -75,3 +118,6 @@ NAMES = ["adv_tri_modal", "adv_tri_nodal", "adv_tri_central", "adv_tri_fd", "adv
          "adv_tet_fd", "vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec",
          "vortex_tri_cons2pt", "euler_tri_std", "tgv_tet_modal", "tgv_tet_ec", "tgv_tet_nodal",
          "tgv_tet_p5", "tgv_tet_p6"]
+# multidimensional (dense V, D, R) approximations: parity, adjoint and mixed cases
+MULTI_NAMES = ["multi_adv_tri", "multi_adv_tri_nodal", "multi_adv_tri_fd", "multi_tri",
+               "multi_tri_nodal", "multi_tri_std", "multi_tri_ec", "multi_tet", "multi_tet_ec"]

@@ -18,7 +18,10 @@ ADJ_NAMES = ["vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec", "tgv_tet_m
              # StandardForm: linear advection (LF / central, modal / nodal, Tri / Tet) and Euler
              "adv_tri_modal", "adv_tri_nodal", "adv_tri_central", "adv_tet_modal", "euler_tri_std",
              # FluxDifferencingForm with the conservative two-point flux
-             "adv_tri_fd", "adv_tet_fd", "vortex_tri_cons2pt"]
+             "adv_tri_fd", "adv_tet_fd", "vortex_tri_cons2pt",
+             # multidimensional (dense V, D, R) approximations
+             "multi_adv_tri", "multi_adv_tri_fd", "multi_tri", "multi_tri_nodal", "multi_tri_std",
+             "multi_tet"]
 
 
 def _dot_rel(a, b, c, d):
@@ -162,7 +165,8 @@ def test_rk_adjoint_checkpoint_interval_invariance(gpu_lib, pkg):
         assert np.array_equal(g, grads[0])
 
 
-@pytest.mark.parametrize("name", ["vortex_tri_modal", "tgv_tet_modal", "tgv_tet_ec", "tgv_tet_p5"])
+@pytest.mark.parametrize("name", ["vortex_tri_modal", "tgv_tet_modal", "tgv_tet_ec", "tgv_tet_p5",
+                                  "multi_tet"])
 def test_mixed_vjp_against_fp64(name, gpu_lib, pkg):
     """The mixed-form VJP (FP32 transposes of the reduced fluxes and of the
     FP32 projection) against the FP64 VJP at the same state, and the

@@ -25,7 +25,8 @@ def _pair(pkg, name):
 
 
 @pytest.mark.parametrize("name", ["vortex_tri_modal", "vortex_tri_nodal", "tgv_tet_modal",
-                                  "tgv_tet_ec", "tgv_tet_p5"])
+                                  "tgv_tet_ec", "tgv_tet_p5", "multi_tri", "multi_tri_nodal",
+                                  "multi_tet"])
 def test_mixed_residual_close_to_fp64(gpu_lib, pkg, name):
     host, u, fp64, mixed = _pair(pkg, name)
     want = fp64.residual(u)
@@ -35,7 +36,8 @@ def test_mixed_residual_close_to_fp64(gpu_lib, pkg, name):
     assert err <= 1e-4
 
 
-@pytest.mark.parametrize("name,steps,dt", [("vortex_tri_modal", 20, 2e-3), ("tgv_tet_modal", 20, 1e-3)])
+@pytest.mark.parametrize("name,steps,dt", [("vortex_tri_modal", 20, 2e-3), ("tgv_tet_modal", 20, 1e-3),
+                                           ("multi_tet", 20, 1e-3)])
 def test_mixed_trajectory_within_1e6(gpu_lib, pkg, name, steps, dt):
     host, u, fp64, mixed = _pair(pkg, name)
     a = u.copy()
@@ -47,7 +49,7 @@ def test_mixed_trajectory_within_1e6(gpu_lib, pkg, name, steps, dt):
     assert err <= 1e-6
 
 
-@pytest.mark.parametrize("name", ["vortex_tri_ec", "tgv_tet_ec"])
+@pytest.mark.parametrize("name", ["vortex_tri_ec", "tgv_tet_ec", "multi_tet_ec"])
 def test_mixed_conservation_and_entropy(gpu_lib, pkg, name):
     host, u, fp64, mixed = _pair(pkg, name)
     du = mixed.residual(u)

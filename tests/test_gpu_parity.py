@@ -41,7 +41,7 @@ def built(gpu_lib):
     return gpu_lib
 
 
-@pytest.mark.parametrize("name", cases.NAMES)
+@pytest.mark.parametrize("name", cases.NAMES + cases.MULTI_NAMES)
 def test_residual_matches_oracle(built, pkg, name):
     host, u = cases.make(name)
     gpu = pkg.GB300Solver(host)

@@ -9,7 +9,7 @@ import cases
 from oracle.oracle import Oracle
 
 
-@pytest.mark.parametrize("name", cases.NAMES)
+@pytest.mark.parametrize("name", cases.NAMES + cases.MULTI_NAMES)
 def test_conservation(name):
     host, u = cases.make(name)
     o = Oracle(host)
@@ -19,7 +19,7 @@ def test_conservation(name):
     assert np.abs(cons).max() < 1e-12 * scale
 
 
-@pytest.mark.parametrize("name", ["vortex_tri_ec", "tgv_tet_ec"])
+@pytest.mark.parametrize("name", ["vortex_tri_ec", "tgv_tet_ec", "multi_tri_ec", "multi_tet_ec"])
 def test_entropy_conservation(name):
     host, u = cases.make(name)
     o = Oracle(host)
@@ -29,7 +29,8 @@ def test_entropy_conservation(name):
     assert abs(s) < 1e-12 * scale
 
 
-@pytest.mark.parametrize("name", ["vortex_tri_modal", "tgv_tet_modal", "tgv_tet_nodal"])
+@pytest.mark.parametrize("name", ["vortex_tri_modal", "tgv_tet_modal", "tgv_tet_nodal", "multi_tri",
+                                  "multi_tri_nodal", "multi_tet"])
 def test_free_stream_preservation(name):
     host, _ = cases.make(name)
     S = cases.S
