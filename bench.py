@@ -67,6 +67,15 @@ WORKLOADS = {
         "metrics": "ChanWilcox (conservative curl)",
         "time_integrator": "CarpenterKennedy2N54 (5 stages per step)",
         "l2_policy": "working set ~40 MB fits in L2; reported as is"},
+    "tgv_multi_p3": {
+        "workload": "3-D Euler Taylor-Green vortex, Mach 0.1, periodic [0,2pi]^3",
+        "mesh": "16^3 hexahedra x 6 = 24576 curved tetrahedra (Chan warp 0.05)",
+        "approximation": "ModalMulti(3) on Tet (dense V, D, R; collapsed LG x LG x GJ(1,0) rules), "
+                         "N_p=20, N_q=64, N_f=64",
+        "form": "FluxDifferencingForm, entropy-conservative (Ranocha) volume flux + Lax-Friedrichs",
+        "metrics": "ChanWilcox (conservative curl)",
+        "time_integrator": "CarpenterKennedy2N54 (5 stages per step)",
+        "l2_policy": "inputs larger than L2: metric terms and states ~0.5 GB read per stage"},
     "tgv_p5": {
         "workload": "3-D Euler Taylor-Green vortex, Mach 0.1, periodic [0,2pi]^3",
         "mesh": "24^3 hexahedra x 6 = 82944 curved tetrahedra (Chan warp 0.05)",
@@ -163,6 +172,8 @@ def build_problem(workload: str, cells: int | None, p: int | None = None):
         pb = s.tgv_tet(cells=cells or 16, p=p or 4, lf=True)
     elif workload == "tgv_p5":
         pb = s.tgv_tet(cells=cells or 24, p=p or 5, lf=True)
+    elif workload == "tgv_multi_p3":
+        pb = s.tgv_tet(cells=cells or 16, p=p or 3, approx="ModalMulti", lf=True)
     elif workload == "vortex_tri":
         pb = s.vortex_tri(cells=cells or 64, p=p or 4)
     elif workload == "advection_tri":

@@ -43,8 +43,23 @@ class Problem:
         return S.HostArrays(self.law, self.sd, self.form)
 
 
+def multi_rules(shape: str, p: int):
+    """Collapsed Gauss rules for ModalMulti / NodalMulti (the tabulated
+    default rules are not restated): Tri LG(p) x LG(p) with LG(p) edges; Tet
+    LG(p) x LG(p) x GJ(1,0)(p) with LG(p) x GJ(1,0)(p) faces."""
+    if shape == "Tri":
+        return (R.LGQuadrature(p), R.LGQuadrature(p)), R.LGQuadrature(p)
+    return ((R.LGQuadrature(p), R.LGQuadrature(p), R.GaussRule(p, 1, 0)),
+            (R.LGQuadrature(p), R.GaussRule(p, 1, 0)))
+
+
 def _disc(approx, shape, p, limits, cells, warp_kind, warp_factor, metrics):
-    ra = R.reference_approximation(approx, shape, p, mapping_degree=p)
+    if approx in ("ModalMulti", "NodalMulti"):
+        vol, fac = multi_rules(shape, p)
+        ra = R.reference_approximation(approx, shape, p, mapping_degree=p,
+                                       volume_quadrature_rule=vol, facet_quadrature_rule=fac)
+    else:
+        ra = R.reference_approximation(approx, shape, p, mapping_degree=p)
     mesh = M.uniform_periodic_mesh(ra, limits, cells)
     L = tuple(hi - lo for lo, hi in limits)
     if warp_factor:

@@ -26,19 +26,9 @@ def _disc(approx, shape, p, cells, L, warp, metrics):
 
 
 def _disc_multi(approx, shape, p, cells, L, warp, metrics):
-    """ModalMulti / NodalMulti with collapsed Gauss rules (Tri: LG x LG;
-    Tet: LG x LG x GJ(1,0), faces LG x GJ(1,0))."""
-    if shape == "Tri":
-        vol, fac = (R.LGQuadrature(p), R.LGQuadrature(p)), R.LGQuadrature(p)
-    else:
-        vol = (R.LGQuadrature(p), R.LGQuadrature(p), R.GaussRule(p, 1, 0))
-        fac = (R.LGQuadrature(p), R.GaussRule(p, 1, 0))
-    ra = R.reference_approximation(approx, shape, p, mapping_degree=p, volume_quadrature_rule=vol,
-                                   facet_quadrature_rule=fac)
+    """ModalMulti / NodalMulti with the collapsed Gauss rules of setups.multi_rules."""
     d = 2 if shape == "Tri" else 3
-    mesh = M.uniform_periodic_mesh(ra, ((0.0, L),) * d, (cells,) * d)
-    mesh = M.warp_mesh(mesh, ra, "Chan", warp, (L,) * d)
-    return M.spatial_discretization(mesh, ra, metrics=metrics)
+    return setups._disc(approx, shape, p, ((0.0, L),) * d, (cells,) * d, "Chan", warp, metrics)
 
 
 def make(name):
