@@ -378,12 +378,8 @@ __global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
   }
   __syncthreads();
   // wbar_q += R^T wbar_f   (into Y)
-  for (int t = lane; t < NC * nq; t += tpe) {
-    const int i = t % nq, e = t / nq;
-    double acc = 0.0;
-    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * Bf[e * nf + op.Rt_idx[q]];
-    Y[t] = op.has_vdm ? Bq[t] + acc : acc;
-  }
+  rt_apply<double, NC>(op, op.Rt_val, Bf, lane, tpe,
+                       [&](int t, double v) { Y[t] = op.has_vdm ? Bq[t] + v : v; });
   __syncthreads();
   if (op.has_vdm) {
     // w_q = V M V^T (WJ c2e(u_q0))  =>  wbar_c2e = WJ .* V M V^T wbar_q
@@ -582,12 +578,7 @@ __global__ void __launch_bounds__(256) adj_std_flux_kernel(KernelArgs ka) {
     }
     __syncthreads();
     double *fn_ = fb + (size_t)n * NC * nq;
-    for (int t = lane; t < NC * nq; t += tpe) {
-      const int i = t % nq, e = t / nq;
-      double acc = 0.0;
-      for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * tf[e * nf + op.Rt_idx[q]];
-      fn_[t] -= acc;
-    }
+    rt_apply<double, NC>(op, op.Rt_val, tf, lane, tpe, [&](int t, double v) { fn_[t] -= v; });
     __syncthreads();
   }
   // f_n = F_n(u_q)  =>  ubar_q = sum_n J_{F_n}^T fbar_n
@@ -847,12 +838,8 @@ __global__ void __launch_bounds__(256) adj_nodal_kernel(KernelArgs ka) {
          *F = base + L.off[4];
   for (int t = lane; t < NC * nf; t += tpe) F[t] = ka.ubar_f[(size_t)kk * NC * nf + t];
   __syncthreads();
-  for (int t = lane; t < NC * nq; t += tpe) {
-    const int i = t % nq, e = t / nq;
-    double acc = 0.0;
-    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * F[e * nf + op.Rt_idx[q]];
-    Y[t] = ka.ubar_q[(size_t)kk * NC * nq + t] + acc;
-  }
+  rt_apply<double, NC>(op, op.Rt_val, F, lane, tpe,
+                       [&](int t, double v) { Y[t] = ka.ubar_q[(size_t)kk * NC * nq + t] + v; });
   __syncthreads();
   vdm_tmul<double, D, NC>(op, Y, X, Z, Wb, lane, tpe);
   __syncthreads();
@@ -1231,12 +1218,7 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   }
   __syncthreads();
   // wbar_q += R^T wbar_f
-  for (int t = lane; t < NC * nq; t += tpe) {
-    const int i = t % nq, e = t / nq;
-    float acc = 0.f;
-    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc = fmaf(op.Rt_valf[q], BF[e * nf + op.Rt_idx[q]], acc);
-    XQ[t] = S1[t] + acc;
-  }
+  rt_apply<float, NC>(op, op.Rt_valf, BF, lane, tpe, [&](int t, float v) { XQ[t] = S1[t] + v; });
   __syncthreads();
   // projection transpose (V M V^T is symmetric): the same operators
   vdm_tmul<float, D, NC>(op, XQ, T1, Zf, Wf, lane, tpe);

@@ -549,12 +549,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
   }
 
   // r_q -= R^T f_f
-  for (int t = lane; t < NC * nq; t += tpe) {
-    int i = t % nq, e = t / nq;
-    double acc = 0.0;
-    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * ff[e * nf + op.Rt_idx[q]];
-    rq[t] -= acc;
-  }
+  rt_apply<double, NC>(op, op.Rt_val, ff, lane, tpe, [&](int t, double v) { rq[t] -= v; });
   __syncthreads();
 
   // dudt = V^T r_q ; mass solve  (the pair buffer is free now: it holds the
@@ -678,12 +673,7 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
   // f_f .*= BJf ; r_q -= R^T f_f
   for (int t = lane; t < NC * nf; t += tpe) ff[t] *= ka.geo.BJf[(size_t)kk * nf + t % nf];
   __syncthreads();
-  for (int t = lane; t < NC * nq; t += tpe) {
-    int i = t % nq, e = t / nq;
-    double acc = 0.0;
-    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc += op.Rt_val[q] * ff[e * nf + op.Rt_idx[q]];
-    rq[t] -= acc;
-  }
+  rt_apply<double, NC>(op, op.Rt_val, ff, lane, tpe, [&](int t, double v) { rq[t] -= v; });
   __syncthreads();
   double *Xm = tmp, *Yq = tmp2;
   vdm_tmul<double, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
@@ -940,12 +930,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
 
   // r_q -= R^T f_f
   const float *Rt = OpVals<float>::Rt(op);
-  for (int t = lane; t < NC * nq; t += tpe) {
-    int i = t % nq, e = t / nq;
-    float acc = 0.f;
-    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) acc = fmaf(Rt[q], ff[e * nf + op.Rt_idx[q]], acc);
-    rq[t] -= acc;
-  }
+  rt_apply<float, NC>(op, Rt, ff, lane, tpe, [&](int t, float v) { rq[t] -= v; });
   __syncthreads();
 
   // the pair buffer holds the modal / nodal buffers and the scratch now

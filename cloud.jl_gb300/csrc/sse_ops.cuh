@@ -13,23 +13,34 @@ namespace sse {
 // scalar type T of the form (double: FP64 form; float: mixed form)
 // ---------------------------------------------------------------------------
 
+// Each operator below gives one thread one output node (or mode) for all NC
+// components at once: the operator entry and the index arithmetic are
+// loaded / computed once and feed NC independent FMA chains.  The summation
+// order of every output is that of the single-component loop.
+
 // y (NC x nq) = V x (NC x np); warped_product_2d.jl:31-55 / _3d.jl:47-84
 template <typename T, int D, int NC>
 __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane, int tpe) {
+  const int np = op.np, nq = op.nq;
   if (!op.has_vdm) {
-    for (int t = lane; t < NC * op.nq; t += tpe) y[t] = x[t];
+    for (int t = lane; t < NC * nq; t += tpe) y[t] = x[t];
     __syncthreads();
     return;
   }
   if (op.dense_v) {
     // dense V (multidimensional.jl:1-41): one row of V per output node
     const T *V = OpVals<T>::Vd(op);
-    const int nq = op.nq, np = op.np;
-    for (int t = lane; t < NC * nq; t += tpe) {
-      const int i = t % nq, e = t / nq;
-      T acc = 0;
-      for (int a = 0; a < np; ++a) acc = fma(V[i + (size_t)nq * a], x[e * np + a], acc);
-      y[t] = acc;
+    for (int i = lane; i < nq; i += tpe) {
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int a = 0; a < np; ++a) {
+        const T v = V[i + (size_t)nq * a];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(v, x[e * np + a], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) y[e * nq + i] = acc[e];
     }
     __syncthreads();
     return;
@@ -38,53 +49,81 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
   const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
   if constexpr (D == 2) {
     // Z[e][b1][a2] = sum_b2 B[a2,b1,b2] x[sigma(b1,b2)]
-    for (int t = lane; t < NC * p1 * M2; t += tpe) {
-      int a2 = t % M2, r = t / M2, b1 = r % p1, e = r / p1;
-      T acc = 0;
+    for (int s = lane; s < p1 * M2; s += tpe) {
+      const int a2 = s % M2, b1 = s / M2;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
       for (int b2 = 0; b2 < p1 - b1; ++b2) {
-        int l = modes_index2(op, b1, b2);
-        acc = fma(B[a2 + M2 * (b1 + p1 * b2)], x[e * op.np + l], acc);
+        const int l = modes_index2(op, b1, b2);
+        const T bv = B[a2 + M2 * (b1 + p1 * b2)];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(bv, x[e * np + l], acc[e]);
       }
-      Z[(e * p1 + b1) * M2 + a2] = acc;
+#pragma unroll
+      for (int e = 0; e < NC; ++e) Z[(e * p1 + b1) * M2 + a2] = acc[e];
     }
     __syncthreads();
-    for (int t = lane; t < NC * M1 * M2; t += tpe) {
-      int a2 = t % M2, r = t / M2, a1 = r % M1, e = r / M1;
-      T acc = 0;
-      for (int b1 = 0; b1 < p1; ++b1) acc = fma(A[a1 + M1 * b1], Z[(e * p1 + b1) * M2 + a2], acc);
-      y[e * op.nq + M2 * a1 + a2] = acc;
+    for (int s = lane; s < M1 * M2; s += tpe) {
+      const int a2 = s % M2, a1 = s / M2;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int b1 = 0; b1 < p1; ++b1) {
+        const T av = A[a1 + M1 * b1];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(av, Z[(e * p1 + b1) * M2 + a2], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) y[e * nq + M2 * a1 + a2] = acc[e];
     }
     __syncthreads();
   } else {
     const T *C = OpVals<T>::C(op);
     const int M3 = op.M3, nb12 = op.nb12;
-    for (int t = lane; t < NC * nb12 * M3; t += tpe) {
-      int a3 = t % M3, r = t / M3, q = r % nb12, e = r / nb12;
-      int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
-      T acc = 0;
+    for (int s = lane; s < nb12 * M3; s += tpe) {
+      const int a3 = s % M3, q = s / M3;
+      const int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
       for (int b3 = 0; b3 < p1 - b1 - b2; ++b3) {
-        int l = modes_index3(op, b1, b2, b3);
-        acc = fma(C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], x[e * op.np + l], acc);
+        const int l = modes_index3(op, b1, b2, b3);
+        const T cv = C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(cv, x[e * np + l], acc[e]);
       }
-      Z[(e * nb12 + q) * M3 + a3] = acc;
+#pragma unroll
+      for (int e = 0; e < NC; ++e) Z[(e * nb12 + q) * M3 + a3] = acc[e];
     }
     __syncthreads();
-    for (int t = lane; t < NC * p1 * M2 * M3; t += tpe) {
-      int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, b1 = r2 % p1, e = r2 / p1;
-      T acc = 0;
+    for (int s = lane; s < p1 * M2 * M3; s += tpe) {
+      const int a3 = s % M3, r = s / M3, a2 = r % M2, b1 = r / M2;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
       for (int b2 = 0; b2 < p1 - b1; ++b2) {
-        int q = op.b12_index[b1 + p1 * b2];
-        acc = fma(B[a2 + M2 * (b1 + p1 * b2)], Z[(e * nb12 + q) * M3 + a3], acc);
+        const int q = op.b12_index[b1 + p1 * b2];
+        const T bv = B[a2 + M2 * (b1 + p1 * b2)];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(bv, Z[(e * nb12 + q) * M3 + a3], acc[e]);
       }
-      W[((e * p1 + b1) * M2 + a2) * M3 + a3] = acc;
+#pragma unroll
+      for (int e = 0; e < NC; ++e) W[((e * p1 + b1) * M2 + a2) * M3 + a3] = acc[e];
     }
     __syncthreads();
-    for (int t = lane; t < NC * M1 * M2 * M3; t += tpe) {
-      int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, a1 = r2 % M1, e = r2 / M1;
-      T acc = 0;
-      for (int b1 = 0; b1 < p1; ++b1)
-        acc = fma(A[a1 + M1 * b1], W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc);
-      y[e * op.nq + (M2 * a1 + a2) * M3 + a3] = acc;
+    for (int s = lane; s < M1 * M2 * M3; s += tpe) {
+      const int a3 = s % M3, r = s / M3, a2 = r % M2, a1 = r / M2;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int b1 = 0; b1 < p1; ++b1) {
+        const T av = A[a1 + M1 * b1];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(av, W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) y[e * nq + (M2 * a1 + a2) * M3 + a3] = acc[e];
     }
     __syncthreads();
   }
@@ -93,21 +132,27 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
 // x (NC x np) = V^T y (NC x nq); warped_product_2d.jl:61-89 / _3d.jl:94-136
 template <typename T, int D, int NC>
 __device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lane, int tpe) {
+  const int np = op.np, nq = op.nq;
   if (!op.has_vdm) {
-    for (int t = lane; t < NC * op.nq; t += tpe) x[t] = y[t];
+    for (int t = lane; t < NC * nq; t += tpe) x[t] = y[t];
     __syncthreads();
     return;
   }
   if (op.dense_v) {
     // V^T with the dense V: one column of V per output mode
     const T *V = OpVals<T>::Vd(op);
-    const int nq = op.nq, np = op.np;
-    for (int t = lane; t < NC * np; t += tpe) {
-      const int a = t % np, e = t / np;
+    for (int a = lane; a < np; a += tpe) {
       const T *col = V + (size_t)nq * a;
-      T acc = 0;
-      for (int i = 0; i < nq; ++i) acc = fma(col[i], y[e * nq + i], acc);
-      x[t] = acc;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int i = 0; i < nq; ++i) {
+        const T v = col[i];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(v, y[e * nq + i], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) x[e * np + a] = acc[e];
     }
     __syncthreads();
     return;
@@ -115,49 +160,79 @@ __device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lan
   const T *A = OpVals<T>::A(op), *B = OpVals<T>::B(op);
   const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
   if constexpr (D == 2) {
-    for (int t = lane; t < NC * p1 * M2; t += tpe) {
-      int a2 = t % M2, r = t / M2, b1 = r % p1, e = r / p1;
-      T acc = 0;
-      for (int a1 = 0; a1 < M1; ++a1) acc = fma(A[a1 + M1 * b1], y[e * op.nq + M2 * a1 + a2], acc);
-      Z[(e * p1 + b1) * M2 + a2] = acc;
+    for (int s = lane; s < p1 * M2; s += tpe) {
+      const int a2 = s % M2, b1 = s / M2;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int a1 = 0; a1 < M1; ++a1) {
+        const T av = A[a1 + M1 * b1];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(av, y[e * nq + M2 * a1 + a2], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) Z[(e * p1 + b1) * M2 + a2] = acc[e];
     }
     __syncthreads();
-    for (int t = lane; t < NC * op.np; t += tpe) {
-      int l = t % op.np, e = t / op.np;
-      int b1 = op.modes[l] & 0xff, b2 = (op.modes[l] >> 8) & 0xff;
-      T acc = 0;
-      for (int a2 = 0; a2 < M2; ++a2) acc = fma(B[a2 + M2 * (b1 + p1 * b2)], Z[(e * p1 + b1) * M2 + a2], acc);
-      x[e * op.np + l] = acc;
+    for (int l = lane; l < np; l += tpe) {
+      const int b1 = op.modes[l] & 0xff, b2 = (op.modes[l] >> 8) & 0xff;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int a2 = 0; a2 < M2; ++a2) {
+        const T bv = B[a2 + M2 * (b1 + p1 * b2)];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(bv, Z[(e * p1 + b1) * M2 + a2], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) x[e * np + l] = acc[e];
     }
     __syncthreads();
   } else {
     const T *C = OpVals<T>::C(op);
     const int M3 = op.M3, nb12 = op.nb12;
-    for (int t = lane; t < NC * p1 * M2 * M3; t += tpe) {
-      int a3 = t % M3, r = t / M3, a2 = r % M2, r2 = r / M2, b1 = r2 % p1, e = r2 / p1;
-      T acc = 0;
-      for (int a1 = 0; a1 < M1; ++a1)
-        acc = fma(A[a1 + M1 * b1], y[e * op.nq + (M2 * a1 + a2) * M3 + a3], acc);
-      W[((e * p1 + b1) * M2 + a2) * M3 + a3] = acc;
+    for (int s = lane; s < p1 * M2 * M3; s += tpe) {
+      const int a3 = s % M3, r = s / M3, a2 = r % M2, b1 = r / M2;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int a1 = 0; a1 < M1; ++a1) {
+        const T av = A[a1 + M1 * b1];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(av, y[e * nq + (M2 * a1 + a2) * M3 + a3], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) W[((e * p1 + b1) * M2 + a2) * M3 + a3] = acc[e];
     }
     __syncthreads();
-    for (int t = lane; t < NC * nb12 * M3; t += tpe) {
-      int a3 = t % M3, r = t / M3, q = r % nb12, e = r / nb12;
-      int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
-      T acc = 0;
-      for (int a2 = 0; a2 < M2; ++a2)
-        acc = fma(B[a2 + M2 * (b1 + p1 * b2)], W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc);
-      Z[(e * nb12 + q) * M3 + a3] = acc;
+    for (int s = lane; s < nb12 * M3; s += tpe) {
+      const int a3 = s % M3, q = s / M3;
+      const int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int a2 = 0; a2 < M2; ++a2) {
+        const T bv = B[a2 + M2 * (b1 + p1 * b2)];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(bv, W[((e * p1 + b1) * M2 + a2) * M3 + a3], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) Z[(e * nb12 + q) * M3 + a3] = acc[e];
     }
     __syncthreads();
-    for (int t = lane; t < NC * op.np; t += tpe) {
-      int l = t % op.np, e = t / op.np;
-      int b1 = op.modes[l] & 0xff, b2 = (op.modes[l] >> 8) & 0xff, b3 = (op.modes[l] >> 16) & 0xff;
-      int q = op.b12_index[b1 + p1 * b2];
-      T acc = 0;
-      for (int a3 = 0; a3 < M3; ++a3)
-        acc = fma(C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))], Z[(e * nb12 + q) * M3 + a3], acc);
-      x[e * op.np + l] = acc;
+    for (int l = lane; l < np; l += tpe) {
+      const int b1 = op.modes[l] & 0xff, b2 = (op.modes[l] >> 8) & 0xff, b3 = (op.modes[l] >> 16) & 0xff;
+      const int q = op.b12_index[b1 + p1 * b2];
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int a3 = 0; a3 < M3; ++a3) {
+        const T cv = C[a3 + M3 * (b1 + p1 * (b2 + p1 * b3))];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(cv, Z[(e * nb12 + q) * M3 + a3], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) x[e * np + l] = acc[e];
     }
     __syncthreads();
   }
@@ -167,11 +242,39 @@ __device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lan
 template <typename T, int NC>
 __device__ void csr_mul(int rows, int cols, const int *ptr, const int *idx, const T *val,
                         const T *x, T *y, int lane, int tpe) {
-  for (int t = lane; t < NC * rows; t += tpe) {
-    int r = t % rows, e = t / rows;
-    T acc = 0;
-    for (int q = ptr[r]; q < ptr[r + 1]; ++q) acc += val[q] * x[e * cols + idx[q]];
-    y[e * rows + r] = acc;
+  for (int r = lane; r < rows; r += tpe) {
+    T acc[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) acc[e] = 0;
+    for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+      const T v = val[q];
+      const int c = idx[q];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] += v * x[e * cols + c];
+    }
+#pragma unroll
+    for (int e = 0; e < NC; ++e) y[e * rows + r] = acc[e];
+  }
+}
+
+// (R^T f)[e][i] for every volume node i (R^T rows in CSR, values Rtval in
+// the form's scalar type), handed to sink(e * nq + i, value)
+template <typename T, int NC, typename Sink>
+__device__ __forceinline__ void rt_apply(const DevOps &op, const T *Rtval, const T *f, int lane,
+                                         int tpe, Sink sink) {
+  const int nq = op.nq, nf = op.nf;
+  for (int i = lane; i < nq; i += tpe) {
+    T acc[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) acc[e] = 0;
+    for (int q = op.Rt_ptr[i]; q < op.Rt_ptr[i + 1]; ++q) {
+      const T v = Rtval[q];
+      const int c = op.Rt_idx[q];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = fma(v, f[e * nf + c], acc[e]);
+    }
+#pragma unroll
+    for (int e = 0; e < NC; ++e) sink(e * nq + i, acc[e]);
   }
 }
 
@@ -181,12 +284,20 @@ template <typename T, int D, int NC>
 __device__ void mass_solve(const DevOps &op, const T *JinvW, const T *WJinv, int wa, T *x, T *Y,
                            T *Z, T *W, int lane, int tpe) {
   if (!wa) {
-    for (int t = lane; t < NC * op.np; t += tpe) x[t] *= WJinv[t % op.np];
+    for (int l = lane; l < op.np; l += tpe) {
+      const T w = WJinv[l];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) x[e * op.np + l] *= w;
+    }
     __syncthreads();
     return;
   }
   vdm_mul<T, D, NC>(op, x, Y, Z, W, lane, tpe);
-  for (int t = lane; t < NC * op.nq; t += tpe) Y[t] *= JinvW[t % op.nq];
+  for (int i = lane; i < op.nq; i += tpe) {
+    const T w = JinvW[i];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) Y[e * op.nq + i] *= w;
+  }
   __syncthreads();
   vdm_tmul<T, D, NC>(op, Y, x, Z, W, lane, tpe);
 }
