@@ -405,6 +405,12 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
     s->nvpS = (size_t)nvp * c.d;
     if ((e = upload(s, vp_ij.data(), vp_ij.size(), &op.vp_ij)) != cudaSuccess) return cuda_fail(s, e, "upload");
     if ((e = upload(s, vp_S.data(), vp_S.size(), &op.vp_S)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    {
+      // S / 2 (exact): the forward EC pair flux takes its metric vector halved
+      std::vector<double> half(vp_S);
+      for (double &v : half) v *= 0.5;
+      if ((e = upload(s, half.data(), half.size(), &op.vp_Sh)) != cudaSuccess) return cuda_fail(s, e, "upload");
+    }
     if ((e = upload(s, inc_ptr.data(), inc_ptr.size(), &op.vp_inc_ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");
     if ((e = upload(s, inc_flat.data(), inc_flat.size(), &op.vp_inc)) != cudaSuccess) return cuda_fail(s, e, "upload");
 
@@ -430,6 +436,11 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
       s->nfpC = fp_C.size();
       if ((e = upload(s, fp_ij.data(), fp_ij.size(), &op.fp_ij)) != cudaSuccess) return cuda_fail(s, e, "upload");
       if ((e = upload(s, fp_C.data(), fp_C.size(), &op.fp_C)) != cudaSuccess) return cuda_fail(s, e, "upload");
+      {
+        std::vector<double> half(fp_C);
+        for (double &v : half) v *= 0.5;
+        if ((e = upload(s, half.data(), half.size(), &op.fp_Ch)) != cudaSuccess) return cuda_fail(s, e, "upload");
+      }
       if ((e = upload(s, qptr.data(), qptr.size(), &op.fp_q_ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");
       if ((e = upload(s, qflat.data(), qflat.size(), &op.fp_q)) != cudaSuccess) return cuda_fail(s, e, "upload");
       if ((e = upload(s, fptr.data(), fptr.size(), &op.fp_f_ptr)) != cudaSuccess) return cuda_fail(s, e, "upload");

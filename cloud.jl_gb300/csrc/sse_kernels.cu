@@ -356,13 +356,13 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
           for (int n = 0; n < D; ++n) G[n] = 0.0;
 #pragma unroll
           for (int m = 0; m < D; ++m) {
-            const double Sm = op.vp_S[pidx * D + m];
+            const double Sm = op.vp_Sh[pidx * D + m];
             if (Sm == 0.0) continue;
 #pragma unroll
             for (int n = 0; n < D; ++n)
               G[n] = fma(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
           }
-          ec_flux_dot<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, dp);
+          ec_flux_dot_half<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, dp);
           continue;
         }
       }
@@ -463,11 +463,11 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
         double *dp = diff + (size_t)(pidx - c0) * NC;
         if constexpr (NC > 1) {
           if (ec) {
-            const double Cij = op.fp_C[pidx];
+            const double Cij = op.fp_Ch[pidx];
             double G[D];
 #pragma unroll
             for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
-            ec_flux_dot<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, dp);
+            ec_flux_dot_half<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, dp);
             continue;
           }
         }

@@ -94,6 +94,14 @@ static void check(std::mt19937_64 &rng, double *worst) {
     for (int m = 0; m < D; ++m) G[m] = U(rng);
     double out[D + 2], F[D + 2][D];
     ec_flux_dot<D>(1 / (g - 1), PL, PR, G, out);
+    {
+      // the halved-vector form must reproduce ec_flux_dot bit for bit
+      double Gh[D], oh[D + 2];
+      for (int m = 0; m < D; ++m) Gh[m] = 0.5 * G[m];
+      ec_flux_dot_half<D>(1 / (g - 1), PL, PR, Gh, oh);
+      for (int e = 0; e < D + 2; ++e)
+        if (oh[e] != out[e]) worst[10] += 1.0;
+    }
     ref_ec_tensor<D>(g, uL, uR, F);
     double scale = 0;
     for (int e = 0; e < D + 2; ++e)
@@ -304,7 +312,7 @@ static void check_mixed_adjoint(std::mt19937_64 &rng, double *worst) {
 
 int main() {
   std::mt19937_64 rng(20261203);
-  double worst[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double worst[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   check<2>(rng, worst);
   check<3>(rng, worst);
   check_mixed<2>(rng, worst);
@@ -316,8 +324,8 @@ int main() {
   std::printf("{\"logmean\": %.3e, \"inv_logmean\": %.3e, \"ec_flux_dot\": %.3e, "
               "\"cons_to_entropy\": %.3e, \"entropy_to_cons\": %.3e, \"mixed_reduced_flux\": %.3e, "
               "\"flux_vjp_vs_fd\": %.3e, \"entropy_jvp_vs_fd\": %.3e, \"entropy_jacobian_symmetry\": %.3e, "
-              "\"mixed_flux_vjp\": %.3e}\n",
+              "\"mixed_flux_vjp\": %.3e, \"ec_flux_half_mismatches\": %.0f}\n",
               worst[0], worst[1], worst[2], worst[3], worst[4], worst[5], worst[6], worst[7], worst[8],
-              worst[9]);
+              worst[9], worst[10]);
   return 0;
 }

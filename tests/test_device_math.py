@@ -33,6 +33,12 @@ def test_contracted_ec_flux(results):
     assert results["ec_flux_dot"] < 2e-14
 
 
+def test_halved_metric_vector_flux_is_bitwise(results):
+    # ec_flux_dot_half(G / 2) takes the 1/2 factors inside the halved vector;
+    # scaling by 1/2 is exact, so every output is bitwise that of ec_flux_dot(G)
+    assert results["ec_flux_half_mismatches"] == 0
+
+
 def test_mixed_reduced_flux(results):
     # FP32 flux on perturbations vs the FP64 flux reduced the same way,
     # relative to the largest reduced flux component, for low-Mach states
