@@ -543,6 +543,15 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
     ka.fd_chunk = chunk;
     ka.vdm_zsz = zsz_e;
     layout(chunk);
+    // the interface flux of one facet node costs about 0.8 of a volume pair
+    // (block timings at p = 4): balance lanes when all pairs are one chunk
+    ka.vp_split = 0;
+    if (chunk >= op.nvp && nf < tpe && op.nvp > 0) {
+      const double unit = (op.nvp + 0.8 * nf) / tpe;
+      int a = (int)std::lround(unit - 0.8);
+      a = std::max(0, std::min(a, op.nvp / nf));
+      ka.vp_split = a;
+    }
   } else {
     finish(ka.layB, {nc * nq, nc * nf, nc * nf, nc * nq, d * nc * nq, nc * nq, nc * nq, 0, zsz, wsz});
   }

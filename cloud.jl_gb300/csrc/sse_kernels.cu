@@ -345,7 +345,15 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
   }
   for (int c0 = 0; c0 < op.nvp; c0 += CH) {
     const int c1 = min(op.nvp, c0 + CH);
-    for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
+    // with all pairs in one chunk, the lanes that also computed an interface
+    // flux take vp_split pairs each from the front of the list and the other
+    // lanes share the rest (which thread computes a pair does not change
+    // the sums, taken in pair order)
+    const bool split = ka.vp_split > 0 && c0 == 0 && c1 == op.nvp;
+    const int pfirst = split ? (lane < nf ? lane : ka.vp_split * nf + (lane - nf)) : c0 + lane;
+    const int pstep = split ? (lane < nf ? nf : tpe - nf) : tpe;
+    const int plast = split ? (lane < nf ? ka.vp_split * nf : c1) : c1;
+    for (int pidx = pfirst; pidx < plast; pidx += pstep) {
       int ij = op.vp_ij[pidx];
       int i = ij & 0xffff, j = ij >> 16;
       double *dp = diff + (size_t)(pidx - c0) * NC;
