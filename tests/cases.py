@@ -93,7 +93,7 @@ def make(name):
             form = S.StandardForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux())
     elif name.startswith("tgv_tet"):
         approx = "NodalTensor" if "nodal" in name else "ModalTensor"
-        p = 6 if "p6" in name else (5 if "p5" in name else (3 if "nodal" in name else 4))
+        p = 6 if "p6" in name else (5 if "p5" in name else (2 if "p2" in name else (3 if "nodal" in name else 4)))
         pb = setups.tgv_tet(cells=2, p=p, approx=approx, lf="ec" not in name)
         sd, law, ic, form = pb.sd, pb.law, pb.initial_data, pb.form
     else:
@@ -107,7 +107,7 @@ def make(name):
 NAMES = ["adv_tri_modal", "adv_tri_nodal", "adv_tri_central", "adv_tri_fd", "adv_tet_modal",
          "adv_tet_fd", "vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec",
          "vortex_tri_cons2pt", "euler_tri_std", "tgv_tet_modal", "tgv_tet_ec", "tgv_tet_nodal",
-         "tgv_tet_p5", "tgv_tet_p6"]
+         "tgv_tet_p5", "tgv_tet_p6", "tgv_tet_p2"]
 # multidimensional (dense V, D, R) approximations: parity, adjoint and mixed cases
 MULTI_NAMES = ["multi_adv_tri", "multi_adv_tri_nodal", "multi_adv_tri_fd", "multi_tri",
                "multi_tri_nodal", "multi_tri_std", "multi_tri_ec", "multi_tet", "multi_tet_ec"]

@@ -14,7 +14,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 ADJ_NAMES = ["vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec", "tgv_tet_modal", "tgv_tet_ec",
-             "tgv_tet_nodal", "tgv_tet_p5",
+             "tgv_tet_nodal", "tgv_tet_p5", "tgv_tet_p2",
              # StandardForm: linear advection (LF / central, modal / nodal, Tri / Tet) and Euler
              "adv_tri_modal", "adv_tri_nodal", "adv_tri_central", "adv_tet_modal", "euler_tri_std",
              # FluxDifferencingForm with the conservative two-point flux

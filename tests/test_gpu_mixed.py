@@ -25,8 +25,8 @@ def _pair(pkg, name):
 
 
 @pytest.mark.parametrize("name", ["vortex_tri_modal", "vortex_tri_nodal", "tgv_tet_modal",
-                                  "tgv_tet_ec", "tgv_tet_p5", "multi_tri", "multi_tri_nodal",
-                                  "multi_tet"])
+                                  "tgv_tet_ec", "tgv_tet_p5", "tgv_tet_p2", "multi_tri",
+                                  "multi_tri_nodal", "multi_tet"])
 def test_mixed_residual_close_to_fp64(gpu_lib, pkg, name):
     host, u, fp64, mixed = _pair(pkg, name)
     want = fp64.residual(u)
