@@ -91,11 +91,18 @@ def make(name):
         form = S.FluxDifferencingForm(inviscid_numerical_flux=nflux, two_point_flux=two)
         if name.startswith("euler_tri"):
             form = S.StandardForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux())
-    elif name.startswith("tgv_tet"):
+    elif name.startswith("tgv_tet") or name.startswith("euler_tet"):
         approx = "NodalTensor" if "nodal" in name else "ModalTensor"
         p = 6 if "p6" in name else (5 if "p5" in name else (2 if "p2" in name else (3 if "nodal" in name else 4)))
+        if name.startswith("euler_tet"):
+            p = 3
         pb = setups.tgv_tet(cells=2, p=p, approx=approx, lf="ec" not in name)
         sd, law, ic, form = pb.sd, pb.law, pb.initial_data, pb.form
+        if "cons2pt" in name:
+            form = S.FluxDifferencingForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux(),
+                                          two_point_flux=S.ConservativeFlux())
+        if name.startswith("euler_tet"):
+            form = S.StandardForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux())
     else:
         raise KeyError(name)
     host = S.HostArrays(law, sd, form)
@@ -107,7 +114,8 @@ def make(name):
 NAMES = ["adv_tri_modal", "adv_tri_nodal", "adv_tri_central", "adv_tri_fd", "adv_tet_modal",
          "adv_tet_fd", "vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec",
          "vortex_tri_cons2pt", "euler_tri_std", "tgv_tet_modal", "tgv_tet_ec", "tgv_tet_nodal",
-         "tgv_tet_p5", "tgv_tet_p6", "tgv_tet_p2"]
+         "tgv_tet_p5", "tgv_tet_p6", "tgv_tet_p2", "tgv_tet_cons2pt", "euler_tet_std"]
 # multidimensional (dense V, D, R) approximations: parity, adjoint and mixed cases
 MULTI_NAMES = ["multi_adv_tri", "multi_adv_tri_nodal", "multi_adv_tri_fd", "multi_tri",
-               "multi_tri_nodal", "multi_tri_std", "multi_tri_ec", "multi_tet", "multi_tet_ec"]
+               "multi_tri_nodal", "multi_tri_std", "multi_tri_ec", "multi_tet", "multi_tet_ec",
+               "multi_tet_nodal"]

@@ -18,7 +18,7 @@ ADJ_NAMES = ["vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec", "tgv_tet_m
              # StandardForm: linear advection (LF / central, modal / nodal, Tri / Tet) and Euler
              "adv_tri_modal", "adv_tri_nodal", "adv_tri_central", "adv_tet_modal", "euler_tri_std",
              # FluxDifferencingForm with the conservative two-point flux
-             "adv_tri_fd", "adv_tet_fd", "vortex_tri_cons2pt",
+             "adv_tri_fd", "adv_tet_fd", "vortex_tri_cons2pt", "tgv_tet_cons2pt", "euler_tet_std",
              # multidimensional (dense V, D, R) approximations
              "multi_adv_tri", "multi_adv_tri_fd", "multi_tri", "multi_tri_nodal", "multi_tri_std",
              "multi_tet"]
