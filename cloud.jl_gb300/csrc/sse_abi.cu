@@ -1605,6 +1605,18 @@ int32_t sse_struct_sizes(int32_t *out) {
   return 6;
 }
 
+int32_t sse_project_function(int32_t n_p, int32_t n_q, int32_t n_c, int64_t n_e,
+                             const double *VDM, const double *W, const double *J_q,
+                             const double *u_q, double *u0, int32_t memory) {
+  g_create_error.clear();
+  try {
+    return project_function_run(n_p, n_q, n_c, n_e, VDM, W, J_q, u_q, u0, memory, &g_create_error);
+  } catch (const std::exception &ex) {
+    g_create_error = ex.what();
+    return SSE_ERR_OUT_OF_MEMORY;
+  }
+}
+
 int32_t sse_geometric_factors(const sse_metric_operators *ops, int64_t n_e,
                               const double *const *xyz,
                               const sse_geometric_factors_out *out, int32_t memory) {

@@ -99,4 +99,8 @@ cudaError_t launch_adj_rk4_stage(double *ybar, double *kbar, const double *mu, c
 int geometric_factors_run(const sse_metric_operators *ops, int64_t n_e, const double *const *xyz,
                           const sse_geometric_factors_out *out, int memory, std::string *err);
 
+// project_function on the device (sse_project.cu); returns an sse_status.
+int project_function_run(int np, int nq, int nc, int64_t ne, const double *V, const double *W,
+                         const double *J, const double *uq, double *u0, int memory, std::string *err);
+
 }  // namespace sse

@@ -27,7 +27,7 @@ EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual",
             "sse_rk_adjoint",
             "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
             "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
-            "sse_create_error", "sse_geometric_factors"]
+            "sse_create_error", "sse_geometric_factors", "sse_project_function"]
 
 _lib = None
 
@@ -86,6 +86,8 @@ def load_library(path: str | None = None):
     L.sse_create_error.restype = C.c_char_p
     L.sse_geometric_factors.argtypes = [vp, C.c_int64, vp, vp, i32]
     L.sse_geometric_factors.restype = i32
+    L.sse_project_function.argtypes = [i32, i32, i32, C.c_int64, vp, vp, vp, vp, vp, i32]
+    L.sse_project_function.restype = i32
     _lib = L
     return L
 
@@ -315,6 +317,37 @@ def geometric_factors(mesh, ra, metrics: str = "Exact", project_jac: bool = True
     if rc != abi.SSE_OK:
         raise SSEError(rc, L.sse_create_error().decode())
     return GeometricFactors(*outs)
+
+
+def project_function(ra, J_q, u_q):
+    """``project_function`` (Solvers.jl:396-418) on the GPU: the L2 projection
+    of nodal initial data u_q (N_e, N_c, N_q numpy, or a CUDA tensor) onto
+    the modal basis of ``ra`` with the element Jacobians J_q (N_e, N_q),
+    by Cholesky of every element's mass matrix (sse_project_function).
+    Returns u0 (N_e, N_c, N_p) in the memory of u_q."""
+    L = load_library()
+    if ra.V is None:
+        raise ValueError("project_function on the GPU needs a modal basis (V is the identity)")
+    V = _fortran(ra.V)
+    W = np.ascontiguousarray(ra.W, dtype=np.float64)
+    N_e, N_c, N_q = u_q.shape
+    N_p = V.shape[1]
+    dp = lambda a: C.c_void_p(a.ctypes.data)
+    if isinstance(u_q, np.ndarray):
+        J = np.ascontiguousarray(J_q, dtype=np.float64)
+        uq = np.ascontiguousarray(u_q, dtype=np.float64)
+        u0 = np.empty((N_e, N_c, N_p))
+        rc = L.sse_project_function(N_p, N_q, N_c, N_e, dp(V), dp(W), dp(J), dp(uq), dp(u0), abi.SSE_HOST)
+    else:
+        import torch
+        J = J_q.contiguous()
+        uq = u_q.contiguous()
+        u0 = torch.empty((N_e, N_c, N_p), dtype=torch.float64, device=uq.device)
+        rc = L.sse_project_function(N_p, N_q, N_c, N_e, dp(V), dp(W), C.c_void_p(J.data_ptr()),
+                                    C.c_void_p(uq.data_ptr()), C.c_void_p(u0.data_ptr()), abi.SSE_DEVICE)
+    if rc != abi.SSE_OK:
+        raise SSEError(rc, L.sse_create_error().decode())
+    return u0
 
 
 @dataclass

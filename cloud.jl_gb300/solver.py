@@ -184,14 +184,22 @@ class EulerPeriodicTest:
 # initialize (Solvers.jl:388-427)
 # ---------------------------------------------------------------------------
 
-def initialize(initial_data, sd: SpatialDiscretization) -> np.ndarray:
+def initialize(initial_data, sd: SpatialDiscretization, projection: str = "host") -> np.ndarray:
     """L2 projection of the initial data onto the approximation space;
-    returns numpy (N_e, N_c, N_p) = Julia (N_p, N_c, N_e)."""
+    returns numpy (N_e, N_c, N_p) = Julia (N_p, N_c, N_e).
+    ``projection="gpu"`` solves the element mass systems on the GPU
+    (sse_project_function) instead of numpy."""
     ra = sd.reference_approximation
     x = sd.mesh.xyzq
     uq = initial_data.evaluate(x, 0.0)                  # (N_e, N_q, N_c)
     if ra.V is None:
         return np.ascontiguousarray(uq.transpose(0, 2, 1))
+    if projection == "gpu":
+        from . import gb300
+        return gb300.project_function(ra, sd.geometric_factors.J_q,
+                                      np.ascontiguousarray(uq.transpose(0, 2, 1)))
+    if projection != "host":
+        raise ValueError(projection)
     V = ra.V
     WJ = ra.W[None, :] * sd.geometric_factors.J_q       # (N_e, N_q)
     out = np.empty((sd.N_e, uq.shape[2], ra.N_p))

@@ -313,6 +313,24 @@ int32_t sse_geometric_factors(const sse_metric_operators *ops, int64_t n_e,
                               const double *const *xyz,
                               const sse_geometric_factors_out *out, int32_t memory);
 
+/* ---- L2 projection of initial data ---------------------------------------
+ *
+ * project_function (src/Solvers/Solvers.jl:396-418) behind initialize
+ * (Solvers.jl:421-427) for a modal basis: for every element
+ *   u0[:, :, k] = M_k \ (VDM' diag(W .* J_q[:, k]) u_q[:, :, k]),
+ *   M_k = VDM' diag(W .* J_q[:, k]) VDM,
+ * with M_k factorised by Cholesky as the reference does (a non-SPD M_k is an
+ * error, SSE_ERR_NONPHYSICAL).  VDM is Matrix(V) (n_q x n_p), W the volume
+ * weights (n_q), J_q (n_q x n_e), u_q the initial data at the volume nodes
+ * (n_q x n_c x n_e, the layout of evaluate(initial_data, xyzq, 0)), u0 the
+ * modal coefficients (n_p x n_c x n_e).  memory = SSE_HOST: J_q, u_q, u0 are
+ * host arrays; SSE_DEVICE: device pointers.  VDM and W are host arrays in both
+ * cases.  FP64, one CTA per element; errors leave their message for
+ * sse_create_error(). */
+int32_t sse_project_function(int32_t n_p, int32_t n_q, int32_t n_c, int64_t n_e,
+                             const double *VDM, const double *W, const double *J_q,
+                             const double *u_q, double *u0, int32_t memory);
+
 /* Measured FMA throughput of the current device in TFLOP/s (2 flops per
  * FMA): out[0] FP64, out[1] FP32 CUDA-core pipes.  The roofline
  * denominators of the residual kernels; no counterpart in the reference. */

@@ -152,3 +152,14 @@ def test_geometric_factors_rejects_invalid_arguments(pkg, lib):
     ops.project_jacobian = 0
     assert lib.sse_geometric_factors(C.byref(ops), 4, xyz, C.byref(res), abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
     assert "output" in lib.sse_create_error().decode()
+
+
+def test_project_function_rejects_invalid_arguments(pkg, lib):
+    abi = pkg.abi
+    x = np.zeros(16)
+    p = C.c_void_p(x.ctypes.data)
+    assert lib.sse_project_function(0, 4, 1, 1, p, p, p, p, p, abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert lib.sse_project_function(5, 4, 1, 1, p, p, p, p, p, abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert "n_p" in lib.sse_create_error().decode()
+    assert lib.sse_project_function(2, 4, 1, 1, None, p, p, p, p, abi.SSE_HOST) == abi.SSE_ERR_INVALID_ARGUMENT
+    assert lib.sse_project_function(2, 4, 1, 1, p, p, p, p, p, 7) == abi.SSE_ERR_INVALID_ARGUMENT
