@@ -25,6 +25,7 @@ SSE_CENTRAL = 1
 SSE_ENTROPY_CONSERVATIVE = 2
 SSE_CONSERVATIVE_FLUX = 0
 SSE_EC_FLUX = 1
+SSE_CHANDRASHEKAR_FLUX = 2
 SSE_WEIGHT_ADJUSTED = 0
 SSE_DIAGONAL = 1
 SSE_FP64 = 0

@@ -218,6 +218,7 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   if (c.form != SSE_STANDARD_FORM && c.form != SSE_FLUX_DIFFERENCING_FORM)
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown form");
   if (c.numerical_flux < 0 || c.numerical_flux > 2) return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown numerical flux");
+  if (c.two_point_flux < 0 || c.two_point_flux > 2) return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown two-point flux");
   if (c.mass_solver != SSE_WEIGHT_ADJUSTED && c.mass_solver != SSE_DIAGONAL)
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown mass solver");
   if (c.law == SSE_EULER && !(c.gamma > 1.0)) return fail(s, SSE_ERR_INVALID_ARGUMENT, "gamma must exceed 1");
@@ -469,6 +470,7 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   ph.law = c.law;
   ph.nflux = c.numerical_flux;
   ph.ec = (c.two_point_flux == SSE_EC_FLUX) ? 1 : 0;
+  ph.chandrashekar = (c.two_point_flux == SSE_CHANDRASHEKAR_FLUX) ? 1 : 0;
   ph.half_lambda = c.half_lambda;
   ph.gamma = c.gamma;
   ph.gm1 = c.gamma - 1.0;
@@ -808,6 +810,8 @@ int enable_adjoint(sse_solver *s) {
   // flux (Euler) or the conservative two-point flux (advection, Euler with
   // ConservativeFlux)
   const bool ec_pairs = c.law == SSE_EULER && c.two_point_flux == SSE_EC_FLUX;
+  if (fd && c.law == SSE_EULER && c.two_point_flux == SSE_CHANDRASHEKAR_FLUX)
+    return fail(s, SSE_ERR_UNSUPPORTED, "the discrete adjoint does not cover Chandrashekar's two-point flux");
   if (!s->mapP_involution)
     return fail(s, SSE_ERR_UNSUPPORTED, "the discrete adjoint needs mapP to pair facet nodes (mapP(mapP(x)) == x)");
   if (s->adj_ready) return SSE_OK;

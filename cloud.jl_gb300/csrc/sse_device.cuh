@@ -110,7 +110,8 @@ struct DevGeo {
 struct Physics {
   int law;       // 0 advection, 1 Euler
   int nflux;     // 0 LF, 1 central, 2 EC numerical flux
-  int ec;        // two-point flux: 1 entropy-conservative (Ranocha), 0 conservative
+  int ec;        // two-point flux: 1 entropy-conservative (Ranocha), 0 otherwise
+  int chandrashekar;  // 1: Chandrashekar's EC flux (taken when ec == 0)
   double half_lambda;
   double gamma, gm1, igm1, log_gm1;
   double a[3];
@@ -904,8 +905,50 @@ __device__ __forceinline__ void euler_flux(const Physics &ph, const double *u, d
   }
 }
 
-// Two-point flux tensor for a pair of states: Euler EC / conservative
-// average, or advection a_m (u_L + u_R)/2.
+// Chandrashekar (2013), entropy conservative and kinetic-energy preserving:
+// with beta = rho / (2 p) and logarithmic means rho_hat, beta_hat,
+//   F_rho = rho_hat Vbar_n,  F_m = F_rho Vbar_m + p_hat delta_mn,
+//   p_hat = avg(rho) / (2 avg(beta)),
+//   F_E = F_rho (1 / (2 (gamma - 1) beta_hat) - avg(|V|^2) / 2) + F_m . Vbar.
+template <int D>
+__device__ __forceinline__ void chandrashekar_flux(const Physics &ph, const double *uL, const double *uR,
+                                                   double F[D + 2][D]) {
+  double VL[D], VR[D], sL = 0.0, sR = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    VL[m] = uL[m + 1] / uL[0];
+    VR[m] = uR[m + 1] / uR[0];
+    sL += VL[m] * VL[m];
+    sR += VR[m] * VR[m];
+  }
+  const double pL = ph.gm1 * (uL[D + 1] - 0.5 * uL[0] * sL);
+  const double pR = ph.gm1 * (uR[D + 1] - 0.5 * uR[0] * sR);
+  const double bL = uL[0] / (2.0 * pL), bR = uR[0] / (2.0 * pR);
+  const double rho_hat = logmean(uL[0], uR[0]);
+  const double beta_hat = logmean(bL, bR);
+  const double p_hat = 0.5 * (uL[0] + uR[0]) / (bL + bR);
+  const double v2avg = 0.5 * (sL + sR);
+  const double h = 1.0 / (2.0 * ph.gm1 * beta_hat) - 0.5 * v2avg;
+  double Vb[D];
+#pragma unroll
+  for (int m = 0; m < D; ++m) Vb[m] = 0.5 * (VL[m] + VR[m]);
+#pragma unroll
+  for (int n = 0; n < D; ++n) {
+    const double frho = rho_hat * Vb[n];
+    F[0][n] = frho;
+    double fe = frho * h;
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      const double fm = frho * Vb[m] + (m == n ? p_hat : 0.0);
+      F[m + 1][n] = fm;
+      fe += fm * Vb[m];
+    }
+    F[D + 1][n] = fe;
+  }
+}
+
+// Two-point flux tensor for a pair of states: Euler EC (Ranocha),
+// Chandrashekar or conservative average, or advection a_m (u_L + u_R)/2.
 template <int D, int NC>
 __device__ __forceinline__ void two_point(const Physics &ph, const double *uL, const double *uR,
                                           double F[NC][D]) {
@@ -917,6 +960,8 @@ __device__ __forceinline__ void two_point(const Physics &ph, const double *uL, c
     if (ph.ec) {
       Prim<D> L = euler_prim<D>(ph, uL), R = euler_prim<D>(ph, uR);
       ec_flux<D>(ph, L, R, F);
+    } else if (ph.chandrashekar) {
+      chandrashekar_flux<D>(ph, uL, uR, F);
     } else {
       double FL[D + 2][D], FR[D + 2][D];
       euler_flux<D>(ph, uL, FL);

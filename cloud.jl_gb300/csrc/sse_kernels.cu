@@ -634,6 +634,7 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
       for (int m = 0; m < D; ++m) n[m] = ka.geo.n_f[m + D * (j + (size_t)nf * kk)];
       Physics ph2 = ph;
       ph2.ec = 0;
+      ph2.chandrashekar = 0;
       two_point<D, NC>(ph2, ui, uo, F);
       double a = 0.0;
       if (ph.nflux == 0) a = ph.half_lambda * wave_speed<D, NC>(ph, ui, uo, n);

@@ -82,6 +82,15 @@ class ConservativeFlux:
 
 
 @dataclass(frozen=True)
+class ChandrashekarFlux:
+    """Chandrashekar's (2013) entropy-conservative and kinetic-energy
+    preserving two-point flux for the Euler equations: an extra option with
+    no counterpart in the reference, whose entropy-conservative flux is
+    Ranocha's (EntropyConservativeFlux)."""
+    pass
+
+
+@dataclass(frozen=True)
 class StandardForm:
     inviscid_numerical_flux: object = field(default_factory=LaxFriedrichsNumericalFlux)
 
@@ -245,6 +254,8 @@ class HostArrays:
         two_pt = abi.SSE_EC_FLUX
         if fd and isinstance(form.two_point_flux, ConservativeFlux):
             two_pt = abi.SSE_CONSERVATIVE_FLUX
+        if fd and isinstance(form.two_point_flux, ChandrashekarFlux):
+            two_pt = abi.SSE_CHANDRASHEKAR_FLUX
         mass = abi.SSE_DIAGONAL if ra.V is None else abi.SSE_WEIGHT_ADJUSTED
         if mass_matrix_solver not in ("default", "WeightAdjusted", "Diagonal"):
             raise ValueError(mass_matrix_solver)

@@ -51,8 +51,11 @@ enum sse_numerical_flux {
   SSE_CENTRAL = 1,               /* CentralNumericalFlux */
   SSE_ENTROPY_CONSERVATIVE = 2   /* EntropyConservativeNumericalFlux */
 };
-/* Two-point flux (ConservationLaws.jl:70-73). */
-enum sse_two_point_flux { SSE_CONSERVATIVE_FLUX = 0, SSE_EC_FLUX = 1 };
+/* Two-point flux (ConservationLaws.jl:70-73): ConservativeFlux,
+ * EntropyConservativeFlux (Ranocha's, euler_navierstokes.jl:171-195), and
+ * Chandrashekar's entropy-conservative, kinetic-energy-preserving flux
+ * (Chandrashekar 2013; an extra option with no reference counterpart). */
+enum sse_two_point_flux { SSE_CONSERVATIVE_FLUX = 0, SSE_EC_FLUX = 1, SSE_CHANDRASHEKAR_FLUX = 2 };
 /* Mass-matrix solver (mass_matrix.jl:1-17). */
 enum sse_mass_solver { SSE_WEIGHT_ADJUSTED = 0, SSE_DIAGONAL = 1 };
 /* Arithmetic of the bulk flux/operator work. */

@@ -223,11 +223,13 @@ static sse_real inv_logmean(sse_real x, sse_real y) {
   return log(y / x) / (y - x);
 }
 
-/* two-point flux tensor F[e + MAXC*n] (e = 0..N_c-1, n = 0..d-1).
- * Euler EC: euler_navierstokes.jl:171-195 (Ranocha); conservative:
- * :152-158; advection: linear_advection_diffusion.jl:113-119. */
-static void two_point_flux(const sse_config *c, int ec, const sse_real *uL, const sse_real *uR,
+/* two-point flux tensor F[e + MAXC*n] (e = 0..N_c-1, n = 0..d-1); kind 1:
+ * Euler EC, euler_navierstokes.jl:171-195 (Ranocha); kind 2: Chandrashekar
+ * (2013), an option with no reference counterpart; kind 0: conservative
+ * average, :152-158; advection: linear_advection_diffusion.jl:113-119. */
+static void two_point_flux(const sse_config *c, int kind, const sse_real *uL, const sse_real *uR,
                            sse_real *F) {
+  const int ec = kind == 1;
   const int d = c->d;
   if (c->law == SSE_LINEAR_ADVECTION) {
     sse_real f1 = 0.5 * (uL[0] + uR[0]);
@@ -254,6 +256,35 @@ static void two_point_flux(const sse_config *c, int ec, const sse_real *uL, cons
       for (int m = 0; m < d; ++m)
         F[m + 1 + MAXC * n] = rho_avg * Vavg[m] * Vavg[n] + (m == n ? pavg : 0.0);
       F[E + MAXC * n] = frho * C + 0.5 * (pL * VR[n] + pR * VL[n]);
+    }
+    return;
+  }
+  if (kind == 2) {
+    /* Chandrashekar: rho_hat, beta_hat logarithmic means, beta = rho / (2 p),
+     * p_hat = avg(rho) / (2 avg(beta)) */
+    sse_real VL[MAXD], VR[MAXD], sL = 0.0, sR = 0.0, Vb[MAXD];
+    for (int m = 0; m < d; ++m) {
+      VL[m] = uL[m + 1] / uL[0];
+      VR[m] = uR[m + 1] / uR[0];
+      sL += VL[m] * VL[m];
+      sR += VR[m] * VR[m];
+      Vb[m] = 0.5 * (VL[m] + VR[m]);
+    }
+    sse_real pL = gm1 * (uL[E] - 0.5 * uL[0] * sL);
+    sse_real pR = gm1 * (uR[E] - 0.5 * uR[0] * sR);
+    sse_real bL = uL[0] / (2.0 * pL), bR = uR[0] / (2.0 * pR);
+    sse_real rho_hat = logmean(uL[0], uR[0]), beta_hat = logmean(bL, bR);
+    sse_real p_hat = 0.5 * (uL[0] + uR[0]) / (bL + bR);
+    sse_real h = 1.0 / (2.0 * gm1 * beta_hat) - 0.25 * (sL + sR);
+    for (int n = 0; n < d; ++n) {
+      sse_real frho = rho_hat * Vb[n], fe = frho * h;
+      F[0 + MAXC * n] = frho;
+      for (int m = 0; m < d; ++m) {
+        sse_real fm = frho * Vb[m] + (m == n ? p_hat : 0.0);
+        F[m + 1 + MAXC * n] = fm;
+        fe += fm * Vb[m];
+      }
+      F[E + MAXC * n] = fe;
     }
     return;
   }
@@ -542,7 +573,7 @@ static void time_derivative_standard(oracle_t *o, sse_real *dudt, int k, scratch
 static void time_derivative_fd(oracle_t *o, sse_real *dudt, int k, scratch_t *s) {
   const sse_config *c = &o->cfg;
   const int nq = c->n_q, nf = c->n_f, nc = c->n_c, np = c->n_p, d = c->d, ne = c->n_e;
-  const int ec = (c->two_point_flux == SSE_EC_FLUX);
+  const int ec = (c->two_point_flux == SSE_EC_FLUX) ? 1 : (c->two_point_flux == SSE_CHANDRASHEKAR_FLUX ? 2 : 0);
   sse_real *uq = o->u_q + (size_t)nq * nc * k;
   sse_real F[MAXC * MAXD], ui[MAXC], uj[MAXC];
   numerical_flux_elem(o, k, ec, s->ff);

@@ -88,6 +88,8 @@ def make(name):
         sd, law, ic = pb.sd, pb.law, pb.initial_data
         nflux = S.EntropyConservativeNumericalFlux() if "ec" in name else S.LaxFriedrichsNumericalFlux()
         two = S.ConservativeFlux() if "cons2pt" in name else S.EntropyConservativeFlux()
+        if "chandra" in name:
+            two = S.ChandrashekarFlux()
         form = S.FluxDifferencingForm(inviscid_numerical_flux=nflux, two_point_flux=two)
         if name.startswith("euler_tri"):
             form = S.StandardForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux())
@@ -101,6 +103,9 @@ def make(name):
         if "cons2pt" in name:
             form = S.FluxDifferencingForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux(),
                                           two_point_flux=S.ConservativeFlux())
+        if "chandra" in name:
+            nflux = S.EntropyConservativeNumericalFlux() if "ec" in name else S.LaxFriedrichsNumericalFlux()
+            form = S.FluxDifferencingForm(inviscid_numerical_flux=nflux, two_point_flux=S.ChandrashekarFlux())
         if name.startswith("euler_tet"):
             form = S.StandardForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux())
     else:
@@ -114,7 +119,8 @@ def make(name):
 NAMES = ["adv_tri_modal", "adv_tri_nodal", "adv_tri_central", "adv_tri_fd", "adv_tet_modal",
          "adv_tet_fd", "vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec",
          "vortex_tri_cons2pt", "euler_tri_std", "tgv_tet_modal", "tgv_tet_ec", "tgv_tet_nodal",
-         "tgv_tet_p5", "tgv_tet_p6", "tgv_tet_p2", "tgv_tet_cons2pt", "euler_tet_std"]
+         "tgv_tet_p5", "tgv_tet_p6", "tgv_tet_p2", "tgv_tet_cons2pt", "euler_tet_std",
+         "vortex_tri_chandra", "tgv_tet_chandra"]
 # multidimensional (dense V, D, R) approximations: parity, adjoint and mixed cases
 MULTI_NAMES = ["multi_adv_tri", "multi_adv_tri_nodal", "multi_adv_tri_fd", "multi_tri",
                "multi_tri_nodal", "multi_tri_std", "multi_tri_ec", "multi_tet", "multi_tet_ec",

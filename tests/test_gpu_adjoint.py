@@ -256,9 +256,15 @@ def test_mixed_vjp_needs_a_modal_basis(gpu_lib, pkg):
 
 
 def test_adjoint_rejections(gpu_lib, pkg):
-    """A pullback without a recording is refused."""
+    """A pullback without a recording is refused, and so is the VJP of
+    Chandrashekar's two-point flux (an extra forward option)."""
     host, u = cases.make("vortex_tri_modal")
     G = pkg.GB300Solver(host)
     with pytest.raises(pkg.SSEError) as e:
         G.rk_adjoint(u)
     assert e.value.code == pkg.abi.SSE_ERR_INVALID_ARGUMENT
+    host, u = cases.make("vortex_tri_chandra")
+    G = pkg.GB300Solver(host)
+    with pytest.raises(pkg.SSEError) as e:
+        G.residual_vjp(u, u)
+    assert e.value.code == pkg.abi.SSE_ERR_UNSUPPORTED

@@ -60,8 +60,9 @@ def test_mixed_conservation_and_entropy(gpu_lib, pkg, name):
     assert abs(out[host.N_c]) <= 1e-5 * scale
 
 
-def test_mixed_rejected_outside_flux_differencing_euler(gpu_lib, pkg):
-    host, _ = cases.make("adv_tri_modal")
+@pytest.mark.parametrize("name", ["adv_tri_modal", "vortex_tri_chandra"])
+def test_mixed_rejected_outside_flux_differencing_euler(gpu_lib, pkg, name):
+    host, _ = cases.make(name)
     gpu = pkg.GB300Solver(host)
     with pytest.raises(pkg.SSEError) as ei:
         gpu.set_precision(pkg.abi.SSE_MIXED)

@@ -19,7 +19,8 @@ def test_conservation(name):
     assert np.abs(cons).max() < 1e-12 * scale
 
 
-@pytest.mark.parametrize("name", ["vortex_tri_ec", "tgv_tet_ec", "multi_tri_ec", "multi_tet_ec"])
+@pytest.mark.parametrize("name", ["vortex_tri_ec", "tgv_tet_ec", "multi_tri_ec", "multi_tet_ec",
+                                  "vortex_tri_chandra_ec", "tgv_tet_chandra_ec"])
 def test_entropy_conservation(name):
     host, u = cases.make(name)
     o = Oracle(host)
@@ -30,7 +31,7 @@ def test_entropy_conservation(name):
 
 
 @pytest.mark.parametrize("name", ["vortex_tri_modal", "tgv_tet_modal", "tgv_tet_nodal", "multi_tri",
-                                  "multi_tri_nodal", "multi_tet"])
+                                  "multi_tri_nodal", "multi_tet", "vortex_tri_chandra", "tgv_tet_chandra"])
 def test_free_stream_preservation(name):
     host, _ = cases.make(name)
     S = cases.S
