@@ -512,6 +512,8 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   // phase-A layout: X, Y, Z, W, F, lane partials; F holds NC x max(N_p, N_q,
   // N_f) (modal scratch, facet values, or V dudt in the conservation kernel)
   finish(ka.layA, {nc * std::max(np, nq), nc * nq, zsz, wsz, nc * std::max({np, nq, nf}), tpe * (nc + 1)});
+  // energy_kernel: X, Y, Z, W as in phase A, the element mass operator, dudt
+  finish(ka.layE, {nc * std::max(np, nq), nc * nq, zsz, wsz, np * np, nc * np});
   if (fd) {
     // the pair buffer holds one chunk of per-pair contributions, and after
     // the pair passes the modal / nodal buffers and the sum-factorisation
@@ -1553,6 +1555,39 @@ int32_t sse_conservation_residual(sse_solver *s, const double *u, const double *
   for (int q = 0; q <= c.n_c; ++q) out[q] = 0.0;
   for (int k = 0; k < c.n_e; ++k)
     for (int q = 0; q <= c.n_c; ++q) out[q] += part[(size_t)k * (c.n_c + 1) + q];
+  return SSE_OK;
+}
+
+int32_t sse_energy_residual(sse_solver *s, const double *u, const double *dudt, double *out,
+                            int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (!u || !dudt || !out) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null argument");
+  const sse_config &c = s->cfg;
+  if ((size_t)s->ka.epb * s->ka.layE.team_doubles * sizeof(double) > 220 * 1024)
+    return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the energy analysis");
+  size_t n = (size_t)c.n_p * c.n_c * c.n_e;
+  cudaError_t e;
+  const double *du = u, *dd = dudt;
+  if (memory == SSE_HOST) {
+    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    if ((e = cudaMemcpyAsync(s->d_tmp, dudt, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    du = s->d_u;
+    dd = s->d_tmp;
+  } else if (memory != SSE_DEVICE) {
+    return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
+  }
+  if ((e = cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream))) return cuda_fail(s, e, "memset");
+  if ((e = launch_energy(s->ka, du, dd, s->d_partial, s->stream))) return cuda_fail(s, e, "energy");
+  std::vector<double> part((size_t)c.n_e * c.n_c);
+  int flag = 0;
+  if ((e = cudaMemcpyAsync(part.data(), s->d_partial, part.size() * 8, cudaMemcpyDeviceToHost, s->stream)) ||
+      (e = cudaMemcpyAsync(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream)))
+    return cuda_fail(s, e, "D2H");
+  if ((e = cudaStreamSynchronize(s->stream))) return cuda_fail(s, e, "sync");
+  if (flag) return fail(s, SSE_ERR_NONPHYSICAL, "an element mass matrix is not positive definite");
+  for (int q = 0; q < c.n_c; ++q) out[q] = 0.0;
+  for (int k = 0; k < c.n_e; ++k)
+    for (int q = 0; q < c.n_c; ++q) out[q] += part[(size_t)k * c.n_c + q];
   return SSE_OK;
 }
 

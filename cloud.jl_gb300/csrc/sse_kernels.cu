@@ -1082,6 +1082,61 @@ __global__ void __launch_bounds__(256) conservation_kernel(KernelArgs ka, const 
   }
 }
 
+// EnergyConservationAnalysis (Analysis/conservation.jl:161-175):
+// partial[k][e] = u[:, e, k]' M_k dudt[:, e, k] with the mass solver's mass
+// matrix (mass_matrix.jl:150-158): WeightAdjustedSolver inv(V' diag(J^-1 W) V)
+// (applied by a Cholesky solve of V' diag(J^-1 W) V, whose columns are the
+// weight-adjusted operator applied to unit vectors), DiagonalSolver W J.
+template <int D, int NC>
+__global__ void __launch_bounds__(256) energy_kernel(KernelArgs ka, const double *u, const double *dudt,
+                                                     double *partial) {
+  extern __shared__ double smem[];
+  __shared__ int bad;
+  const DevOps &op = ka.op;
+  const Layout &L = ka.layE;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3],
+         *A = base + L.off[4], *R = base + L.off[5];
+  if (threadIdx.x == 0) bad = 0;
+  for (int t = lane; t < NC * np; t += tpe) R[t] = dudt[(size_t)kk * NC * np + t];
+  __syncthreads();
+  if (ka.mass_wa) {
+    const double *JinvW = ka.geo.JinvW + (size_t)kk * nq;
+    // columns b0 .. b0 + NC - 1 of A = V' diag(J^-1 W) V per pass
+    for (int b0 = 0; b0 < np; b0 += NC) {
+      for (int t = lane; t < NC * np; t += tpe) {
+        const int e = t / np, l = t - e * np;
+        X[t] = (l == b0 + e) ? 1.0 : 0.0;
+      }
+      __syncthreads();
+      mass_solve<double, D, NC>(op, JinvW, nullptr, 1, X, Y, Z, Wb, lane, tpe);
+      for (int t = lane; t < NC * np; t += tpe) {
+        const int e = t / np, l = t - e * np;
+        if (b0 + e < np) A[l * np + (b0 + e)] = X[t];
+      }
+      __syncthreads();
+    }
+    team_cholesky_solve(A, np, R, NC, lane, tpe, &bad);  // R <- A^-1 dudt = M_WA dudt
+  } else {
+    const double *WJ = ka.geo.WJ + (size_t)kk * nq;  // n_p == n_q: M = diag(W J)
+    for (int t = lane; t < NC * np; t += tpe) R[t] *= WJ[t % np];
+    __syncthreads();
+  }
+  if (lane < NC && live) {
+    const double *uk = u + (size_t)kk * NC * np + (size_t)lane * np;
+    double s = 0.0;
+    for (int l = 0; l < np; ++l) s = fma(uk[l], R[lane * np + l], s);
+    partial[(size_t)k * NC + lane] = s;
+  }
+  if (threadIdx.x == 0 && bad) ka.flag_nonphysical();
+}
+
 // ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
@@ -1174,6 +1229,18 @@ cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st) {
   } else {
     SSE_DISPATCH(D, NC, (std_time_derivative_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka)));
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_energy(const KernelArgs &ka, const double *u, const double *dudt, double *partial,
+                          cudaStream_t st) {
+  int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  size_t sm = (size_t)ka.epb * ka.layE.team_doubles * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  SSE_DISPATCH(D, NC, (e = cudaFuncSetAttribute(energy_kernel<D, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sm)));
+  if (e != cudaSuccess) return e;
+  SSE_DISPATCH(D, NC, (energy_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka, u, dudt, partial)));
   return cudaGetLastError();
 }
 

@@ -47,6 +47,7 @@ struct KernelArgs {
   double *ubar_f;    // adjoint of u_f                (nf x nc x ne, element-major)
   Layout layAdjB1, layAdjB2, layAdjA;
   Layout layAdjS;                          // StandardForm flux-transpose layout
+  Layout layE;                             // energy_kernel layout (doubles)
   Layout layAdjG;                          // conservative-two-point pair-transpose layout
   int pair_chunk;    // pairs per shared-memory chunk in the pair-adjoint passes
   int pair_chunk_generic;  // the same for the conservative two-point flux
@@ -71,6 +72,8 @@ cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_projection_of_one(const KernelArgs &ka, double *P1, double *RP1, cudaStream_t st);
 cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka);
 cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st);
+cudaError_t launch_energy(const KernelArgs &ka, const double *u, const double *dudt, double *partial,
+                          cudaStream_t st);
 cudaError_t launch_conservation(const KernelArgs &ka, const double *u, const double *dudt,
                                 double *partial, cudaStream_t st);
 cudaError_t launch_ck_stage(double *u, double *tmp, const double *k, double a, double b, double dt,

@@ -302,6 +302,44 @@ __device__ void mass_solve(const DevOps &op, const T *JinvW, const T *WJinv, int
   vdm_tmul<T, D, NC>(op, Y, x, Z, W, lane, tpe);
 }
 
+// In-place Cholesky factorisation of the SPD n x n matrix M (row-major,
+// lower triangle; the factor overwrites it) and solve of M y = b for nrhs
+// right-hand sides Y[r][n], by the threads of one element team.  Sets *bad
+// (shared) when a pivot is not positive.
+__device__ __forceinline__ void team_cholesky_solve(double *M, int n, double *Y, int nrhs, int lane,
+                                                    int tpe, int *bad) {
+  for (int j = 0; j < n; ++j) {
+    if (lane == 0) {
+      double d = M[j * n + j];
+      for (int q = 0; q < j; ++q) d = fma(-M[j * n + q], M[j * n + q], d);
+      if (!(d > 0.0)) { *bad = 1; d = 1.0; }
+      M[j * n + j] = sqrt(d);
+    }
+    __syncthreads();
+    const double ljj = M[j * n + j];
+    for (int i = j + 1 + lane; i < n; i += tpe) {
+      double s = M[i * n + j];
+      for (int q = 0; q < j; ++q) s = fma(-M[i * n + q], M[j * n + q], s);
+      M[i * n + j] = s / ljj;
+    }
+    __syncthreads();
+  }
+  for (int e = lane; e < nrhs; e += tpe) {
+    double *y = Y + (size_t)e * n;
+    for (int r = 0; r < n; ++r) {
+      double s = y[r];
+      for (int q = 0; q < r; ++q) s = fma(-M[r * n + q], y[q], s);
+      y[r] = s / M[r * n + r];
+    }
+    for (int r = n - 1; r >= 0; --r) {
+      double s = y[r];
+      for (int q = r + 1; q < n; ++q) s = fma(-M[q * n + r], y[q], s);
+      y[r] = s / M[r * n + r];
+    }
+  }
+  __syncthreads();
+}
+
 // Store one nodal state value: FP64 form -> the double scratch; mixed form ->
 // the float scratch as a perturbation from the reference state.
 template <int NC>

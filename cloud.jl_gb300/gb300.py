@@ -27,7 +27,8 @@ EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual",
             "sse_rk_adjoint",
             "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
             "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
-            "sse_create_error", "sse_geometric_factors", "sse_project_function"]
+            "sse_create_error", "sse_geometric_factors", "sse_project_function",
+            "sse_energy_residual"]
 
 _lib = None
 
@@ -71,6 +72,8 @@ def load_library(path: str | None = None):
     L.sse_rk_adjoint.restype = i32
     L.sse_conservation_residual.argtypes = [vp, vp, vp, vp, i32]
     L.sse_conservation_residual.restype = i32
+    L.sse_energy_residual.argtypes = [vp, vp, vp, vp, i32]
+    L.sse_energy_residual.restype = i32
     L.sse_set_precision.argtypes = [vp, i32]
     L.sse_set_precision.restype = i32
     L.sse_set_stream.argtypes = [vp, vp]
@@ -222,6 +225,16 @@ class GB300Solver:
         pd, md = _addr(dudt)
         assert mu == md
         self._check(self.L.sse_conservation_residual(self.h, pu, pd, C.c_void_p(out.ctypes.data), mu))
+        return out
+
+    def energy_residual(self, u, dudt) -> np.ndarray:
+        """EnergyConservationAnalysis residual: sum_k u' M_k dudt per component
+        with the mass solver's own mass matrix (sse_energy_residual)."""
+        out = np.zeros(self.host.N_c)
+        pu, mu = _addr(u)
+        pd, md = _addr(dudt)
+        assert mu == md
+        self._check(self.L.sse_energy_residual(self.h, pu, pd, C.c_void_p(out.ctypes.data), mu))
         return out
 
     def set_precision(self, precision: int):

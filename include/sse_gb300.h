@@ -239,11 +239,22 @@ int32_t sse_rk_steps_snapshots(sse_solver *s, double *u, int32_t n_steps, double
                                double *residuals, double *t, int32_t memory);
 
 /* FP64 reductions of Analysis/conservation.jl:145-189 for one (u, dudt):
- * out[0..N_c-1] = sum_k 1' WJ V dudt[:, e, k]       (primary conservation)
- * out[N_c]      = sum_k (P w)' M dudt               (entropy production, Euler)
- *               = sum_k u' M dudt                   (energy, advection) */
+ * out[0..N_c-1] = sum_k 1' WJ V dudt[:, e, k]       (PrimaryConservationAnalysis)
+ * out[N_c]      = sum_k (P w)' M dudt               (EntropyConservationAnalysis,
+ *                 :177-189; P = M^-1 V' WJ, so this is w_q' WJ V dudt for any
+ *                 mass solver; for linear advection w = u, the entropy u^2/2).
+ * EnergyConservationAnalysis (:161-175, u' M dudt with the mass solver's own
+ * mass matrix) is sse_energy_residual. */
 int32_t sse_conservation_residual(sse_solver *s, const double *u, const double *dudt,
                                   double *out, int32_t memory);
+
+/* EnergyConservationAnalysis residual (Analysis/conservation.jl:161-175):
+ * out[e] = sum_k u[:, e, k]' M_k dudt[:, e, k], e = 0 .. N_c-1, with the mass
+ * solver's own mass matrix (mass_matrix.jl:150-158): inv(V' diag(J^-1 W) V)
+ * for WeightAdjustedSolver (applied through a Cholesky solve per element),
+ * diag(W J) for DiagonalSolver.  FP64. */
+int32_t sse_energy_residual(sse_solver *s, const double *u, const double *dudt, double *out,
+                            int32_t memory);
 
 /* SSE_FP64 (default, the drop-in) or SSE_MIXED (FP32 fluxes and operator
  * arithmetic, FP64 geometry, RK accumulation and reductions). */

@@ -161,3 +161,34 @@ def test_dense_operators_match_oracle(name, gpu_lib, pkg):
     want = Oracle(host).residual(u)
     floor = roundoff_floor(host, u)
     assert rel2(got, want) <= max(1e-12, 4 * floor), (rel2(got, want), floor)
+
+
+def _energy_rates_host(host, u, du):
+    """EnergyConservationAnalysis (conservation.jl:161-175) on the host:
+    sum_k u' M_k dudt per component, M_k = inv(V' diag(W/J) V) (weight
+    adjusted) or diag(W J) (diagonal)."""
+    V = host.sd.reference_approximation.V
+    out = np.zeros(host.N_c)
+    for k in range(host.N_e):
+        if V is None:
+            M = np.diag(host.WJ[k])
+        else:
+            M = np.linalg.inv(V.T @ (host.JinvW[k][:, None] * V))
+        for e in range(host.N_c):
+            out[e] += u[k, e] @ M @ du[k, e]
+    return out
+
+
+@pytest.mark.parametrize("name", ["adv_tri_modal", "adv_tri_central", "adv_tri_nodal", "adv_tet_modal",
+                                  "vortex_tri_modal", "tgv_tet_modal"])
+def test_energy_residual_matches_host(built, pkg, name):
+    host, u = cases.make(name)
+    gpu = pkg.GB300Solver(host)
+    du = gpu.residual(u)
+    got = gpu.energy_residual(u, du)
+    want = _energy_rates_host(host, u, du)
+    scale = np.abs(u).max() * np.abs(du).max() * np.abs(host.WJ).sum()
+    assert np.abs(got - want).max() <= 1e-12 * scale, (got, want)
+    if name == "adv_tri_central":
+        # the central flux conserves the discrete energy (test/runtests.jl:57-59)
+        assert abs(got[0]) <= 1e-12 * scale
