@@ -490,14 +490,27 @@ SSE_HD void entropy_to_cons_jvp(double gamma, double gm1, double igm1, double lo
 //   rho e = rhoe_ref exp(dX),  dX = (-gamma log(a/a_ref) - (sv - sv_ref))/(gamma-1)
 // (euler_navierstokes.jl:100-131).
 // ---------------------------------------------------------------------------
+// FP64 reciprocal for the mixed form's entropy maps: the FP32 reciprocal
+// refined by one Newton-Raphson step r + r (1 - x r), relative error about
+// the square of the FP32 one (~1e-14); x within the FP32 range (densities,
+// pressures and entropy variables of physical states).
+SSE_HD double rcp_refined(double x) {
+#ifdef __CUDA_ARCH__
+  const double r = (double)__frcp_rn((float)x);
+  return fma(r, fma(-x, r, 1.0), r);
+#else
+  return 1.0 / x;
+#endif
+}
+
 template <int D>
 __device__ __forceinline__ void cons_to_entropy_mixed(const Physics &ph, const double *u, double *w) {
   double s2 = 0.0;
 #pragma unroll
   for (int m = 0; m < D; ++m) s2 = fma(u[m + 1], u[m + 1], s2);
-  const double k = 0.5 * s2 * sse_rcp(u[0]);
+  const double k = 0.5 * s2 * rcp_refined(u[0]);
   const double p = ph.gm1 * (u[D + 1] - k);
-  const double ip = sse_rcp(p);
+  const double ip = rcp_refined(p);
   const float lp = log1pf((float)((p - ph.p_ref) * ph.ip_ref));
   const float lr = log1pf((float)((u[0] - ph.rho_ref) * ph.irho_ref));
   const double ls = ph.s_ref + (double)lp - ph.gamma * (double)lr;
@@ -515,7 +528,7 @@ __device__ __forceinline__ void entropy_to_cons_mixed(const Physics &ph, const d
   double s2 = 0.0;
 #pragma unroll
   for (int m = 0; m < D; ++m) s2 = fma(wg[m + 1], wg[m + 1], s2);
-  const double k = 0.5 * s2 * sse_rcp(wg[D + 1]);
+  const double k = 0.5 * s2 * rcp_refined(wg[D + 1]);
   const double sv = ph.gamma - wg[0] + k;
   const double a = -wg[D + 1];
   const float la = log1pf((float)((a - ph.a_ref) * ph.ia_ref));
