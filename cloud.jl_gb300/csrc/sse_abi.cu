@@ -587,6 +587,23 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   // opt in to large dynamic shared memory for every kernel instantiation used
   size_t smA = (size_t)epb * ka.layA.team_doubles * 8, smB = (size_t)epb * ka.layB.team_doubles * 8;
   if ((e = sse_set_smem_limits(ka, smA, smB)) != cudaSuccess) return cuda_fail(s, e, "cudaFuncSetAttribute");
+
+  // the weight-adjusted mass operator V' diag(J^-1 W) V of every element,
+  // built once when it takes at most a quarter of the free device memory:
+  // each mass solve is then one dense n_p x n_p product instead of two
+  // sum-factorised applications of V
+  ka.Ak = nullptr;
+  if (has_vdm && c.mass_solver == SSE_WEIGHT_ADJUSTED) {
+    const size_t bytes = (size_t)c.n_e * np * np * 8;
+    size_t freeb = 0, totalb = 0;
+    if ((e = cudaMemGetInfo(&freeb, &totalb))) return cuda_fail(s, e, "cudaMemGetInfo");
+    if (bytes <= freeb / 4) {
+      if ((e = alloc(s, bytes, &p))) return cuda_fail(s, e, "alloc mass operators");
+      if ((e = launch_mass_operator(ka, (double *)p, s->stream))) return cuda_fail(s, e, "mass operators");
+      if ((e = cudaStreamSynchronize(s->stream))) return cuda_fail(s, e, "mass operators");
+      ka.Ak = (const double *)p;
+    }
+  }
   return SSE_OK;
 }
 

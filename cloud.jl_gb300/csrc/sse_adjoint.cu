@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(256) adj_lift_kernel(KernelArgs ka) {
   // dudt = M V^T r_q  =>  rbar_q = V M^T lam (M symmetric)
   mass_solve<double, D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
                             ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, X, Y,
-                            Z, Wb, lane, tpe);
+                            Z, Wb, lane, tpe, ka.Ak ? ka.Ak + (size_t)kk * op.np * op.np : nullptr);
   vdm_mul<double, D, NC>(op, X, Y, Z, Wb, lane, tpe);
   if (live)
     for (int t = lane; t < NC * nq; t += tpe) ka.rbar_q[(size_t)kk * NC * nq + t] = Y[t];
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
   __syncthreads();
   if (op.has_vdm) {
     vdm_tmul<double, D, NC>(op, X, F, Z, Wb, lane, tpe);
-    mass_solve<double, D, NC>(op, JinvW, nullptr, 1, F, X, Z, Wb, lane, tpe);
+    mass_solve<double, D, NC>(op, JinvW, nullptr, 1, F, X, Z, Wb, lane, tpe, ka.Ak ? ka.Ak + (size_t)kk * op.np * op.np : nullptr);
     vdm_mul<double, D, NC>(op, F, Wq, Z, Wb, lane, tpe);  // projected w_q
   } else {
     for (int t = lane; t < NC * nq; t += tpe) Wq[t] = X[t];
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
   if (op.has_vdm) {
     // w_q = V M V^T (WJ c2e(u_q0))  =>  wbar_c2e = WJ .* V M V^T wbar_q
     vdm_tmul<double, D, NC>(op, Y, F, Z, Wb, lane, tpe);
-    mass_solve<double, D, NC>(op, JinvW, nullptr, 1, F, X, Z, Wb, lane, tpe);
+    mass_solve<double, D, NC>(op, JinvW, nullptr, 1, F, X, Z, Wb, lane, tpe, ka.Ak ? ka.Ak + (size_t)kk * op.np * op.np : nullptr);
     vdm_mul<double, D, NC>(op, F, Y, Z, Wb, lane, tpe);
     for (int t = lane; t < NC * nq; t += tpe) Y[t] *= WJ[t % nq];
     __syncthreads();

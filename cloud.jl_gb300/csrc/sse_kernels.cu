@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
         // X holds WJ w_q (NC x nq): w = V^T (WJ w_q); mass solve; w_q = V w
         double *Wm = F;  // NC x np modal scratch (F is large enough, see layout)
         vdm_tmul<double, D, NC>(op, X, Wm, Z, Wb, lane, tpe);
-        mass_solve<double, D, NC>(op, ka.geo.JinvW + (size_t)kk * nq, nullptr, 1, Wm, X, Z, Wb, lane, tpe);
+        mass_solve<double, D, NC>(op, ka.geo.JinvW + (size_t)kk * nq, nullptr, 1, Wm, X, Z, Wb, lane, tpe,
+                                  ka.Ak ? ka.Ak + (size_t)kk * op.np * op.np : nullptr);
         vdm_mul<double, D, NC>(op, Wm, X, Z, Wb, lane, tpe);  // X = w_q (projected)
         // u_q = e2c(w_q)
         for (int i = lane; i < nq; i += tpe) {
@@ -568,7 +569,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
   vdm_tmul<double, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
   mass_solve<double, D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
                     ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq,
-                    Z, Wb, lane, tpe);
+                    Z, Wb, lane, tpe, ka.Ak ? ka.Ak + (size_t)kk * op.np * op.np : nullptr);
   double *out = ka.dudt + (size_t)kk * NC * np;
   if (live)
     for (int t = lane; t < NC * np; t += tpe) {
@@ -688,7 +689,7 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
   vdm_tmul<double, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
   mass_solve<double, D, NC>(op, ka.geo.JinvW ? ka.geo.JinvW + (size_t)kk * nq : nullptr,
                     ka.geo.WJinv ? ka.geo.WJinv + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq,
-                    Z, Wb, lane, tpe);
+                    Z, Wb, lane, tpe, ka.Ak ? ka.Ak + (size_t)kk * op.np * op.np : nullptr);
   double *out = ka.dudt + (size_t)kk * NC * np;
   if (live)
     for (int t = lane; t < NC * np; t += tpe) {
@@ -1082,6 +1083,41 @@ __global__ void __launch_bounds__(256) conservation_kernel(KernelArgs ka, const 
   }
 }
 
+// The weight-adjusted mass operator V' diag(J^-1 W) V of every element
+// (mass_matrix.jl:185-196 applies it as V' (J^-1 W .* (V x))), built once
+// column by column from the sum-factorised operator applied to unit
+// vectors, n_p x n_p row-major per element.
+template <int D, int NC>
+__global__ void __launch_bounds__(256) mass_operator_kernel(KernelArgs ka, double *Ak) {
+  extern __shared__ double smem[];
+  const DevOps &op = ka.op;
+  const Layout &L = ka.layA;
+  const int tpe = blockDim.x / ka.epb;
+  const int team = threadIdx.x / tpe, lane = threadIdx.x % tpe;
+  const int k = blockIdx.x * ka.epb + team;
+  const bool live = k < ka.ne;
+  const int kk = live ? k : 0;
+  const int np = op.np, nq = op.nq;
+  double *base = smem + (size_t)team * L.team_doubles;
+  double *X = base + L.off[0], *Y = base + L.off[1], *Z = base + L.off[2], *Wb = base + L.off[3];
+  const double *JinvW = ka.geo.JinvW + (size_t)kk * nq;
+  double *out = Ak + (size_t)kk * np * np;
+  for (int b0 = 0; b0 < np; b0 += NC) {
+    for (int t = lane; t < NC * np; t += tpe) {
+      const int e = t / np, l = t - e * np;
+      X[t] = (l == b0 + e) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    mass_solve<double, D, NC>(op, JinvW, nullptr, 1, X, Y, Z, Wb, lane, tpe);
+    if (live)
+      for (int t = lane; t < NC * np; t += tpe) {
+        const int e = t / np, l = t - e * np;
+        if (b0 + e < np) out[(size_t)l * np + (b0 + e)] = X[t];
+      }
+    __syncthreads();
+  }
+}
+
 // EnergyConservationAnalysis (Analysis/conservation.jl:161-175):
 // partial[k][e] = u[:, e, k]' M_k dudt[:, e, k] with the mass solver's mass
 // matrix (mass_matrix.jl:150-158): WeightAdjustedSolver inv(V' diag(J^-1 W) V)
@@ -1229,6 +1265,17 @@ cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st) {
   } else {
     SSE_DISPATCH(D, NC, (std_time_derivative_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka)));
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mass_operator(const KernelArgs &ka, double *Ak, cudaStream_t st) {
+  int grid = (ka.ne + ka.epb - 1) / ka.epb;
+  size_t sm = (size_t)ka.epb * ka.layA.team_doubles * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  SSE_DISPATCH(D, NC, (e = cudaFuncSetAttribute(mass_operator_kernel<D, NC>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)));
+  if (e != cudaSuccess) return e;
+  SSE_DISPATCH(D, NC, (mass_operator_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka, Ak)));
   return cudaGetLastError();
 }
 

@@ -29,6 +29,7 @@ struct KernelArgs {
   Layout layAm;      // mixed-form phase A layout (doubles; FP32 arrays from off[4], in floats)
   Layout layP1;      // projection of the constant function (NC = 1), doubles
   int ne, epb, tpb;
+  const double *Ak;  // per-element weight-adjusted mass operators (n_p x n_p), or null
   int fd, project_entropy, mass_wa;
   const double *u;   // modal state (np x nc x ne)
   double *dudt;      // residual   (np x nc x ne)
@@ -72,6 +73,7 @@ cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_projection_of_one(const KernelArgs &ka, double *P1, double *RP1, cudaStream_t st);
 cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka);
 cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st);
+cudaError_t launch_mass_operator(const KernelArgs &ka, double *Ak, cudaStream_t st);
 cudaError_t launch_energy(const KernelArgs &ka, const double *u, const double *dudt, double *partial,
                           cudaStream_t st);
 cudaError_t launch_conservation(const KernelArgs &ka, const double *u, const double *dudt,

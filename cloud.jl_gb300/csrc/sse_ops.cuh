@@ -280,9 +280,31 @@ __device__ __forceinline__ void rt_apply(const DevOps &op, const T *Rtval, const
 
 // WeightAdjustedSolver (M^-1 = I): x <- V^T diag(JinvW) V x;
 // DiagonalSolver: x <- WJinv .* x (mass_matrix.jl:177-196)
+// With Ak (the element's V' diag(J^-1 W) V, n_p x n_p row-major, built once by
+// mass_operator_kernel) the weight-adjusted solve is one dense product.
 template <typename T, int D, int NC>
 __device__ void mass_solve(const DevOps &op, const T *JinvW, const T *WJinv, int wa, T *x, T *Y,
-                           T *Z, T *W, int lane, int tpe) {
+                           T *Z, T *W, int lane, int tpe, const T *Ak = nullptr) {
+  if (wa && Ak) {
+    const int np = op.np;
+    for (int a = lane; a < np; a += tpe) {
+      const T *row = Ak + (size_t)a * np;
+      T acc[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) acc[e] = 0;
+      for (int b = 0; b < np; ++b) {
+        const T v = row[b];
+#pragma unroll
+        for (int e = 0; e < NC; ++e) acc[e] = fma(v, x[e * np + b], acc[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) Y[e * np + a] = acc[e];
+    }
+    __syncthreads();
+    for (int t = lane; t < NC * np; t += tpe) x[t] = Y[t];
+    __syncthreads();
+    return;
+  }
   if (!wa) {
     for (int l = lane; l < op.np; l += tpe) {
       const T w = WJinv[l];
