@@ -878,7 +878,7 @@ __global__ void __launch_bounds__(256) adj_lift_mixed_kernel(KernelArgs ka) {
   __syncthreads();
   mass_solve<float, D, NC>(op, ka.geo.JinvWf ? ka.geo.JinvWf + (size_t)kk * nq : nullptr,
                            ka.geo.WJinvf ? ka.geo.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, X, Y, Z,
-                           Wb, lane, tpe);
+                           Wb, lane, tpe, ka.Akf ? ka.Akf + (size_t)kk * op.np * op.np : nullptr);
   vdm_mul<float, D, NC>(op, X, Y, Z, Wb, lane, tpe);
   float *rbq = reinterpret_cast<float *>(ka.rbar_q);
   float *gbf = reinterpret_cast<float *>(ka.gbar_f);
@@ -1190,7 +1190,7 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   }
   __syncthreads();
   vdm_tmul<float, D, NC>(op, XQ, T1, Zf, Wf, lane, tpe);
-  mass_solve<float, D, NC>(op, JinvWf, nullptr, 1, T1, S1, Zf, Wf, lane, tpe);
+  mass_solve<float, D, NC>(op, JinvWf, nullptr, 1, T1, S1, Zf, Wf, lane, tpe, ka.Akf ? ka.Akf + (size_t)kk * op.np * op.np : nullptr);
   vdm_mul<float, D, NC>(op, T1, WQ, Zf, Wf, lane, tpe);                      // w'_q
   csr_mul<float, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_valf, WQ, WF, lane, tpe);  // w'_f
   __syncthreads();
@@ -1222,7 +1222,7 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   __syncthreads();
   // projection transpose (V M V^T is symmetric): the same operators
   vdm_tmul<float, D, NC>(op, XQ, T1, Zf, Wf, lane, tpe);
-  mass_solve<float, D, NC>(op, JinvWf, nullptr, 1, T1, S1, Zf, Wf, lane, tpe);
+  mass_solve<float, D, NC>(op, JinvWf, nullptr, 1, T1, S1, Zf, Wf, lane, tpe, ka.Akf ? ka.Akf + (size_t)kk * op.np * op.np : nullptr);
   vdm_mul<float, D, NC>(op, T1, XQ, Zf, Wf, lane, tpe);
   // ubar_q0 = J_c2e(u_q0)^T (W J x), symmetric Jacobian
   for (int i = lane; i < nq; i += tpe) {

@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
   }
   __syncthreads();
   vdm_tmul<float, D, NC>(op, Af, Cf, Zf, Wf, lane, tpe);                               // V^T x'
-  mass_solve<float, D, NC>(op, ka.geo.JinvWf + (size_t)kk * nq, nullptr, 1, Cf, Af, Zf, Wf, lane, tpe);
+  mass_solve<float, D, NC>(op, ka.geo.JinvWf + (size_t)kk * nq, nullptr, 1, Cf, Af, Zf, Wf, lane, tpe, ka.Akf ? ka.Akf + (size_t)kk * op.np * op.np : nullptr);
   vdm_mul<float, D, NC>(op, Cf, Bf, Zf, Wf, lane, tpe);                                // w'_q
   csr_mul<float, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_valf, Bf, Af, lane, tpe);        // w'_f
   __syncthreads();
@@ -950,7 +950,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   vdm_tmul<float, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
   mass_solve<float, D, NC>(op, g.JinvWf ? g.JinvWf + (size_t)kk * nq : nullptr,
                            g.WJinvf ? g.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq, Z,
-                           Wb, lane, tpe);
+                           Wb, lane, tpe, ka.Akf ? ka.Akf + (size_t)kk * op.np * op.np : nullptr);
   // energy residual = H_ref x density residual + reduced-flux residual, in FP64
   double *outp = ka.dudt + (size_t)kk * NC * np;
   if (live)

@@ -30,6 +30,7 @@ struct KernelArgs {
   Layout layP1;      // projection of the constant function (NC = 1), doubles
   int ne, epb, tpb;
   const double *Ak;  // per-element weight-adjusted mass operators (n_p x n_p), or null
+  const float *Akf;  // their FP32 roundings for the mixed form, or null
   int fd, project_entropy, mass_wa;
   const double *u;   // modal state (np x nc x ne)
   double *dudt;      // residual   (np x nc x ne)
