@@ -88,9 +88,9 @@ WORKLOADS = {
 
 # DRAM bytes (read + write) per element of one fd_time_derivative_kernel<3,5>
 # / nodal_values_kernel<3,5> launch at p = 4, from ncu captures of the same
-# kernels on the 8^3 x 6 = 3,072-tet case (118.2 MB and 10.6 MB per launch);
+# kernels on the 8^3 x 6 = 3,072-tet case (145.7 MB and 37.9 MB per launch);
 # reads scale with the element count
-TRAFFIC_PER_ELEMENT = {"tgv_p4": {"B": 38_483, "A": 3_450}}
+TRAFFIC_PER_ELEMENT = {"tgv_p4": {"B": 47_429, "A": 12_341}}
 
 
 def env_rank():

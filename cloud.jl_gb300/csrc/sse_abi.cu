@@ -648,9 +648,17 @@ int enable_mixed(sse_solver *s) {
   if ((e = rounded(op.A, s->nA, &op.Af)) || (e = rounded(op.B, s->nB, &op.Bf)) ||
       (e = rounded(op.C, s->nC, &op.Cf)) || (e = rounded(op.R_val, s->nnzR, &op.R_valf)) ||
       (e = rounded(op.Rt_val, s->nnzR, &op.Rt_valf)) || (e = rounded(op.vp_S, s->nvpS, &op.vp_Sf)) ||
-      (e = rounded(op.fp_C, s->nfpC, &op.fp_Cf)) || (e = rounded(op.Vd, s->nVd, &op.Vdf)) ||
-      (e = rounded(ka.Ak, ka.Ak ? (size_t)c.n_e * c.n_p * c.n_p : 0, &ka.Akf)))
+      (e = rounded(op.fp_C, s->nfpC, &op.fp_Cf)) || (e = rounded(op.Vd, s->nVd, &op.Vdf)))
     return cuda_fail(s, e, "mixed operators");
+  // the per-element mass operators in FP32, transposed to row-major (the FP32
+  // dense solve gives each thread one row)
+  ka.Akf = nullptr;
+  if (ka.Ak) {
+    if ((e = alloc(s, (size_t)c.n_e * c.n_p * c.n_p * sizeof(float), &p)) ||
+        (e = launch_round_transpose(ka.Ak, (float *)p, c.n_e, c.n_p, s->stream)))
+      return cuda_fail(s, e, "mixed mass operators");
+    ka.Akf = (const float *)p;
+  }
   if ((e = rounded(g.BJf, nf * ne, &g.BJff)) || (e = rounded(g.n_f, d * nf * ne, &g.n_ff)) ||
       (e = rounded(g.Lambda_q, nq * d * d * ne, &g.Lambda_qf)) ||
       (e = rounded(g.halfnJf, d * nf * ne, &g.halfnJff)) ||

@@ -999,6 +999,18 @@ __global__ void round_to_float_kernel(const double *__restrict__ in, float *__re
     out[x] = (float)in[x];
 }
 
+// FP64 -> FP32 rounding of nmat n x n matrices with a transpose of each: the
+// column-major FP64 mass operators become row-major FP32 ones
+__global__ void round_transpose_kernel(const double *__restrict__ in, float *__restrict__ out, size_t nmat,
+                                       int n) {
+  const size_t nn = (size_t)n * n, total = nmat * nn;
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = x / nn;
+    const int r = (int)(x - k * nn), a = r / n, b = r - a * n;
+    out[x] = (float)in[k * nn + (size_t)b * n + a];
+  }
+}
+
 // classic RK4 stage helpers
 __global__ void rk4_stage_kernel(const double *__restrict__ u, double *__restrict__ ust,
                                  double *__restrict__ acc, const double *__restrict__ k,
@@ -1086,7 +1098,7 @@ __global__ void __launch_bounds__(256) conservation_kernel(KernelArgs ka, const 
 // The weight-adjusted mass operator V' diag(J^-1 W) V of every element
 // (mass_matrix.jl:185-196 applies it as V' (J^-1 W .* (V x))), built once
 // column by column from the sum-factorised operator applied to unit
-// vectors, n_p x n_p row-major per element.
+// vectors, n_p x n_p column-major per element.
 template <int D, int NC>
 __global__ void __launch_bounds__(256) mass_operator_kernel(KernelArgs ka, double *Ak) {
   extern __shared__ double smem[];
@@ -1112,7 +1124,7 @@ __global__ void __launch_bounds__(256) mass_operator_kernel(KernelArgs ka, doubl
     if (live)
       for (int t = lane; t < NC * np; t += tpe) {
         const int e = t / np, l = t - e * np;
-        if (b0 + e < np) out[(size_t)l * np + (b0 + e)] = X[t];
+        if (b0 + e < np) out[(size_t)(b0 + e) * np + l] = X[t];   // column b0 + e
       }
     __syncthreads();
   }
@@ -1320,6 +1332,12 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
 cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   round_to_float_kernel<<<elementwise_grid(n), 256, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_round_transpose(const double *in, float *out, size_t nmat, int n, cudaStream_t st) {
+  if (nmat == 0 || n == 0) return cudaSuccess;
+  round_transpose_kernel<<<elementwise_grid(nmat * n * n), 256, 0, st>>>(in, out, nmat, n);
   return cudaGetLastError();
 }
 

@@ -29,8 +29,8 @@ struct KernelArgs {
   Layout layAm;      // mixed-form phase A layout (doubles; FP32 arrays from off[4], in floats)
   Layout layP1;      // projection of the constant function (NC = 1), doubles
   int ne, epb, tpb;
-  const double *Ak;  // per-element weight-adjusted mass operators (n_p x n_p), or null
-  const float *Akf;  // their FP32 roundings for the mixed form, or null
+  const double *Ak;  // per-element weight-adjusted mass operators (n_p x n_p, column-major), or null
+  const float *Akf;  // their FP32 roundings for the mixed form (row-major), or null
   int fd, project_entropy, mass_wa;
   const double *u;   // modal state (np x nc x ne)
   double *dudt;      // residual   (np x nc x ne)
@@ -70,6 +70,7 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
                                         double a, double b, double dt, int first, size_t n,
                                         cudaStream_t st);
 cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st);
+cudaError_t launch_round_transpose(const double *in, float *out, size_t nmat, int n, cudaStream_t st);
 cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_projection_of_one(const KernelArgs &ka, double *P1, double *RP1, cudaStream_t st);
 cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka);

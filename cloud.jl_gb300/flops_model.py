@@ -5,7 +5,8 @@ Counting convention: add, subtract, multiply = 1 flop; fused multiply-add =
 once per unique node pair, contractions once per (pair, direction)
 incidence, as the reference's sparse loops perform them
 (flux_differencing_form.jl:37-75, 126-168).  Bytes are the minimal HBM
-traffic of the FP64 form: every array read or written once per phase.
+traffic of the FP64 form: every array read or written once per phase,
+the per-element dense mass operator included where a phase applies it.
 The same numbers feed ``roofline.achieved`` in bench.py and the reports.
 """
 from __future__ import annotations
@@ -45,6 +46,17 @@ def vdm_flops(ra) -> float:
     return 2.0 * (M3 * ra.N_p + nb12 * M2 * M3 + M1 * p1 * M2 * M3)
 
 
+def mass_solve_flops(ra) -> float:
+    """One weight-adjusted mass solve of one component.  The reference
+    applies V and V^T around the weighted diagonal (mass_matrix.jl:185-196);
+    the kernels apply the precomputed per-element operator V^T diag(W/J) V,
+    a dense n_p x n_p product.  The cheaper of the two is counted, so the
+    model never credits work that is not done."""
+    if ra.V is None:
+        return 0.0
+    return min(2.0 * vdm_flops(ra), 2.0 * ra.N_p * ra.N_p)
+
+
 def ec_flux_flops(d: int) -> float:
     """Ranocha's two-point flux tensor from per-node primitives
     (euler_navierstokes.jl:171-195; logmean series branch)."""
@@ -58,6 +70,8 @@ def model(host) -> Work:
     d, nc, nq, nf, np_ = ra.d, host.N_c, host.N_q, host.N_f, host.N_p
     nnzR = host.R.nnz
     vf = vdm_flops(ra)
+    mf = mass_solve_flops(ra)
+    mb = 8.0 * np_ * np_ if ra.V is not None else 0.0   # the element's dense mass operator
     euler = nc > 1
     fd = host.S != []
     f8 = 8.0
@@ -65,14 +79,14 @@ def model(host) -> Work:
     if fd and euler:
         c2e = 3 * d + 12
         e2c = nc + 3 * d + 14
-        nV = 5 if ra.V is not None else 0
-        flops_A = nc * nV * vf + nc * 2 * nnzR + nq * (c2e + nc) + nq * nc + (nq + nf) * e2c
-        bytes_A = f8 * (np_ * nc + 2 * nq + nq * nc + nf * nc)
+        nV = 3 if ra.V is not None else 0                # V u, V^T, V (+ one mass solve)
+        flops_A = nc * (nV * vf + mf) + nc * 2 * nnzR + nq * (c2e + nc) + nq * nc + (nq + nf) * e2c
+        bytes_A = f8 * (np_ * nc + 2 * nq + nq * nc + nf * nc) + mb
     else:
         flops_A = nc * (vf + 2 * nnzR)
         bytes_A = f8 * (np_ * nc + nq * nc + nf * nc)
     # ---- phase B
-    nV_B = 3 if ra.V is not None else 0
+    nV_B = 1 if ra.V is not None else 0                  # V^T (+ one mass solve)
     if fd:
         S_inc = sum(s.nnz for s in host.S) // 2          # (pair, m) incidences with i < j
         pairs = _unique_pairs(host)
@@ -85,22 +99,22 @@ def model(host) -> Work:
             flops_B = ((nq + nf) * prim + nf * flux_fac + pairs * pair_flux
                        + S_inc * (d + nc * (2 * d + 2) + 2 * nc)
                        + nfp * (pair_flux + d + nc * (2 * d + 3))
-                       + nc * 2 * nnzR + nq * nc + nc * nV_B * vf + nq * nc)
+                       + nc * 2 * nnzR + nq * nc + nc * (nV_B * vf + mf) + nq * nc)
         else:
             pair_flux = 2 + d
             flops_B = (nf * (pair_flux + 2 * d + 4) + pairs * pair_flux
                        + S_inc * (d + 2 * d + 2 + 2) + nfp * (pair_flux + d + 2 * d + 3)
-                       + 2 * nnzR + nq + nV_B * vf + nq)
+                       + 2 * nnzR + nq + nV_B * vf + mf + nq)
         bytes_B = f8 * (nq * nc + 2 * nf * nc + d * d * nq + d * ra.reference_element.num_faces * nq
-                        + 2 * d * nf + nf + nq + np_ * nc) + 4.0 * nf
+                        + 2 * d * nf + nf + nq + np_ * nc) + 4.0 * nf + mb
     else:
         nnzD = sum(D.nnz for D in host.D)
         phys = (d + 2) * d * 2 if euler else d
         flops_B = (nq * phys + nf * (4 * d + 10) * nc
                    + d * d * nc * (2 * nq + 4 * nnzD / d)
                    + d * nc * (2 * nnzR + 2 * nf) + nc * nf + nc * 2 * nnzR + nc * nq
-                   + nc * nV_B * vf + nq * nc)
-        bytes_B = f8 * (nq * nc + 2 * nf * nc + d * d * nq + d * nf + nf + nq + np_ * nc) + 4.0 * nf
+                   + nc * (nV_B * vf + mf) + nq * nc)
+        bytes_B = f8 * (nq * nc + 2 * nf * nc + d * d * nq + d * nf + nf + nq + np_ * nc) + 4.0 * nf + mb
     bytes_stage = f8 * 5 * np_ * nc
     return Work(float(flops_A), float(flops_B), bytes_A, bytes_B, bytes_stage)
 
