@@ -488,14 +488,19 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   // 192 volume and facet nodes (measured against 128 threads: phase B 7.6 %
   // and 5.4 % faster at p = 4 and 5, mixed phase A 1.75x -- the FP64 pipe
   // idles less with eight warps per element -- but 15 % slower at p = 3,
-  // whose 128 nodes leave half the threads idle).  Tris: four elements of 32
-  // threads per block (measured against 64 x 4 and 32 x 8).
-  const int tpe = nq < 64 ? 32 : (nq + nf > 192 ? 256 : 128);
+  // whose 128 nodes leave half the threads idle).  Small elements: 128-thread
+  // blocks of 32-thread teams (measured against 64 x 4 and 32 x 8), or of
+  // 16-thread teams for flux differencing on triangles whose volume and
+  // facet nodes fit in the node slots of 16 threads: two teams share a warp,
+  // so loops over N_p or N_f outputs leave fewer lanes of each warp idle
+  // (2-D vortex at p = 4: phase A 0.212 -> 0.178 ms, phase B 0.428 -> 0.396
+  // ms; at p = 2 on tets phase B was 43 % slower, and the StandardForm
+  // advection mesh of 512 triangles would fill half as many SMs).
+  const bool narrow = d == 2 && fd && nq + nf <= kMaxNodeSlots * 16;
+  const int tpe = nq < 64 ? (narrow ? 16 : 32) : (nq + nf > 192 ? 256 : 128);
+  auto epb_for = [](int tpe_) { return tpe_ < 128 ? 128 / tpe_ : 1; };
   // doubles of shared memory per element team that keep two blocks per SM
-  auto team_budget = [](int tpe_) {
-    const int epb_ = (tpe_ == 32) ? 4 : 1;
-    return (int)((size_t)110 * 1024 / 8 / epb_);
-  };
+  auto team_budget = [&](int tpe_) { return (int)((size_t)110 * 1024 / 8 / epb_for(tpe_)); };
   if (nq + nf > kMaxNodeSlots * tpe)
     return fail(s, SSE_ERR_UNSUPPORTED, "n_q + n_f too large for one element team");
   int zsz = 0, wsz = 0;
@@ -537,7 +542,7 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
       // chunks of at least one pass of the element's threads: two blocks per
       // SM when that leaves room for them, else one block per SM
       const int fixed = layout(0) - ((std::max(0, final_scratch) + 1) & ~1);
-      const int cap1 = (int)((size_t)220 * 1024 / 8 / ((tpe == 32) ? 4 : 1));
+      const int cap1 = (int)((size_t)220 * 1024 / 8 / epb_for(tpe));
       int room = budget - fixed;
       if (room / nc < std::min(tpe, max_pairs)) room = cap1 - fixed;
       chunk = std::max(1, room / nc);
@@ -548,18 +553,28 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
     ka.vdm_zsz = zsz_e;
     layout(chunk);
     // the interface flux of one facet node costs about 0.8 of a volume pair
-    // (block timings at p = 4): balance lanes when all pairs are one chunk
+    // (block timings at p = 4): balance lanes when all pairs are one chunk.
+    // Teams narrower than a warp share warps, and a warp waits for its
+    // slowest lane: there the split is kept only when the lanes left for the
+    // rest of the pairs finish no later than all lanes taking the pairs and
+    // the interface flux in turn
     ka.vp_split = 0;
     if (chunk >= op.nvp && nf < tpe && op.nvp > 0) {
       const double unit = (op.nvp + 0.8 * nf) / tpe;
       int a = (int)std::lround(unit - 0.8);
       a = std::max(0, std::min(a, op.nvp / nf));
+      if (tpe < 32) {
+        const int rest = tpe - nf;
+        const double split_cost = std::max(a + 0.8, (double)((op.nvp - a * nf + rest - 1) / rest));
+        const double plain_cost = (double)((op.nvp + tpe - 1) / tpe) + 0.8;
+        if (split_cost > plain_cost) a = 0;
+      }
       ka.vp_split = a;
     }
   } else {
     finish(ka.layB, {nc * nq, nc * nf, nc * nf, nc * nq, d * nc * nq, nc * nq, nc * nq, 0, zsz, wsz});
   }
-  int epb = (tpe == 32) ? 4 : 1;
+  int epb = epb_for(tpe);
   const size_t smem_cap = 220 * 1024;
   while (epb > 1 && (size_t)epb * std::max(ka.layA.team_doubles, ka.layB.team_doubles) * 8 > smem_cap) epb /= 2;
   if ((size_t)epb * std::max(ka.layA.team_doubles, ka.layB.team_doubles) * 8 > smem_cap)
@@ -687,7 +702,12 @@ int enable_mixed(sse_solver *s) {
   const int zsz4 = r4(zsz);
   const int final_m = nc * (np + (int)nq) + zsz4 + wsz;
   const int max_pairs = std::max(op.nvp, op.nfp);
-  const int tpe_m = ka.tpb / ka.epb;
+  // phase B in FP32 keeps teams of at least 32 threads in blocks of the same
+  // size (16-thread teams made the 2-D vortex's phase B 39 % slower: it is
+  // latency-bound, and narrower teams lengthen each element's chains)
+  const int tpe_fp64 = ka.tpb / ka.epb;
+  const int tpe_m = std::max(32, tpe_fp64);
+  ka.epb_bm = std::max(1, ka.epb * tpe_fp64 / tpe_m);
   auto layout_m = [&](int chunk) {
     const int sizes[8] = {nc * (int)nq, nc * (int)nf, nc * (int)nf, nc * (int)nq,
                           std::max(chunk * nc, final_m), (int)(d * d * nq),
@@ -698,7 +718,7 @@ int enable_mixed(sse_solver *s) {
     ka.layBm.team_doubles = off;  // counted in floats for this layout
     return off;
   };
-  const int budget_m = (int)((size_t)55 * 1024 / 4 / ka.epb);
+  const int budget_m = (int)((size_t)55 * 1024 / 4 / ka.epb_bm);
   int chunk_m = max_pairs;
   if (layout_m(chunk_m) > budget_m) {
     // four blocks per SM when chunks of at least one pass of the element's
@@ -707,7 +727,7 @@ int enable_mixed(sse_solver *s) {
     const int need = std::min(tpe_m, max_pairs) * nc;
     int room = budget_m - fixed;
     if (room < need) room = 2 * budget_m - fixed;
-    if (room < need) room = (int)((size_t)220 * 1024 / 4 / ka.epb) - fixed;
+    if (room < need) room = (int)((size_t)220 * 1024 / 4 / ka.epb_bm) - fixed;
     chunk_m = std::max(1, room / nc);
     if (chunk_m >= tpe_m) chunk_m = chunk_m / tpe_m * tpe_m;
     chunk_m = std::max(1, std::min(chunk_m, max_pairs));
@@ -715,7 +735,7 @@ int enable_mixed(sse_solver *s) {
   ka.fd_chunk_mixed = chunk_m;
   ka.vdm_zsz_mixed = zsz4;
   const int off = layout_m(chunk_m);
-  size_t smm = (size_t)ka.epb * off * sizeof(float);
+  size_t smm = (size_t)ka.epb_bm * off * sizeof(float);
   if (smm > 220 * 1024) return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed kernel");
   if ((e = sse_set_smem_limit_mixed(ka, smm))) return cuda_fail(s, e, "cudaFuncSetAttribute");
   if (op.has_vdm) {

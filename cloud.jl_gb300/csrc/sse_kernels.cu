@@ -1266,9 +1266,14 @@ cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st) {
   int grid = (ka.ne + ka.epb - 1) / ka.epb;
   size_t sm = (size_t)ka.epb * ka.layB.team_doubles * sizeof(double);
   if (ka.mixed) {
-    size_t smm = (size_t)ka.epb * ka.layBm.team_doubles * sizeof(float);
-    if (ka.op.d == 2 && ka.op.nc == 4) fd_time_derivative_mixed_kernel<2, 4><<<grid, ka.tpb, smm, st>>>(ka);
-    else if (ka.op.d == 3 && ka.op.nc == 5) fd_time_derivative_mixed_kernel<3, 5><<<grid, ka.tpb, smm, st>>>(ka);
+    // the FP32 phase B has its own team geometry (epb_bm elements per block
+    // of the same tpb threads)
+    KernelArgs km = ka;
+    km.epb = ka.epb_bm;
+    const int gridm = (ka.ne + km.epb - 1) / km.epb;
+    size_t smm = (size_t)km.epb * ka.layBm.team_doubles * sizeof(float);
+    if (ka.op.d == 2 && ka.op.nc == 4) fd_time_derivative_mixed_kernel<2, 4><<<gridm, ka.tpb, smm, st>>>(km);
+    else if (ka.op.d == 3 && ka.op.nc == 5) fd_time_derivative_mixed_kernel<3, 5><<<gridm, ka.tpb, smm, st>>>(km);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
   }
