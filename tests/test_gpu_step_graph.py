@@ -71,3 +71,42 @@ def test_snapshot_hook(scheme, device, gpu_lib, pkg):
         assert np.array_equal(res[i], G.residual(w))
     G.rk_steps(w, 1, dt, scheme)
     assert np.array_equal(u, w)
+
+
+# Carpenter & Kennedy (1994) five-stage fourth-order 2N-storage coefficients
+_CK_A = (0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+         -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0)
+_CK_B = (1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+         1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+         2277821191437.0 / 14882151754819.0)
+
+
+@pytest.mark.parametrize("name,mixed", [("vortex_tri_modal", False), ("tgv_tet_modal", False),
+                                        ("vortex_tri_modal", True), ("tgv_tet_modal", True)])
+def test_ck_steps_match_explicit_stages(name, mixed, gpu_lib, pkg):
+    """sse_rk_steps' CarpenterKennedy2N54 steps (residual kernels and the
+    stage-update kernel replayed as one captured step) equal the explicit
+    low-storage recurrence tmp = a tmp + dt r, u += b tmp on residuals
+    evaluated one call at a time, up to the rounding of the stage arithmetic
+    (contracted multiply-adds, compensated summation in the mixed form,
+    whose FP32 perturbations can round differently once the states differ
+    in their last bits)."""
+    import torch
+    host, u0 = cases.make(name)
+    G = pkg.GB300Solver(host)
+    if mixed:
+        G.set_precision(pkg.abi.SSE_MIXED)
+    dt = 1e-3
+    fused = torch.from_numpy(u0.copy()).cuda()
+    G.rk_steps(fused, 2, dt, 0)
+    u = torch.from_numpy(u0.copy()).cuda()
+    tmp = torch.zeros_like(u)
+    for _ in range(2):
+        for a, b in zip(_CK_A, _CK_B):
+            r = G.residual(u)
+            tmp = a * tmp + dt * r
+            u = u + b * tmp
+    torch.cuda.synchronize()
+    change = float(torch.linalg.norm(u - torch.from_numpy(u0).cuda()))
+    assert change > 0
+    assert float(torch.linalg.norm(fused - u)) <= (1e-5 if mixed else 1e-11) * change
