@@ -584,11 +584,13 @@ def main():
                  "residual_rel_err_vs_fp64": res_err,
                  "conservation_residual_fp64_reduction": [float(x) for x in cons[: host.N_c]],
                  "entropy_production_fp64_reduction": float(cons[host.N_c]),
-                 "phase_ms": {"nodal_values_fp64": mphases[0], "time_derivative_fp32": mphases[1],
+                 "phase_ms": {"nodal_values_fp32": mphases[0], "time_derivative_fp32": mphases[1],
                               "rk_stage_update_compensated": mphases[2]},
-                 "precision": "entropy projection FP64; fluxes, flux differencing, facet correction, "
-                              "lifting and mass solve FP32 on perturbations from a constant reference "
-                              "state; FP64 compensated stage accumulation and reductions"}
+                 "precision": "entropy projection (V, entropy-variable maps, weight-adjusted projection, "
+                              "R) FP32 on perturbations from a constant reference state, the projection "
+                              "of the constant function FP64; fluxes, flux differencing, facet "
+                              "correction, lifting and mass solve FP32 on perturbations; FP64 "
+                              "compensated stage accumulation and reductions"}
     except pkg.SSEError as ex:
         mixed = {"unavailable": str(ex)}
         gpu.set_precision(abi.SSE_FP64)

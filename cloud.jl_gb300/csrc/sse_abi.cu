@@ -813,10 +813,8 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
     for (int e = 0; e < 5; ++e) ph.u_ref_modal[e] = s->phi0 != 0.0 ? uref[e] / s->phi0 : 0.0;
     ph.ip_ref = 1.0 / ph.p_ref;
     ph.irho_ref = 1.0 / ph.rho_ref;
-    ph.s_ref = std::log(ph.p_ref) - ph.gamma * std::log(ph.rho_ref);
     ph.a_ref = -ph.gm1 * ph.w_ref[c.n_c - 1];
     ph.ia_ref = 1.0 / ph.a_ref;
-    ph.sv_ref = ph.gamma - ph.gm1 * ph.w_ref[0];
     ph.rhoe_ref = ph.E_ref;  // internal energy p_ref / (gamma - 1) at zero velocity
   }
   if (!(ph.rho_ref > 0.0) || !(ph.p_ref > 0.0))

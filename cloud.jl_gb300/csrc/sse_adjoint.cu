@@ -1146,7 +1146,10 @@ __global__ void __launch_bounds__(256) adj_flux_mixed_kernel(KernelArgs ka) {
   }
 }
 
-// transpose of the mixed-form entropy projection (nodal_values_mixed_kernel)
+// transpose of the mixed-form entropy projection (nodal_values_mixed_kernel):
+// the forward recompute uses the same FP32 perturbation maps, and the
+// entropy-map Jacobians (symmetric, so the transposes are JVPs) are applied in
+// FP32 at the absolute FP32 states
 template <int D, int NC>
 __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka) {
   static_assert(NC == D + 2, "mixed form of the Euler entropy projection");
@@ -1177,16 +1180,17 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   }
   __syncthreads();
   vdm_mul<float, D, NC>(op, U1, Q0, Zf, Wf, lane, tpe);  // u_q0'
+  const EntropyRefF cr = entropy_ref_f(ph);
+  const float gam = (float)ph.gamma, gm1 = (float)ph.gm1, igm1 = (float)ph.igm1;
+  const float E_ref = (float)ph.E_ref;
   for (int i = lane; i < nq; i += tpe) {
-    double ui[NC], wi[NC];
+    float ui[NC], wi[NC];
 #pragma unroll
-    for (int e = 0; e < NC; ++e) {
-      const double ref = (e == 0) ? ph.rho_ref : ((e == NC - 1) ? ph.E_ref : 0.0);
-      ui[e] = ref + (double)Q0[e * nq + i];
-    }
-    cons_to_entropy_mixed<D>(ph, ui, wi);
+    for (int e = 0; e < NC; ++e) ui[e] = Q0[e * nq + i];
+    cons_to_entropy_pert<D>(cr, ui, wi);
+    const float wj = (float)WJ[i];
 #pragma unroll
-    for (int e = 0; e < NC; ++e) XQ[e * nq + i] = (float)(WJ[i] * (wi[e] - ph.w_ref[e]));
+    for (int e = 0; e < NC; ++e) XQ[e * nq + i] = wj * wi[e];
   }
   __syncthreads();
   vdm_tmul<float, D, NC>(op, XQ, T1, Zf, Wf, lane, tpe);
@@ -1201,20 +1205,22 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   for (int t = lane; t < nq + nf; t += tpe) {
     const bool vol = t < nq;
     const int r = vol ? t : t - nq;
-    const double p1 = vol ? P1[r] : RP1[r];
+    const float p1m1 = (float)((vol ? P1[r] : RP1[r]) - 1.0);
     const float *src = vol ? WQ + r : WF + r;
     const int stride = vol ? nq : nf;
-    double wi[NC], bi[NC], ri[NC];
+    float dwi[NC], wi[NC], bi[NC], ri[NC];
 #pragma unroll
     for (int e = 0; e < NC; ++e) {
-      wi[e] = fma(ph.w_ref[e], p1, (double)src[e * stride]);
-      bi[e] = vol ? (double)ubq[(size_t)kk * NC * nq + e * nq + r] : (double)ubf[((size_t)kk * NC + e) * nf + r];
+      dwi[e] = fmaf(cr.w_ref[e], p1m1, src[e * stride]);
+      wi[e] = cr.w_ref[e] + dwi[e];
+      bi[e] = vol ? ubq[(size_t)kk * NC * nq + e * nq + r] : ubf[((size_t)kk * NC + e) * nf + r];
     }
-    const double rhoe = entropy_to_cons_mixed_rhoe<D>(ph, wi);
-    entropy_to_cons_jvp_rhoe<D>(ph.gm1, ph.igm1, ph.gamma, wi, rhoe, bi, ri);
+    float alpha, beta, kin;
+    entropy_pert_core<D>(cr, dwi, alpha, beta, kin);
+    entropy_to_cons_jvp_rhoe_f<D>(gm1, igm1, gam, wi, cr.rhoe_ref * (1.f + beta), bi, ri);
     float *dst = vol ? S1 + r : BF + r;
 #pragma unroll
-    for (int e = 0; e < NC; ++e) dst[e * stride] = (float)ri[e];
+    for (int e = 0; e < NC; ++e) dst[e * stride] = ri[e];
   }
   __syncthreads();
   // wbar_q += R^T wbar_f
@@ -1226,16 +1232,17 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   vdm_mul<float, D, NC>(op, T1, XQ, Zf, Wf, lane, tpe);
   // ubar_q0 = J_c2e(u_q0)^T (W J x), symmetric Jacobian
   for (int i = lane; i < nq; i += tpe) {
-    double ui[NC], bi[NC], ri[NC];
+    float ui[NC], bi[NC], ri[NC];
+    const float wj = (float)WJ[i];
 #pragma unroll
     for (int e = 0; e < NC; ++e) {
-      const double ref = (e == 0) ? ph.rho_ref : ((e == NC - 1) ? ph.E_ref : 0.0);
-      ui[e] = ref + (double)Q0[e * nq + i];
-      bi[e] = WJ[i] * (double)XQ[e * nq + i];
+      const float ref = (e == 0) ? cr.rho_ref : ((e == NC - 1) ? E_ref : 0.f);
+      ui[e] = ref + Q0[e * nq + i];
+      bi[e] = wj * XQ[e * nq + i];
     }
-    cons_to_entropy_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ui, bi, ri);
+    cons_to_entropy_jvp_f<D>(gam, gm1, igm1, ui, bi, ri);
 #pragma unroll
-    for (int e = 0; e < NC; ++e) XQ[e * nq + i] = (float)ri[e];
+    for (int e = 0; e < NC; ++e) XQ[e * nq + i] = ri[e];
   }
   __syncthreads();
   vdm_tmul<float, D, NC>(op, XQ, T1, Zf, Wf, lane, tpe);  // mu = V^T ubar_q0

@@ -126,9 +126,7 @@ struct Physics {
   int mode0;         // modal index of the constant basis function
   double u_ref_modal[5];
   double ip_ref, irho_ref;  // 1 / p_ref, 1 / rho_ref
-  double s_ref;             // log(p_ref) - gamma log(rho_ref)
   double a_ref, ia_ref;     // a_ref and 1 / a_ref with a = -(gamma-1) w_E
-  double sv_ref;            // gamma - (gamma-1) w_0 of the reference state
   double rhoe_ref;          // (rho e) of the reference state: p_ref / (gamma-1)
 };
 
@@ -483,64 +481,6 @@ SSE_HD void entropy_to_cons_jvp(double gamma, double gm1, double igm1, double lo
 }
 
 // ---------------------------------------------------------------------------
-// Mixed-form entropy-variable maps: the algebra in FP64, the logarithms and
-// the exponential of the small relative deviations from the reference state
-// in FP32 (log1pf / expm1f), so their error is relative to the deviation:
-//   log p - gamma log rho = s_ref + log1p(dp/p_ref) - gamma log1p(drho/rho_ref)
-//   rho e = rhoe_ref exp(dX),  dX = (-gamma log(a/a_ref) - (sv - sv_ref))/(gamma-1)
-// (euler_navierstokes.jl:100-131).
-// ---------------------------------------------------------------------------
-// FP64 reciprocal for the mixed form's entropy maps: the FP32 reciprocal
-// refined by one Newton-Raphson step r + r (1 - x r), relative error about
-// the square of the FP32 one (~1e-14); x within the FP32 range (densities,
-// pressures and entropy variables of physical states).
-SSE_HD double rcp_refined(double x) {
-#ifdef __CUDA_ARCH__
-  const double r = (double)__frcp_rn((float)x);
-  return fma(r, fma(-x, r, 1.0), r);
-#else
-  return 1.0 / x;
-#endif
-}
-
-template <int D>
-__device__ __forceinline__ void cons_to_entropy_mixed(const Physics &ph, const double *u, double *w) {
-  double s2 = 0.0;
-#pragma unroll
-  for (int m = 0; m < D; ++m) s2 = fma(u[m + 1], u[m + 1], s2);
-  const double k = 0.5 * s2 * rcp_refined(u[0]);
-  const double p = ph.gm1 * (u[D + 1] - k);
-  const double ip = rcp_refined(p);
-  const float lp = log1pf((float)((p - ph.p_ref) * ph.ip_ref));
-  const float lr = log1pf((float)((u[0] - ph.rho_ref) * ph.irho_ref));
-  const double ls = ph.s_ref + (double)lp - ph.gamma * (double)lr;
-  w[0] = fma(ph.igm1, ph.gamma - ls, -k * ip);
-#pragma unroll
-  for (int m = 0; m < D; ++m) w[m + 1] = u[m + 1] * ip;
-  w[D + 1] = -u[0] * ip;
-}
-
-template <int D>
-__device__ __forceinline__ void entropy_to_cons_mixed(const Physics &ph, const double *w_in, double *u) {
-  double wg[D + 2];
-#pragma unroll
-  for (int e = 0; e < D + 2; ++e) wg[e] = w_in[e] * ph.gm1;
-  double s2 = 0.0;
-#pragma unroll
-  for (int m = 0; m < D; ++m) s2 = fma(wg[m + 1], wg[m + 1], s2);
-  const double k = 0.5 * s2 * rcp_refined(wg[D + 1]);
-  const double sv = ph.gamma - wg[0] + k;
-  const double a = -wg[D + 1];
-  const float la = log1pf((float)((a - ph.a_ref) * ph.ia_ref));
-  const double dX = ph.igm1 * (-ph.gamma * (double)la - (sv - ph.sv_ref));
-  const double rhoe = fma(ph.rhoe_ref, (double)expm1f((float)dX), ph.rhoe_ref);
-  u[0] = a * rhoe;
-#pragma unroll
-  for (int m = 0; m < D; ++m) u[m + 1] = wg[m + 1] * rhoe;
-  u[D + 1] = rhoe * (1.0 - k);
-}
-
-// ---------------------------------------------------------------------------
 // Mixed form: FP32 arithmetic on perturbations u' = u - u_ref from a constant
 // reference state u_ref = (rho_ref, 0, ..., 0, E_ref) with p_ref =
 // (gamma - 1) E_ref.  At Mach 0.1 the pressure (~71) exceeds its fluctuations
@@ -597,6 +537,134 @@ SSE_HD float inv_logmean_mixed(float x, float y) {
 // correction, interface flux including its dissipation) is reduced the same
 // way, so the energy residual equals H_ref times the density residual plus
 // the residual of the reduced fluxes; that sum is formed in FP64 at the end.
+
+// Constants of the FP32 perturbation entropy maps, rounded once from the FP64
+// reference state (w_ref: its entropy variables).
+struct EntropyRefF {
+  float gamma, gm1, igm1, rho_ref, p_ref, ip_ref, irho_ref, a_ref, ia_ref, rhoe_ref;
+  float w_ref[5];
+};
+
+SSE_HD EntropyRefF entropy_ref_f(const Physics &ph) {
+  EntropyRefF c;
+  c.gamma = (float)ph.gamma;
+  c.gm1 = (float)ph.gm1;
+  c.igm1 = (float)ph.igm1;
+  c.rho_ref = (float)ph.rho_ref;
+  c.p_ref = (float)ph.p_ref;
+  c.ip_ref = (float)ph.ip_ref;
+  c.irho_ref = (float)ph.irho_ref;
+  c.a_ref = (float)ph.a_ref;
+  c.ia_ref = (float)ph.ia_ref;
+  c.rhoe_ref = (float)ph.rhoe_ref;
+  for (int e = 0; e < 5; ++e) c.w_ref[e] = (float)ph.w_ref[e];
+  return c;
+}
+
+// Entropy variables as perturbations, in FP32: dw = w(u_ref + du) - w_ref for
+// du = u - u_ref (cons_to_entropy, euler_navierstokes.jl:100-115).  Every term
+// is formed from perturbations -- s - s_ref = log1p(dp/p_ref) - gamma
+// log1p(drho/rho_ref), rho/p - rho_ref/p_ref = (drho - rho_ref dp/p_ref)/p --
+// so FP32 keeps its relative accuracy on dw, which is small where the flow is
+// near the reference state (no difference of two O(1) entropy variables).
+template <int D>
+SSE_HD void cons_to_entropy_pert(const EntropyRefF &c, const float *du, float *dw) {
+  float s2 = 0.f;
+#pragma unroll
+  for (int m = 0; m < D; ++m) s2 = fmaf(du[m + 1], du[m + 1], s2);
+  const float k = 0.5f * sse_fdiv(s2, c.rho_ref + du[0]);   // kinetic energy
+  const float dp = c.gm1 * (du[D + 1] - k);                   // p - p_ref
+  const float ip = sse_fdiv(1.f, c.p_ref + dp);
+  const float dpr = dp * c.ip_ref;
+  const float ds = log1pf(dpr) - c.gamma * log1pf(du[0] * c.irho_ref);  // s - s_ref
+  dw[0] = -fmaf(c.igm1, ds, k * ip);
+#pragma unroll
+  for (int m = 0; m < D; ++m) dw[m + 1] = du[m + 1] * ip;
+  dw[D + 1] = -fmaf(-c.rho_ref, dpr, du[0]) * ip;
+}
+
+// Conservative perturbations from entropy-variable perturbations, in FP32:
+// du = u(w_ref + dw) - u_ref (entropy_to_cons, euler_navierstokes.jl:117-131).
+// With a = -(gamma-1) w_E = a_ref (1 + alpha), k = |(gamma-1) w_m|^2 / (2 (gamma-1)
+// w_E) and (rho e) = (rho e)_ref (1 + beta):  drho = rho_ref (alpha + beta +
+// alpha beta), m = (gamma-1) w_m (rho e), dE = (rho e)_ref (beta - k (1 + beta)).
+template <int D>
+SSE_HD void entropy_pert_core(const EntropyRefF &c, const float *dw, float &alpha, float &beta, float &k) {
+  float s2 = 0.f;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    const float g = c.gm1 * dw[m + 1];
+    s2 = fmaf(g, g, s2);
+  }
+  const float gw = c.gm1 * dw[D + 1];
+  alpha = -gw * c.ia_ref;                                      // a / a_ref - 1
+  k = -0.5f * sse_fdiv(s2, c.a_ref - gw);
+  const float dX = dw[0] - c.igm1 * fmaf(c.gamma, log1pf(alpha), k);
+  beta = expm1f(dX);                                           // (rho e) / (rho e)_ref - 1
+}
+
+template <int D>
+SSE_HD void entropy_to_cons_pert(const EntropyRefF &c, const float *dw, float *du) {
+  float alpha, beta, k;
+  entropy_pert_core<D>(c, dw, alpha, beta, k);
+  const float rhoe = c.rhoe_ref * (1.f + beta);
+  du[0] = c.rho_ref * fmaf(alpha, beta, alpha + beta);
+#pragma unroll
+  for (int m = 0; m < D; ++m) du[m + 1] = c.gm1 * dw[m + 1] * rhoe;
+  du[D + 1] = c.rhoe_ref * fmaf(-k, 1.f + beta, beta);
+}
+
+// FP32 JVPs of the entropy-variable maps for the mixed-form VJP (both
+// Jacobians are symmetric, so the transposes are these JVPs), at absolute
+// FP32 states: the Jacobian entries are O(1) functions of the state, which
+// FP32 resolves to its own relative accuracy.  Same formulas as
+// cons_to_entropy_jvp and entropy_to_cons_jvp, the latter given rho e.
+template <int D>
+SSE_HD void cons_to_entropy_jvp_f(float gamma, float gm1, float igm1, const float *u, const float *du,
+                                  float *dw) {
+  const float rho = u[0], rr = sse_fdiv(1.f, rho);
+  float s = 0.f, vdm = 0.f;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    s = fmaf(u[m + 1], u[m + 1], s);
+    vdm = fmaf(u[m + 1] * rr, du[m + 1], vdm);
+  }
+  const float k = 0.5f * s * rr;
+  const float dk = vdm - 0.5f * s * rr * rr * du[0];
+  const float p = gm1 * (u[D + 1] - k);
+  const float dp = gm1 * (du[D + 1] - dk);
+  const float ip = sse_fdiv(1.f, p);
+  dw[0] = -igm1 * (dp * ip - gamma * du[0] * rr) - (dk * ip - k * dp * ip * ip);
+#pragma unroll
+  for (int m = 0; m < D; ++m) dw[m + 1] = du[m + 1] * ip - u[m + 1] * dp * ip * ip;
+  dw[D + 1] = -du[0] * ip + rho * dp * ip * ip;
+}
+
+template <int D>
+SSE_HD void entropy_to_cons_jvp_rhoe_f(float gm1, float igm1, float gamma, const float *w_in, float rhoe,
+                                       const float *dw_in, float *du) {
+  float w[D + 2], dw[D + 2];
+#pragma unroll
+  for (int e = 0; e < D + 2; ++e) {
+    w[e] = w_in[e] * gm1;
+    dw[e] = dw_in[e] * gm1;
+  }
+  float s = 0.f, ds = 0.f;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    s = fmaf(w[m + 1], w[m + 1], s);
+    ds = fmaf(w[m + 1], dw[m + 1], ds);
+  }
+  const float iwE = sse_fdiv(1.f, w[D + 1]);
+  const float k = 0.5f * s * iwE;
+  const float dk = ds * iwE - k * dw[D + 1] * iwE;
+  const float dsv = -dw[0] + dk;
+  const float drhoe = rhoe * igm1 * (-gamma * dw[D + 1] * iwE - dsv);
+  du[0] = -dw[D + 1] * rhoe - w[D + 1] * drhoe;
+#pragma unroll
+  for (int m = 0; m < D; ++m) du[m + 1] = dw[m + 1] * rhoe + w[m + 1] * drhoe;
+  du[D + 1] = drhoe * (1.f - k) - rhoe * dk;
+}
 
 // FP32 primitives from a perturbation du = u - u_ref, layout
 // [rho, rho - rho_ref, theta - theta_ref, V_1..V_D, p - p_ref].
@@ -809,50 +877,6 @@ SSE_HD void euler_prim_mixed_bwd(float gm1, float theta_ref, const float *P, con
   ub[D + 1] += gm1 * pb;
 }
 
-// (rho e) of entropy_to_cons_mixed(w) alone
-template <int D>
-__device__ __forceinline__ double entropy_to_cons_mixed_rhoe(const Physics &ph, const double *w_in) {
-  double wg[D + 2];
-#pragma unroll
-  for (int e = 0; e < D + 2; ++e) wg[e] = w_in[e] * ph.gm1;
-  double s2 = 0.0;
-#pragma unroll
-  for (int m = 0; m < D; ++m) s2 = fma(wg[m + 1], wg[m + 1], s2);
-  const double k = 0.5 * s2 * sse_rcp(wg[D + 1]);
-  const double sv = ph.gamma - wg[0] + k;
-  const double a = -wg[D + 1];
-  const float la = log1pf((float)((a - ph.a_ref) * ph.ia_ref));
-  const double dX = ph.igm1 * (-ph.gamma * (double)la - (sv - ph.sv_ref));
-  return fma(ph.rhoe_ref, (double)expm1f((float)dX), ph.rhoe_ref);
-}
-
-// Directional derivative of entropy_to_cons at w along dw given rhoe
-// (the internal energy rho e of the state, from entropy_to_cons_mixed)
-template <int D>
-SSE_HD void entropy_to_cons_jvp_rhoe(double gm1, double igm1, double gamma, const double *w_in,
-                                     double rhoe, const double *dw_in, double *du) {
-  double w[D + 2], dw[D + 2];
-#pragma unroll
-  for (int e = 0; e < D + 2; ++e) {
-    w[e] = w_in[e] * gm1;
-    dw[e] = dw_in[e] * gm1;
-  }
-  double s = 0.0, ds = 0.0;
-#pragma unroll
-  for (int m = 0; m < D; ++m) {
-    s = fma(w[m + 1], w[m + 1], s);
-    ds = fma(w[m + 1], dw[m + 1], ds);
-  }
-  const double iwE = sse_rcp(w[D + 1]);
-  const double k = 0.5 * s * iwE;
-  const double dk = ds * iwE - k * dw[D + 1] * iwE;
-  const double dsv = -dw[0] + dk;
-  const double drhoe = rhoe * igm1 * (-gamma * dw[D + 1] * iwE - dsv);
-  du[0] = -dw[D + 1] * rhoe - w[D + 1] * drhoe;
-#pragma unroll
-  for (int m = 0; m < D; ++m) du[m + 1] = dw[m + 1] * rhoe + w[m + 1] * drhoe;
-  du[D + 1] = drhoe * (1 - k) - rhoe * dk;
-}
 
 // Primitive quantities of one Euler state, computed once per node so that
 // the pairwise loops do no per-pair divisions for them.

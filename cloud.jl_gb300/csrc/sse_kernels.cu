@@ -181,7 +181,9 @@ __device__ void facet_flux(const KernelArgs &ka, int kk, const double *uf, doubl
 //   P w = w_ref P(1) + P(w - w_ref):
 // P(1) and R P(1) are precomputed per element in FP64, and P is applied in
 // FP32 only to the perturbation w - w_ref, which is small where the flow is
-// near the reference state.  V u and the entropy-variable maps stay FP64.
+// near the reference state.  V u runs in FP32 on u - u_ref, and both
+// entropy-variable maps run in FP32 on perturbations (cons_to_entropy_pert,
+// entropy_to_cons_pert), so the kernel has almost no FP64 work.
 // ---------------------------------------------------------------------------
 template <int D, int NC>
 __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) {
@@ -211,18 +213,17 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
   }
   __syncthreads();
   vdm_mul<float, D, NC>(op, Cf, Bf, Zf, Wf, lane, tpe);
-  // x' = W J (c2e(u_q) - w_ref), rounded to FP32
+  const EntropyRefF cr = entropy_ref_f(ph);
+  // x' = W J (c2e(u_q) - w_ref)
   for (int i = lane; i < nq; i += tpe) {
-    double ui[NC], wi[NC];
+    float ui[NC], wi[NC];
 #pragma unroll
-    for (int e = 0; e < NC; ++e) {
-      const double ref = (e == 0) ? ph.rho_ref : ((e == NC - 1) ? ph.E_ref : 0.0);
-      ui[e] = ref + (double)Bf[e * nq + i];
-    }
-    if (!(ui[0] > 0.0)) ka.flag_nonphysical();
-    cons_to_entropy_mixed<D>(ph, ui, wi);
+    for (int e = 0; e < NC; ++e) ui[e] = Bf[e * nq + i];
+    if (!(cr.rho_ref + ui[0] > 0.f)) ka.flag_nonphysical();
+    cons_to_entropy_pert<D>(cr, ui, wi);
+    const float wj = (float)WJ[i];
 #pragma unroll
-    for (int e = 0; e < NC; ++e) Af[e * nq + i] = (float)(WJ[i] * (wi[e] - ph.w_ref[e]));
+    for (int e = 0; e < NC; ++e) Af[e * nq + i] = wj * wi[e];
   }
   __syncthreads();
   vdm_tmul<float, D, NC>(op, Af, Cf, Zf, Wf, lane, tpe);                               // V^T x'
@@ -231,22 +232,25 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
   csr_mul<float, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_valf, Bf, Af, lane, tpe);        // w'_f
   __syncthreads();
   const double *P1 = ka.geo.P1 + (size_t)kk * nq, *RP1 = ka.geo.RP1 + (size_t)kk * nf;
+  // w - w_ref = w_ref (P(1) - 1) + P(w - w_ref) at the volume and facet
+  // nodes; u' = e2c(w) - u_ref, stored as the FP32 states of phase B
   for (int t = lane; t < nq + nf; t += tpe) {
     const bool vol = t < nq;
     const int r = vol ? t : t - nq;
-    const double p1 = vol ? P1[r] : RP1[r];
+    const float p1m1 = (float)((vol ? P1[r] : RP1[r]) - 1.0);
     const float *src = vol ? Bf + r : Af + r;
     const int stride = vol ? nq : nf;
-    double wi[NC], ui[NC];
+    float wi[NC], ui[NC];
 #pragma unroll
-    for (int e = 0; e < NC; ++e) wi[e] = fma(ph.w_ref[e], p1, (double)src[e * stride]);
-    entropy_to_cons_mixed<D>(ph, wi, ui);
+    for (int e = 0; e < NC; ++e) wi[e] = fmaf(cr.w_ref[e], p1m1, src[e * stride]);
+    entropy_to_cons_pert<D>(cr, wi, ui);
     const size_t o = (size_t)kk * NC * (vol ? nq : nf) + r;
+    float *dst = vol ? ka.u_qf : ka.u_ff;
+    if (!(cr.rho_ref + ui[0] > 0.f)) ka.flag_nonphysical();
 #pragma unroll
     for (int e = 0; e < NC; ++e) {
-      if (live)
-        store_state<NC>(ka, vol ? ka.u_q : ka.u_f, vol ? ka.u_qf : ka.u_ff, o + (size_t)e * stride, e, ui[e]);
-      if (!(ui[0] > 0.0) || !isfinite(ui[e])) ka.flag_nonphysical();
+      if (live) dst[o + (size_t)e * stride] = ui[e];
+      if (!isfinite(ui[e])) ka.flag_nonphysical();
     }
   }
 }

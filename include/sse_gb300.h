@@ -256,8 +256,9 @@ int32_t sse_conservation_residual(sse_solver *s, const double *u, const double *
 int32_t sse_energy_residual(sse_solver *s, const double *u, const double *dudt, double *out,
                             int32_t memory);
 
-/* SSE_FP64 (default, the drop-in) or SSE_MIXED (FP32 fluxes and operator
- * arithmetic, FP64 geometry, RK accumulation and reductions). */
+/* SSE_FP64 (default, the drop-in) or SSE_MIXED (FP32 fluxes, operator
+ * arithmetic and entropy-variable maps on perturbations from a constant
+ * reference state; FP64 geometry, RK accumulation and reductions). */
 int32_t sse_set_precision(sse_solver *s, int32_t precision);
 
 /* Run this handle's work on the caller's CUDA stream (a cudaStream_t; NULL

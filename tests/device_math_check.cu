@@ -310,9 +310,96 @@ static void check_mixed_adjoint(std::mt19937_64 &rng, double *worst) {
   }
 }
 
+// FP32 perturbation entropy maps of the mixed form's phase A against the
+// FP64 maps: dw = w(u_ref + du) - w_ref and du = u(w_ref + dw) - u_ref, with
+// the FP32 inputs taken exactly, relative to the largest component of the
+// perturbation.  Low-Mach states (pressure 71.4, unit velocities) with
+// density and pressure perturbations of 0.1 %, 3 % and 30 %.
+template <int D>
+static void check_entropy_pert(std::mt19937_64 &rng, double *worst) {
+  const double g = 1.4, gm1 = g - 1, igm1 = 1 / gm1, lg = std::log(gm1);
+  std::uniform_real_distribution<double> U(-1, 1);
+  Physics ph{};
+  ph.gamma = g; ph.gm1 = gm1; ph.igm1 = igm1;
+  ph.rho_ref = 1.0; ph.E_ref = 71.4 / gm1; ph.p_ref = gm1 * ph.E_ref;
+  double uref[D + 2] = {};
+  uref[0] = ph.rho_ref;
+  uref[D + 1] = ph.E_ref;
+  cons_to_entropy_fast<D>(g, gm1, igm1, uref, ph.w_ref);
+  ph.ip_ref = 1 / ph.p_ref;
+  ph.irho_ref = 1 / ph.rho_ref;
+  ph.a_ref = -gm1 * ph.w_ref[D + 1];
+  ph.ia_ref = 1 / ph.a_ref;
+  ph.rhoe_ref = ph.E_ref;
+  const EntropyRefF c = entropy_ref_f(ph);
+  for (int trial = 0; trial < 30000; ++trial) {
+    const double amp = (trial % 3 == 0) ? 1e-3 : ((trial % 3 == 1) ? 3e-2 : 0.3);
+    double u[D + 2];
+    const double rho = 1.0 + amp * U(rng), p = ph.p_ref * (1.0 + amp * U(rng));
+    double ke = 0;
+    u[0] = rho;
+    for (int m = 0; m < D; ++m) { const double v = U(rng); u[m + 1] = rho * v; ke += 0.5 * rho * v * v; }
+    u[D + 1] = p / gm1 + ke;
+    float du[D + 2], dw[D + 2];
+    double ud[D + 2], w[D + 2];
+    for (int e = 0; e < D + 2; ++e) {
+      du[e] = (float)(u[e] - uref[e]);
+      ud[e] = uref[e] + (double)du[e];
+    }
+    cons_to_entropy_fast<D>(g, gm1, igm1, ud, w);
+    cons_to_entropy_pert<D>(c, du, dw);
+    double scale = 0, err = 0;
+    for (int e = 0; e < D + 2; ++e) scale = std::fmax(scale, std::fabs(w[e] - ph.w_ref[e]));
+    for (int e = 0; e < D + 2; ++e) err = std::fmax(err, std::fabs((double)dw[e] - (w[e] - ph.w_ref[e])));
+    worst[11] = std::fmax(worst[11], err / scale);
+    // inverse map from the FP32 rounding of the exact perturbation
+    float dwf[D + 2], dub[D + 2];
+    double wd[D + 2], ub[D + 2];
+    for (int e = 0; e < D + 2; ++e) {
+      dwf[e] = (float)(w[e] - ph.w_ref[e]);
+      wd[e] = ph.w_ref[e] + (double)dwf[e];
+    }
+    // FP32 JVPs of both maps at the absolute FP32 state against the FP64 ones
+    {
+      double v[D + 2], jd[D + 2], jd2[D + 2], rhoe = ud[D + 1];
+      float uf[D + 2], wf[D + 2], vf[D + 2], jf[D + 2], jf2[D + 2];
+      for (int m = 0; m < D; ++m) rhoe -= 0.5 * ud[m + 1] * ud[m + 1] / ud[0];
+      for (int e = 0; e < D + 2; ++e) {
+        v[e] = U(rng);
+        vf[e] = (float)v[e];
+        v[e] = (double)vf[e];
+        uf[e] = (float)ud[e];
+        wf[e] = (float)w[e];
+      }
+      double udf[D + 2], wdf[D + 2];
+      for (int e = 0; e < D + 2; ++e) { udf[e] = (double)uf[e]; wdf[e] = (double)wf[e]; }
+      cons_to_entropy_jvp<D>(g, gm1, igm1, udf, v, jd);
+      cons_to_entropy_jvp_f<D>((float)g, (float)gm1, (float)igm1, uf, vf, jf);
+      entropy_to_cons_jvp<D>(g, gm1, igm1, lg, wdf, v, jd2);
+      entropy_to_cons_jvp_rhoe_f<D>((float)gm1, (float)igm1, (float)g, wf, (float)rhoe, vf, jf2);
+      double s1 = 0, e1 = 0, s2 = 0, e2 = 0;
+      for (int e = 0; e < D + 2; ++e) {
+        s1 = std::fmax(s1, std::fabs(jd[e]));
+        e1 = std::fmax(e1, std::fabs((double)jf[e] - jd[e]));
+        s2 = std::fmax(s2, std::fabs(jd2[e]));
+        e2 = std::fmax(e2, std::fabs((double)jf2[e] - jd2[e]));
+      }
+      worst[13] = std::fmax(worst[13], e1 / s1);
+      worst[14] = std::fmax(worst[14], e2 / s2);
+    }
+    entropy_to_cons_fast<D>(g, gm1, igm1, lg, wd, ub);
+    entropy_to_cons_pert<D>(c, dwf, dub);
+    scale = 0;
+    err = 0;
+    for (int e = 0; e < D + 2; ++e) scale = std::fmax(scale, std::fabs(ub[e] - uref[e]));
+    for (int e = 0; e < D + 2; ++e) err = std::fmax(err, std::fabs((double)dub[e] - (ub[e] - uref[e])));
+    worst[12] = std::fmax(worst[12], err / scale);
+  }
+}
+
 int main() {
   std::mt19937_64 rng(20261203);
-  double worst[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double worst[15] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   check<2>(rng, worst);
   check<3>(rng, worst);
   check_mixed<2>(rng, worst);
@@ -321,11 +408,15 @@ int main() {
   check_adjoint<3>(rng, worst);
   check_mixed_adjoint<2>(rng, worst);
   check_mixed_adjoint<3>(rng, worst);
+  check_entropy_pert<2>(rng, worst);
+  check_entropy_pert<3>(rng, worst);
   std::printf("{\"logmean\": %.3e, \"inv_logmean\": %.3e, \"ec_flux_dot\": %.3e, "
               "\"cons_to_entropy\": %.3e, \"entropy_to_cons\": %.3e, \"mixed_reduced_flux\": %.3e, "
               "\"flux_vjp_vs_fd\": %.3e, \"entropy_jvp_vs_fd\": %.3e, \"entropy_jacobian_symmetry\": %.3e, "
-              "\"mixed_flux_vjp\": %.3e, \"ec_flux_half_mismatches\": %.0f}\n",
+              "\"mixed_flux_vjp\": %.3e, \"ec_flux_half_mismatches\": %.0f, "
+              "\"cons_to_entropy_pert\": %.3e, \"entropy_to_cons_pert\": %.3e, "
+              "\"cons_to_entropy_jvp_f\": %.3e, \"entropy_to_cons_jvp_f\": %.3e}\n",
               worst[0], worst[1], worst[2], worst[3], worst[4], worst[5], worst[6], worst[7], worst[8],
-              worst[9], worst[10]);
+              worst[9], worst[10], worst[11], worst[12], worst[13], worst[14]);
   return 0;
 }
