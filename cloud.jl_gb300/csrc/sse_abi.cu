@@ -753,6 +753,11 @@ int enable_mixed(sse_solver *s) {
     const int nfloats = A.off[9] + ev(wsz);
     for (int i = 10; i < 12; ++i) A.off[i] = 0;
     A.team_doubles = A.off[4] + nfloats / 2;
+    // the FP32 phase A (barrier- and issue-bound) on 128-thread teams, two
+    // elements per block, where the FP64 form uses 256 threads and the
+    // element's volume and facet nodes fit in two passes of 128 (p = 4 tets:
+    // 0.525 -> 0.400 ms per stage; p = 5 unchanged, p = 6 0.57 -> 0.72 ms)
+    ka.epb_am = (tpe_fp64 >= 256 && nq + nf <= 256) ? ka.epb * (tpe_fp64 / 128) : ka.epb;
     int zsz1 = 0, wsz1 = 0;
     if (c.d == 2) zsz1 = op.p1 * op.M2;
     else { zsz1 = op.nb12 * op.M3; wsz1 = op.p1 * op.M2 * op.M3; }
@@ -763,7 +768,7 @@ int enable_mixed(sse_solver *s) {
     for (int i = 0; i < 5; ++i) { P.off[i] = o1; o1 += ev(sizes1[i]); }
     for (int i = 5; i < 12; ++i) P.off[i] = o1;
     P.team_doubles = o1;
-    if ((size_t)ka.epb * std::max(A.team_doubles, P.team_doubles) * 8 > 220 * 1024)
+    if ((size_t)std::max(ka.epb_am * A.team_doubles, ka.epb * P.team_doubles) * 8 > 220 * 1024)
       return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed projection kernel");
     if ((e = sse_set_smem_limits_mixed_a(ka))) return cuda_fail(s, e, "cudaFuncSetAttribute");
     if ((e = alloc(s, nq * ne * sizeof(double), &p))) return cuda_fail(s, e, "alloc");

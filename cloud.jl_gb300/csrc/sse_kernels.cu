@@ -1216,9 +1216,14 @@ cudaError_t sse_set_smem_limits(const KernelArgs &ka, size_t smA, size_t smB) {
 cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st) {
   int grid = (ka.ne + ka.epb - 1) / ka.epb;
   if (ka.mixed && ka.op.has_vdm && ka.geo.P1) {
-    size_t sm = (size_t)ka.epb * ka.layAm.team_doubles * sizeof(double);
-    if (ka.op.d == 2 && ka.op.nc == 4) nodal_values_mixed_kernel<2, 4><<<grid, ka.tpb, sm, st>>>(ka);
-    else if (ka.op.d == 3 && ka.op.nc == 5) nodal_values_mixed_kernel<3, 5><<<grid, ka.tpb, sm, st>>>(ka);
+    // the mixed phase A has its own team geometry (epb_am elements per block
+    // of the same tpb threads)
+    KernelArgs km = ka;
+    km.epb = ka.epb_am;
+    const int grida = (ka.ne + km.epb - 1) / km.epb;
+    size_t sm = (size_t)km.epb * ka.layAm.team_doubles * sizeof(double);
+    if (ka.op.d == 2 && ka.op.nc == 4) nodal_values_mixed_kernel<2, 4><<<grida, ka.tpb, sm, st>>>(km);
+    else if (ka.op.d == 3 && ka.op.nc == 5) nodal_values_mixed_kernel<3, 5><<<grida, ka.tpb, sm, st>>>(km);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
   }
@@ -1237,7 +1242,7 @@ cudaError_t launch_projection_of_one(const KernelArgs &ka, double *P1, double *R
 
 cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka) {
   cudaError_t e = cudaSuccess;
-  const int am = (int)((size_t)ka.epb * ka.layAm.team_doubles * sizeof(double));
+  const int am = (int)((size_t)ka.epb_am * ka.layAm.team_doubles * sizeof(double));
   const int p1 = (int)((size_t)ka.epb * ka.layP1.team_doubles * sizeof(double));
   if (ka.op.d == 2 && ka.op.nc == 4) {
     e = cudaFuncSetAttribute((const void *)nodal_values_mixed_kernel<2, 4>,
