@@ -599,8 +599,14 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking))) return cuda_fail(s, e, "stream");
   s->own_stream = true;
 
+  // phase A on 128-thread teams, two elements per block, where phase B uses
+  // 256 threads and the element's volume and facet nodes fit in two passes
+  // of 128 (p = 4 tets: 3.14 -> 3.09 ms per stage, fewer barrier stalls)
+  ka.epb_a = (tpe >= 256 && nq + nf <= 256) ? epb * (tpe / 128) : epb;
+  if ((size_t)ka.epb_a * ka.layA.team_doubles * 8 > 220 * 1024) ka.epb_a = epb;
   // opt in to large dynamic shared memory for every kernel instantiation used
-  size_t smA = (size_t)epb * ka.layA.team_doubles * 8, smB = (size_t)epb * ka.layB.team_doubles * 8;
+  size_t smA = (size_t)std::max(epb, ka.epb_a) * ka.layA.team_doubles * 8,
+         smB = (size_t)epb * ka.layB.team_doubles * 8;
   if ((e = sse_set_smem_limits(ka, smA, smB)) != cudaSuccess) return cuda_fail(s, e, "cudaFuncSetAttribute");
 
   // the weight-adjusted mass operator V' diag(J^-1 W) V of every element,

@@ -1227,8 +1227,13 @@ cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st) {
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
   }
-  size_t sm = (size_t)ka.epb * ka.layA.team_doubles * sizeof(double);
-  SSE_DISPATCH(D, NC, (nodal_values_kernel<D, NC><<<grid, ka.tpb, sm, st>>>(ka)));
+  // the FP64 phase A has its own team geometry (epb_a elements per block of
+  // the same tpb threads)
+  KernelArgs ka2 = ka;
+  ka2.epb = ka.epb_a;
+  const int grid2 = (ka.ne + ka2.epb - 1) / ka2.epb;
+  size_t sm = (size_t)ka2.epb * ka.layA.team_doubles * sizeof(double);
+  SSE_DISPATCH(D, NC, (nodal_values_kernel<D, NC><<<grid2, ka.tpb, sm, st>>>(ka2)));
   return cudaGetLastError();
 }
 

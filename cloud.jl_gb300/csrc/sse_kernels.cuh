@@ -57,6 +57,7 @@ struct KernelArgs {
   int vp_split;      // volume pairs per interface lane in the one-chunk pass (0: even split)
   int epb_bm;        // elements per block of the FP32 phase-B kernel (blocks of tpb threads)
   int epb_am;        // elements per block of the mixed phase-A kernel (blocks of tpb threads)
+  int epb_a;         // elements per block of the FP64 phase-A kernel (blocks of tpb threads)
   int vdm_zsz;       // doubles of the first sum-factorisation scratch (even)
   int fd_chunk_mixed;  // pairs per chunk in the mixed-form FP32 passes
   Layout layAdjB1m, layAdjB2m, layAdjAm;  // mixed-form VJP layouts (floats)
