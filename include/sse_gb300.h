@@ -141,7 +141,11 @@ int32_t sse_abi_version(void);
 /* Build a handle: validates sizes and indices, deep-copies operators and
  * geometry to the current CUDA device and allocates the per-element scratch
  * (u_q, u_f) that Solver.preallocated_arrays holds in the reference
- * (Solvers.jl:183-209).  Replaces Solver(...) + the Threaded/Serial parallelism
+ * (Solvers.jl:183-209).  With a weight-adjusted mass solver it also builds
+ * each element's mass operator V' diag(J^-1 W) V (N_p x N_p doubles per
+ * element) when they take at most a quarter of the free device memory; the
+ * mass solves are then dense products, otherwise two sum-factorised
+ * applications of V.  Replaces Solver(...) + the Threaded/Serial parallelism
  * tag (Solvers.jl:287-333, 429-452). */
 int32_t sse_create(const sse_config *cfg, const sse_operators *ops,
                    const sse_geometry *geo, sse_solver **out);
