@@ -455,6 +455,50 @@ def geometry_workload(pkg, pb, fp64_peak):
                          "algorithmic_flops_per_element": flops / sd.N_e}}
 
 
+def rel2(got, want) -> float:
+    return float(np.linalg.norm(got - want) / np.linalg.norm(want))
+
+
+def e2e_drop_in(pkg, gpu, pb, host, steps, world):
+    """The drop-in end to end: the Runge-Kutta loop on the host calling the
+    residual through the C-ABI with pinned host buffers once per stage
+    (sse_residual(..., SSE_HOST): H2D of u, both phases, D2H of dudt), the
+    stage arithmetic in place on the host -- what OrdinaryDiffEq does with
+    the ODEProblem of semidiscretize.  Wall-clock seconds over ``steps``."""
+    import torch
+    alg = "RK4" if pb.scheme == 1 else "CarpenterKennedy2N54"
+    ode = pkg.gb300.ODEProblem(pkg.gb300.semi_discrete_residual, torch.from_numpy(pb.u0.copy()).pin_memory(),
+                               (0.0, 1.0), gpu)
+    pkg.timestepping.solve(ode, pb.dt, 1, alg)            # warm-up (pinned buffers, first launches)
+    u = ode.u0.clone().pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pkg.timestepping.solve(ode, pb.dt, steps, alg, u=u)
+    secs = time.perf_counter() - t0
+    nbytes = host.dof * 8 * pb.stages_per_step
+    return {"value": world * host.dof * pb.stages_per_step * steps / secs, "unit": UNIT,
+            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+            "call": f"{alg} on the host, sse_residual(u_host, dudt_host, SSE_HOST) once per stage, "
+                    f"stage updates in place on pinned torch CPU tensors "
+                    f"({torch.get_num_threads()} threads)",
+            "steps": steps, "seconds": secs}
+
+
+def vortex_exact_error(pkg, pb, states, T):
+    """L2 error (ErrorAnalysis, volume quadrature, normalised by the domain
+    volume) of each state against the isentropic vortex advected exactly by
+    the free stream to time T (the reference's ``evaluate`` ignores t)."""
+    ic = pb.initial_data
+    exact = lambda x, t: ic.evaluate(x, t, translated=True)
+    out = {"T": T, "norm": "sqrt(sum_k sum_q W J (u_exact - V u)^2 / |Omega|) per conserved variable"}
+    for key, st in states.items():
+        out[key] = [float(x) for x in pkg.timestepping.l2_error(pb.sd, st, exact, T, normalize=True)]
+    out["l2_err_at_t0"] = [float(x) for x in pkg.timestepping.l2_error(pb.sd, pb.u0, exact, 0.0, normalize=True)]
+    f, m = np.array(out["fp64"]), np.array(out["mixed"])
+    out["mixed_minus_fp64_rel"] = float(np.abs(m - f).max() / np.abs(f).max())
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -544,6 +588,7 @@ def main():
     # initial state, error against the FP64 trajectory at equal step count
     abi = pkg.abi
     mixed = None
+    exact_err = None
     try:
         gpu.set_precision(abi.SSE_MIXED)
         um = torch.from_numpy(pb.u0).cuda()
@@ -564,6 +609,15 @@ def main():
         r_fp64 = gpu.residual(u0d).cpu().numpy()
         state_err = float(torch.linalg.norm(um - u) / torch.linalg.norm(u))
         res_err = float(np.linalg.norm(r_mixed - r_fp64) / np.linalg.norm(r_fp64))
+        # the increment u(T) - u(0): a short run moves the state little, so
+        # the state error alone would hide the error of the residual
+        du64, dum = (u - u0d).cpu().numpy(), (um - u0d).cpu().numpy()
+        inc_err = rel2(dum, du64)
+        inc_comp = [rel2(dum[:, c], du64[:, c]) for c in range(host.N_c)]
+        res_comp = [rel2(r_mixed[:, c], r_fp64[:, c]) for c in range(host.N_c)]
+        if args.workload == "vortex_tri":
+            exact_err = vortex_exact_error(pkg, pb, {"fp64": u.cpu().numpy(), "mixed": um.cpu().numpy()},
+                                           (args.warmup + args.steps) * dt)
         cons = gpu.conservation_residual(u0d, torch.from_numpy(r_mixed).cuda())
         mvalue = world * host.dof * stages * args.steps / (mms * 1e-3)
         # roofline of the FP32 phase B: max(FP32 pipe, HBM) with the
@@ -581,7 +635,10 @@ def main():
                  "speedup_vs_fp64": mvalue / value,
                  "state_rel_err_vs_fp64": state_err,
                  "state_err_after_steps": args.warmup + args.steps,
+                 "increment_rel_err_vs_fp64": inc_err,
+                 "increment_rel_err_per_variable": inc_comp,
                  "residual_rel_err_vs_fp64": res_err,
+                 "residual_rel_err_per_variable": res_comp,
                  "conservation_residual_fp64_reduction": [float(x) for x in cons[: host.N_c]],
                  "entropy_production_fp64_reduction": float(cons[host.N_c]),
                  "phase_ms": {"nodal_values_fp32": mphases[0], "time_derivative_fp32": mphases[1],
@@ -591,6 +648,8 @@ def main():
                               "of the constant function FP64; fluxes, flux differencing, facet "
                               "correction, lifting and mass solve FP32 on perturbations; FP64 "
                               "compensated stage accumulation and reductions"}
+        if exact_err is not None:
+            mixed["exact_solution_error"] = exact_err
     except pkg.SSEError as ex:
         mixed = {"unavailable": str(ex)}
         gpu.set_precision(abi.SSE_FP64)
@@ -606,18 +665,24 @@ def main():
 
     geometry = None if args.no_geometry else geometry_workload(pkg, pb, fp64_peak)
 
-    # ---- end to end through the C-ABI with host (pinned) buffers
+    # ---- end to end through the C-ABI with host (pinned) buffers: the
+    # drop-in as OrdinaryDiffEq drives it (sse_residual on host arrays once
+    # per stage, stage arithmetic on the host), and beside it the fused
+    # device time loop called with a host state once per step
+    e2e_steps = max(2, args.steps // 2)
+    e2e = e2e_drop_in(pkg, gpu, pb, host, e2e_steps, world)
     u_host = torch.from_numpy(pb.u0.copy()).pin_memory()
     gpu.rk_steps(u_host, 1, dt, scheme)
     torch.cuda.synchronize()
-    e2e_steps = max(2, args.steps // 2)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         gpu.rk_steps(u_host, 1, dt, scheme)   # H2D copy, all stages, D2H copy
     e2e_s = time.perf_counter() - t0
     nbytes = host.dof * 8
-    e2e = {"value": world * host.dof * stages * e2e_steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+    e2e_fused = {"value": world * host.dof * stages * e2e_steps / e2e_s, "unit": UNIT,
+                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                 "call": "sse_rk_steps(u_host, 1 step) per step: one H2D and one D2H of the state "
+                         "per step, every stage on the device"}
 
     # per stage: phase A, phase B and one stage-update kernel
     launches = args.steps * stages * 3
@@ -625,7 +690,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args, host, world),
-            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+            "clocks": clocks, "e2e": e2e, "e2e_fused_time_loop": e2e_fused,
+            "gpu_launches": launches, "roofline": roofline,
             "mixed": mixed, "adjoint": adjoint, "geometric_factors": geometry}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pb, host, args.cpu_budget)

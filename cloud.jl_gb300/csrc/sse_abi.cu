@@ -66,6 +66,8 @@ struct sse_solver {
   bool mixed_ready = false; // FP32 copies allocated
   bool ref_ready = false;   // reference state of the mixed form chosen
   double *d_comp = nullptr; // compensation of the mixed form's stage accumulation
+  double *d_rref = nullptr; // FP64 residual of the mixed form's reference state
+  std::vector<double> h_partial;  // host copy of the per-element sums (sized once)
   // one Runge-Kutta step captured as a CUDA graph, replayed by sse_rk_steps;
   // rebuilt when any of the values it was captured with changes
   struct StepGraph {
@@ -693,6 +695,12 @@ int enable_mixed(sse_solver *s) {
   ka.u_ff = (float *)p;
   if ((e = alloc(s, (size_t)c.n_p * c.n_c * ne * sizeof(double), &p))) return cuda_fail(s, e, "alloc");
   s->d_comp = (double *)p;
+  // the reference state's FP64 residual (filled when the state is chosen)
+  // and the host buffer of the reduction that chooses it: allocated here so
+  // that no later call allocates
+  if ((e = alloc(s, (size_t)c.n_p * c.n_c * ne * sizeof(double), &p))) return cuda_fail(s, e, "alloc");
+  s->d_rref = (double *)p;
+  s->h_partial.assign((size_t)c.n_e * (c.n_c + 1), 0.0);
   // phase-B layout in floats (primitives carry p - p_ref as well)
   const int nc = c.n_c, np = c.n_p;
   int zsz = 0, wsz = 0;
@@ -799,7 +807,7 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
   const sse_config &c = s->cfg;
   cudaError_t e = launch_conservation(s->ka, u_dev, u_dev, s->d_partial, s->stream);
   if (e != cudaSuccess) return cuda_fail(s, e, "reference state");
-  std::vector<double> part((size_t)c.n_e * (c.n_c + 1));
+  std::vector<double> &part = s->h_partial;
   if ((e = cudaMemcpyAsync(part.data(), s->d_partial, part.size() * 8, cudaMemcpyDeviceToHost, s->stream)) ||
       (e = cudaStreamSynchronize(s->stream)))
     return cuda_fail(s, e, "reference state");
@@ -830,6 +838,23 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
   }
   if (!(ph.rho_ref > 0.0) || !(ph.p_ref > 0.0))
     return fail(s, SSE_ERR_NONPHYSICAL, "mixed form: mean density or energy not positive");
+  // The FP32 phase B leaves the reference pressure out of every momentum
+  // flux; those terms are the FP64 phase-B residual of u_ref at its nodal
+  // states.  Evaluate it once (FP64 phase B on constant nodal scratch) for
+  // the mixed phase B to add back: on metrics that do not preserve a free
+  // stream (exact metrics on curved tets) it is O(p_ref), not round-off.
+  {
+    double uref[5] = {ph.rho_ref, 0.0, 0.0, 0.0, 0.0};
+    uref[c.n_c - 1] = ph.E_ref;
+    KernelArgs kb = s->ka;
+    kb.mixed = 0;
+    kb.dudt = s->d_rref;
+    if ((e = launch_fill_constant_state(kb.u_q, c.n_q, c.n_c, c.n_e, uref, s->stream)) ||
+        (e = launch_fill_constant_state(kb.u_f, c.n_f, c.n_c, c.n_e, uref, s->stream)) ||
+        (e = launch_time_derivative(kb, s->stream)) || (e = cudaStreamSynchronize(s->stream)))
+      return cuda_fail(s, e, "reference-state residual");
+    s->ka.geo.Rref = s->d_rref;
+  }
   s->ref_ready = true;
   return SSE_OK;
 }
@@ -839,16 +864,13 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
 // when given, receive the FP64 nodal states instead of the handle's scratch.
 cudaError_t residual_device(sse_solver *s, const double *u, double *dudt, double *u_q = nullptr,
                             double *u_f = nullptr) {
+  if (s->ka.mixed && !s->ref_ready && ensure_reference(s, u) != SSE_OK) return cudaErrorInvalidValue;
   KernelArgs ka = s->ka;
   ka.u = u;
   ka.dudt = dudt;
   if (u_q) {
     ka.u_q = u_q;
     ka.u_f = u_f;
-  }
-  if (ka.mixed && !s->ref_ready) {
-    if (ensure_reference(s, u) != SSE_OK) return cudaErrorInvalidValue;
-    ka.ph = s->ka.ph;
   }
   cudaError_t e = launch_nodal_values(ka, s->stream);
   if (e != cudaSuccess) return e;
@@ -1205,21 +1227,34 @@ int32_t sse_residual_static_scratch(sse_solver *s, const double *u_dev, double *
   if (!s) return SSE_ERR_INVALID_ARGUMENT;
   if (!u_dev || !dudt_dev) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u/dudt");
   const sse_config &c = s->cfg;
+  // the handle's precision: FP64 nodal states in the FP64 form, FP32
+  // perturbation states in the mixed form (half the bytes per node)
+  const bool mixed = s->ka.mixed != 0;
+  const size_t word = mixed ? sizeof(float) : sizeof(double);
   const size_t nq = (size_t)c.n_q * c.n_c * c.n_e, nf = (size_t)c.n_f * c.n_c * c.n_e;
-  if (nq + nf > kStaticScratchDoubles)
+  if ((nq + nf) * word > SSE_STATIC_SCRATCH_BYTES)
     return fail(s, SSE_ERR_INVALID_ARGUMENT,
-                "mesh too large for the static scratch: needs " + std::to_string((nq + nf) * 8) +
+                "mesh too large for the static scratch: needs " + std::to_string((nq + nf) * word) +
                     " bytes of nodal states, the fixed buffer holds " +
-                    std::to_string(kStaticScratchDoubles * 8) + " (use sse_residual)");
+                    std::to_string((size_t)SSE_STATIC_SCRATCH_BYTES) + " (use sse_residual)");
   double *scratch = nullptr;
   int rc = static_scratch_address(s, &scratch);
   if (rc != SSE_OK) return rc;
+  // the mixed form picks its reference state on its first call; that uses
+  // buffers the handle allocated when SSE_MIXED was set, and synchronises
+  if (mixed && (rc = ensure_reference(s, u_dev)) != SSE_OK) return rc;
   KernelArgs ka = s->ka;
-  ka.mixed = 0;           // FP64 form
   ka.u = u_dev;
   ka.dudt = dudt_dev;
-  ka.u_q = scratch;       // fully written by phase A before phase B reads it:
-  ka.u_f = scratch + nq;  // no clearing needed between calls
+  // the nodal states are fully written by phase A before phase B reads
+  // them: no clearing needed between calls
+  if (mixed) {
+    ka.u_qf = reinterpret_cast<float *>(scratch);
+    ka.u_ff = ka.u_qf + nq;
+  } else {
+    ka.u_q = scratch;
+    ka.u_f = scratch + nq;
+  }
   cudaError_t e = launch_nodal_values(ka, s->stream);
   if (e == cudaSuccess) e = launch_time_derivative(ka, s->stream);
   if (e != cudaSuccess) return cuda_fail(s, e, "residual (static scratch)");

@@ -105,6 +105,12 @@ struct DevGeo {
   // mixed form: the entropy projection of the constant function 1 at the
   // volume nodes (V M^-1 V^T (W J), nq x ne) and its facet values (R P1, nf x ne)
   const double *P1, *RP1;
+  // mixed form: the FP64 phase-B residual of the constant reference state
+  // (np x nc x ne), i.e. the reference-pressure terms the FP32 fluxes leave
+  // out; zero to round-off on free-stream-preserving metrics, O(1) on curved
+  // tets with the exact metrics.  Added back in the mixed phase B's FP64
+  // epilogue; null until the reference state is chosen.
+  const double *Rref;
 };
 
 struct Physics {
@@ -487,9 +493,14 @@ SSE_HD void entropy_to_cons_jvp(double gamma, double gm1, double igm1, double lo
 // by three orders of magnitude; an FP32 state would lose them, a perturbation
 // keeps them.  The reference pressure is dropped from every momentum flux
 // (volume pairs, facet correction, interface flux): for the constant state
-// u_ref all fluxes reduce to that isotropic pressure term, and the discrete
-// residual of a constant state is zero (free-stream preservation of the
-// conservative-curl metrics), so the dropped terms sum to zero exactly.
+// u_ref all fluxes reduce to that isotropic pressure term, so the dropped
+// terms are, together, the FP64 residual of u_ref evaluated at its nodal
+// states -- a constant of the mesh (DevGeo::Rref).  It vanishes to round-off
+// where the metric terms preserve a free stream (conservative-curl metrics,
+// straight or 2-D elements) and is O(p_ref) on curved tets with the exact
+// metrics (the reference's default); phase B adds it back in FP64, so the
+// mixed residual equals the FP64 one on both.  Being constant in u, it
+// changes no Jacobian: the mixed-form VJP needs no counterpart.
 // ---------------------------------------------------------------------------
 
 // FP32 quotient for the mixed form: the fast reciprocal-based division

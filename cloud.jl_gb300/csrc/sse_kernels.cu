@@ -955,12 +955,16 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   mass_solve<float, D, NC>(op, g.JinvWf ? g.JinvWf + (size_t)kk * nq : nullptr,
                            g.WJinvf ? g.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq, Z,
                            Wb, lane, tpe, ka.Akf ? ka.Akf + (size_t)kk * op.np * op.np : nullptr);
-  // energy residual = H_ref x density residual + reduced-flux residual, in FP64
+  // energy residual = H_ref x density residual + reduced-flux residual, in
+  // FP64, plus the reference state's own FP64 residual (the dropped
+  // reference-pressure terms)
   double *outp = ka.dudt + (size_t)kk * NC * np;
+  const double *rref = g.Rref ? g.Rref + (size_t)kk * NC * np : nullptr;
   if (live)
     for (int t = lane; t < NC * np; t += tpe) {
       double v = (double)Xm[t];
       if (t >= (NC - 1) * np) v = fma(ph.H_ref, (double)Xm[t - (NC - 1) * np], v);
+      if (rref) v += rref[t];
       outp[t] = v;
       if (!isfinite(Xm[t])) ka.flag_nonphysical();
     }
@@ -998,6 +1002,17 @@ __global__ void ck_stage_compensated_kernel(double *__restrict__ u, double *__re
 }
 
 // FP64 -> FP32 rounding of metric terms and operator values for the mixed form
+// Every volume and facet node of every element set to one constant state
+// (FP64 nodal scratch layouts: u_q element-major (nq, nc) blocks, u_f
+// element-major (nf, nc) blocks): the nodal states of the mixed form's
+// reference state, whose phase-B residual the mixed form adds back.
+__global__ void fill_constant_state_kernel(double *__restrict__ buf, int nodes, int nc, size_t n,
+                                           double s0, double s1, double s2, double s3, double s4) {
+  const double s[5] = {s0, s1, s2, s3, s4};
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    buf[i] = s[(i / nodes) % nc];
+}
+
 __global__ void round_to_float_kernel(const double *__restrict__ in, float *__restrict__ out, size_t n) {
   for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x)
     out[x] = (float)in[x];
@@ -1351,6 +1366,16 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
 cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   round_to_float_kernel<<<elementwise_grid(n), 256, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_constant_state(double *buf, int nodes, int nc, size_t ne, const double *state,
+                                       cudaStream_t st) {
+  const size_t n = (size_t)nodes * nc * ne;
+  if (n == 0) return cudaSuccess;
+  double s[5] = {0, 0, 0, 0, 0};
+  for (int e = 0; e < nc && e < 5; ++e) s[e] = state[e];
+  fill_constant_state_kernel<<<elementwise_grid(n), 256, 0, st>>>(buf, nodes, nc, n, s[0], s[1], s[2], s[3], s[4]);
   return cudaGetLastError();
 }
 

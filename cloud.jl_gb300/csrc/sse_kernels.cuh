@@ -73,6 +73,8 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
                                         double a, double b, double dt, int first, size_t n,
                                         cudaStream_t st);
 cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st);
+cudaError_t launch_fill_constant_state(double *buf, int nodes, int nc, size_t ne, const double *state,
+                                       cudaStream_t st);
 cudaError_t launch_round_transpose(const double *in, float *out, size_t nmat, int n, cudaStream_t st);
 cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_projection_of_one(const KernelArgs &ka, double *P1, double *RP1, cudaStream_t st);

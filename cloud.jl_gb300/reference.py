@@ -6,7 +6,7 @@ Host-side FP64 restatement of ``ReferenceApproximation`` for
 (src/SpatialDiscretizations/tensor_simplex.jl:142-306), its
 ``RefElemData`` (src/SpatialDiscretizations/ref_elem_data.jl:1-134) and the
 collapsed quadrature rules (src/SpatialDiscretizations/quadrature_rules.jl:
-388-472).  Array layouts follow the reference (Julia column-major): the
+76-166).  Array layouts follow the reference (Julia column-major): the
 volume node index is sigma_out = M2*M3*(i1-1) + M3*(i2-1) + i3, i.e. eta_1
 slowest and eta_d fastest, and a Kronecker product ``A (x) B`` acts with B on
 the fast index, which is numpy's ``np.kron`` convention as well.

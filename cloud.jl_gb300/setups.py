@@ -80,13 +80,15 @@ def advection_tri(cells: int = 16, p: int = 4, approx: str = "ModalTensor") -> P
 
 
 def vortex_tri(cells: int = 64, p: int = 4, approx: str = "ModalTensor",
-               strength: float = 5.0, shift: float = 0.0) -> Problem:
+               strength: float = 5.0, shift: float = 0.0, metrics: str = "ChanWilcox") -> Problem:
     """Isentropic vortex of strength 5 in a (1,1) free stream: the
     reference's ``IsentropicVortex`` with Ma = sqrt(2), theta = pi/4, R = 1,
     sigma = 1, beta = strength * e^{1/2} / (2 pi) (the classical Gaussian
-    vortex velocity eps/(2 pi) exp((1-r^2)/2)), centred in [0,10]^2."""
+    vortex velocity eps/(2 pi) exp((1-r^2)/2)), centred in [0,10]^2.
+    ``metrics`` "ChanWilcox" (conservative curl) or "Exact", the
+    reference's default."""
     L = 10.0
-    sd = _disc(approx, "Tri", p, ((0.0, L), (0.0, L)), (cells, cells), "Chan", 0.1, "ChanWilcox")
+    sd = _disc(approx, "Tri", p, ((0.0, L), (0.0, L)), (cells, cells), "Chan", 0.1, metrics)
     law = S.EulerEquations(2, 1.4)
     ic = S.IsentropicVortex(gamma=1.4, Ma=math.sqrt(2.0), theta=math.pi / 4, R=1.0,
                             beta=strength * math.exp(0.5) / (2 * math.pi), sigma=1.0,
@@ -99,9 +101,14 @@ def vortex_tri(cells: int = 64, p: int = 4, approx: str = "ModalTensor",
     return Problem("vortex_tri", law, sd, form, ic, u0, dt, 0, 5)
 
 
-def tgv_tet(cells: int = 16, p: int = 4, approx: str = "ModalTensor", lf: bool = True) -> Problem:
+def tgv_tet(cells: int = 16, p: int = 4, approx: str = "ModalTensor", lf: bool = True,
+            metrics: str = "ChanWilcox") -> Problem:
+    """``metrics`` "ChanWilcox" (conservative curl: a constant state is
+    preserved to round-off, needed for round-off entropy conservation) or
+    "Exact", the reference's default, which on these curved tets does not
+    preserve a free stream."""
     L = 2 * math.pi
-    sd = _disc(approx, "Tet", p, ((0.0, L),) * 3, (cells,) * 3, "Chan", 0.05, "ChanWilcox")
+    sd = _disc(approx, "Tet", p, ((0.0, L),) * 3, (cells,) * 3, "Chan", 0.05, metrics)
     law = S.EulerEquations(3, 1.4)
     ic = S.TaylorGreenVortex(1.4, 0.1)
     nflux = S.LaxFriedrichsNumericalFlux() if lf else S.EntropyConservativeNumericalFlux()

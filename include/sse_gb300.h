@@ -157,23 +157,30 @@ int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t,
                      int32_t memory);
 
 /* Capacity of the fixed device buffer used by sse_residual_static_scratch:
- * 32 MiB, i.e. room for (n_q + n_f) * n_c * n_e doubles up to 4,194,304
- * (for example 8192 Euler triangles at p = 4, not the 24,576-tet mesh). */
+ * 32 MiB, i.e. room for (n_q + n_f) * n_c * n_e nodal values up to 4,194,304
+ * doubles in the FP64 form (for example 8192 Euler triangles at p = 4, not
+ * the 24,576-tet mesh) or 8,388,608 floats in the mixed form. */
 #define SSE_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 
-/* dudt <- R(u) like sse_residual, for callers that cannot allocate GPU
+/* dudt <- R(u) exactly like sse_residual on the same handle, in the handle's
+ * precision (SSE_FP64 or SSE_MIXED), for callers that cannot allocate GPU
  * memory while they run: code that must not call cudaMalloc inside its time
  * loop (a real-time or latency-bound step whose memory is fixed up front, a
  * host framework that owns the device memory pool and forbids raw
- * allocation), after the handle was created at set-up.  This call allocates
- * nothing: the element nodal states that the residual's two kernels hand to
- * each other live in one file-scope device array of SSE_STATIC_SCRATCH_BYTES
- * that every GPU loading the library holds until the process exits; u_dev and
- * dudt_dev are device pointers supplied by the caller.  Meshes whose
- * (n_q + n_f) * n_c * n_e doubles exceed that size are rejected with
+ * allocation), after the handle was created (and its precision set) at
+ * set-up.  This call allocates nothing: the element nodal states that the
+ * residual's two kernels hand to each other (FP64 states, or the mixed
+ * form's FP32 perturbation states) live in one file-scope device array of
+ * SSE_STATIC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits; u_dev and dudt_dev are device pointers supplied by the
+ * caller.  Meshes whose nodal states exceed that size are rejected with
  * SSE_ERR_INVALID_ARGUMENT.  The first call on each device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the one
+ * make that first call before any stream capture.  On an SSE_MIXED handle
+ * whose reference state is not yet chosen, the call chooses it first (a
+ * reduction over u and one FP64 evaluation, in buffers sse_set_precision
+ * allocated).  Every call synchronises the handle's stream before it
+ * returns, to read the non-physical-state flag.  All calls share the one
  * array: calls that overlap on the GPU (other handles, other streams, other
  * threads) race and must be serialised by the caller.  Each call rewrites
  * the whole part of the array it reads, so nothing needs clearing between

@@ -84,7 +84,8 @@ def make(name):
         ic = Ic()
     elif name.startswith("vortex_tri") or name.startswith("euler_tri"):
         approx = "NodalTensor" if "nodal" in name else "ModalTensor"
-        pb = setups.vortex_tri(cells=8, p=3, approx=approx)
+        pb = setups.vortex_tri(cells=8, p=3, approx=approx,
+                               metrics="Exact" if "exact" in name else "ChanWilcox")
         sd, law, ic = pb.sd, pb.law, pb.initial_data
         nflux = S.EntropyConservativeNumericalFlux() if "ec" in name else S.LaxFriedrichsNumericalFlux()
         two = S.ConservativeFlux() if "cons2pt" in name else S.EntropyConservativeFlux()
@@ -98,7 +99,8 @@ def make(name):
         p = 6 if "p6" in name else (5 if "p5" in name else (2 if "p2" in name else (3 if "nodal" in name else 4)))
         if name.startswith("euler_tet"):
             p = 3
-        pb = setups.tgv_tet(cells=2, p=p, approx=approx, lf="ec" not in name)
+        pb = setups.tgv_tet(cells=2, p=p, approx=approx, lf="ec" not in name,
+                            metrics="Exact" if "exact" in name else "ChanWilcox")
         sd, law, ic, form = pb.sd, pb.law, pb.initial_data, pb.form
         if "cons2pt" in name:
             form = S.FluxDifferencingForm(inviscid_numerical_flux=S.LaxFriedrichsNumericalFlux(),
@@ -120,7 +122,11 @@ NAMES = ["adv_tri_modal", "adv_tri_nodal", "adv_tri_central", "adv_tri_fd", "adv
          "adv_tet_fd", "vortex_tri_modal", "vortex_tri_nodal", "vortex_tri_ec",
          "vortex_tri_cons2pt", "euler_tri_std", "tgv_tet_modal", "tgv_tet_ec", "tgv_tet_nodal",
          "tgv_tet_p5", "tgv_tet_p6", "tgv_tet_p2", "tgv_tet_cons2pt", "euler_tet_std",
-         "vortex_tri_chandra", "tgv_tet_chandra"]
+         "vortex_tri_chandra", "tgv_tet_chandra", "vortex_tri_exact", "tgv_tet_exact",
+         "tgv_tet_ec_exact", "tgv_tet_nodal_exact"]
+# Euler FD meshes built with the reference's default exact metrics, which on
+# curved tets do not preserve a free stream
+EXACT_NAMES = ["vortex_tri_exact", "tgv_tet_exact", "tgv_tet_ec_exact", "tgv_tet_nodal_exact"]
 # multidimensional (dense V, D, R) approximations: parity, adjoint and mixed cases
 MULTI_NAMES = ["multi_adv_tri", "multi_adv_tri_nodal", "multi_adv_tri_fd", "multi_tri",
                "multi_tri_nodal", "multi_tri_std", "multi_tri_ec", "multi_tet", "multi_tet_ec",

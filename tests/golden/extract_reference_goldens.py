@@ -57,4 +57,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python extract_reference_goldens.py <path to the reference checkout>")
+    main(sys.argv[1])

@@ -22,11 +22,7 @@ S, M, R = PKG.solver, PKG.mesh, PKG.reference
 
 def l2_error(sd, u, exact):
     """ErrorAnalysis with the volume quadrature (Analysis/error.jl:58-91)."""
-    ra = sd.reference_approximation
-    ue = exact(sd.mesh.xyzq)
-    ua = np.einsum("qp,kcp->kqc", ra.V_dense, u)
-    w = ra.W[None, :, None] * sd.geometric_factors.J_q[:, :, None]
-    return np.sqrt(((ue - ua) ** 2 * w).sum(axis=(0, 1)))
+    return PKG.timestepping.l2_error(sd, u, lambda x, t: exact(x))
 
 
 def advection_2d():
