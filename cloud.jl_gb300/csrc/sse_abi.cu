@@ -128,9 +128,12 @@ cudaError_t upload(sse_solver *s, const T *host, size_t n, const T **dev) {
   return e;
 }
 
+// Device buffers owned by the handle carry 64 bytes of slack at the end: the
+// kernels stage per-element slabs with bulk copies of their 16-byte-aligned
+// spans, which may reach up to 15 bytes past the last slab.
 cudaError_t alloc(sse_solver *s, size_t bytes, void **out) {
   void *p = nullptr;
-  cudaError_t e = cudaMalloc(&p, bytes > 0 ? bytes : 8);
+  cudaError_t e = cudaMalloc(&p, bytes + 64);
   if (e != cudaSuccess) return e;
   s->allocations.push_back(p);
   *out = p;
@@ -638,6 +641,7 @@ int check_flag(sse_solver *s) {
   if (h) {
     cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream);
     cudaStreamSynchronize(s->stream);
+    if (h & 2) return fail(s, SSE_ERR_CUDA, "a kernel's bounded wait for its shared-memory copies gave up");
     return fail(s, SSE_ERR_NONPHYSICAL, "non-physical state (density/pressure <= 0 or non-finite residual)");
   }
   return SSE_OK;
@@ -722,10 +726,17 @@ int enable_mixed(sse_solver *s) {
   const int tpe_fp64 = ka.tpb / ka.epb;
   const int tpe_m = std::max(32, tpe_fp64);
   ka.epb_bm = std::max(1, ka.epb * tpe_fp64 / tpe_m);
-  auto layout_m = [&](int chunk) {
-    const int sizes[8] = {nc * (int)nq, nc * (int)nf, nc * (int)nf, nc * (int)nq,
-                          std::max(chunk * nc, final_m), (int)(d * d * nq),
-                          op.nfp > 0 ? (int)(d * c.num_faces * nq) : 0, (int)((nq + nf) * (4 + d))};
+  // Shared regions of the staged slabs: n floats plus the alignment margin
+  // of a bulk copy (the slab lands at its source address modulo 16).
+  auto staged = [&](int n) { return r4(n + 8); };
+  const int np2 = ka.Akf ? np * np : 0;
+  auto layout_m = [&](int chunk, bool geo, bool rref, bool ak) {
+    const int sizes[11] = {staged(nc * (int)nq), staged(nc * (int)nf), nc * (int)nf,
+                           ak && np2 ? staged(np2) : 0, std::max(chunk * nc, final_m),
+                           staged((int)(d * d * nq)), op.nfp > 0 ? staged((int)(d * c.num_faces * nq)) : 0,
+                           (int)((nq + nf) * (4 + d)),
+                           geo ? 2 * staged((int)(d * nf)) + staged((int)nf) : 0,
+                           rref ? staged(2 * nc * np) : 0, 4};
     int off = 0, i = 0;
     for (int sz : sizes) { ka.layBm.off[i++] = off; off += r4(sz); }
     for (; i < 12; ++i) ka.layBm.off[i] = off;
@@ -734,10 +745,10 @@ int enable_mixed(sse_solver *s) {
   };
   const int budget_m = (int)((size_t)55 * 1024 / 4 / ka.epb_bm);
   int chunk_m = max_pairs;
-  if (layout_m(chunk_m) > budget_m) {
+  if (layout_m(chunk_m, false, false, false) > budget_m) {
     // four blocks per SM when chunks of at least one pass of the element's
     // threads fit, else two, else one
-    const int fixed = layout_m(0) - r4(final_m);
+    const int fixed = layout_m(0, false, false, false) - r4(final_m);
     const int need = std::min(tpe_m, max_pairs) * nc;
     int room = budget_m - fixed;
     if (room < need) room = 2 * budget_m - fixed;
@@ -748,7 +759,18 @@ int enable_mixed(sse_solver *s) {
   }
   ka.fd_chunk_mixed = chunk_m;
   ka.vdm_zsz_mixed = zsz4;
-  const int off = layout_m(chunk_m);
+  // The facet geometry, the reference residual and the mass operator are
+  // staged as well where that keeps the blocks per SM (228 KB of shared
+  // memory, 1 KB reserved per block), else read from global memory.
+  auto blocks_per_sm = [&](int floats) {
+    return (int)((size_t)228 * 1024 / ((size_t)ka.epb_bm * floats * 4 + 1024));
+  };
+  bool geo = false, rref = false, ak = false;
+  const int blocks0 = blocks_per_sm(layout_m(chunk_m, false, false, false));
+  if (blocks_per_sm(layout_m(chunk_m, true, false, false)) >= blocks0) geo = true;
+  if (blocks_per_sm(layout_m(chunk_m, geo, true, false)) >= blocks0) rref = true;
+  if (blocks_per_sm(layout_m(chunk_m, geo, rref, true)) >= blocks0) ak = true;
+  const int off = layout_m(chunk_m, geo, rref, ak);
   size_t smm = (size_t)ka.epb_bm * off * sizeof(float);
   if (smm > 220 * 1024) return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed kernel");
   if ((e = sse_set_smem_limit_mixed(ka, smm))) return cuda_fail(s, e, "cudaFuncSetAttribute");
@@ -1232,7 +1254,10 @@ int32_t sse_residual_static_scratch(sse_solver *s, const double *u_dev, double *
   const bool mixed = s->ka.mixed != 0;
   const size_t word = mixed ? sizeof(float) : sizeof(double);
   const size_t nq = (size_t)c.n_q * c.n_c * c.n_e, nf = (size_t)c.n_f * c.n_c * c.n_e;
-  if ((nq + nf) * word > SSE_STATIC_SCRATCH_BYTES)
+  // the mixed phase B stages each element's states with bulk copies of
+  // their 16-byte-aligned spans, which may reach 15 bytes past the last one
+  const size_t slack = mixed ? 64 : 0;
+  if ((nq + nf) * word + slack > SSE_STATIC_SCRATCH_BYTES)
     return fail(s, SSE_ERR_INVALID_ARGUMENT,
                 "mesh too large for the static scratch: needs " + std::to_string((nq + nf) * word) +
                     " bytes of nodal states, the fixed buffer holds " +

@@ -15,6 +15,7 @@
 //          std_time_derivative_kernel  time_derivative! StandardForm (standard_form_first_order.jl:16-63)
 #include "sse_device.cuh"
 #include "sse_kernels.cuh"
+#include "sse_tma.cuh"
 #include "sse_ops.cuh"
 
 namespace sse {
@@ -711,7 +712,7 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
 template <int D, int NC>
 __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArgs ka) {
   static_assert(NC == D + 2, "the mixed form covers the Euler equations");
-  extern __shared__ double smem_raw[];
+  extern __shared__ __align__(16) double smem_raw[];
   float *smem = reinterpret_cast<float *>(smem_raw);
   const DevOps &op = ka.op;
   const Physics &ph = ka.ph;
@@ -724,24 +725,75 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   const int kk = live ? k : 0;
   const int np = op.np, nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
   float *base = smem + (size_t)team * L.team_doubles;  // team size in floats for this layout
-  float *uq = base + L.off[0], *uf = base + L.off[1], *ff = base + L.off[2], *rq = base + L.off[3],
-        *diff = base + L.off[4], *Lam = base + L.off[5], *hnq = base + L.off[6],
-        *prim = base + L.off[7];
+  float *rq = base + L.off[0], *ff = base + L.off[2], *diff = base + L.off[4], *prim = base + L.off[7];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base + L.off[10]);
   const int PS = 4 + D;
   const float gm1 = (float)ph.gm1, igm1 = (float)ph.igm1, gam = (float)ph.gamma;
   const float rho_ref = (float)ph.rho_ref, p_ref = (float)ph.p_ref, hl = (float)ph.half_lambda;
   const float theta_ref = (float)ph.theta_ref, H_ref = (float)ph.H_ref;
 
+  // The element's slabs (FP32 nodal states, Lambda_q, halfnJq, and where
+  // the layout gives them room the facet geometry, the mass operator and the
+  // reference residual) move into shared memory as bulk copies issued by one
+  // thread of the team, completed on the team's mbarrier.
   const float *uqg = ka.u_qf + (size_t)kk * NC * nq;
   const float *ufg = ka.u_ff + (size_t)kk * NC * nf;
-  for (int t = lane; t < NC * nq; t += tpe) uq[t] = uqg[t];
-  for (int t = lane; t < NC * nf; t += tpe) uf[t] = ufg[t];
   const float *Lg = g.Lambda_qf + (size_t)kk * nq * D * D;
-  for (int t = lane; t < nq * D * D; t += tpe) Lam[t] = Lg[t];
   const float *Hg = g.halfnJqf + (size_t)kk * D * nfac * nq;
-  if (op.nfp > 0)
-    for (int t = lane; t < D * nfac * nq; t += tpe) hnq[t] = Hg[t];
-  __syncthreads();
+  const float *nfg = g.n_ff + (size_t)kk * D * nf, *bjg = g.BJff + (size_t)kk * nf;
+  const float *hfg = g.halfnJff + (size_t)kk * D * nf;
+  const float *Akg = ka.Akf ? ka.Akf + (size_t)kk * np * np : nullptr;
+  const double *Rg = g.Rref ? g.Rref + (size_t)kk * NC * np : nullptr;
+  const bool st_ak = Akg && L.off[4] > L.off[3];
+  const bool st_geo = L.off[9] > L.off[8];
+  const bool st_rref = Rg && L.off[10] > L.off[9];
+  const bool st_hnq = op.nfp > 0;
+  float *geo_r = base + L.off[8];
+  float *geo_b = geo_r + ((D * nf + 8 + 3) & ~3), *geo_h = geo_b + ((nf + 8 + 3) & ~3);
+  const float *uq = staged_ptr(base + L.off[0], uqg), *uf = staged_ptr(base + L.off[1], ufg);
+  const float *Lam = staged_ptr(base + L.off[5], Lg);
+  const float *hnq = st_hnq ? staged_ptr(base + L.off[6], Hg) : Hg;
+  const float *nfv = st_geo ? staged_ptr(geo_r, nfg) : nfg, *bjf = st_geo ? staged_ptr(geo_b, bjg) : bjg;
+  const float *hnf = st_geo ? staged_ptr(geo_h, hfg) : hfg;
+  const float *Aks = st_ak ? staged_ptr(base + L.off[3], Akg) : Akg;
+  const double *Rs = st_rref ? staged_ptr(base + L.off[9], Rg) : Rg;
+  if (lane == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+    const uint32_t bq = NC * nq * 4, bf = NC * nf * 4, bl = nq * D * D * 4, bh = D * nfac * nq * 4;
+    const uint32_t bn = D * nf * 4, bb = nf * 4, ba = np * np * 4, br = NC * np * 8;
+    uint32_t tx = staged_span(uqg, bq) + staged_span(ufg, bf) + staged_span(Lg, bl);
+    if (st_hnq) tx += staged_span(Hg, bh);
+    if (st_geo) tx += staged_span(nfg, bn) + staged_span(bjg, bb) + staged_span(hfg, bn);
+    if (st_ak) tx += staged_span(Akg, ba);
+    if (st_rref) tx += staged_span(Rg, br);
+    mbar_arrive_expect_tx(bar, tx);
+    stage_slab(base + L.off[0], uqg, bq, bar);
+    stage_slab(base + L.off[1], ufg, bf, bar);
+    stage_slab(base + L.off[5], Lg, bl, bar);
+    if (st_hnq) stage_slab(base + L.off[6], Hg, bh, bar);
+    if (st_geo) {
+      stage_slab(geo_r, nfg, bn, bar);
+      stage_slab(geo_b, bjg, bb, bar);
+      stage_slab(geo_h, hfg, bn, bar);
+    }
+    if (st_ak) stage_slab(base + L.off[3], Akg, ba, bar);
+    if (st_rref) stage_slab(base + L.off[9], Rg, br, bar);
+  }
+  // meanwhile: the neighbour's facet states of this thread's first facet node
+  float uo0[NC];
+  if (lane < nf) {
+    const int P = g.mapP[(size_t)kk * nf + lane];
+    const int jn = P % nf, kn = P / nf;
+#pragma unroll
+    for (int e = 0; e < NC; ++e) uo0[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
+  }
+  __syncthreads();  // the mbarrier is initialised
+  if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
+    if (lane == 0) ka.flag_timeout();
+    mbar_wait_bounded(bar, 0);  // give copies still in flight a bounded time to land
+    return;
+  }
   for (int i = lane; i < nq + nf; i += tpe) {
     float du[NC];
 #pragma unroll
@@ -752,13 +804,18 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
 
   // interface flux: EC flux . n + Lax-Friedrichs, scaled by BJf
   for (int j = lane; j < nf; j += tpe) {
-    int P = g.mapP[(size_t)kk * nf + j];
-    int jn = P % nf, kn = P / nf;
     float uo[NC], n[D], Po[4 + D], out[NC];
+    if (j == lane) {
 #pragma unroll
-    for (int e = 0; e < NC; ++e) uo[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
+      for (int e = 0; e < NC; ++e) uo[e] = uo0[e];
+    } else {
+      const int P = g.mapP[(size_t)kk * nf + j];
+      const int jn = P % nf, kn = P / nf;
 #pragma unroll
-    for (int m = 0; m < D; ++m) n[m] = g.n_ff[m + D * (j + (size_t)nf * kk)];
+      for (int e = 0; e < NC; ++e) uo[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
+    }
+#pragma unroll
+    for (int m = 0; m < D; ++m) n[m] = nfv[m + D * j];
     const float *Pi = prim + (size_t)(nq + j) * PS;
     euler_prim_mixed<D>(gm1, rho_ref, p_ref, uo, Po);
     ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, Pi, Po, n, out);
@@ -770,7 +827,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
       float ci = sqrtf(gam * (theta_ref + Pi[2])), co = sqrtf(gam * (theta_ref + Po[2]));
       a = hl * (fmaxf(fabsf(vni), fabsf(vno)) + fmaxf(ci, co));
     }
-    const float bjf = g.BJff[(size_t)kk * nf + j];
+    const float bj = bjf[j];
     float jump[NC];
 #pragma unroll
     for (int e = 0; e < NC; ++e) jump[e] = uf[e * nf + j] - uo[e];
@@ -778,7 +835,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
 #pragma unroll
     for (int e = 0; e < NC; ++e) {
       float fs = (ph.nflux == 0) ? fmaf(a, jump[e], out[e]) : out[e];
-      ff[e * nf + j] = fs * bjf;
+      ff[e * nf + j] = fs * bj;
     }
   }
 
@@ -868,7 +925,6 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
 
   // facet correction, chunked the same way
   if (op.nfp > 0) {
-    const float *hnf = g.halfnJff + (size_t)kk * D * nf;
     const float *fpC = OpVals<float>::fpC(op);
 #pragma unroll
     for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
@@ -954,12 +1010,12 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   vdm_tmul<float, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);
   mass_solve<float, D, NC>(op, g.JinvWf ? g.JinvWf + (size_t)kk * nq : nullptr,
                            g.WJinvf ? g.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq, Z,
-                           Wb, lane, tpe, ka.Akf ? ka.Akf + (size_t)kk * op.np * op.np : nullptr);
+                           Wb, lane, tpe, Aks);
   // energy residual = H_ref x density residual + reduced-flux residual, in
   // FP64, plus the reference state's own FP64 residual (the dropped
   // reference-pressure terms)
   double *outp = ka.dudt + (size_t)kk * NC * np;
-  const double *rref = g.Rref ? g.Rref + (size_t)kk * NC * np : nullptr;
+  const double *rref = Rs;
   if (live)
     for (int t = lane; t < NC * np; t += tpe) {
       double v = (double)Xm[t];

@@ -25,7 +25,12 @@ struct KernelArgs {
   DevGeo geo;
   Physics ph;
   Layout layA, layB;
-  Layout layBm;      // mixed-form phase B layout, offsets and team size in floats
+  Layout layBm;      // mixed-form phase B layout, offsets and team size in floats:
+                     // 0 volume states (then r_q), 1 facet states, 2 facet fluxes,
+                     // 3 mass operator, 4 pair buffer, 5 Lambda_q, 6 halfnJq,
+                     // 7 primitives, 8 facet geometry, 9 reference residual,
+                     // 10 mbarrier; a zero-sized optional region is read from
+                     // global memory instead
   Layout layAm;      // mixed-form phase A layout (doubles; FP32 arrays from off[4], in floats)
   Layout layP1;      // projection of the constant function (NC = 1), doubles
   int ne, epb, tpb;
@@ -65,6 +70,8 @@ struct KernelArgs {
   int vdm_zsz_mixed;   // floats of the first sum-factorisation scratch (multiple of 4)
 
   __device__ __forceinline__ void flag_nonphysical() const { atomicOr(flag, 1); }
+  // a bounded wait on a device copy gave up (reported as SSE_ERR_CUDA)
+  __device__ __forceinline__ void flag_timeout() const { atomicOr(flag, 2); }
 };
 
 cudaError_t sse_set_smem_limits(const KernelArgs &ka, size_t smA, size_t smB);
