@@ -760,10 +760,12 @@ int enable_mixed(sse_solver *s) {
   ka.fd_chunk_mixed = chunk_m;
   ka.vdm_zsz_mixed = zsz4;
   // The facet geometry, the reference residual and the mass operator are
-  // staged as well where that keeps the blocks per SM (228 KB of shared
-  // memory, 1 KB reserved per block), else read from global memory.
+  // staged as well where that keeps the resident blocks per SM (shared
+  // memory, registers and threads together), else read from global memory.
   auto blocks_per_sm = [&](int floats) {
-    return (int)((size_t)228 * 1024 / ((size_t)ka.epb_bm * floats * 4 + 1024));
+    int nb = 0;
+    if (sse_mixed_b_blocks_per_sm(ka, (size_t)ka.epb_bm * floats * 4, &nb) != cudaSuccess) return 0;
+    return nb;
   };
   bool geo = false, rref = false, ak = false;
   const int blocks0 = blocks_per_sm(layout_m(chunk_m, false, false, false));

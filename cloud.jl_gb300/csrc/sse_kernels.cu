@@ -710,7 +710,7 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
 // residual is written in FP64 for the FP64 stage accumulation.
 // ---------------------------------------------------------------------------
 template <int D, int NC>
-__global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArgs ka) {
+__global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(KernelArgs ka) {
   static_assert(NC == D + 2, "the mixed form covers the Euler equations");
   extern __shared__ __align__(16) double smem_raw[];
   float *smem = reinterpret_cast<float *>(smem_raw);
@@ -853,15 +853,27 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
   }
   for (int c0 = 0; c0 < op.nvp; c0 += CH) {
     const int c1 = min(op.nvp, c0 + CH);
+    int ijn = c0 + lane < c1 ? __ldg(op.vp_ij + c0 + lane) : 0;
+    float Sn[D];
+#pragma unroll
+    for (int m = 0; m < D; ++m) Sn[m] = c0 + lane < c1 ? __ldg(vpS + (c0 + lane) * D + m) : 0.f;
     for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
-      int ij = op.vp_ij[pidx];
+      const int ij = ijn;
+      float Sv[D];
+#pragma unroll
+      for (int m = 0; m < D; ++m) Sv[m] = Sn[m];
+      if (pidx + tpe < c1) {
+        ijn = __ldg(op.vp_ij + pidx + tpe);
+#pragma unroll
+        for (int m = 0; m < D; ++m) Sn[m] = __ldg(vpS + (pidx + tpe) * D + m);
+      }
       int i = ij & 0xffff, j = ij >> 16;
       float G[D], out[NC];
 #pragma unroll
       for (int n = 0; n < D; ++n) G[n] = 0.f;
 #pragma unroll
       for (int m = 0; m < D; ++m) {
-        const float Sm = vpS[pidx * D + m];
+        const float Sm = Sv[m];
         if (Sm == 0.f) continue;
 #pragma unroll
         for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
@@ -877,16 +889,26 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
         float acc[NC];
 #pragma unroll
         for (int e = 0; e < NC; ++e) acc[e] = 0.f;
-        for (int q = op.vp_inc_ptr[i]; q < op.vp_inc_ptr[i + 1]; ++q) {
-          const int inc = op.vp_inc[q];
-          const float *dp = diff + (size_t)(inc >> 1) * NC;
-          if (inc & 1) {
+        const int qa = op.vp_inc_ptr[i], qb = op.vp_inc_ptr[i + 1];
+        int q = qa;
+        for (; q + 4 <= qb; q += 4) {
+          int inc[4];
 #pragma unroll
-            for (int e = 0; e < NC; ++e) acc[e] -= dp[e];
-          } else {
+          for (int r = 0; r < 4; ++r) inc[r] = __ldg(op.vp_inc + q + r);
 #pragma unroll
-            for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+          for (int r = 0; r < 4; ++r) {
+            const float *dp = diff + (size_t)(inc[r] >> 1) * NC;
+            const float sg = (inc[r] & 1) ? -1.f : 1.f;
+#pragma unroll
+            for (int e = 0; e < NC; ++e) acc[e] = fmaf(sg, dp[e], acc[e]);
           }
+        }
+        for (; q < qb; ++q) {
+          const int inc = __ldg(op.vp_inc + q);
+          const float *dp = diff + (size_t)(inc >> 1) * NC;
+          const float sg = (inc & 1) ? -1.f : 1.f;
+#pragma unroll
+          for (int e = 0; e < NC; ++e) acc[e] = fmaf(sg, dp[e], acc[e]);
         }
 #pragma unroll
         for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
@@ -933,11 +955,17 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
     }
     for (int c0 = 0; c0 < op.nfp; c0 += CH) {
       const int c1 = min(op.nfp, c0 + CH);
+      int ijn = c0 + lane < c1 ? __ldg(op.fp_ij + c0 + lane) : 0;
+      float Cn = c0 + lane < c1 ? __ldg(fpC + c0 + lane) : 0.f;
       for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
-        int ij = op.fp_ij[pidx];
+        const int ij = ijn;
+        const float Cij = Cn;
+        if (pidx + tpe < c1) {
+          ijn = __ldg(op.fp_ij + pidx + tpe);
+          Cn = __ldg(fpC + pidx + tpe);
+        }
         int i = ij & 0xffff, j = ij >> 16;
         int f = j / npf;
-        const float Cij = fpC[pidx];
         float G[D], out[NC];
 #pragma unroll
         for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
@@ -956,8 +984,21 @@ __global__ void __launch_bounds__(256) fd_time_derivative_mixed_kernel(KernelArg
           const int r = vol ? t : t - nq;
           const int *ptr = vol ? op.fp_q_ptr : op.fp_f_ptr;
           const int *lst = vol ? op.fp_q : op.fp_f;
-          for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
-            const float *dp = diff + (size_t)lst[q] * NC;
+          const int qa = ptr[r], qb = ptr[r + 1];
+          int q = qa;
+          for (; q + 4 <= qb; q += 4) {
+            int id[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) id[u] = __ldg(lst + q + u);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float *dp = diff + (size_t)id[u] * NC;
+#pragma unroll
+              for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+            }
+          }
+          for (; q < qb; ++q) {
+            const float *dp = diff + (size_t)__ldg(lst + q) * NC;
 #pragma unroll
             for (int e = 0; e < NC; ++e) acc[e] += dp[e];
           }
@@ -1334,6 +1375,16 @@ cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka) {
                                           : (const void *)projection_of_one_kernel<3>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, p1);
   return e;
+}
+
+cudaError_t sse_mixed_b_blocks_per_sm(const KernelArgs &ka, size_t smBm, int *blocks) {
+  const void *f = nullptr;
+  if (ka.op.d == 2 && ka.op.nc == 4) f = (const void *)fd_time_derivative_mixed_kernel<2, 4>;
+  else if (ka.op.d == 3 && ka.op.nc == 5) f = (const void *)fd_time_derivative_mixed_kernel<3, 5>;
+  else return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, f, ka.tpb, smBm);
 }
 
 cudaError_t sse_set_smem_limit_mixed(const KernelArgs &ka, size_t smBm) {

@@ -76,6 +76,9 @@ struct KernelArgs {
 
 cudaError_t sse_set_smem_limits(const KernelArgs &ka, size_t smA, size_t smB);
 cudaError_t sse_set_smem_limit_mixed(const KernelArgs &ka, size_t smBm);
+// resident blocks per SM of the mixed phase-B kernel with smBm bytes of
+// dynamic shared memory (registers, threads and shared memory together)
+cudaError_t sse_mixed_b_blocks_per_sm(const KernelArgs &ka, size_t smBm, int *blocks);
 cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, const double *k,
                                         double a, double b, double dt, int first, size_t n,
                                         cudaStream_t st);
