@@ -862,6 +862,16 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
   }
   if (!(ph.rho_ref > 0.0) || !(ph.p_ref > 0.0))
     return fail(s, SSE_ERR_NONPHYSICAL, "mixed form: mean density or energy not positive");
+  ph.f_gamma = (float)ph.gamma;
+  ph.f_gm1 = (float)ph.gm1;
+  ph.f_igm1 = (float)ph.igm1;
+  ph.f_half_lambda = (float)ph.half_lambda;
+  ph.f_rho_ref = (float)ph.rho_ref;
+  ph.f_p_ref = (float)ph.p_ref;
+  ph.f_theta_ref = (float)ph.theta_ref;
+  ph.f_H_ref = (float)ph.H_ref;
+  ph.f_E_ref = (float)ph.E_ref;
+  ph.cref = entropy_ref_f(ph);
   // The FP32 phase B leaves the reference pressure out of every momentum
   // flux; those terms are the FP64 phase-B residual of u_ref at its nodal
   // states.  Evaluate it once (FP64 phase B on constant nodal scratch) for

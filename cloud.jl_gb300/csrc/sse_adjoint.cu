@@ -121,6 +121,7 @@ __global__ void __launch_bounds__(256) adj_flux_kernel(KernelArgs ka) {
   const bool live = k < ka.ne;
   const int kk = live ? k : 0;
   const int nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  const float rnpf = qrcp(npf > 0 ? npf : 1);
   const int PS = 3 + D;
   double *base = smem + (size_t)team * L.team_doubles;
   double *uq = base + L.off[0], *uf = base + L.off[1], *rb = base + L.off[2], *fb = base + L.off[3],
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(256) adj_flux_kernel(KernelArgs ka) {
       for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
         const int ij = op.fp_ij[pidx];
         const int i = ij & 0xffff, j = ij >> 16;
-        const int f = j / npf;
+        const int f = qdiv(j, rnpf);
         const double Cij = op.fp_C[pidx];
         double G[D], db[NC];
 #pragma unroll
@@ -655,6 +656,7 @@ __global__ void __launch_bounds__(256) adj_flux_generic_kernel(KernelArgs ka) {
   const bool live = k < ka.ne;
   const int kk = live ? k : 0;
   const int nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  const float rnpf = qrcp(npf > 0 ? npf : 1);
   double *base = smem + (size_t)team * L.team_doubles;
   double *uq = base + L.off[0], *uf = base + L.off[1], *rb = base + L.off[2], *fb = base + L.off[3],
          *ubq = base + L.off[4], *ubf = base + L.off[5], *Lam = base + L.off[6], *hnq = base + L.off[7],
@@ -772,7 +774,7 @@ __global__ void __launch_bounds__(256) adj_flux_generic_kernel(KernelArgs ka) {
       for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
         const int ij = op.fp_ij[pidx];
         const int i = ij & 0xffff, j = ij >> 16;
-        const int f = j / npf;
+        const int f = qdiv(j, rnpf);
         const double Cij = op.fp_C[pidx];
         double nJ[D], ui[NC], uj[NC], Fb[NC][D];
 #pragma unroll
@@ -903,7 +905,7 @@ __device__ void lf_flux_mixed_bwd(const Physics &ph, float igm1, float rho_ref, 
 #pragma unroll
   for (int c = 0; c < 4 + D; ++c) Pb[c] += Pself[c];
   if (ph.nflux != 0) return;
-  const float hl = (float)ph.half_lambda, gam = (float)ph.gamma;
+  const float hl = ph.f_half_lambda, gam = ph.f_gamma;
   float vni = 0.f, vno = 0.f;
 #pragma unroll
   for (int m = 0; m < D; ++m) { vni = fmaf(Pin[3 + m], n[m], vni); vno = fmaf(Pout[3 + m], n[m], vno); }
@@ -947,10 +949,11 @@ __global__ void __launch_bounds__(256) adj_flux_mixed_kernel(KernelArgs ka) {
   const bool live = k < ka.ne;
   const int kk = live ? k : 0;
   const int nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  const float rnpf = qrcp(npf > 0 ? npf : 1);
   const int PS = 4 + D;
-  const float gm1 = (float)ph.gm1, igm1 = (float)ph.igm1;
-  const float rho_ref = (float)ph.rho_ref, p_ref = (float)ph.p_ref;
-  const float theta_ref = (float)ph.theta_ref, H_ref = (float)ph.H_ref;
+  const float gm1 = ph.f_gm1, igm1 = ph.f_igm1;
+  const float rho_ref = ph.f_rho_ref, p_ref = ph.f_p_ref;
+  const float theta_ref = ph.f_theta_ref, H_ref = ph.f_H_ref;
   float *base = smem + (size_t)team * L.team_doubles;
   float *uq = base + L.off[0], *uf = base + L.off[1], *rb = base + L.off[2], *fb = base + L.off[3],
         *prim = base + L.off[4], *Pb = base + L.off[5], *ubd = base + L.off[6], *Lam = base + L.off[7],
@@ -1087,7 +1090,7 @@ __global__ void __launch_bounds__(256) adj_flux_mixed_kernel(KernelArgs ka) {
       for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
         const int ij = op.fp_ij[pidx];
         const int i = ij & 0xffff, j = ij >> 16;
-        const int f = j / npf;
+        const int f = qdiv(j, rnpf);
         const float Cij = fpC[pidx];
         float G[D], db[NC];
 #pragma unroll
@@ -1180,9 +1183,9 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   }
   __syncthreads();
   vdm_mul<float, D, NC>(op, U1, Q0, Zf, Wf, lane, tpe);  // u_q0'
-  const EntropyRefF cr = entropy_ref_f(ph);
-  const float gam = (float)ph.gamma, gm1 = (float)ph.gm1, igm1 = (float)ph.igm1;
-  const float E_ref = (float)ph.E_ref;
+  const EntropyRefF &cr = ph.cref;
+  const float gam = ph.f_gamma, gm1 = ph.f_gm1, igm1 = ph.f_igm1;
+  const float E_ref = ph.f_E_ref;
   for (int i = lane; i < nq; i += tpe) {
     float ui[NC], wi[NC];
 #pragma unroll

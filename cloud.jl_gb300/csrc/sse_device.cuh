@@ -113,6 +113,13 @@ struct DevGeo {
   const double *Rref;
 };
 
+// Constants of the FP32 perturbation entropy maps, rounded once from the FP64
+// reference state (w_ref: its entropy variables).
+struct EntropyRefF {
+  float gamma, gm1, igm1, rho_ref, p_ref, ip_ref, irho_ref, a_ref, ia_ref, rhoe_ref;
+  float w_ref[5];
+};
+
 struct Physics {
   int law;       // 0 advection, 1 Euler
   int nflux;     // 0 LF, 1 central, 2 EC numerical flux
@@ -134,7 +141,21 @@ struct Physics {
   double ip_ref, irho_ref;  // 1 / p_ref, 1 / rho_ref
   double a_ref, ia_ref;     // a_ref and 1 / a_ref with a = -(gamma-1) w_E
   double rhoe_ref;          // (rho e) of the reference state: p_ref / (gamma-1)
+  // FP32 roundings of the constants the mixed-form kernels use, made once on
+  // the host when the reference state is chosen (a conversion in every
+  // thread would run on the FP64 pipe, 1/64 of the FP32 rate)
+  float f_gamma, f_gm1, f_igm1, f_half_lambda, f_rho_ref, f_p_ref, f_theta_ref, f_H_ref, f_E_ref;
+  EntropyRefF cref;
 };
+
+// Integer quotient a / b for 0 <= a < 2^21 and b >= 1 through the
+// correctly rounded FP32 reciprocal rb = 1/b (qrcp): the exact value
+// (a + 1/2)/b lies at least 1/(2b) from the nearest integer, and the two
+// roundings of the product move it by at most (a + 1/2) 2^-23 / b < 1/(4b),
+// so truncation gives floor(a / b) exactly -- a few instructions instead of
+// an integer division by a value known only at run time.
+__device__ __forceinline__ float qrcp(int b) { return __frcp_rn((float)b); }
+__device__ __forceinline__ int qdiv(int a, float rb) { return __float2int_rz(__fmul_rn((float)a + 0.5f, rb)); }
 
 // ---------------------------------------------------------------------------
 // logmean / inverse logmean (ConservationLaws.jl:132-156)
@@ -549,12 +570,6 @@ SSE_HD float inv_logmean_mixed(float x, float y) {
 // way, so the energy residual equals H_ref times the density residual plus
 // the residual of the reduced fluxes; that sum is formed in FP64 at the end.
 
-// Constants of the FP32 perturbation entropy maps, rounded once from the FP64
-// reference state (w_ref: its entropy variables).
-struct EntropyRefF {
-  float gamma, gm1, igm1, rho_ref, p_ref, ip_ref, irho_ref, a_ref, ia_ref, rhoe_ref;
-  float w_ref[5];
-};
 
 SSE_HD EntropyRefF entropy_ref_f(const Physics &ph) {
   EntropyRefF c;

@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
   }
   __syncthreads();
   vdm_mul<float, D, NC>(op, Cf, Bf, Zf, Wf, lane, tpe);
-  const EntropyRefF cr = entropy_ref_f(ph);
+  const EntropyRefF &cr = ph.cref;
   // x' = W J (c2e(u_q) - w_ref)
   for (int i = lane; i < nq; i += tpe) {
     float ui[NC], wi[NC];
@@ -300,6 +300,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
   const bool live = k < ka.ne;
   const int kk = live ? k : 0;
   const int np = op.np, nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  const float rnpf = qrcp(npf > 0 ? npf : 1);
   double *base = smem + (size_t)team * L.team_doubles;
   double *uq = base + L.off[0], *uf = base + L.off[1], *ff = base + L.off[2], *rq = base + L.off[3],
          *diff = base + L.off[4], *Lam = base + L.off[5], *hnq = base + L.off[6],
@@ -473,7 +474,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
       for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
         int ij = op.fp_ij[pidx];
         int i = ij & 0xffff, j = ij >> 16;
-        int f = j / npf;
+        int f = qdiv(j, rnpf);
         double *dp = diff + (size_t)(pidx - c0) * NC;
         if constexpr (NC > 1) {
           if (ec) {
@@ -724,13 +725,14 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   const bool live = k < ka.ne;
   const int kk = live ? k : 0;
   const int np = op.np, nq = op.nq, nf = op.nf, nfac = op.nfac, npf = op.npf;
+  const float rnpf = qrcp(npf > 0 ? npf : 1);
   float *base = smem + (size_t)team * L.team_doubles;  // team size in floats for this layout
   float *rq = base + L.off[0], *ff = base + L.off[2], *diff = base + L.off[4], *prim = base + L.off[7];
   uint64_t *bar = reinterpret_cast<uint64_t *>(base + L.off[10]);
   const int PS = 4 + D;
-  const float gm1 = (float)ph.gm1, igm1 = (float)ph.igm1, gam = (float)ph.gamma;
-  const float rho_ref = (float)ph.rho_ref, p_ref = (float)ph.p_ref, hl = (float)ph.half_lambda;
-  const float theta_ref = (float)ph.theta_ref, H_ref = (float)ph.H_ref;
+  const float gm1 = ph.f_gm1, igm1 = ph.f_igm1, gam = ph.f_gamma;
+  const float rho_ref = ph.f_rho_ref, p_ref = ph.f_p_ref, hl = ph.f_half_lambda;
+  const float theta_ref = ph.f_theta_ref, H_ref = ph.f_H_ref;
 
   // The element's slabs (FP32 nodal states, Lambda_q, halfnJq, and where
   // the layout gives them room the facet geometry, the mass operator and the
@@ -965,7 +967,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
           Cn = __ldg(fpC + pidx + tpe);
         }
         int i = ij & 0xffff, j = ij >> 16;
-        int f = j / npf;
+        int f = qdiv(j, rnpf);
         float G[D], out[NC];
 #pragma unroll
         for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);

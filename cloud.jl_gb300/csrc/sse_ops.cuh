@@ -47,10 +47,11 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
   }
   const T *A = OpVals<T>::A(op), *B = OpVals<T>::B(op);
   const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
+  const float rM2 = qrcp(M2), rM3 = qrcp(op.M3 > 0 ? op.M3 : 1);
   if constexpr (D == 2) {
     // Z[e][b1][a2] = sum_b2 B[a2,b1,b2] x[sigma(b1,b2)]
     for (int s = lane; s < p1 * M2; s += tpe) {
-      const int a2 = s % M2, b1 = s / M2;
+      const int b1 = qdiv(s, rM2), a2 = s - b1 * M2;
       T acc[NC];
 #pragma unroll
       for (int e = 0; e < NC; ++e) acc[e] = 0;
@@ -65,7 +66,7 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
     }
     __syncthreads();
     for (int s = lane; s < M1 * M2; s += tpe) {
-      const int a2 = s % M2, a1 = s / M2;
+      const int a1 = qdiv(s, rM2), a2 = s - a1 * M2;
       T acc[NC];
 #pragma unroll
       for (int e = 0; e < NC; ++e) acc[e] = 0;
@@ -82,7 +83,7 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
     const T *C = OpVals<T>::C(op);
     const int M3 = op.M3, nb12 = op.nb12;
     for (int s = lane; s < nb12 * M3; s += tpe) {
-      const int a3 = s % M3, q = s / M3;
+      const int q = qdiv(s, rM3), a3 = s - q * M3;
       const int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
       T acc[NC];
 #pragma unroll
@@ -98,7 +99,7 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
     }
     __syncthreads();
     for (int s = lane; s < p1 * M2 * M3; s += tpe) {
-      const int a3 = s % M3, r = s / M3, a2 = r % M2, b1 = r / M2;
+      const int r = qdiv(s, rM3), a3 = s - r * M3, b1 = qdiv(r, rM2), a2 = r - b1 * M2;
       T acc[NC];
 #pragma unroll
       for (int e = 0; e < NC; ++e) acc[e] = 0;
@@ -113,7 +114,7 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
     }
     __syncthreads();
     for (int s = lane; s < M1 * M2 * M3; s += tpe) {
-      const int a3 = s % M3, r = s / M3, a2 = r % M2, a1 = r / M2;
+      const int r = qdiv(s, rM3), a3 = s - r * M3, a1 = qdiv(r, rM2), a2 = r - a1 * M2;
       T acc[NC];
 #pragma unroll
       for (int e = 0; e < NC; ++e) acc[e] = 0;
@@ -159,9 +160,10 @@ __device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lan
   }
   const T *A = OpVals<T>::A(op), *B = OpVals<T>::B(op);
   const int p1 = op.p1, M1 = op.M1, M2 = op.M2;
+  const float rM2 = qrcp(M2), rM3 = qrcp(op.M3 > 0 ? op.M3 : 1);
   if constexpr (D == 2) {
     for (int s = lane; s < p1 * M2; s += tpe) {
-      const int a2 = s % M2, b1 = s / M2;
+      const int b1 = qdiv(s, rM2), a2 = s - b1 * M2;
       T acc[NC];
 #pragma unroll
       for (int e = 0; e < NC; ++e) acc[e] = 0;
@@ -192,7 +194,7 @@ __device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lan
     const T *C = OpVals<T>::C(op);
     const int M3 = op.M3, nb12 = op.nb12;
     for (int s = lane; s < p1 * M2 * M3; s += tpe) {
-      const int a3 = s % M3, r = s / M3, a2 = r % M2, b1 = r / M2;
+      const int r = qdiv(s, rM3), a3 = s - r * M3, b1 = qdiv(r, rM2), a2 = r - b1 * M2;
       T acc[NC];
 #pragma unroll
       for (int e = 0; e < NC; ++e) acc[e] = 0;
@@ -206,7 +208,7 @@ __device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lan
     }
     __syncthreads();
     for (int s = lane; s < nb12 * M3; s += tpe) {
-      const int a3 = s % M3, q = s / M3;
+      const int q = qdiv(s, rM3), a3 = s - q * M3;
       const int b1 = op.b12[q] & 0xff, b2 = op.b12[q] >> 8;
       T acc[NC];
 #pragma unroll
