@@ -782,25 +782,26 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
     if (st_ak) stage_slab(base + L.off[3], Akg, ba, bar);
     if (st_rref) stage_slab(base + L.off[9], Rg, br, bar);
   }
-  // meanwhile: the neighbour's facet states of this thread's first facet node
-  float uo0[NC];
-  if (lane < nf) {
-    const int P = g.mapP[(size_t)kk * nf + lane];
-    const int jn = P % nf, kn = P / nf;
-#pragma unroll
-    for (int e = 0; e < NC; ++e) uo0[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
-  }
+  // meanwhile: where the neighbour's facet state of this thread's first
+  // facet node lives (its gather overlaps the primitives below)
+  const int P0 = lane < nf ? __ldg(g.mapP + (size_t)kk * nf + lane) : 0;
   __syncthreads();  // the mbarrier is initialised
   if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
     if (lane == 0) ka.flag_timeout();
     mbar_wait_bounded(bar, 0);  // give copies still in flight a bounded time to land
     return;
   }
+  float uo0[NC];
+  if (lane < nf) {
+    const int jn = P0 % nf, kn = P0 / nf;
+#pragma unroll
+    for (int e = 0; e < NC; ++e) uo0[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
+  }
   for (int i = lane; i < nq + nf; i += tpe) {
     float du[NC];
 #pragma unroll
     for (int e = 0; e < NC; ++e) du[e] = (i < nq) ? uq[e * nq + i] : uf[e * nf + (i - nq)];
-    euler_prim_mixed<D>(gm1, rho_ref, p_ref, du, prim + (size_t)i * PS);
+    euler_prim_mixed<D>(gm1, rho_ref, p_ref, du, prim + (int)i * PS);
   }
   __syncthreads();
 
@@ -818,7 +819,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
     }
 #pragma unroll
     for (int m = 0; m < D; ++m) n[m] = nfv[m + D * j];
-    const float *Pi = prim + (size_t)(nq + j) * PS;
+    const float *Pi = prim + (int)(nq + j) * PS;
     euler_prim_mixed<D>(gm1, rho_ref, p_ref, uo, Po);
     ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, Pi, Po, n, out);
     float a = 0.f;
@@ -880,9 +881,9 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
 #pragma unroll
         for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
       }
-      ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)j * PS, G, out);
+      ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (int)i * PS, prim + (int)j * PS, G, out);
 #pragma unroll
-      for (int e = 0; e < NC; ++e) diff[(size_t)(pidx - c0) * NC + e] = out[e];
+      for (int e = 0; e < NC; ++e) diff[(int)(pidx - c0) * NC + e] = out[e];
     }
     __syncthreads();
     if (CH >= op.nvp) {
@@ -899,7 +900,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
           for (int r = 0; r < 4; ++r) inc[r] = __ldg(op.vp_inc + q + r);
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
-            const float *dp = diff + (size_t)(inc[r] >> 1) * NC;
+            const float *dp = diff + (int)(inc[r] >> 1) * NC;
             const float sg = (inc[r] & 1) ? -1.f : 1.f;
 #pragma unroll
             for (int e = 0; e < NC; ++e) acc[e] = fmaf(sg, dp[e], acc[e]);
@@ -907,7 +908,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         }
         for (; q < qb; ++q) {
           const int inc = __ldg(op.vp_inc + q);
-          const float *dp = diff + (size_t)(inc >> 1) * NC;
+          const float *dp = diff + (int)(inc >> 1) * NC;
           const float sg = (inc & 1) ? -1.f : 1.f;
 #pragma unroll
           for (int e = 0; e < NC; ++e) acc[e] = fmaf(sg, dp[e], acc[e]);
@@ -931,7 +932,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         const int inc = op.vp_inc[q];
         const int pidx = inc >> 1;
         if (pidx >= c1) break;
-        const float *dp = diff + (size_t)(pidx - c0) * NC;
+        const float *dp = diff + (int)(pidx - c0) * NC;
         if (inc & 1) {
 #pragma unroll
           for (int e = 0; e < NC; ++e) acc[e] -= dp[e];
@@ -971,9 +972,9 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         float G[D], out[NC];
 #pragma unroll
         for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
-        ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, out);
+        ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (int)i * PS, prim + (int)(nq + j) * PS, G, out);
 #pragma unroll
-        for (int e = 0; e < NC; ++e) diff[(size_t)(pidx - c0) * NC + e] = out[e];
+        for (int e = 0; e < NC; ++e) diff[(int)(pidx - c0) * NC + e] = out[e];
       }
       __syncthreads();
       if (CH >= op.nfp) {
@@ -985,24 +986,33 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
           const bool vol = t < nq;
           const int r = vol ? t : t - nq;
           const int *ptr = vol ? op.fp_q_ptr : op.fp_f_ptr;
-          const int *lst = vol ? op.fp_q : op.fp_f;
           const int qa = ptr[r], qb = ptr[r + 1];
-          int q = qa;
-          for (; q + 4 <= qb; q += 4) {
-            int id[4];
+          if (vol) {
+            int q = qa;
+            for (; q + 4 <= qb; q += 4) {
+              int id[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) id[u] = __ldg(lst + q + u);
+              for (int u = 0; u < 4; ++u) id[u] = __ldg(op.fp_q + q + u);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const float *dp = diff + (size_t)id[u] * NC;
+              for (int u = 0; u < 4; ++u) {
+                const float *dp = diff + id[u] * NC;
+#pragma unroll
+                for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+              }
+            }
+            for (; q < qb; ++q) {
+              const float *dp = diff + __ldg(op.fp_q + q) * NC;
 #pragma unroll
               for (int e = 0; e < NC; ++e) acc[e] += dp[e];
             }
-          }
-          for (; q < qb; ++q) {
-            const float *dp = diff + (size_t)__ldg(lst + q) * NC;
+          } else {
+            // the pairs are enumerated facet node by facet node (the columns
+            // of C): a facet node's pairs are the consecutive ids qa..qb-1
+            for (int q = qa; q < qb; ++q) {
+              const float *dp = diff + q * NC;
 #pragma unroll
-            for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+              for (int e = 0; e < NC; ++e) acc[e] += dp[e];
+            }
           }
           float *dst = vol ? rq + r : ff + r;
           const int stride = vol ? nq : nf;
@@ -1021,13 +1031,13 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         for (int e = 0; e < NC; ++e) acc[e] = 0.f;
         const bool vol = t < nq;
         const int r = vol ? t : t - nq;
-        const int *lst = vol ? op.fp_q : op.fp_f;
         const int qe = vol ? op.fp_q_ptr[r + 1] : op.fp_f_ptr[r + 1];
         int q = cur[sl];
         for (; q < qe; ++q) {
-          const int pidx = lst[q];
+          // a facet node's pairs are its consecutive ids (C's columns)
+          const int pidx = vol ? __ldg(op.fp_q + q) : q;
           if (pidx >= c1) break;
-          const float *dp = diff + (size_t)(pidx - c0) * NC;
+          const float *dp = diff + (int)(pidx - c0) * NC;
 #pragma unroll
           for (int e = 0; e < NC; ++e) acc[e] += dp[e];
         }
@@ -1047,7 +1057,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   __syncthreads();
 
   // the pair buffer holds the modal / nodal buffers and the scratch now
-  float *Xm = diff, *Yq = diff + (size_t)NC * np;
+  float *Xm = diff, *Yq = diff + (int)NC * np;
   float *Z = Yq + (size_t)NC * nq;
   float *Wb = Z + ka.vdm_zsz_mixed;
   vdm_tmul<float, D, NC>(op, rq, Xm, Z, Wb, lane, tpe);

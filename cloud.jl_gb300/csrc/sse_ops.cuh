@@ -303,18 +303,31 @@ __device__ void mass_solve(const DevOps &op, const T *JinvW, const T *WJinv, int
         Y[t] = acc;
       }
     } else {
-      for (int a = lane; a < np; a += tpe) {
-        const T *row = Ak + (size_t)a * np;
+      // one row per S consecutive lanes (S = 1, 2 or 4, as many as the team
+      // has threads for), each lane summing every S-th column, the partial
+      // sums combined by shuffles in a fixed order; the team's warps run
+      // the same number of rounds, so every shuffle sees its whole warp
+      const int S = tpe >= 4 * np ? 4 : (tpe >= 2 * np ? 2 : 1);
+      const int rounds = (np * S + tpe - 1) / tpe;
+      for (int rd = 0; rd < rounds; ++rd) {
+        const int t = rd * tpe + lane, a = t / S, sub = t - a * S;
+        const bool act = a < np;
+        const T *row = Ak + (size_t)(act ? a : 0) * np;
         T acc[NC];
 #pragma unroll
         for (int e = 0; e < NC; ++e) acc[e] = 0;
-        for (int b = 0; b < np; ++b) {
-          const T v = row[b];
+        if (act)
+          for (int b = sub; b < np; b += S) {
+            const T v = row[b];
 #pragma unroll
-          for (int e = 0; e < NC; ++e) acc[e] = fma(v, x[e * np + b], acc[e]);
-        }
+            for (int e = 0; e < NC; ++e) acc[e] = fma(v, x[e * np + b], acc[e]);
+          }
+        for (int o = 1; o < S; o <<= 1)
 #pragma unroll
-        for (int e = 0; e < NC; ++e) Y[e * np + a] = acc[e];
+          for (int e = 0; e < NC; ++e) acc[e] += __shfl_xor_sync(0xffffffffu, acc[e], o);
+        if (act && sub == 0)
+#pragma unroll
+          for (int e = 0; e < NC; ++e) Y[e * np + a] = acc[e];
       }
     }
     __syncthreads();
