@@ -100,6 +100,15 @@ struct sse_solver {
     double *w_u = nullptr, *w_tmp = nullptr, *w_comp = nullptr, *w_dudt = nullptr;
     double *w_acc = nullptr, *w_ust = nullptr;
     double *ybar = nullptr, *qbar = nullptr, *yp = nullptr;
+    // binomial schedule (sse_rk_record_binomial): checkpoint slots 0..ckpts
+    // (slot 0 the initial state), stage data of one step, the action list of
+    // the whole reversal, and how far the recording run carried it
+    bool binomial = false;
+    int ckpts = 0;
+    std::vector<int> plan;   // action kind << 28 | argument
+    size_t plan_pos = 0;     // the recorded leaf's action while the descent is intact
+    bool descent_intact = false;
+    long long plan_steps = 0;  // forward steps the whole action list evaluates
   } tape;
 };
 
@@ -1132,6 +1141,87 @@ cudaError_t tape_step(sse_solver *s, double *u, int slot) {
 }
 
 // ---------------------------------------------------------------------------
+// Binomial checkpointing of the Runge-Kutta trajectory (Griewank, Optim.
+// Methods Softw. 1 (1992) 35-54; Griewank & Walther, ACM TOMS 26 (2000)
+// 19-45, "revolve").  F(n, c) is the fewest extra forward steps that
+// reverse n steps, the state before the first being held, with c free
+// checkpoint slots:
+//   F(1, c) = 0,  F(n, 0) = n (n - 1) / 2,
+//   F(n, c) = min over 1 <= m < n of  m + F(n - m, c - 1) + F(m, c)
+// (advance m steps, keep that state in a free slot, reverse the last n - m
+// steps with one slot fewer, then the first m with all of them).  The table
+// holds the optimum and its split m for n up to kBinomialMaxDP steps (fewer
+// when many checkpoints would make it costlier than about 2e8 operations);
+// longer horizons are halved until they reach it.
+// ---------------------------------------------------------------------------
+constexpr int kBinomialMaxDP = 2048;
+
+struct BinomialTable {
+  int N = 0, C = 0;
+  std::vector<long long> F;
+  std::vector<int> M;
+  long long &f(int n, int c) { return F[(size_t)n * (C + 1) + c]; }
+  int &m(int n, int c) { return M[(size_t)n * (C + 1) + c]; }
+  void build(int n_max, int c_max) {
+    // the table costs about N^2 C operations: at most 2e8 (more than N - 1
+    // checkpoints never help for N steps)
+    N = std::min(n_max, kBinomialMaxDP);
+    while (N > 1 && (double)N * N * (std::min(c_max, N - 1) + 1) > 2e8) N = N * 3 / 4;
+    C = std::max(0, std::min(c_max, N - 1));
+    F.assign((size_t)(N + 1) * (C + 1), 0);
+    M.assign((size_t)(N + 1) * (C + 1), 0);
+    for (int n = 1; n <= N; ++n)
+      for (int c = 0; c <= C; ++c) {
+        if (n == 1) { f(n, c) = 0; m(n, c) = 0; continue; }
+        if (c == 0) { f(n, c) = (long long)n * (n - 1) / 2; m(n, c) = 0; continue; }
+        long long best = -1;
+        int arg = 1;
+        for (int k = 1; k < n; ++k) {
+          const long long v = k + f(n - k, c - 1) + f(k, c);
+          if (best < 0 || v < best) { best = v; arg = k; }
+        }
+        f(n, c) = best;
+        m(n, c) = arg;
+      }
+  }
+  // with a slot for every step the optimum keeps every state (split 1)
+  int split(int n, int c) { return c >= n - 1 ? 1 : (n <= N ? m(n, std::min(c, C)) : n / 2); }
+};
+
+enum : int { kActLoad = 0, kActAdvance = 1, kActStore = 2, kActRecRev = 3 };
+inline int act(int kind, int arg) { return kind << 28 | arg; }
+inline int act_kind(int a) { return a >> 28; }
+inline int act_arg(int a) { return a & ((1 << 28) - 1); }
+
+// The actions that reverse steps [l, r) with the state at l in slot sl and
+// slots sl+1 .. sl+c free; returns the forward steps they evaluate.
+long long binomial_plan(int l, int r, int c, int sl, BinomialTable &tab, std::vector<int> &out) {
+  if (r - l == 1) {
+    out.push_back(act(kActLoad, sl));
+    out.push_back(act(kActRecRev, l));
+    return 1;
+  }
+  if (c == 0) {
+    long long steps = 0;
+    for (int i = r - 1; i >= l; --i) {
+      out.push_back(act(kActLoad, sl));
+      if (i > l) out.push_back(act(kActAdvance, i - l));
+      out.push_back(act(kActRecRev, i));
+      steps += i - l + 1;
+    }
+    return steps;
+  }
+  const int m = l + tab.split(r - l, c);
+  out.push_back(act(kActLoad, sl));
+  out.push_back(act(kActAdvance, m - l));
+  out.push_back(act(kActStore, sl + 1));
+  long long steps = m - l;
+  steps += binomial_plan(m, r, c - 1, sl + 1, tab, out);
+  steps += binomial_plan(l, m, c, sl, tab, out);
+  return steps;
+}
+
+// ---------------------------------------------------------------------------
 // Fixed device scratch for sse_residual_static_scratch.
 //
 // The residual's two phases hand the element's volume and facet nodal states
@@ -1469,11 +1559,12 @@ int32_t sse_residual_vjp(sse_solver *s, const double *u, const double *lam, doub
   return check_flag(s);
 }
 
-int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme,
-                      int32_t checkpoint_every, double *t, int32_t memory) {
-  if (!s) return SSE_ERR_INVALID_ARGUMENT;
-  if (!u || n_steps < 1 || checkpoint_every < 0)
-    return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u, n_steps < 1 or negative checkpoint_every");
+// Common set-up of a recording: validates the arguments, fixes the tape's
+// scheme and precision, and returns the bytes of one checkpointed state and
+// of one stage's recorded data.
+static int tape_begin(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme, int32_t memory,
+                      size_t *ckpt_state, size_t *stage_bytes) {
+  if (!u || n_steps < 1) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u or n_steps < 1");
   if (scheme != SSE_CARPENTER_KENNEDY_2N54 && scheme != SSE_RK4)
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown scheme");
   if (memory != SSE_HOST && memory != SSE_DEVICE)
@@ -1486,33 +1577,49 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
   sse_solver::Tape &T = s->tape;
   T.valid = false;
   T.slots_seg = -1;
+  T.binomial = false;
+  T.descent_intact = false;
+  T.plan.clear();
   T.n_steps = n_steps;
   T.scheme = scheme;
   T.stages = scheme == SSE_RK4 ? 4 : 5;
   T.mixed = s->ka.mixed != 0;
   T.nodal = !T.mixed;
   T.dt = dt;
-  const size_t ckpt_state = (T.mixed ? 2 : 1) * n * 8;
-  const size_t stage_bytes = (n + (T.nodal ? nqs + nfs : 0)) * 8;
-  // fixed work buffers: u, tmp, comp, dudt, acc, ust, ybar, qbar, ybar'
-  // (every buffer padded to 256 bytes)
-  const size_t fixed = 9 * (n * 8 + 256);
-  auto need = [&](int every) {
-    const size_t nseg = (n_steps + every - 1) / every;
-    return nseg * ckpt_state + (size_t)every * T.stages * stage_bytes + fixed + 8 * 256;
-  };
+  *ckpt_state = (T.mixed ? 2 : 1) * n * 8;
+  *stage_bytes = (n + (T.nodal ? nqs + nfs : 0)) * 8;
+  return SSE_OK;
+}
+
+// Bytes of a recording with nckpt checkpointed states and the stage data of
+// slot_steps steps: fixed work buffers u, tmp, comp, dudt, acc, ust, ybar,
+// qbar, ybar' (every buffer padded to 256 bytes).
+static size_t tape_bytes(const sse_solver *s, size_t nckpt, size_t slot_steps, size_t ckpt_state,
+                         size_t stage_bytes) {
+  const size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
+  return nckpt * ckpt_state + slot_steps * s->tape.stages * stage_bytes + 9 * (n * 8 + 256) + 8 * 256;
+}
+
+// Device memory a recording may use: 3/4 of what is free (counting the
+// tape's own block) less 512 MiB.
+static int tape_budget(sse_solver *s, double *budget) {
+  size_t free_b = 0, total_b = 0;
+  cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+  if (e != cudaSuccess) return cuda_fail(s, e, "cudaMemGetInfo");
+  *budget = 0.75 * (double)(free_b + s->tape.capacity) - (double)((size_t)512 << 20);
+  return SSE_OK;
+}
+
+// (Re)allocates the tape's block for nckpt checkpoints and slot_steps steps
+// of stage data and carves it.
+static int tape_alloc(sse_solver *s, size_t nckpt, size_t slot_steps, size_t ckpt_state, size_t stage_bytes,
+                      const char *hint) {
+  sse_solver::Tape &T = s->tape;
+  const sse_config &c = s->cfg;
+  const size_t n = (size_t)c.n_p * c.n_c * c.n_e;
+  const size_t nqs = (size_t)c.n_q * c.n_c * c.n_e, nfs = (size_t)c.n_f * c.n_c * c.n_e;
+  const size_t bytes = tape_bytes(s, nckpt, slot_steps, ckpt_state, stage_bytes);
   cudaError_t e;
-  int every = checkpoint_every > 0 ? std::min(checkpoint_every, (int)n_steps) : 1;
-  if (checkpoint_every == 0) {
-    // the longest segments that fit in 3/4 of the free device memory (less
-    // 512 MiB): fewest segments to recompute in the reverse sweep
-    size_t free_b = 0, total_b = 0;
-    if ((e = cudaMemGetInfo(&free_b, &total_b))) return cuda_fail(s, e, "cudaMemGetInfo");
-    const double budget = 0.75 * (double)(free_b + T.capacity) - (double)((size_t)512 << 20);
-    for (int c2 = n_steps; c2 >= 1; --c2)
-      if ((double)need(c2) <= budget) { every = c2; break; }
-  }
-  const size_t bytes = need(every);
   if (bytes > T.capacity) {
     // grow: release the old block first, then check what is free
     if (s->stream && (e = cudaStreamSynchronize(s->stream))) return cuda_fail(s, e, "sync");
@@ -1524,32 +1631,116 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
     if (bytes + ((size_t)256 << 20) > free_b)
       return fail(s, SSE_ERR_OUT_OF_MEMORY,
                   "recording needs " + std::to_string(bytes >> 20) + " MiB of device memory, " +
-                      std::to_string(free_b >> 20) + " MiB free (choose another checkpoint_every)");
+                      std::to_string(free_b >> 20) + " MiB free (" + hint + ")");
     if ((e = cudaMalloc(&T.block, bytes))) {
       T.block = nullptr;
       return fail(s, SSE_ERR_OUT_OF_MEMORY, std::string("recording: ") + cudaGetErrorString(e));
     }
     T.capacity = bytes;
   }
+  T.bytes = bytes;
+  char *cur = (char *)T.block;
+  auto carve = [&](size_t count) {
+    double *p = (double *)cur;
+    cur += (count * 8 + 255) / 256 * 256;
+    return p;
+  };
+  const size_t slots = slot_steps * T.stages;
+  T.ckpt = carve(nckpt * n);
+  T.ckpt_comp = T.mixed ? carve(nckpt * n) : nullptr;
+  T.seg_y = carve(slots * n);
+  T.seg_uq = T.nodal ? carve(slots * nqs) : nullptr;
+  T.seg_uf = T.nodal ? carve(slots * nfs) : nullptr;
+  T.w_u = carve(n); T.w_tmp = carve(n); T.w_comp = carve(n); T.w_dudt = carve(n);
+  T.w_acc = carve(n); T.w_ust = carve(n); T.ybar = carve(n); T.qbar = carve(n); T.yp = carve(n);
+  return SSE_OK;
+}
+
+// Copies between the working state (and the mixed form's compensation) and
+// checkpoint slot g.
+static cudaError_t tape_save(sse_solver *s, const double *u, size_t g) {
+  sse_solver::Tape &T = s->tape;
+  const size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
+  cudaError_t e = cudaMemcpyAsync(T.ckpt + g * n, u, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess && T.mixed)
+    e = cudaMemcpyAsync(T.ckpt_comp + g * n, T.w_comp, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+  return e;
+}
+
+static cudaError_t tape_load(sse_solver *s, size_t g) {
+  sse_solver::Tape &T = s->tape;
+  const size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
+  cudaError_t e = cudaMemcpyAsync(T.w_u, T.ckpt + g * n, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess && T.mixed)
+    e = cudaMemcpyAsync(T.w_comp, T.ckpt_comp + g * n, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+  return e;
+}
+
+// Reverse of one recorded step whose stage data sits in slots q0 ..
+// q0 + stages - 1: ybar <- (du_{i+1}/du_i)^T ybar.
+static cudaError_t reverse_step(sse_solver *s, size_t q0) {
+  sse_solver::Tape &T = s->tape;
+  const sse_config &c = s->cfg;
+  const size_t n = (size_t)c.n_p * c.n_c * c.n_e;
+  const size_t nqs = (size_t)c.n_q * c.n_c * c.n_e, nfs = (size_t)c.n_f * c.n_c * c.n_e;
+  const double dt = T.dt;
+  auto stage_vjp = [&](size_t q, const double *lam) -> cudaError_t {
+    if (T.mixed) return vjp_device_mixed(s, T.seg_y + q * n, lam, s->d_mu);
+    const double *uq = T.nodal ? T.seg_uq + q * nqs : nullptr;
+    const double *uf = T.nodal ? T.seg_uf + q * nfs : nullptr;
+    return vjp_device(s, T.seg_y + q * n, lam, s->d_mu, uq, uf);
+  };
+  cudaError_t e;
+  if (T.scheme == SSE_CARPENTER_KENNEDY_2N54) {
+    e = launch_adj_lincomb(T.qbar, T.ybar, 0.0, kCKB[4], n, s->stream);
+    for (int st = 4; st >= 0 && e == cudaSuccess; --st) {
+      e = stage_vjp(q0 + st, T.qbar);
+      if (e == cudaSuccess)
+        e = launch_adj_ck_stage(T.ybar, T.qbar, s->d_mu, dt, kCKA[st], st > 0 ? kCKB[st - 1] : 0.0, n, s->stream);
+    }
+    return e;
+  }
+  // u' = u + dt/6 (k1 + 2 k2 + 2 k3 + k4), stages y1 = u, y2 = u + dt/2 k1,
+  // y3 = u + dt/2 k2, y4 = u + dt k3
+  e = cudaMemcpyAsync(T.yp, T.ybar, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = launch_adj_lincomb(T.qbar, T.ybar, 0.0, dt / 6, n, s->stream);
+  const double cy[4] = {0.0, dt / 6, dt / 3, dt / 3};  // kbar of stage st-1: cy ybar' + cm mu
+  const double cm[4] = {0.0, dt / 2, dt / 2, dt};
+  for (int st = 3; st >= 0 && e == cudaSuccess; --st) {
+    e = stage_vjp(q0 + st, T.qbar);
+    if (e == cudaSuccess)
+      e = launch_adj_rk4_stage(T.ybar, T.qbar, s->d_mu, T.yp, cy[st], cm[st], st == 0, n, s->stream);
+  }
+  return e;
+}
+
+int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme,
+                      int32_t checkpoint_every, double *t, int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (checkpoint_every < 0) return fail(s, SSE_ERR_INVALID_ARGUMENT, "negative checkpoint_every");
+  size_t ckpt_state = 0, stage_bytes = 0;
+  int rc = tape_begin(s, u, n_steps, dt, scheme, memory, &ckpt_state, &stage_bytes);
+  if (rc != SSE_OK) return rc;
+  const size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
+  sse_solver::Tape &T = s->tape;
+  auto need = [&](int every) {
+    const size_t nseg = (n_steps + every - 1) / every;
+    return tape_bytes(s, nseg, every, ckpt_state, stage_bytes);
+  };
+  cudaError_t e;
+  int every = checkpoint_every > 0 ? std::min(checkpoint_every, (int)n_steps) : 1;
+  if (checkpoint_every == 0) {
+    // the longest segments that fit: fewest segments to recompute in the
+    // reverse sweep
+    double budget = 0;
+    if ((rc = tape_budget(s, &budget)) != SSE_OK) return rc;
+    for (int c2 = n_steps; c2 >= 1; --c2)
+      if ((double)need(c2) <= budget) { every = c2; break; }
+  }
   T.every = every;
   T.nseg = (n_steps + every - 1) / every;
-  T.bytes = bytes;
-  {
-    char *cur = (char *)T.block;
-    auto carve = [&](size_t count) {
-      double *p = (double *)cur;
-      cur += (count * 8 + 255) / 256 * 256;
-      return p;
-    };
-    const size_t slots = (size_t)every * T.stages;
-    T.ckpt = carve(T.nseg * n);
-    T.ckpt_comp = T.mixed ? carve(T.nseg * n) : nullptr;
-    T.seg_y = carve(slots * n);
-    T.seg_uq = T.nodal ? carve(slots * nqs) : nullptr;
-    T.seg_uf = T.nodal ? carve(slots * nfs) : nullptr;
-    T.w_u = carve(n); T.w_tmp = carve(n); T.w_comp = carve(n); T.w_dudt = carve(n);
-    T.w_acc = carve(n); T.w_ust = carve(n); T.ybar = carve(n); T.qbar = carve(n); T.yp = carve(n);
-  }
+  if ((rc = tape_alloc(s, T.nseg, every, ckpt_state, stage_bytes, "choose another checkpoint_every")) != SSE_OK)
+    return rc;
   double *du = u;
   if (memory == SSE_HOST) {
     if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
@@ -1557,14 +1748,7 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
   }
   if (T.mixed && (e = cudaMemsetAsync(T.w_comp, 0, n * 8, s->stream))) return cuda_fail(s, e, "memset");
   for (int step = 0; step < n_steps; ++step) {
-    if (step % every == 0) {
-      const size_t g = step / every;
-      if ((e = cudaMemcpyAsync(T.ckpt + g * n, du, n * 8, cudaMemcpyDeviceToDevice, s->stream)))
-        return cuda_fail(s, e, "checkpoint");
-      if (T.mixed && (e = cudaMemcpyAsync(T.ckpt_comp + g * n, T.w_comp, n * 8, cudaMemcpyDeviceToDevice,
-                                          s->stream)))
-        return cuda_fail(s, e, "checkpoint");
-    }
+    if (step % every == 0 && (e = tape_save(s, du, step / every))) return cuda_fail(s, e, "checkpoint");
     // the last segment's stage data is kept from this run: the reverse
     // sweep starts without recomputing it
     const int last0 = (T.nseg - 1) * every;
@@ -1579,6 +1763,66 @@ int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int3
   return rc;
 }
 
+int32_t sse_rk_record_binomial(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme,
+                               int32_t n_checkpoints, double *t, int32_t memory) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (n_checkpoints < 0) return fail(s, SSE_ERR_INVALID_ARGUMENT, "negative n_checkpoints");
+  size_t ckpt_state = 0, stage_bytes = 0;
+  int rc = tape_begin(s, u, n_steps, dt, scheme, memory, &ckpt_state, &stage_bytes);
+  if (rc != SSE_OK) return rc;
+  const size_t n = (size_t)s->cfg.n_p * s->cfg.n_c * s->cfg.n_e;
+  sse_solver::Tape &T = s->tape;
+  int c = std::min(n_checkpoints, n_steps - 1);
+  if (n_checkpoints == 0) {
+    // as many checkpoints as the budget holds (at most one per step)
+    double budget = 0;
+    if ((rc = tape_budget(s, &budget)) != SSE_OK) return rc;
+    c = 0;
+    for (int k = n_steps - 1; k >= 0; --k)
+      if ((double)tape_bytes(s, (size_t)k + 1, 1, ckpt_state, stage_bytes) <= budget) { c = k; break; }
+  }
+  if ((rc = tape_alloc(s, (size_t)c + 1, 1, ckpt_state, stage_bytes, "choose fewer checkpoints")) != SSE_OK)
+    return rc;
+  T.binomial = true;
+  T.ckpts = c;
+  T.every = 0;
+  T.nseg = c + 1;
+  {
+    BinomialTable tab;
+    tab.build(n_steps, c);
+    T.plan.clear();
+    T.plan_steps = binomial_plan(0, n_steps, c, 0, tab, T.plan);
+  }
+  cudaError_t e;
+  double *du = u;
+  if (memory == SSE_HOST) {
+    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+    du = s->d_u;
+  }
+  if (T.mixed && (e = cudaMemsetAsync(T.w_comp, 0, n * 8, s->stream))) return cuda_fail(s, e, "memset");
+  if ((e = tape_save(s, du, 0))) return cuda_fail(s, e, "checkpoint");
+  // the first descent of the schedule: advance and keep checkpoints down to
+  // the last step, which is taken with its stage data recorded
+  size_t i = 0;
+  for (; i < T.plan.size() && e == cudaSuccess; ++i) {
+    const int a = T.plan[i], k = act_kind(a), arg = act_arg(a);
+    if (k == kActLoad) e = tape_load(s, arg);
+    else if (k == kActStore) e = tape_save(s, T.w_u, arg);
+    else if (k == kActAdvance) for (int j = 0; j < arg && e == cudaSuccess; ++j) e = tape_step(s, T.w_u, -1);
+    else { e = tape_step(s, T.w_u, 0); break; }
+  }
+  if (e != cudaSuccess) return cuda_fail(s, e, "recording");
+  T.plan_pos = i;
+  if ((e = cudaMemcpyAsync(du, T.w_u, n * 8, cudaMemcpyDeviceToDevice, s->stream))) return cuda_fail(s, e, "state");
+  if (memory == SSE_HOST && (e = cudaMemcpyAsync(u, s->d_u, n * 8, cudaMemcpyDeviceToHost, s->stream)))
+    return cuda_fail(s, e, "D2H");
+  if (t) *t += n_steps * dt;
+  rc = check_flag(s);
+  T.valid = rc == SSE_OK;
+  T.descent_intact = T.valid;
+  return rc;
+}
+
 int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double *out_info, int32_t memory) {
   if (!s) return SSE_ERR_INVALID_ARGUMENT;
   if (!lam_T || !lam_0) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null lam_T/lam_0");
@@ -1588,8 +1832,6 @@ int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double
   if (!T.valid) return fail(s, SSE_ERR_INVALID_ARGUMENT, "no recorded trajectory (call sse_rk_record first)");
   const sse_config &c = s->cfg;
   const size_t n = (size_t)c.n_p * c.n_c * c.n_e;
-  const size_t nqs = (size_t)c.n_q * c.n_c * c.n_e, nfs = (size_t)c.n_f * c.n_c * c.n_e;
-  const double dt = T.dt;
   cudaError_t e;
   cudaMemcpyKind kin = memory == SSE_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   if ((e = cudaMemcpyAsync(T.ybar, lam_T, n * 8, kin, s->stream))) return cuda_fail(s, e, "copy lam_T");
@@ -1598,51 +1840,45 @@ int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double
   s->ka.mixed = T.mixed ? 1 : 0;
   if (T.mixed) {
     int rc = enable_adjoint_mixed(s);
-    if (rc != SSE_OK) return rc;
+    if (rc != SSE_OK) { s->ka.mixed = saved_mixed; return rc; }
   }
-  auto stage_vjp = [&](size_t q, const double *lam) -> cudaError_t {
-    if (T.mixed) return vjp_device_mixed(s, T.seg_y + q * n, lam, s->d_mu);
-    const double *uq = T.nodal ? T.seg_uq + q * nqs : nullptr;
-    const double *uf = T.nodal ? T.seg_uf + q * nfs : nullptr;
-    return vjp_device(s, T.seg_y + q * n, lam, s->d_mu, uq, uf);
-  };
-  int recomputed = 0;
-  for (int seg = T.nseg - 1; seg >= 0 && e == cudaSuccess; --seg) {
-    const int s0 = seg * T.every, m = std::min(T.n_steps, s0 + T.every) - s0;
-    if (T.slots_seg != seg) {
-      // recompute the segment from its checkpoint, storing its stage data
-      T.slots_seg = -1;
-      e = cudaMemcpyAsync(T.w_u, T.ckpt + (size_t)seg * n, n * 8, cudaMemcpyDeviceToDevice, s->stream);
-      if (e == cudaSuccess && T.mixed)
-        e = cudaMemcpyAsync(T.w_comp, T.ckpt_comp + (size_t)seg * n, n * 8, cudaMemcpyDeviceToDevice,
-                            s->stream);
-      for (int i = 0; i < m && e == cudaSuccess; ++i) e = tape_step(s, T.w_u, i);
-      if (e == cudaSuccess) T.slots_seg = seg;
-      ++recomputed;
+  long long recomputed = 0;
+  if (T.binomial) {
+    // the schedule's actions; the leaf the recording run took is reversed
+    // from its stage data while the descent's checkpoints are intact
+    size_t i = 0;
+    if (T.descent_intact) {
+      e = reverse_step(s, 0);
+      i = T.plan_pos + 1;
     }
-    for (int i = m - 1; i >= 0 && e == cudaSuccess; --i) {
-      const size_t q0 = (size_t)i * T.stages;
-      if (T.scheme == SSE_CARPENTER_KENNEDY_2N54) {
-        e = launch_adj_lincomb(T.qbar, T.ybar, 0.0, kCKB[4], n, s->stream);
-        for (int st = 4; st >= 0 && e == cudaSuccess; --st) {
-          e = stage_vjp(q0 + st, T.qbar);
-          if (e == cudaSuccess)
-            e = launch_adj_ck_stage(T.ybar, T.qbar, s->d_mu, dt, kCKA[st], st > 0 ? kCKB[st - 1] : 0.0, n,
-                                    s->stream);
-        }
+    for (; i < T.plan.size() && e == cudaSuccess; ++i) {
+      const int a = T.plan[i], k = act_kind(a), arg = act_arg(a);
+      if (k == kActLoad) {
+        e = tape_load(s, arg);
+      } else if (k == kActStore) {
+        e = tape_save(s, T.w_u, arg);
+      } else if (k == kActAdvance) {
+        for (int j = 0; j < arg && e == cudaSuccess; ++j) e = tape_step(s, T.w_u, -1);
+        recomputed += arg;
       } else {
-        // u' = u + dt/6 (k1 + 2 k2 + 2 k3 + k4), stages y1 = u, y2 = u + dt/2 k1,
-        // y3 = u + dt/2 k2, y4 = u + dt k3
-        e = cudaMemcpyAsync(T.yp, T.ybar, n * 8, cudaMemcpyDeviceToDevice, s->stream);
-        if (e == cudaSuccess) e = launch_adj_lincomb(T.qbar, T.ybar, 0.0, dt / 6, n, s->stream);
-        const double cy[4] = {0.0, dt / 6, dt / 3, dt / 3};  // kbar of stage st-1: cy ybar' + cm mu
-        const double cm[4] = {0.0, dt / 2, dt / 2, dt};
-        for (int st = 3; st >= 0 && e == cudaSuccess; --st) {
-          e = stage_vjp(q0 + st, T.qbar);
-          if (e == cudaSuccess)
-            e = launch_adj_rk4_stage(T.ybar, T.qbar, s->d_mu, T.yp, cy[st], cm[st], st == 0, n, s->stream);
-        }
+        e = tape_step(s, T.w_u, 0);
+        if (e == cudaSuccess) e = reverse_step(s, 0);
+        ++recomputed;
       }
+    }
+    T.descent_intact = false;  // the reversal reused the descent's slots
+  } else {
+    for (int seg = T.nseg - 1; seg >= 0 && e == cudaSuccess; --seg) {
+      const int s0 = seg * T.every, m = std::min(T.n_steps, s0 + T.every) - s0;
+      if (T.slots_seg != seg) {
+        // recompute the segment from its checkpoint, storing its stage data
+        T.slots_seg = -1;
+        e = tape_load(s, seg);
+        for (int i = 0; i < m && e == cudaSuccess; ++i) e = tape_step(s, T.w_u, i);
+        if (e == cudaSuccess) T.slots_seg = seg;
+        ++recomputed;
+      }
+      for (int i = m - 1; i >= 0 && e == cudaSuccess; --i) e = reverse_step(s, (size_t)i * T.stages);
     }
   }
   s->ka.mixed = saved_mixed;
@@ -1651,11 +1887,26 @@ int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double
   if ((e = cudaMemcpyAsync(lam_0, T.ybar, n * 8, kout, s->stream))) return cuda_fail(s, e, "copy lam_0");
   if (out_info) {
     out_info[0] = T.nseg;
-    out_info[1] = T.every;
+    out_info[1] = T.binomial ? -1 : T.every;
     out_info[2] = (double)T.bytes;
-    out_info[3] = recomputed;
+    out_info[3] = (double)recomputed;
   }
   return check_flag(s);
+}
+
+// Forward steps (beyond the recorded ones) of the optimal binomial schedule
+// for n_steps steps and n_checkpoints free slots; host only.
+int32_t sse_binomial_schedule(int32_t n_steps, int32_t n_checkpoints, int64_t *extra_steps,
+                              int32_t *first_split) {
+  if (n_steps < 1 || n_checkpoints < 0 || !extra_steps) return SSE_ERR_INVALID_ARGUMENT;
+  const int c = std::min(n_checkpoints, n_steps - 1);
+  BinomialTable tab;
+  tab.build(n_steps, c);
+  std::vector<int> plan;
+  const long long steps = binomial_plan(0, n_steps, c, 0, tab, plan);
+  *extra_steps = steps - n_steps;
+  if (first_split) *first_split = n_steps > 1 && c > 0 ? tab.split(n_steps, c) : 0;
+  return SSE_OK;
 }
 
 int32_t sse_conservation_residual(sse_solver *s, const double *u, const double *dudt, double *out,

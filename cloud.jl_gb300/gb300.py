@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libsse_gb300.so")
 EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual",
             "sse_residual_static_scratch", "sse_nodal_values",
             "sse_rk_steps", "sse_rk_steps_snapshots", "sse_residual_vjp", "sse_rk_record",
-            "sse_rk_adjoint",
+            "sse_rk_adjoint", "sse_rk_record_binomial", "sse_binomial_schedule",
             "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
             "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
             "sse_create_error", "sse_geometric_factors", "sse_project_function",
@@ -70,6 +70,10 @@ def load_library(path: str | None = None):
     L.sse_rk_record.restype = i32
     L.sse_rk_adjoint.argtypes = [vp, vp, vp, vp, i32]
     L.sse_rk_adjoint.restype = i32
+    L.sse_rk_record_binomial.argtypes = [vp, vp, i32, dp, i32, i32, C.POINTER(dp), i32]
+    L.sse_rk_record_binomial.restype = i32
+    L.sse_binomial_schedule.argtypes = [i32, i32, C.POINTER(C.c_int64), C.POINTER(i32)]
+    L.sse_binomial_schedule.restype = i32
     L.sse_conservation_residual.argtypes = [vp, vp, vp, vp, i32]
     L.sse_conservation_residual.restype = i32
     L.sse_energy_residual.argtypes = [vp, vp, vp, vp, i32]
@@ -206,6 +210,17 @@ class GB300Solver:
                                          C.byref(tt), mu))
         return tt.value
 
+    def rk_record_binomial(self, u, n_steps: int, dt: float, scheme: int = abi.SSE_CARPENTER_KENNEDY_2N54,
+                           n_checkpoints: int = 0, t: float = 0.0) -> float:
+        """``rk_steps`` that records for ``rk_adjoint`` on the binomial
+        (revolve) schedule with ``n_checkpoints`` checkpoints (0: as many as
+        fit)."""
+        pu, mu = _addr(u)
+        tt = C.c_double(t)
+        self._check(self.L.sse_rk_record_binomial(self.h, pu, n_steps, dt, scheme, n_checkpoints,
+                                                  C.byref(tt), mu))
+        return tt.value
+
     def rk_adjoint(self, lam_T, lam_0=None) -> dict:
         """(du(T)/du(0))^T lam_T for the last ``rk_record``; returns
         {"lam_0", "segments", "checkpoint_every", "bytes", "recomputed"}."""
@@ -247,6 +262,17 @@ class GB300Solver:
         out = np.zeros(3)
         self._check(self.L.sse_phase_timings(self.h, _addr(u_dev)[0], n_iter, C.c_void_p(out.ctypes.data)))
         return out
+
+
+def binomial_schedule(n_steps: int, n_checkpoints: int):
+    """(extra forward steps, first checkpoint position) of the optimal
+    binomial schedule (sse_binomial_schedule; host arithmetic only)."""
+    L = load_library()
+    extra, first = C.c_int64(0), C.c_int32(0)
+    rc = L.sse_binomial_schedule(n_steps, n_checkpoints, C.byref(extra), C.byref(first))
+    if rc != abi.SSE_OK:
+        raise SSEError(rc, "invalid binomial schedule arguments")
+    return int(extra.value), int(first.value)
 
 
 def measure_fma_peaks():

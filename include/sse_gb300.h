@@ -225,16 +225,42 @@ int32_t sse_residual_vjp(sse_solver *s, const double *u, const double *lam, doub
 int32_t sse_rk_record(sse_solver *s, double *u, int32_t n_steps, double dt, int32_t scheme,
                       int32_t checkpoint_every, double *t, int32_t memory);
 
-/* Reverse sweep of the last sse_rk_record: lam_0 <- (du(T)/du(0))^T lam_T,
- * the gradient of J(u(T)) w.r.t. the initial state when lam_T = dJ/du(T)
- * (both N_p x N_c x N_e, host or device).  Each checkpoint segment is
- * recomputed once, in the precision it was recorded in, storing its RK
- * stage states; the stage adjoints use sse_residual_vjp's kernels at those
- * states, in the recorded precision.  The segment whose stage data is still held (the last one, after
- * sse_rk_record) is not recomputed.  The recording stays valid for further
- * calls.  out_info, if not NULL, receives {segments, checkpoint_every,
- * recording bytes, segments recomputed by this call}.  The pullback half of
- * the stepper's rrule; no counterpart in the reference. */
+/* sse_rk_steps that records the trajectory for sse_rk_adjoint on the
+ * binomial ("revolve") schedule of Griewank & Walther (ACM TOMS 26, 2000),
+ * for horizons whose uniform recording does not fit: only n_checkpoints
+ * states (0: as many as fit in 3/4 of the free device memory less 512 MiB,
+ * at most n_steps - 1) plus the stage data of one step are kept, and the
+ * reverse sweep recomputes the fewest forward steps any schedule with that
+ * many checkpoints can (optimal split table for up to 2048 steps, fewer
+ * when the checkpoints are many, halving beyond).  The gradient is bitwise that of sse_rk_record.  Fails with
+ * SSE_ERR_OUT_OF_MEMORY when even that does not fit.  No counterpart in the
+ * reference. */
+int32_t sse_rk_record_binomial(sse_solver *s, double *u, int32_t n_steps, double dt,
+                               int32_t scheme, int32_t n_checkpoints, double *t,
+                               int32_t memory);
+
+/* Extra forward steps (beyond the n_steps recorded ones) of the optimal
+ * binomial schedule for n_steps steps and n_checkpoints checkpoints, and the
+ * first step at which it places a checkpoint (0 when it places none).  Host
+ * arithmetic only, no device work. */
+int32_t sse_binomial_schedule(int32_t n_steps, int32_t n_checkpoints, int64_t *extra_steps,
+                              int32_t *first_split);
+
+/* Reverse sweep of the last sse_rk_record or sse_rk_record_binomial:
+ * lam_0 <- (du(T)/du(0))^T lam_T, the gradient of J(u(T)) w.r.t. the
+ * initial state when lam_T = dJ/du(T) (both N_p x N_c x N_e, host or
+ * device).  Uniform recording: each checkpoint segment is recomputed once,
+ * in the precision it was recorded in, storing its RK stage states; the
+ * segment whose stage data is still held (the last one, after
+ * sse_rk_record) is not recomputed.  Binomial recording: the schedule's
+ * steps are recomputed from its checkpoints, one step's stage data at a
+ * time.  The stage adjoints use sse_residual_vjp's kernels at the stage
+ * states, in the recorded precision.  The recording stays valid for
+ * further calls.  out_info, if not NULL, receives {segments (binomial:
+ * checkpoint slots including the initial state), checkpoint_every
+ * (binomial: -1), recording bytes, segments (binomial: forward steps)
+ * recomputed by this call}.  The pullback half of the stepper's rrule; no
+ * counterpart in the reference. */
 int32_t sse_rk_adjoint(sse_solver *s, const double *lam_T, double *lam_0, double *out_info,
                        int32_t memory);
 

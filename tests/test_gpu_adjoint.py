@@ -167,6 +167,77 @@ def test_rk_adjoint_checkpoint_interval_invariance(gpu_lib, pkg):
         assert np.array_equal(g, grads[0])
 
 
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_binomial_schedule_matches_uniform_bitwise(scheme, gpu_lib, pkg):
+    """sse_rk_record_binomial: the same gradient, bit for bit, as the uniform
+    recording for any number of checkpoints; the final state is the forward
+    run's; the first pullback recomputes the schedule's extra steps F(n, c),
+    a second one (the descent's slots were reused) all n + F(n, c)."""
+    pb, host = _vortex(pkg)
+    u0 = pkg.setups.perturbed(pb.u0, 41, 1e-3)
+    n_steps = 9
+    G = pkg.GB300Solver(host)
+    lamT = np.random.default_rng(42).standard_normal(u0.shape)
+    uT = u0.copy()
+    G.rk_record(uT, n_steps, pb.dt, scheme, 0)
+    want = G.rk_adjoint(lamT)["lam_0"]
+    for c in (0, 1, 2, 3, 8):
+        u = u0.copy()
+        G.rk_record_binomial(u, n_steps, pb.dt, scheme, c)
+        assert np.array_equal(u, uT)
+        first = G.rk_adjoint(lamT)
+        extra, _ = pkg.gb300.binomial_schedule(n_steps, c if c else n_steps - 1)
+        assert first["checkpoint_every"] == -1
+        assert first["recomputed"] == extra, (c, first["recomputed"], extra)
+        assert np.array_equal(first["lam_0"], want), c
+        second = G.rk_adjoint(lamT)
+        assert second["recomputed"] == n_steps + extra
+        assert np.array_equal(second["lam_0"], want)
+    # the uniform recording still works after a binomial one
+    u = u0.copy()
+    G.rk_record(u, n_steps, pb.dt, scheme, 4)
+    assert np.array_equal(G.rk_adjoint(lamT)["lam_0"], want)
+
+
+def test_binomial_schedule_against_trajectory_tangent(gpu_lib, pkg):
+    pb, host = _vortex(pkg)
+    u0 = pkg.setups.perturbed(pb.u0, 43, 1e-3)
+    n_steps = 11
+    G = pkg.GB300Solver(host)
+    uT = u0.copy()
+    G.rk_record_binomial(uT, n_steps, pb.dt, 0, 2)
+    rng = np.random.default_rng(44)
+    lamT = rng.standard_normal(u0.shape)
+    lam0 = G.rk_adjoint(lamT)["lam_0"]
+    T = O.TangentOracle(host)
+    v = rng.standard_normal(u0.shape)
+    uT_o, w = T.rk_jvp(u0, v, n_steps, pb.dt, 0)
+    assert _dot_rel(lamT, w, lam0, v) < 1e-11
+    assert O.rel2(uT, uT_o) < 1e-12
+
+
+def test_binomial_schedule_mixed_recording(gpu_lib, pkg):
+    """A mixed-form recording on the binomial schedule: the gradient of the
+    uniform mixed recording, bit for bit, within 1e-4 of the FP64 one."""
+    pb, host = _vortex(pkg)
+    u0 = pkg.setups.perturbed(pb.u0, 45, 1e-3)
+    G = pkg.GB300Solver(host)
+    lamT = np.random.default_rng(46).standard_normal(u0.shape)
+    u = u0.copy()
+    G.rk_record(u, 6, pb.dt, 0, 2)
+    g64 = G.rk_adjoint(lamT)["lam_0"]
+    G.set_precision(pkg.abi.SSE_MIXED)
+    u = u0.copy()
+    G.rk_record(u, 6, pb.dt, 0, 0)
+    gm = G.rk_adjoint(lamT)["lam_0"]
+    ub = u0.copy()
+    G.rk_record_binomial(ub, 6, pb.dt, 0, 2)
+    gb = G.rk_adjoint(lamT)["lam_0"]
+    assert np.array_equal(ub, u)
+    assert np.array_equal(gb, gm)
+    assert O.rel2(gb, g64) < 1e-4
+
+
 @pytest.mark.parametrize("name", ["vortex_tri_modal", "tgv_tet_modal", "tgv_tet_ec", "tgv_tet_p5",
                                   "multi_tet", "tgv_tet_exact", "tgv_tet_ec_exact", "vortex_tri_exact"])
 def test_mixed_vjp_against_fp64(name, gpu_lib, pkg):
