@@ -275,9 +275,14 @@ def adjoint_workload(pkg, gpu, host, u0_np, dt, steps, fwd_ms, stream):
                     "checkpoint_every_steps": info["checkpoint_every"], "segments": info["segments"],
                     "segments_recomputed": info["recomputed"], "recording_bytes": info["bytes"]}
         out["kinetic_energy_T"] = ke
+    # the binomial (revolve) schedule with three checkpoints: a fraction of
+    # the memory, more recomputation, the same gradient
+    out["binomial_3_checkpoints"] = binomial_leg(pkg, gpu, host, u0_np, dt, steps, 3, fwd_ms, stream)
+    grads["binomial"] = out["binomial_3_checkpoints"].pop("lam_0")
     g = grads["memory_sized"]
     out["grad_norm_momentum"] = float(np.linalg.norm(g[:, 1:-1]))
     out["gradients_identical_across_intervals"] = bool(np.array_equal(g, grads["every_2_steps"]))
+    out["binomial_gradient_identical"] = bool(np.array_equal(g, grads["binomial"]))
     out["adjoint_over_forward"] = out["every_2_steps"]["adjoint_over_forward"]
     # the same pullback of a mixed-form recording (mixed-form VJP), against
     # the mixed forward of the same steps
@@ -303,6 +308,25 @@ def adjoint_workload(pkg, gpu, host, u0_np, dt, steps, fwd_ms, stream):
     finally:
         gpu.set_precision(abi.SSE_FP64)
     return out
+
+
+def binomial_leg(pkg, gpu, host, u0_np, dt, steps, n_checkpoints, fwd_ms, stream):
+    """Kinetic-energy pullback recorded on the binomial schedule
+    (sse_rk_record_binomial) with n_checkpoints checkpoints."""
+    import torch
+    gpu.rk_record_binomial(torch.from_numpy(u0_np).cuda(), min(steps, 2), dt, 0, n_checkpoints)  # warm-up
+    u = torch.from_numpy(u0_np).cuda()
+    rec_ms, _ = timed(stream, lambda: gpu.rk_record_binomial(u, steps, dt, 0, n_checkpoints))
+    ke, dke = pkg.objectives.kinetic_energy(host, u.cpu().numpy())
+    lamT = torch.from_numpy(dke).cuda()
+    lam0 = torch.empty_like(lamT)
+    adj_ms, info = timed(stream, lambda: gpu.rk_adjoint(lamT, lam0))
+    extra, first = pkg.gb300.binomial_schedule(steps, n_checkpoints)
+    return {"checkpoints": n_checkpoints, "record_ms": rec_ms, "adjoint_ms": adj_ms,
+            "adjoint_over_forward": adj_ms / fwd_ms, "record_over_forward": rec_ms / fwd_ms,
+            "steps_recomputed": info["recomputed"], "schedule_extra_steps": extra,
+            "first_checkpoint_step": first, "recording_bytes": info["bytes"],
+            "lam_0": lam0.cpu().numpy()}
 
 
 def adjoint_mixed_workload(pkg, gpu, host, u0_np, dt, steps, stream):
@@ -332,6 +356,12 @@ def adjoint_mixed_workload(pkg, gpu, host, u0_np, dt, steps, stream):
                     "segments_recomputed": info["recomputed"], "recording_bytes": info["bytes"],
                     "kinetic_energy_T": ke}
     gpu.set_precision(abi.SSE_FP64)
+    # the FP64 pullback again on the binomial schedule with eight checkpoints
+    # (a few GB instead of the uniform recording's block)
+    out["fp64_binomial_8_checkpoints"] = binomial_leg(pkg, gpu, host, u0_np, dt, steps, 8,
+                                                      out["fp64"]["forward_ms"], stream)
+    gb = out["fp64_binomial_8_checkpoints"].pop("lam_0")
+    out["fp64_binomial_8_checkpoints"]["gradient_identical_to_uniform"] = bool(np.array_equal(gb, grads["fp64"]))
     gm, g64 = grads["mixed"][:, 1:-1], grads["fp64"][:, 1:-1]
     out["gradient_rel_err_mixed_vs_fp64_adjoint"] = float(np.linalg.norm(gm - g64) / np.linalg.norm(g64))
     out["adjoint_over_forward"] = out["mixed"]["adjoint_over_forward"]
