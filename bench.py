@@ -220,9 +220,12 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def cpu_baseline(pb, host, budget_s: float):
+def cpu_baseline(pb, host, budget_s: float, nthreads: int | None = None):
+    """The reference's residual restated in C, timed on the host cores with
+    OpenMP over elements (the reference's Threaded() strategy), on all
+    cores or on nthreads."""
     from oracle.oracle import Oracle
-    o = Oracle(host)
+    o = Oracle(host, nthreads=nthreads)
     u = pb.u0
     o.residual(u)
     n, t0 = 0, time.perf_counter()
@@ -725,6 +728,7 @@ def main():
             "mixed": mixed, "adjoint": adjoint, "geometric_factors": geometry}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pb, host, args.cpu_budget)
+        line["cpu_baseline_1_core"] = cpu_baseline(pb, host, args.cpu_budget / 2, nthreads=1)
     if rank == 0:
         print(json.dumps(line))
 

@@ -181,6 +181,59 @@ class TangentOracle:
         return u, v
 
 
+EXTENDED_SRC = os.path.join(HERE, "sse_oracle_extended.cpp")
+
+
+def build_extended(force: bool = False) -> str:
+    """Compile the extended-precision (long double) build of the same
+    oracle source (g++ -O3 -fopenmp, no contraction beyond explicit fma())."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = os.path.join(BUILD, "libsse_oracle_extended.so")
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR), os.path.getmtime(EXTENDED_SRC))
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return out
+    cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           EXTENDED_SRC, "-o", out + ".tmp", "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+_extended_lib = None
+
+
+class ExtendedOracle:
+    """The oracle's residual evaluated in long double (the reference for
+    measuring how far an FP64 residual is from the exact one)."""
+
+    def __init__(self, host, nthreads: int | None = None):
+        global _extended_lib
+        if _extended_lib is None:
+            L = C.CDLL(build_extended())
+            L.oracle_extended_create.restype = C.c_void_p
+            L.oracle_extended_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+            L.oracle_extended_destroy.argtypes = [C.c_void_p]
+            L.oracle_extended_residual.argtypes = [C.c_void_p] * 3
+            L.oracle_extended_digits.restype = C.c_int
+            _extended_lib = L
+        self.L = _extended_lib
+        self.host = host
+        self.digits = self.L.oracle_extended_digits()
+        self.h = self.L.oracle_extended_create(C.byref(host.cfg), C.byref(host.ops), C.byref(host.geo),
+                                               nthreads or lib().oracle_threads())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.oracle_extended_destroy(self.h)
+            self.h = None
+
+    def residual(self, u: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.empty_like(u)
+        self.L.oracle_extended_residual(self.h, _ptr(u), _ptr(out))
+        return out
+
+
 def rel2(got, want) -> float:
     """Whole-vector relative error ||got - want||_2 / ||want||_2."""
     got = np.asarray(got, dtype=np.float64)

@@ -307,6 +307,34 @@ def test_gradient_against_central_differences(gpu_lib, pkg):
         assert abs(fd - ad) <= 1e-5 * max(abs(ad), 1e-3 * np.linalg.norm(grad)), (fd, ad)
 
 
+def test_c4_submesh_gradient_against_dual_numbers(gpu_lib, pkg):
+    """The C4 adjoint configuration on its 4 x 4 sub-mesh (32 curved
+    triangles, ModalTensor(4), FD + LF): J = 1/2 ||u(T) - u_target||^2_M
+    after 400 CarpenterKennedy2N54 stages with checkpoints every 20 stages,
+    u_target the perturbed vortex of strength 5.5 shifted by 0.3.  The GPU
+    gradient against forward-mode dual numbers through the oracle's
+    residual along 8 seeded directions: dJ . v = <M (u(T) - u_target),
+    (du(T)/du(0)) v>."""
+    pb = pkg.setups.vortex_tri(cells=4, p=4)
+    host = pb.host_arrays()
+    tgt = pkg.setups.perturbed(pkg.setups.vortex_tri(cells=4, p=4, strength=5.5, shift=0.3).u0,
+                               20261207, 1e-3)
+    obj = pkg.objectives
+    n_steps, dt = 80, pb.dt
+    G = pkg.GB300Solver(host)
+    uT = pb.u0.copy()
+    G.rk_record(uT, n_steps, dt, 0, 4)
+    _, dJ = obj.mass_misfit(host, uT, tgt)
+    grad = G.rk_adjoint(dJ)["lam_0"]
+    T = O.TangentOracle(host)
+    rng = np.random.default_rng(20261208)
+    for _ in range(8):
+        v = rng.standard_normal(pb.u0.shape)
+        uT_o, w = T.rk_jvp(pb.u0, v, n_steps, dt, 0)
+        assert _dot_rel(dJ, w, grad, v) < 1e-11
+    assert O.rel2(uT, uT_o) < 1e-12
+
+
 def test_recording_larger_than_memory_is_refused(gpu_lib, pkg):
     """A recording that cannot fit is refused on the host before any step
     runs (the state is left as it was)."""

@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 import cases
-from oracle.oracle import Oracle, rel2, roundoff_floor
+from oracle.oracle import ExtendedOracle, Oracle, rel2, roundoff_floor
 
 pytestmark = pytest.mark.gpu
 
@@ -52,6 +52,39 @@ def test_residual_matches_oracle(built, pkg, name):
     print(f"{name}: rel2 {err:.2e}  oracle floor {floor:.2e}")
     assert err <= max(TOL, 4.0 * floor)
     assert relerr(got, want) <= TOL_COMPONENT
+
+
+def _c3_like(pkg, cells, p):
+    """The C3 configuration (Taylor-Green, Mach 0.1, Chan warp 0.05, FD with
+    EC volume flux + LF) on a coarser mesh, with the parity perturbation."""
+    pb = pkg.setups.tgv_tet(cells=cells, p=p)
+    return pb.host_arrays(), pkg.setups.perturbed(pb.u0, 20261203 + cells + p, 1.0e-3)
+
+
+@pytest.mark.parametrize("name", ["vortex_tri_modal", "tgv_tet_modal", "tgv_tet_p5", "tgv_tet_exact",
+                                  "tgv_tet_nodal", "c3_384", "c5_162"])
+def test_error_against_extended_precision(built, pkg, name):
+    """Cancellation-aware FP64 parity: the library's residual and the FP64
+    oracle's both measured against the oracle evaluated in extended
+    precision (long double).  On the low-Mach Taylor-Green tets with
+    Lax-Friedrichs dissipation a residual entry is a small difference of
+    flux contributions ~1e4 times larger, and every FP64 evaluation lands
+    about 1e-12 from the exact residual; the library must be no farther from
+    it than the FP64 oracle is (within 1.5x, summation order differs), and
+    within 1e-12 wherever the FP64 oracle is."""
+    if name == "c3_384":
+        host, u = _c3_like(pkg, 4, 4)
+    elif name == "c5_162":
+        host, u = _c3_like(pkg, 3, 5)
+    else:
+        host, u = cases.make(name)
+    rx = ExtendedOracle(host).residual(u)
+    e_gpu = rel2(pkg.GB300Solver(host).residual(u), rx)
+    e_64 = max(rel2(Oracle(host).residual(u), rx), rel2(Oracle(host, variant="fma").residual(u), rx))
+    print(f"{name}: vs extended precision: GPU {e_gpu:.2e}, FP64 oracle {e_64:.2e}")
+    assert e_gpu <= 1.5 * e_64 + 1e-15
+    if e_64 <= 1e-12:
+        assert e_gpu <= 1e-12
 
 
 @pytest.mark.parametrize("name", ["adv_tri_modal", "vortex_tri_modal", "vortex_tri_nodal",
