@@ -316,17 +316,21 @@ def tri_nodes(n: int, alpha: float = 0.0):
     return r, s
 
 
-def tet_nodes(n: int):
-    """Degree-``n`` interpolation nodes on the tetrahedron.
+def _face_warp(n: int, l1, l2, l3):
+    """Warp-and-blend shift (dx, dy) of points of an equilateral triangle
+    with barycentric coordinates l1, l2, l3 (alpha = 0): the 1-D warp of the
+    edge opposite each vertex blended by the product of the other two
+    coordinates -- the triangle construction of tri_nodes, in the form
+    Warburton (2006) uses on the faces of the tetrahedron."""
+    w1 = 4.0 * l2 * l3 * _warp_factor(n, l3 - l2)
+    w2 = 4.0 * l1 * l3 * _warp_factor(n, l1 - l3)
+    w3 = 4.0 * l1 * l2 * _warp_factor(n, l2 - l1)
+    dx = w1 + math.cos(2.0 * math.pi / 3.0) * w2 + math.cos(4.0 * math.pi / 3.0) * w3
+    dy = math.sin(2.0 * math.pi / 3.0) * w2 + math.sin(4.0 * math.pi / 3.0) * w3
+    return dx, dy
 
-    Equispaced lattice in barycentric coordinates, ordered with the
-    lattice index of the t-direction outermost.  For n = 1 these are the
-    vertices (-1,-1,-1), (1,-1,-1), (-1,1,-1), (-1,-1,1).  The nodes only
-    carry the polynomial mapping; any unisolvent set gives the same
-    degree-n interpolant of an analytic warp up to the interpolation error,
-    and at the degrees used here (n <= 6) the equispaced set is well
-    conditioned.
-    """
+
+def _tet_equispaced(n: int):
     r, s, t = [], [], []
     for k in range(n + 1):
         for j in range(n + 1 - k):
@@ -335,3 +339,57 @@ def tet_nodes(n: int):
                 s.append(-1.0 + 2.0 * j / n)
                 t.append(-1.0 + 2.0 * k / n)
     return np.array(r), np.array(s), np.array(t)
+
+
+def tet_nodes(n: int, kind: str = "warp_blend"):
+    """Degree-``n`` interpolation nodes on the tetrahedron.
+
+    ``kind="warp_blend"`` (default): Warburton's warp-and-blend nodes (T.
+    Warburton, J. Eng. Math. 56 (2006) 247-262), the tetrahedral counterpart
+    of tri_nodes with the same blending exponent alpha = 0: the equispaced
+    lattice in an equilateral tetrahedron is shifted, face by face, by the
+    triangle's warp in the face's tangent plane, blended into the volume by
+    Lb Lc Ld / ((Lb + La/2)(Lc + La/2)(Ld + La/2)) for the face La = 0; on
+    the faces the nodes are exactly the triangle's, on the edges the
+    Gauss-Lobatto points.  ``kind="equispaced"``: the plain lattice.
+    Ordering (both): the lattice index of t outermost, r innermost; for n =
+    1 the vertices (-1,-1,-1), (1,-1,-1), (-1,1,-1), (-1,-1,1).  These are
+    the mapping nodes of the curved tetrahedra (``nodes(Tet(), N)`` of the
+    reference's RefElemData, ref_elem_data.jl:77).
+    """
+    r, s, t = _tet_equispaced(n)
+    if kind == "equispaced" or n <= 2:
+        # degrees <= 2: the Gauss-Lobatto points are equispaced
+        return r, s, t
+    if kind != "warp_blend":
+        raise ValueError(kind)
+    L1, L2 = (1.0 + t) / 2.0, (1.0 + s) / 2.0
+    L3, L4 = -(1.0 + r + s + t) / 2.0, (1.0 + r) / 2.0
+    v1 = np.array([-1.0, -1.0 / math.sqrt(3.0), -1.0 / math.sqrt(6.0)])
+    v2 = np.array([1.0, -1.0 / math.sqrt(3.0), -1.0 / math.sqrt(6.0)])
+    v3 = np.array([0.0, 2.0 / math.sqrt(3.0), -1.0 / math.sqrt(6.0)])
+    v4 = np.array([0.0, 0.0, 3.0 / math.sqrt(6.0)])
+    # orthonormal tangents of the four faces
+    t1 = [v2 - v1, v2 - v1, v3 - v2, v3 - v1]
+    t2 = [v3 - 0.5 * (v1 + v2), v4 - 0.5 * (v1 + v2), v4 - 0.5 * (v2 + v3), v4 - 0.5 * (v1 + v3)]
+    t1 = [x / np.linalg.norm(x) for x in t1]
+    t2 = [x / np.linalg.norm(x) for x in t2]
+    xyz = np.outer(L3, v1) + np.outer(L4, v2) + np.outer(L2, v3) + np.outer(L1, v4)
+    shift = np.zeros_like(xyz)
+    tol = 1.0e-10
+    faces = [(L1, L2, L3, L4), (L2, L1, L3, L4), (L3, L1, L4, L2), (L4, L1, L3, L2)]
+    for f, (La, Lb, Lc, Ld) in enumerate(faces):
+        w1, w2 = _face_warp(n, Lb, Lc, Ld)
+        blend = Lb * Lc * Ld
+        denom = (Lb + 0.5 * La) * (Lc + 0.5 * La) * (Ld + 0.5 * La)
+        blend = np.where(denom > tol, blend / np.where(denom > tol, denom, 1.0), blend)
+        shift += np.outer(blend * w1, t1[f]) + np.outer(blend * w2, t2[f])
+        # nodes of this face that lie on an edge take the face's warp alone
+        on_edge = (La < tol) & (((Lb > tol).astype(int) + (Lc > tol) + (Ld > tol)) < 3)
+        shift[on_edge] = np.outer(w1[on_edge], t1[f]) + np.outer(w2[on_edge], t2[f])
+    xyz = xyz + shift
+    # equilateral -> reference coordinates: xyz = v1 + (r+1)/2 (v2-v1) + (s+1)/2 (v3-v1) + (t+1)/2 (v4-v1)
+    A = 0.5 * np.column_stack([v2 - v1, v3 - v1, v4 - v1])
+    rhs = xyz - 0.5 * (v2 + v3 + v4 - v1)
+    rst = np.linalg.solve(A, rhs.T)
+    return rst[0], rst[1], rst[2]

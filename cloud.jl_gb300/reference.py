@@ -240,8 +240,13 @@ def _simplex_basis(shape, N, *rst):
     return V, (Vr, Vs, Vt)
 
 
+# mapping nodes of the tetrahedron: Warburton's warp-and-blend set (the
+# counterpart of the triangle's), or "equispaced"
+TET_MAPPING_NODES = "warp_blend"
+
+
 def simplex_nodes(shape: str, N: int):
-    return P.tri_nodes(N) if shape == "Tri" else P.tet_nodes(N)
+    return P.tri_nodes(N) if shape == "Tri" else P.tet_nodes(N, TET_MAPPING_NODES)
 
 
 def _ref_elem(shape: str, N: int, rstq, wq, rstf, wf, nrstJ, num_faces) -> RefElem:

@@ -64,3 +64,37 @@ def test_warp_and_blend_vertices_and_edges(pkg):
     r, s = P.tri_nodes(4)
     edge = np.sort(r[np.abs(s + 1) < 1e-14])
     assert np.abs(edge - P.gauss_lobatto_nodes(4)).max() < 1e-14
+
+
+def _sorted_barycentric(points):
+    """Each point's barycentric coordinates, sorted, as a sorted array (a
+    set invariant under the simplex's symmetries)."""
+    b = np.sort(np.round(np.asarray(points), 11) + 0.0, axis=1)
+    return b[np.lexsort(b.T[::-1])]
+
+
+@pytest.mark.parametrize("n", [3, 4, 5, 6])
+def test_tet_warp_and_blend_faces_and_edges(pkg, n):
+    """Every face of the tetrahedral set carries the triangle's warp-and-blend
+    nodes and every edge the Gauss-Lobatto points; all nodes lie in the
+    element, and n = 1 gives the vertices in the lattice order."""
+    P = pkg.polynomials
+    r, s, t = P.tet_nodes(n)
+    lam = np.stack([(1 + t) / 2, (1 + s) / 2, -(1 + r + s + t) / 2, (1 + r) / 2], 1)
+    assert lam.min() > -1e-13
+    tr, ts = P.tri_nodes(n)
+    tri = _sorted_barycentric(np.stack([(1 + ts) / 2, -(tr + ts) / 2, (1 + tr) / 2], 1))
+    for f in range(4):
+        on = np.abs(lam[:, f]) < 1e-12
+        face = _sorted_barycentric(np.delete(lam[on], f, axis=1))
+        assert face.shape == tri.shape and np.abs(face - tri).max() < 1e-12, f
+    lgl = np.sort((1 + P.gauss_lobatto_nodes(n)) / 2)
+    for a in range(4):
+        for b in range(a + 1, 4):
+            rest = [c for c in range(4) if c not in (a, b)]
+            on = np.all(np.abs(lam[:, rest]) < 1e-12, axis=1)
+            assert np.abs(np.sort(lam[on, a]) - lgl).max() < 1e-12, (a, b)
+    r1, s1, t1 = P.tet_nodes(1)
+    assert np.allclose(np.stack([r1, s1, t1], 1), [[-1, -1, -1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]])
+    re, se, te = P.tet_nodes(n, "equispaced")
+    assert np.allclose(np.sort(re), np.sort(-1 + 2 * np.round((re + 1) * n / 2) / n))
