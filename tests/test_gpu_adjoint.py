@@ -5,6 +5,8 @@ small mesh, the adjoint Runge-Kutta sweep against the tangent of the whole
 oracle trajectory, checkpoint-interval invariance, the mixed-form
 recording, and central differences of an objective through the GPU
 forward."""
+import math
+
 import numpy as np
 import pytest
 
@@ -310,7 +312,8 @@ def test_gradient_against_central_differences(gpu_lib, pkg):
 def test_c4_submesh_gradient_against_dual_numbers(gpu_lib, pkg):
     """The C4 adjoint configuration on its 4 x 4 sub-mesh (32 curved
     triangles, ModalTensor(4), FD + LF): J = 1/2 ||u(T) - u_target||^2_M
-    after 400 CarpenterKennedy2N54 stages with checkpoints every 20 stages,
+    after 400 CarpenterKennedy2N54 stages of C4's time step, checkpoints
+    every 20 stages,
     u_target the perturbed vortex of strength 5.5 shifted by 0.3.  The GPU
     gradient against forward-mode dual numbers through the oracle's
     residual along 8 seeded directions: dJ . v = <M (u(T) - u_target),
@@ -320,7 +323,10 @@ def test_c4_submesh_gradient_against_dual_numbers(gpu_lib, pkg):
     tgt = pkg.setups.perturbed(pkg.setups.vortex_tri(cells=4, p=4, strength=5.5, shift=0.3).u0,
                                20261207, 1e-3)
     obj = pkg.objectives
-    n_steps, dt = 80, pb.dt
+    # the time step of the C4 configuration itself (8192 triangles: h =
+    # 10 / sqrt(N_p N_e), CFL 0.1 against |V| + c = sqrt(2) + 1)
+    n_steps = 80
+    dt = 0.1 * (10.0 / math.sqrt(15 * 8192)) / (math.sqrt(2.0) + 1.0)
     G = pkg.GB300Solver(host)
     uT = pb.u0.copy()
     G.rk_record(uT, n_steps, dt, 0, 4)
