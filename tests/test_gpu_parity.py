@@ -71,8 +71,8 @@ def test_error_against_extended_precision(built, pkg, name):
     flux contributions ~1e4 times larger, and every FP64 evaluation lands
     about 1e-12 from the exact residual; the library must be no farther from
     it than about the FP64 oracle is (within 2x: the summation orders and
-    contractions differ; measured 1.3-1.5x), and
-    within 1e-12 wherever the FP64 oracle is."""
+    contractions differ; measured 1.2-1.5x), and within 1e-12 wherever an
+    FP64 evaluation reaches 5e-13."""
     if name == "c3_384":
         host, u = _c3_like(pkg, 4, 4)
     elif name == "c5_162":
@@ -84,7 +84,7 @@ def test_error_against_extended_precision(built, pkg, name):
     e_64 = max(rel2(Oracle(host).residual(u), rx), rel2(Oracle(host, variant="fma").residual(u), rx))
     print(f"{name}: vs extended precision: GPU {e_gpu:.2e}, FP64 oracle {e_64:.2e}")
     assert e_gpu <= 2.0 * e_64 + 1e-15
-    if e_64 <= 1e-12:
+    if e_64 <= 0.5e-12:
         assert e_gpu <= 1e-12
 
 
