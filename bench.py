@@ -590,15 +590,21 @@ def main():
     work = pkg.flops_model.model(host)
     fp64_peak, fp32_peak = pkg.gb300.measure_fma_peaks()
     ne = host.N_e
+    one_kernel = gpu.kernel_path() == pkg.abi.SSE_PATH_ONE_KERNEL
     dom = "B" if phases[1] >= phases[0] else "A"
     dom_ms = phases[1] if dom == "B" else phases[0]
     dom_flops = (work.flops_B if dom == "B" else work.flops_A) * ne
     dom_bytes = (work.bytes_B if dom == "B" else work.bytes_A) * ne
+    if one_kernel:
+        # one kernel evaluates the whole residual: both phases' algorithmic work
+        dom_flops = work.flops * ne
+        dom_bytes = pkg.flops_model.one_kernel_bytes(host) * ne
     achieved = dom_flops / (dom_ms * 1e-3) / 1e12
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    kernel_B = "fd_time_derivative_kernel" if fd else "std_time_derivative_kernel"
+    kernel_B = "fd_time_derivative_kernel" if fd else (
+        "std_compact_kernel" if one_kernel else "std_time_derivative_kernel")
     traffic = TRAFFIC_PER_ELEMENT.get(args.workload) if not (args.cells or args.p) else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak,
@@ -615,6 +621,8 @@ def main():
                 "algorithmic_flops_per_element": {"nodal_values": work.flops_A,
                                                   "time_derivative": work.flops_B},
                 "whole_stage_frac": (work.flops * ne) / ((phases[0] + phases[1]) * 1e-3) / 1e12 / fp64_peak,
+                "kernel_path": "one kernel per residual and per stage (std_compact_kernel)" if one_kernel
+                else "two phases (nodal values, time derivative)",
                 "fp32_peak_tflops": fp32_peak}
 
     # ---- mixed FP32/FP64 form on the same handle: same steps from the same
@@ -717,8 +725,9 @@ def main():
                  "call": "sse_rk_steps(u_host, 1 step) per step: one H2D and one D2H of the state "
                          "per step, every stage on the device"}
 
-    # per stage: phase A, phase B and one stage-update kernel
-    launches = args.steps * stages * 3
+    # per stage: phase A, phase B and one stage-update kernel, or the one
+    # kernel that evaluates the stage's residual and applies its update
+    launches = args.steps * stages * (1 if one_kernel else 3)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

@@ -30,6 +30,8 @@ SSE_WEIGHT_ADJUSTED = 0
 SSE_DIAGONAL = 1
 SSE_FP64 = 0
 SSE_MIXED = 1
+SSE_PATH_TWO_PHASE = 0
+SSE_PATH_ONE_KERNEL = 1
 SSE_HOST = 0
 SSE_DEVICE = 1
 SSE_CARPENTER_KENNEDY_2N54 = 0

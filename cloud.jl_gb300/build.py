@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsse_gb300.so")
-SOURCES = ["sse_kernels.cu", "sse_adjoint.cu", "sse_abi.cu", "sse_peaks.cu", "sse_geometry.cu", "sse_project.cu"]
+SOURCES = ["sse_kernels.cu", "sse_adjoint.cu", "sse_abi.cu", "sse_peaks.cu", "sse_geometry.cu", "sse_project.cu", "sse_compact.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -58,6 +58,7 @@ struct sse_solver {
   double *d_u = nullptr, *d_dudt = nullptr, *d_tmp = nullptr, *d_acc = nullptr, *d_ust = nullptr;
   double *d_partial = nullptr, *d_uf_ref = nullptr;
   int *d_flag = nullptr;
+  int *h_flag = nullptr;    // pinned host copy of the flag (read after each call)
   int precision = SSE_FP64;
   std::string last_error;
   // element counts of the device operator arrays (for the FP32 roundings)
@@ -67,6 +68,8 @@ struct sse_solver {
   bool ref_ready = false;   // reference state of the mixed form chosen
   double *d_comp = nullptr; // compensation of the mixed form's stage accumulation
   double *d_rref = nullptr; // FP64 residual of the mixed form's reference state
+  bool compact_ok = false;  // std_compact_kernel applies to this configuration
+  double *d_ust2 = nullptr; // second stage buffer of the one-kernel stages
   std::vector<double> h_partial;  // host copy of the per-element sums (sized once)
   // one Runge-Kutta step captured as a CUDA graph, replayed by sse_rk_steps;
   // rebuilt when any of the values it was captured with changes
@@ -74,7 +77,7 @@ struct sse_solver {
     cudaGraphExec_t exec = nullptr;
     double *u = nullptr;
     double dt = 0.0;
-    int scheme = -1, mixed = -1;
+    int scheme = -1, mixed = -1, compact = -1;
     cudaStream_t stream = nullptr;
   } step_graph;
   // discrete adjoint: VJP scratch (allocated on first use)
@@ -124,12 +127,13 @@ int cuda_fail(sse_solver *s, cudaError_t e, const char *where) {
   return fail(s, SSE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// (uploaded arrays carry the same 64 bytes of slack as alloc's buffers)
 template <typename T>
 cudaError_t upload(sse_solver *s, const T *host, size_t n, const T **dev) {
   *dev = nullptr;
   if (n == 0) return cudaSuccess;
   void *p = nullptr;
-  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T) + 64);
   if (e != cudaSuccess) return e;
   s->allocations.push_back(p);
   e = cudaMemcpy(p, host, n * sizeof(T), cudaMemcpyHostToDevice);
@@ -217,6 +221,150 @@ size_t geo_len(const sse_config &c, int what) {
     case 5: return d * c.num_faces * nq * ne;  // halfnJq
   }
   return 0;
+}
+
+// dense rows x cols copy of a Julia CSC matrix (column-major)
+std::vector<double> csc_dense(const sse_csc &A, int rows, int cols) {
+  std::vector<double> out((size_t)rows * cols, 0.0);
+  for (int j = 0; j < cols; ++j)
+    for (int64_t q = A.colptr[j] - 1; q < A.colptr[j + 1] - 1; ++q)
+      out[(size_t)j * rows + (A.rowval[q] - 1)] += A.nzval[q];
+  return out;
+}
+
+// The one-kernel StandardForm path (std_compact_kernel): StandardForm on
+// elements with at most 32 volume, facet and modal nodes, each face meeting
+// one neighbour element, with the element's dense weight-adjusted mass
+// operator or a diagonal mass matrix.  Packs V, R V, V^T, R, R^T, D_m and
+// D_m^T column-major (leading dimension = rows) and turns the path on; a
+// configuration outside that scope keeps the two-phase kernels.
+int setup_compact(sse_solver *s, const sse_operators *ops, const std::vector<int> &mapP) {
+  const sse_config &c = s->cfg;
+  KernelArgs &ka = s->ka;
+  const int np = c.n_p, nq = c.n_q, nf = c.n_f, d = c.d, nc = c.n_c;
+  const int npf = c.nodes_per_face, nfac = c.num_faces;
+  ka.compact = 0;
+  s->compact_ok = false;
+  if (ka.fd || nq > 32 || nf > 32 || np > 32) return SSE_OK;
+  if (ka.mass_wa ? !ka.Ak : !ka.geo.WJinv) return SSE_OK;
+  for (int64_t k = 0; k < c.n_e; ++k)
+    for (int f = 0; f < nfac; ++f) {
+      const size_t b = (size_t)k * nf + (size_t)f * npf;
+      for (int j = 1; j < npf; ++j)
+        if (mapP[b + j] / nf != mapP[b] / nf) return SSE_OK;
+    }
+  const bool has_vdm = ka.op.has_vdm != 0;
+  cudaError_t e;
+  std::vector<double> V;
+  if (has_vdm) {
+    V.resize((size_t)nq * np);
+    if (ka.op.dense_v) {
+      std::memcpy(V.data(), ops->V_dense, V.size() * sizeof(double));
+    } else {
+      void *p;
+      if ((e = alloc(s, V.size() * sizeof(double), &p))) return cuda_fail(s, e, "alloc dense V");
+      if ((e = launch_dense_vdm(ka, (double *)p, s->stream)) ||
+          (e = cudaMemcpyAsync(V.data(), p, V.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream)) ||
+          (e = cudaStreamSynchronize(s->stream)))
+        return cuda_fail(s, e, "dense V");
+    }
+  }
+  const std::vector<double> R = csc_dense(ops->R, nf, nq);
+  std::vector<double> VR((size_t)nf * np, 0.0);  // R V (R when V = I)
+  for (int a = 0; a < np; ++a)
+    for (int j = 0; j < nf; ++j) {
+      double acc = 0.0;
+      if (has_vdm)
+        for (int q = 0; q < nq; ++q) acc += R[(size_t)q * nf + j] * V[(size_t)a * nq + q];
+      else
+        acc = R[(size_t)a * nf + j];
+      VR[(size_t)a * nf + j] = acc;
+    }
+  std::vector<double> pack;
+  std::vector<int> ipack;
+  auto region = [&](int slot, const std::vector<double> &m) {
+    ka.cop_off[slot] = (int)pack.size();
+    pack.insert(pack.end(), m.begin(), m.end());
+    if (pack.size() & 1) pack.push_back(0.0);
+  };
+  // a sparse operator (rows x cols, column-major dense copy m) as padded
+  // rows: its k-th nonzero of row r at [k * rows + r] in increasing column
+  // order, the column index beside it; kept dense when the widest row holds
+  // more than three quarters of the columns
+  auto sparse_region = [&](int slot, const std::vector<double> &m, int rows, int cols) {
+    std::vector<std::vector<int>> nz(rows);
+    size_t w = 0;
+    for (int r = 0; r < rows; ++r) {
+      for (int q = 0; q < cols; ++q)
+        if (m[(size_t)q * rows + r] != 0.0) nz[r].push_back(q);
+      w = std::max(w, nz[r].size());
+    }
+    if (4 * w > (size_t)3 * cols || w == 0) {
+      ka.cop_w[slot] = 0;
+      region(slot, m);
+      return;
+    }
+    std::vector<double> val(w * rows, 0.0);
+    std::vector<int> idx(w * rows, 0);
+    for (int r = 0; r < rows; ++r)
+      for (size_t k = 0; k < nz[r].size(); ++k) {
+        val[k * rows + r] = m[(size_t)nz[r][k] * rows + r];
+        idx[k * rows + r] = nz[r][k];
+      }
+    ka.cop_w[slot] = (int)w;
+    ka.cop_i[slot] = (int)ipack.size();
+    ipack.insert(ipack.end(), idx.begin(), idx.end());
+    region(slot, val);
+  };
+  for (int i = 0; i < 12; ++i) { ka.cop_off[i] = 0; ka.cop_w[i] = 0; ka.cop_i[i] = 0; }
+  if (has_vdm) {
+    region(kCopV, V);
+    std::vector<double> VT((size_t)np * nq);
+    for (int i = 0; i < nq; ++i)
+      for (int a = 0; a < np; ++a) VT[(size_t)i * np + a] = V[(size_t)a * nq + i];
+    region(kCopVT, VT);
+  }
+  region(kCopVR, VR);
+  sparse_region(kCopR, R, nf, nq);
+  {
+    std::vector<double> RT((size_t)nq * nf);
+    for (int j = 0; j < nf; ++j)
+      for (int i = 0; i < nq; ++i) RT[(size_t)j * nq + i] = R[(size_t)i * nf + j];
+    sparse_region(kCopRT, RT, nq, nf);
+  }
+  for (int m = 0; m < d; ++m) {
+    const std::vector<double> Dm = csc_dense(ops->D[m], nq, nq);
+    std::vector<double> DT((size_t)nq * nq);
+    for (int q = 0; q < nq; ++q)
+      for (int i = 0; i < nq; ++i) DT[(size_t)q * nq + i] = Dm[(size_t)i * nq + q];
+    sparse_region(kCopD + m, Dm, nq, nq);
+    sparse_region(kCopDT + m, DT, nq, nq);
+  }
+  ka.cop_doubles = (int)pack.size();
+  while (ipack.size() & 3) ipack.push_back(0);
+  ka.copi_ints = (int)ipack.size();
+  const size_t ops_doubles = (size_t)ka.cop_doubles + ka.copi_ints / 2;
+  // per-element regions
+  const int sizes[10] = {(1 + nfac) * nc * np, 0, nc * nq, d * nc * nq, d * nc * nq, nc * nf, nc * nq, nc * np,
+                         d * d * nq + 4,       ka.mass_wa ? np * np + 4 : 0};
+  int off = 0;
+  for (int i = 0; i < 10; ++i) { ka.ct_off[i] = off; off += (sizes[i] + 1) & ~1; }
+  ka.ct_doubles = off;
+  // four elements (warps) per block; fewer when shared memory is short
+  const size_t cap = 220 * 1024;
+  int epb = std::min(4, kMaxCompactEpb);
+  while (epb > 1 && (ops_doubles + (size_t)epb * ka.ct_doubles) * 8 > cap) epb /= 2;
+  if ((ops_doubles + (size_t)epb * ka.ct_doubles) * 8 > cap) return SSE_OK;
+  ka.epb_c = epb;
+  if ((e = upload(s, pack.data(), pack.size(), &ka.cops))) return cuda_fail(s, e, "upload compact operators");
+  ka.copi = nullptr;
+  if (!ipack.empty() && (e = upload(s, ipack.data(), ipack.size(), &ka.copi)))
+    return cuda_fail(s, e, "upload compact operators");
+  if ((e = sse_set_smem_limit_compact(ka, (ops_doubles + (size_t)epb * ka.ct_doubles) * 8)))
+    return cuda_fail(s, e, "cudaFuncSetAttribute");
+  s->compact_ok = true;
+  ka.compact = 1;
+  return SSE_OK;
 }
 
 int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const sse_geometry *geo) {
@@ -610,6 +758,8 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   if ((e = alloc(s, sizeof(int), &p))) return cuda_fail(s, e, "alloc"); s->d_flag = (int *)p;
   ka.flag = s->d_flag;
   if ((e = cudaMemset(s->d_flag, 0, sizeof(int)))) return cuda_fail(s, e, "memset");
+  if ((e = cudaHostAlloc((void **)&s->h_flag, sizeof(int), cudaHostAllocDefault))) return cuda_fail(s, e, "pinned flag");
+  *s->h_flag = 0;
   if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking))) return cuda_fail(s, e, "stream");
   s->own_stream = true;
 
@@ -639,14 +789,16 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
       ka.Ak = (const double *)p;
     }
   }
-  return SSE_OK;
+  return setup_compact(s, ops, mapP);
 }
 
+// Reads the device flag into pinned host memory behind the stream's work:
+// one synchronisation covers that work and the read.
 int check_flag(sse_solver *s) {
-  int h = 0;
-  cudaError_t e = cudaMemcpyAsync(&h, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+  cudaError_t e = cudaMemcpyAsync(s->h_flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return cuda_fail(s, e, "flag read");
+  const int h = *s->h_flag;
   if (h) {
     cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream);
     cudaStreamSynchronize(s->stream);
@@ -905,10 +1057,21 @@ int ensure_reference(sse_solver *s, const double *u_dev) {
 // one residual evaluation on device buffers (no synchronisation in the FP64
 // form; the mixed form synchronises once, on its first call).  u_q / u_f,
 // when given, receive the FP64 nodal states instead of the handle's scratch.
+// The one-kernel StandardForm path runs unless nodal states are asked for or
+// two_phase is set.
 cudaError_t residual_device(sse_solver *s, const double *u, double *dudt, double *u_q = nullptr,
-                            double *u_f = nullptr) {
+                            double *u_f = nullptr, bool two_phase = false) {
   if (s->ka.mixed && !s->ref_ready && ensure_reference(s, u) != SSE_OK) return cudaErrorInvalidValue;
   KernelArgs ka = s->ka;
+  // (a residual written over its own input, which the neighbours' traces
+  // read, takes the two-phase kernels)
+  if (ka.compact && !u_q && !two_phase && dudt != u) {
+    CompactStage st{};
+    st.mode = kCompactResidual;
+    st.uin = u;
+    st.out = dudt;
+    return launch_std_compact(ka, st, s->stream);
+  }
   ka.u = u;
   ka.dudt = dudt;
   if (u_q) {
@@ -1111,13 +1274,15 @@ cudaError_t tape_step(sse_solver *s, double *u, int slot) {
   const double dt = T.dt;
   cudaError_t e;
   auto stage_residual = [&](const double *y, int st) -> cudaError_t {
-    if (slot < 0) return residual_device(s, y, T.w_dudt);
+    // the recording and every recomputation take the same two-phase kernels,
+    // so each state of the trajectory is the same bits whichever produced it
+    if (slot < 0) return residual_device(s, y, T.w_dudt, nullptr, nullptr, true);
     const size_t q = (size_t)slot * T.stages + st;
     double *ys = T.seg_y + q * n;
     cudaError_t err = cudaMemcpyAsync(ys, y, n * 8, cudaMemcpyDeviceToDevice, s->stream);
     if (err != cudaSuccess) return err;
     if (T.nodal) return residual_device(s, ys, T.w_dudt, T.seg_uq + q * nqs, T.seg_uf + q * nfs);
-    return residual_device(s, ys, T.w_dudt);
+    return residual_device(s, ys, T.w_dudt, nullptr, nullptr, true);
   };
   if (T.scheme == SSE_CARPENTER_KENNEDY_2N54) {
     for (int st = 0; st < 5; ++st) {
@@ -1299,6 +1464,7 @@ int32_t sse_destroy(sse_solver *s) {
   if (s->tape.block) cudaFree(s->tape.block);
   if (s->step_graph.exec) cudaGraphExecDestroy(s->step_graph.exec);
   for (void *p : s->allocations) cudaFree(p);
+  if (s->h_flag) cudaFreeHost(s->h_flag);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return SSE_OK;
@@ -1350,6 +1516,16 @@ int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t, int
 int32_t sse_residual_static_scratch(sse_solver *s, const double *u_dev, double *dudt_dev) {
   if (!s) return SSE_ERR_INVALID_ARGUMENT;
   if (!u_dev || !dudt_dev) return fail(s, SSE_ERR_INVALID_ARGUMENT, "null u/dudt");
+  if (s->ka.compact && dudt_dev != u_dev) {
+    // the one-kernel StandardForm path keeps no nodal states at all
+    CompactStage st{};
+    st.mode = kCompactResidual;
+    st.uin = u_dev;
+    st.out = dudt_dev;
+    cudaError_t e = launch_std_compact(s->ka, st, s->stream);
+    if (e != cudaSuccess) return cuda_fail(s, e, "residual (static scratch)");
+    return check_flag(s);
+  }
   const sse_config &c = s->cfg;
   // the handle's precision: FP64 nodal states in the FP64 form, FP32
   // perturbation states in the mixed form (half the bytes per node)
@@ -1443,6 +1619,11 @@ static int32_t rk_run(sse_solver *s, double *u, int32_t n_steps, double dt, int3
     if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_ust = (double *)p;
   }
   const bool mixed = s->ka.mixed;
+  const bool compact = s->ka.compact != 0;
+  if (compact && !s->d_ust2) {
+    void *p;
+    if ((e = alloc(s, n * 8, &p))) return cuda_fail(s, e, "alloc"); s->d_ust2 = (double *)p;
+  }
   if (mixed && (e = cudaMemsetAsync(s->d_comp, 0, n * 8, s->stream))) return cuda_fail(s, e, "memset");
   // the mixed form picks its reference state (a synchronising reduction)
   // before any step is launched or captured
@@ -1450,8 +1631,54 @@ static int32_t rk_run(sse_solver *s, double *u, int32_t n_steps, double dt, int3
     int rc = ensure_reference(s, du);
     if (rc != SSE_OK) return rc;
   }
+  // one-kernel stages: each launch evaluates the stage's residual and
+  // applies its update.  The neighbours read the stage input for their facet
+  // traces, so the update goes to another buffer: CK2N54 alternates u and
+  // d_ust2 (five stages end in d_ust2, copied back), RK4 alternates the
+  // stage inputs d_ust and d_ust2 and writes u in place on its last stage
+  auto compact_step = [&]() -> cudaError_t {
+    cudaError_t err;
+    CompactStage cs{};
+    if (scheme == SSE_CARPENTER_KENNEDY_2N54) {
+      double *buf[2] = {du, s->d_ust2};
+      for (int st = 0; st < 5; ++st) {
+        cs = CompactStage{};
+        cs.mode = kCompactCK;
+        cs.first = st == 0;
+        cs.a = kCKA[st]; cs.b = kCKB[st]; cs.dt = dt;
+        cs.uin = buf[st & 1];
+        cs.acc = s->d_tmp;
+        cs.out = buf[(st + 1) & 1];
+        if ((err = launch_std_compact(s->ka, cs, s->stream))) return err;
+      }
+      return cudaMemcpyAsync(du, s->d_ust2, n * 8, cudaMemcpyDeviceToDevice, s->stream);
+    }
+    const double cst[3] = {dt / 2, dt / 2, dt};
+    const double *in[4] = {du, s->d_ust, s->d_ust2, s->d_ust};
+    double *out[3] = {s->d_ust, s->d_ust2, s->d_ust};
+    for (int st = 0; st < 4; ++st) {
+      cs = CompactStage{};
+      cs.uin = in[st];
+      cs.ubase = du;
+      cs.acc = s->d_acc;
+      if (st < 3) {
+        cs.mode = kCompactRK4;
+        cs.first = st == 0;
+        cs.w = st == 0 ? 0.0 : 2.0;
+        cs.c = cst[st];
+        cs.out = out[st];
+      } else {
+        cs.mode = kCompactRK4Final;
+        cs.c = dt / 6;
+        cs.out = du;
+      }
+      if ((err = launch_std_compact(s->ka, cs, s->stream))) return err;
+    }
+    return cudaSuccess;
+  };
   auto step_once = [&]() -> cudaError_t {
     cudaError_t err;
+    if (compact) return compact_step();
     if (scheme == SSE_CARPENTER_KENNEDY_2N54) {
       for (int st = 0; st < 5; ++st) {
         if ((err = residual_device(s, du, s->d_dudt))) return err;
@@ -1478,7 +1705,7 @@ static int32_t rk_run(sse_solver *s, double *u, int32_t n_steps, double dt, int3
   sse_solver::StepGraph &G = s->step_graph;
   if (n_steps >= 2) {
     const bool same = G.exec && G.u == du && G.dt == dt && G.scheme == scheme && G.mixed == (int)mixed &&
-                      G.stream == s->stream;
+                      G.compact == (int)compact && G.stream == s->stream;
     if (!same) {
       if (G.exec) cudaGraphExecDestroy(G.exec);
       G = sse_solver::StepGraph{};
@@ -1488,7 +1715,8 @@ static int32_t rk_run(sse_solver *s, double *u, int32_t n_steps, double dt, int3
         cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
         if (ec == cudaSuccess && ee == cudaSuccess && graph &&
             cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess) {
-          G.u = du; G.dt = dt; G.scheme = scheme; G.mixed = (int)mixed; G.stream = s->stream;
+          G.u = du; G.dt = dt; G.scheme = scheme; G.mixed = (int)mixed; G.compact = (int)compact;
+          G.stream = s->stream;
         } else {
           G.exec = nullptr;
         }
@@ -1986,11 +2214,16 @@ int32_t sse_phase_timings(sse_solver *s, const double *u_dev, int32_t n_iter, do
   for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
   float ta = 0, tb = 0, tc = 0;
   cudaError_t e = cudaSuccess;
+  CompactStage cst{};
+  cst.mode = kCompactResidual;
+  cst.uin = u_dev;
+  cst.out = s->d_dudt;
   for (int it = 0; it < n_iter && e == cudaSuccess; ++it) {
     cudaEventRecord(ev[0], s->stream);
-    e = launch_nodal_values(ka, s->stream);
+    // the one-kernel StandardForm path has no separate phase A (out[0] = 0)
+    if (!ka.compact) e = launch_nodal_values(ka, s->stream);
     cudaEventRecord(ev[1], s->stream);
-    if (e == cudaSuccess) e = launch_time_derivative(ka, s->stream);
+    if (e == cudaSuccess) e = ka.compact ? launch_std_compact(ka, cst, s->stream) : launch_time_derivative(ka, s->stream);
     cudaEventRecord(ev[2], s->stream);
     // stage update into the host-staging buffer (never the caller's state)
     if (e == cudaSuccess && s->d_u != u_dev)
@@ -2005,10 +2238,29 @@ int32_t sse_phase_timings(sse_solver *s, const double *u_dev, int32_t n_iter, do
   }
   for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
   if (e != cudaSuccess) return cuda_fail(s, e, "timing");
-  out[0] = ta / n_iter;
+  out[0] = ka.compact ? 0.0 : ta / n_iter;
   out[1] = tb / n_iter;
   out[2] = tc / n_iter;
   return check_flag(s);
+}
+
+int32_t sse_kernel_path(const sse_solver *s) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  return s->ka.compact ? SSE_PATH_ONE_KERNEL : SSE_PATH_TWO_PHASE;
+}
+
+int32_t sse_set_kernel_path(sse_solver *s, int32_t path) {
+  if (!s) return SSE_ERR_INVALID_ARGUMENT;
+  if (path == SSE_PATH_TWO_PHASE) {
+    s->ka.compact = 0;
+    return SSE_OK;
+  }
+  if (path != SSE_PATH_ONE_KERNEL) return fail(s, SSE_ERR_INVALID_ARGUMENT, "unknown kernel path");
+  if (!s->compact_ok)
+    return fail(s, SSE_ERR_UNSUPPORTED,
+                "the one-kernel path covers StandardForm with at most 32 volume, facet and modal nodes per element");
+  s->ka.compact = 1;
+  return SSE_OK;
 }
 
 // sizeof checks for foreign-language bindings

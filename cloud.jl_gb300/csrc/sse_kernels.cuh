@@ -68,13 +68,58 @@ struct KernelArgs {
   Layout layAdjB1m, layAdjB2m, layAdjAm;  // mixed-form VJP layouts (floats)
   int pair_chunk_mixed;  // pairs per chunk in the mixed-form pair-adjoint passes
   int vdm_zsz_mixed;   // floats of the first sum-factorisation scratch (multiple of 4)
+  // one-kernel StandardForm path (std_compact_kernel) for elements with at
+  // most 32 volume, facet and modal nodes: one warp per element, the dense
+  // operators staged once per block in shared memory
+  int compact;         // 1: residuals and stages run std_compact_kernel
+  const double *cops;  // packed dense operators (column-major, leading dimension = rows)
+  int cop_off[12];     // offsets (doubles): kCopV, kCopVR, kCopVT, kCopR, kCopRT, kCopD + m, kCopDT + m
+  int cop_doubles;     // total doubles of the packed operators (even)
+  int cop_w[12];       // 0: dense (column-major); > 0: padded-row (ELL) width of a sparse operator
+  int cop_i[12];       // ELL operators: offset of their column indices in copi
+  const int *copi;     // ELL column indices (same layout as the values)
+  int copi_ints;       // total ints of copi (a multiple of 4)
+  int ct_off[10];      // per-element shared-memory offsets (doubles), kCt* below
+  int ct_doubles;      // doubles per element (even)
+  int epb_c;           // elements (warps) per block of std_compact_kernel
 
   __device__ __forceinline__ void flag_nonphysical() const { atomicOr(flag, 1); }
   // a bounded wait on a device copy gave up (reported as SSE_ERR_CUDA)
   __device__ __forceinline__ void flag_timeout() const { atomicOr(flag, 2); }
 };
 
+// most elements (warps) per block of std_compact_kernel
+constexpr int kMaxCompactEpb = 8;
+// packed dense operators of the compact StandardForm path
+enum { kCopV = 0, kCopVR = 1, kCopVT = 2, kCopR = 3, kCopRT = 4, kCopD = 5, kCopDT = 8 };
+// per-element shared-memory regions of std_compact_kernel: modal state
+// followed by the neighbours' modal states (one per face; kCtUN unused),
+// volume states, physical fluxes f_n, contracted fluxes g_m, facet fluxes,
+// volume residual, modal residual, and the bulk-copied halfWLambda and mass
+// operator (each with 32 spare bytes for its 16-byte-aligned span)
+enum { kCtU = 0, kCtUN, kCtUQ, kCtF, kCtG, kCtFF, kCtRQ, kCtBM, kCtHW, kCtAK };
+
+// what std_compact_kernel writes after the element's residual k:
+//   kCompactResidual  out = k
+//   kCompactRK4       acc = first ? k : acc + w k ;  out = ubase + c k
+//   kCompactRK4Final  out = ubase + c (acc + k)           (out may be ubase)
+//   kCompactCK        t = first ? dt k : a acc + dt k ; acc = t ; out = uin + b t
+// out never aliases uin, which the neighbours read for their facet traces.
+enum { kCompactResidual = 0, kCompactRK4 = 1, kCompactRK4Final = 2, kCompactCK = 3 };
+struct CompactStage {
+  int mode, first;
+  double a, b, c, w, dt;
+  const double *uin;    // the stage's input state (this element and its neighbours)
+  const double *ubase;  // RK4: the step's initial state
+  double *acc;          // RK4 accumulator / CK2N54 register
+  double *out;
+};
+
 cudaError_t sse_set_smem_limits(const KernelArgs &ka, size_t smA, size_t smB);
+cudaError_t sse_set_smem_limit_compact(const KernelArgs &ka, size_t bytes);
+cudaError_t launch_std_compact(const KernelArgs &ka, const CompactStage &st, cudaStream_t s);
+// column a of V (np blocks; V applied to the unit vectors), nq x np column-major
+cudaError_t launch_dense_vdm(const KernelArgs &ka, double *out, cudaStream_t s);
 cudaError_t sse_set_smem_limit_mixed(const KernelArgs &ka, size_t smBm);
 // resident blocks per SM of the mixed phase-B kernel with smBm bytes of
 // dynamic shared memory (registers, threads and shared memory together)

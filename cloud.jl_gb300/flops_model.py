@@ -119,6 +119,18 @@ def model(host) -> Work:
     return Work(float(flops_A), float(flops_B), bytes_A, bytes_B, bytes_stage)
 
 
+def one_kernel_bytes(host) -> float:
+    """Algorithmic HBM bytes per element of the one-kernel StandardForm
+    residual (std_compact_kernel): the element's modal state and its
+    neighbours' (one per face), halfWLambda, the facet normals, BJf and mapP,
+    the dense mass operator, and the residual written; no nodal states."""
+    ra = host.sd.reference_approximation
+    d, nc, nq, nf, np_ = ra.d, host.N_c, host.N_q, host.N_f, host.N_p
+    nfac = ra.reference_element.num_faces
+    mb = 8.0 * np_ * np_ if ra.V is not None else 0.0
+    return 8.0 * (np_ * nc * (1 + nfac) + d * d * nq + d * nf + nf + np_ * nc) + 4.0 * nf + mb
+
+
 def _unique_pairs(host) -> int:
     seen = set()
     for S in host.S:

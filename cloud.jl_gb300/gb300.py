@@ -28,7 +28,7 @@ EXPORTED = ["sse_abi_version", "sse_create", "sse_destroy", "sse_residual",
             "sse_conservation_residual", "sse_set_precision", "sse_set_stream",
             "sse_phase_timings", "sse_struct_sizes", "sse_measure_fma_peaks", "sse_last_error",
             "sse_create_error", "sse_geometric_factors", "sse_project_function",
-            "sse_energy_residual"]
+            "sse_energy_residual", "sse_kernel_path", "sse_set_kernel_path"]
 
 _lib = None
 
@@ -84,6 +84,10 @@ def load_library(path: str | None = None):
     L.sse_set_stream.restype = i32
     L.sse_phase_timings.argtypes = [vp, vp, i32, vp]
     L.sse_phase_timings.restype = i32
+    L.sse_kernel_path.argtypes = [vp]
+    L.sse_kernel_path.restype = i32
+    L.sse_set_kernel_path.argtypes = [vp, i32]
+    L.sse_set_kernel_path.restype = i32
     L.sse_measure_fma_peaks.argtypes = [vp]
     L.sse_measure_fma_peaks.restype = i32
     L.sse_struct_sizes.argtypes = [vp]
@@ -257,6 +261,16 @@ class GB300Solver:
 
     def set_stream(self, stream_handle: int):
         self._check(self.L.sse_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    def kernel_path(self) -> int:
+        """SSE_PATH_TWO_PHASE or SSE_PATH_ONE_KERNEL (sse_kernel_path)."""
+        r = self.L.sse_kernel_path(self.h)
+        if r < 0:
+            self._check(r)
+        return r
+
+    def set_kernel_path(self, path: int):
+        self._check(self.L.sse_set_kernel_path(self.h, path))
 
     def phase_timings(self, u_dev, n_iter: int) -> np.ndarray:
         out = np.zeros(3)

@@ -184,7 +184,10 @@ int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t,
  * array: calls that overlap on the GPU (other handles, other streams, other
  * threads) race and must be serialised by the caller.  Each call rewrites
  * the whole part of the array it reads, so nothing needs clearing between
- * calls.  No counterpart in the reference, which has no device memory. */
+ * calls.  On a handle running the one-kernel StandardForm path
+ * (sse_kernel_path) the residual keeps no nodal states: the call uses
+ * neither the array nor its size limit.  No counterpart in the reference,
+ * which has no device memory. */
 int32_t sse_residual_static_scratch(sse_solver *s, const double *u_dev, double *dudt_dev);
 
 /* Phase A alone: nodal_values! for every element (standard_form_first_order.jl:
@@ -306,10 +309,33 @@ int32_t sse_set_stream(sse_solver *s, void *stream);
 /* Average device time in milliseconds of each residual phase over n_iter
  * evaluations at the device state u_dev, timed with CUDA events on the
  * handle's stream: out[0] nodal values (phase A), out[1] time derivative
- * (phase B), out[2] one Runge-Kutta stage update.  No counterpart in the
- * reference; mirrors the "nodal values" / "time deriv." TimerOutputs
- * sections of Solvers.jl:474-489. */
+ * (phase B), out[2] one Runge-Kutta stage update.  On the one-kernel
+ * StandardForm path out[0] is 0 and out[1] times that kernel.  No
+ * counterpart in the reference; mirrors the "nodal values" / "time deriv."
+ * TimerOutputs sections of Solvers.jl:474-489. */
 int32_t sse_phase_timings(sse_solver *s, const double *u_dev, int32_t n_iter, double *out);
+
+/* Which kernels evaluate the residual.  SSE_PATH_TWO_PHASE: phase A
+ * (nodal_values!) then phase B (time_derivative!), the element nodal states
+ * handed over through device memory.  SSE_PATH_ONE_KERNEL: StandardForm on
+ * elements with at most 32 volume, facet and modal nodes, each face meeting
+ * one neighbour element, with a weight-adjusted mass solver whose dense
+ * per-element operators fit in device memory or a diagonal one: one kernel
+ * per residual (and per Runge-Kutta stage in sse_rk_steps, with the stage
+ * update applied by the same kernel), one warp per element, the facet traces
+ * R V u evaluated from the modal coefficients of the element and of its
+ * neighbours.  Handles start on the one-kernel path where it applies.
+ * sse_residual_vjp, sse_nodal_values and the recordings of sse_rk_record /
+ * sse_rk_record_binomial always take the two-phase kernels.  Both paths
+ * restate the same reference algorithm; their results differ by round-off
+ * (the traces are (R V) u instead of R (V u), and the contracted fluxes are
+ * summed before the D_m^T product).  No counterpart in the reference. */
+enum sse_kernel_path_kind { SSE_PATH_TWO_PHASE = 0, SSE_PATH_ONE_KERNEL = 1 };
+/* returns SSE_PATH_TWO_PHASE or SSE_PATH_ONE_KERNEL (negative: error) */
+int32_t sse_kernel_path(const sse_solver *s);
+/* SSE_ERR_UNSUPPORTED when SSE_PATH_ONE_KERNEL is asked for a configuration
+ * outside its scope; the handle's path is then unchanged. */
+int32_t sse_set_kernel_path(sse_solver *s, int32_t path);
 
 /* ---- Geometric factors on the device -------------------------------------
  *
