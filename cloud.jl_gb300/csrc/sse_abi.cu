@@ -977,6 +977,16 @@ int enable_mixed(sse_solver *s) {
     if ((e = launch_projection_of_one(ka, P1, RP1, s->stream))) return cuda_fail(s, e, "projection of 1");
     g.P1 = P1;
     g.RP1 = RP1;
+    void *q1, *q2, *q3;
+    if ((e = alloc(s, nq * ne * sizeof(float), &q1)) || (e = alloc(s, nf * ne * sizeof(float), &q2)) ||
+        (e = alloc(s, nq * ne * sizeof(float), &q3)) ||
+        (e = launch_round_to_float(P1, (float *)q1, nq * ne, s->stream, -1.0)) ||
+        (e = launch_round_to_float(RP1, (float *)q2, nf * ne, s->stream, -1.0)) ||
+        (e = launch_round_to_float(g.WJ, (float *)q3, nq * ne, s->stream)))
+      return cuda_fail(s, e, "mixed projection constants");
+    g.P1m1f = (const float *)q1;
+    g.RP1m1f = (const float *)q2;
+    g.WJf = (const float *)q3;
   }
   if ((e = cudaStreamSynchronize(s->stream))) return cuda_fail(s, e, "sync");
   s->mixed_ready = true;

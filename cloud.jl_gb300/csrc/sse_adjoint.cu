@@ -1171,9 +1171,9 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   float *U1 = base + L.off[0], *Q0 = base + L.off[1], *XQ = base + L.off[2], *WQ = base + L.off[3],
         *WF = base + L.off[4], *T1 = base + L.off[5], *S1 = base + L.off[6], *Zf = base + L.off[7],
         *Wf = base + L.off[8], *BF = base + L.off[9];
-  const double *WJ = ka.geo.WJ + (size_t)kk * nq;
+  const float *WJf = ka.geo.WJf + (size_t)kk * nq;
   const float *JinvWf = ka.geo.JinvWf + (size_t)kk * nq;
-  const double *P1 = ka.geo.P1 + (size_t)kk * nq, *RP1 = ka.geo.RP1 + (size_t)kk * nf;
+  const float *P1m1 = ka.geo.P1m1f + (size_t)kk * nq, *RP1m1 = ka.geo.RP1m1f + (size_t)kk * nf;
 
   // ---- forward recompute (as nodal_values_mixed_kernel)
   const double *uk = ka.u + (size_t)kk * NC * np;
@@ -1191,7 +1191,7 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
 #pragma unroll
     for (int e = 0; e < NC; ++e) ui[e] = Q0[e * nq + i];
     cons_to_entropy_pert<D>(cr, ui, wi);
-    const float wj = (float)WJ[i];
+    const float wj = WJf[i];
 #pragma unroll
     for (int e = 0; e < NC; ++e) XQ[e * nq + i] = wj * wi[e];
   }
@@ -1208,7 +1208,7 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   for (int t = lane; t < nq + nf; t += tpe) {
     const bool vol = t < nq;
     const int r = vol ? t : t - nq;
-    const float p1m1 = (float)((vol ? P1[r] : RP1[r]) - 1.0);
+    const float p1m1 = vol ? P1m1[r] : RP1m1[r];
     const float *src = vol ? WQ + r : WF + r;
     const int stride = vol ? nq : nf;
     float dwi[NC], wi[NC], bi[NC], ri[NC];
@@ -1236,7 +1236,7 @@ __global__ void __launch_bounds__(256) adj_projection_mixed_kernel(KernelArgs ka
   // ubar_q0 = J_c2e(u_q0)^T (W J x), symmetric Jacobian
   for (int i = lane; i < nq; i += tpe) {
     float ui[NC], bi[NC], ri[NC];
-    const float wj = (float)WJ[i];
+    const float wj = WJf[i];
 #pragma unroll
     for (int e = 0; e < NC; ++e) {
       const float ref = (e == 0) ? cr.rho_ref : ((e == NC - 1) ? E_ref : 0.f);

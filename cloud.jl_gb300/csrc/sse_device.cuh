@@ -105,6 +105,9 @@ struct DevGeo {
   // mixed form: the entropy projection of the constant function 1 at the
   // volume nodes (V M^-1 V^T (W J), nq x ne) and its facet values (R P1, nf x ne)
   const double *P1, *RP1;
+  // their FP32 roundings less one (P(1) - 1, R P(1) - 1) and of W J, for the
+  // FP32 phase A (the FP64 difference and conversion made once on the device)
+  const float *P1m1f, *RP1m1f, *WJf;
   // mixed form: the FP64 phase-B residual of the constant reference state
   // (np x nc x ne), i.e. the reference-pressure terms the FP32 fluxes leave
   // out; zero to round-off on free-stream-preserving metrics, O(1) on curved

@@ -203,7 +203,6 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
   float *fb = reinterpret_cast<float *>(base + L.off[4]);
   float *Af = fb + L.off[5], *Bf = fb + L.off[6], *Cf = fb + L.off[7], *Zf = fb + L.off[8],
         *Wf = fb + L.off[9];
-  const double *WJ = ka.geo.WJ + (size_t)kk * nq;
 
   // u - u_ref in modal coefficients (only the constant mode changes), FP32;
   // u_q = u_ref + V (u - u_ref) with V applied in FP32
@@ -222,7 +221,7 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
     for (int e = 0; e < NC; ++e) ui[e] = Bf[e * nq + i];
     if (!(cr.rho_ref + ui[0] > 0.f)) ka.flag_nonphysical();
     cons_to_entropy_pert<D>(cr, ui, wi);
-    const float wj = (float)WJ[i];
+    const float wj = ka.geo.WJf[(size_t)kk * nq + i];
 #pragma unroll
     for (int e = 0; e < NC; ++e) Af[e * nq + i] = wj * wi[e];
   }
@@ -232,13 +231,13 @@ __global__ void __launch_bounds__(256) nodal_values_mixed_kernel(KernelArgs ka) 
   vdm_mul<float, D, NC>(op, Cf, Bf, Zf, Wf, lane, tpe);                                // w'_q
   csr_mul<float, NC>(nf, nq, op.R_ptr, op.R_idx, op.R_valf, Bf, Af, lane, tpe);        // w'_f
   __syncthreads();
-  const double *P1 = ka.geo.P1 + (size_t)kk * nq, *RP1 = ka.geo.RP1 + (size_t)kk * nf;
+  const float *P1m1 = ka.geo.P1m1f + (size_t)kk * nq, *RP1m1 = ka.geo.RP1m1f + (size_t)kk * nf;
   // w - w_ref = w_ref (P(1) - 1) + P(w - w_ref) at the volume and facet
   // nodes; u' = e2c(w) - u_ref, stored as the FP32 states of phase B
   for (int t = lane; t < nq + nf; t += tpe) {
     const bool vol = t < nq;
     const int r = vol ? t : t - nq;
-    const float p1m1 = (float)((vol ? P1[r] : RP1[r]) - 1.0);
+    const float p1m1 = vol ? P1m1[r] : RP1m1[r];
     const float *src = vol ? Bf + r : Af + r;
     const int stride = vol ? nq : nf;
     float wi[NC], ui[NC];
@@ -1122,9 +1121,11 @@ __global__ void fill_constant_state_kernel(double *__restrict__ buf, int nodes, 
     buf[i] = s[(i / nodes) % nc];
 }
 
-__global__ void round_to_float_kernel(const double *__restrict__ in, float *__restrict__ out, size_t n) {
+// out = (float)(in + shift)
+__global__ void round_to_float_kernel(const double *__restrict__ in, float *__restrict__ out, size_t n,
+                                      double shift) {
   for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x)
-    out[x] = (float)in[x];
+    out[x] = (float)(in[x] + shift);
 }
 
 // FP64 -> FP32 rounding of nmat n x n matrices with a transpose of each: the
@@ -1482,9 +1483,9 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
   return cudaGetLastError();
 }
 
-cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st) {
+cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st, double shift) {
   if (n == 0) return cudaSuccess;
-  round_to_float_kernel<<<elementwise_grid(n), 256, 0, st>>>(in, out, n);
+  round_to_float_kernel<<<elementwise_grid(n), 256, 0, st>>>(in, out, n, shift);
   return cudaGetLastError();
 }
 

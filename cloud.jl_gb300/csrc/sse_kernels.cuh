@@ -127,7 +127,8 @@ cudaError_t sse_mixed_b_blocks_per_sm(const KernelArgs &ka, size_t smBm, int *bl
 cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, const double *k,
                                         double a, double b, double dt, int first, size_t n,
                                         cudaStream_t st);
-cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st);
+// out = (float)(in + shift)
+cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st, double shift = 0.0);
 cudaError_t launch_fill_constant_state(double *buf, int nodes, int nc, size_t ne, const double *state,
                                        cudaStream_t st);
 cudaError_t launch_round_transpose(const double *in, float *out, size_t nmat, int n, cudaStream_t st);
