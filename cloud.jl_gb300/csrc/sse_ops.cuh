@@ -18,7 +18,7 @@ namespace sse {
 // loaded / computed once and feed NC independent FMA chains.  The summation
 // order of every output is that of the single-component loop.
 
-// y (NC x nq) = V x (NC x np); warped_product_2d.jl:31-55 / _3d.jl:47-84
+// y (NC x nq) = V x (NC x np); warped_product_2d.jl:31-55 / warped_product_3d.jl:47-84
 template <typename T, int D, int NC>
 __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane, int tpe) {
   const int np = op.np, nq = op.nq;
@@ -130,7 +130,7 @@ __device__ void vdm_mul(const DevOps &op, const T *x, T *y, T *Z, T *W, int lane
   }
 }
 
-// x (NC x np) = V^T y (NC x nq); warped_product_2d.jl:61-89 / _3d.jl:94-136
+// x (NC x np) = V^T y (NC x nq); warped_product_2d.jl:61-89 / warped_product_3d.jl:94-136
 template <typename T, int D, int NC>
 __device__ void vdm_tmul(const DevOps &op, const T *y, T *x, T *Z, T *W, int lane, int tpe) {
   const int np = op.np, nq = op.nq;

@@ -401,7 +401,7 @@ def reference_approximation(approx_type: str, shape: str, p: int,
         R = np.vstack([np.kron(e1_to_f, RL[1]), np.kron(RR[0], e2_to_f),
                        np.kron(RL[0], e2_to_f)])
         D = (np.kron(D1[0], I[1]), np.kron(I[0], D1[1]))
-        # volume quadrature (quadrature_rules.jl:431-447)
+        # volume quadrature (quadrature_rules.jl:125-141)
         g1, g2 = _meshgrid_flat(eta[0], eta[1])
         w2 = np.multiply(*_meshgrid_flat(wts[0], wts[1]))
         rq, sq = chi_tri(g1, g2)
@@ -430,7 +430,7 @@ def reference_approximation(approx_type: str, shape: str, p: int,
         w3 = np.prod(_meshgrid_flat(wts[0], wts[1], wts[2]), axis=0)
         rq, sq, tq = chi_tet(g1, g2, g3)
         wq = 0.125 * (1.0 - g2) * (1.0 - g3) * w3     # (0,0),(0,0),(1,0) rule
-        # facet rule: collapsed triangle (LG x GJ(1,0)) (quadrature_rules.jl:441-443)
+        # facet rule: collapsed triangle (LG x GJ(1,0)) (ref_elem_data.jl:87-88, quadrature_rules.jl:125-141)
         a2, b2 = _meshgrid_flat(ef1, ef2)
         w2 = np.multiply(*_meshgrid_flat(wf1, wf2))
         r2, s2 = chi_tri(a2, b2)

@@ -26,7 +26,7 @@
  * Time stepping restates OrdinaryDiffEq's fixed-step CarpenterKennedy2N54
  * (Carpenter & Kennedy 1994, NASA TM-109112, 5-stage 4th-order 2N-storage
  * scheme) and classic RK4 as the reference's tests call them
- * (test/test_driver.jl:221-227).
+ * (test/test_driver.jl:78-84).
  */
 #include <math.h>
 #include <stdint.h>

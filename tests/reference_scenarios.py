@@ -1,7 +1,7 @@
 """The reference's own end-to-end test scenarios on the hot path, set up
 through the host mirror exactly as the reference's tests do.
 
-advection_2d: test/runtests.jl:38-60 via test/test_driver.jl:158-254
+advection_2d: test/runtests.jl:38-60 via test/test_driver.jl:1-110
   (ModalTensor(4) Tri, mapping_degree 4, 2x2 periodic cells on [0,1]^2,
   DelRey warp 0.1, ExactMetrics with project_jacobian, StandardForm with
   LaxFriedrichsNumericalFlux(0.0), CarpenterKennedy2N54 with dt = 0.01 to
