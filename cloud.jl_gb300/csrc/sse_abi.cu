@@ -887,13 +887,46 @@ int enable_mixed(sse_solver *s) {
   const int tpe_fp64 = ka.tpb / ka.epb;
   const int tpe_m = std::max(32, tpe_fp64);
   ka.epb_bm = std::max(1, ka.epb * tpe_fp64 / tpe_m);
+  // The tail operators E_k = A_k V^T [I | -R^T]: phase B's lift, V^T and
+  // weight-adjusted mass solve as one per-element product, built once in
+  // FP64 and rounded to FP32, where the FP64 mass operators exist, the
+  // element's threads cover its n_p rows, and the operators take at most a
+  // quarter of the free device memory.
+  ka.Ekf = nullptr;
+  ka.ek_quads = 0;
+  if (ka.Ak && ka.Akf && op.has_vdm && tpe_m >= np) {
+    const int quads = (int)((nq + nf + 3) / 4);
+    const size_t bytes = (size_t)ne * quads * np * 16;
+    size_t freeb = 0, totalb = 0;
+    if ((e = cudaMemGetInfo(&freeb, &totalb))) return cuda_fail(s, e, "cudaMemGetInfo");
+    if (bytes <= freeb / 4) {
+      const double *Vd = op.dense_v ? op.Vd : nullptr;
+      if (!Vd) {
+        if ((e = alloc(s, nq * np * sizeof(double), &p))) return cuda_fail(s, e, "alloc dense V");
+        if ((e = launch_dense_vdm(ka, (double *)p, s->stream))) return cuda_fail(s, e, "dense V");
+        Vd = (const double *)p;
+      }
+      void *pm = nullptr, *pe = nullptr;
+      if ((e = alloc(s, (size_t)np * 4 * quads * sizeof(double), &pm)) || (e = alloc(s, bytes, &pe)) ||
+          (e = launch_tail_operators(ka, Vd, (double *)pm, (float *)pe, quads, s->stream)))
+        return cuda_fail(s, e, "mixed tail operators");
+      ka.Ekf = (const float *)pe;
+      ka.ek_quads = quads;
+    }
+  }
+  const bool et = ka.Ekf != nullptr;
   // Shared regions of the staged slabs: n floats plus the alignment margin
   // of a bulk copy (the slab lands at its source address modulo 16).
   auto staged = [&](int n) { return r4(n + 8); };
-  const int np2 = ka.Akf ? np * np : 0;
+  const int np2 = ka.Akf && !et ? np * np : 0;
+  // with the tail operators: region 2 holds the node-major residuals (8
+  // floats per node, the last column quad's padding nodes included) and the
+  // pair buffer later the G = tpe / n_p partial rows of the tail product
+  const int region2 = et ? 32 * ka.ek_quads : nc * (int)nf;
+  const int final_e = et ? (tpe_m / np) * np * 8 : final_m;
   auto layout_m = [&](int chunk, bool geo, bool rref, bool ak) {
-    const int sizes[11] = {staged(nc * (int)nq), staged(nc * (int)nf), nc * (int)nf,
-                           ak && np2 ? staged(np2) : 0, std::max(chunk * nc, final_m),
+    const int sizes[11] = {staged(nc * (int)nq), staged(nc * (int)nf), region2,
+                           ak && np2 ? staged(np2) : 0, std::max(chunk * nc, final_e),
                            staged((int)(d * d * nq)), op.nfp > 0 ? staged((int)(d * c.num_faces * nq)) : 0,
                            (int)((nq + nf) * (4 + d)),
                            geo ? 2 * staged((int)(d * nf)) + staged((int)nf) : 0,
@@ -909,7 +942,7 @@ int enable_mixed(sse_solver *s) {
   if (layout_m(chunk_m, false, false, false) > budget_m) {
     // four blocks per SM when chunks of at least one pass of the element's
     // threads fit, else two, else one
-    const int fixed = layout_m(0, false, false, false) - r4(final_m);
+    const int fixed = layout_m(0, false, false, false) - r4(final_e);
     const int need = std::min(tpe_m, max_pairs) * nc;
     int room = budget_m - fixed;
     if (room < need) room = 2 * budget_m - fixed;

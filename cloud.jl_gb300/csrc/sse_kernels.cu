@@ -708,8 +708,45 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
 // the same steps as fd_time_derivative_kernel in FP32 on the perturbation
 // states u_qf/u_ff written by phase A, FP32 metric terms and operators; the
 // residual is written in FP64 for the FP64 stage accumulation.
+//
+// ET (a per-element tail operator E_k = A_k V^T [I | -R^T] exists): the
+// volume and facet residuals live node-major in one array X (8 floats per
+// node, volume nodes then facet nodes), and the lift R^T, V^T and the mass
+// solve are one product with E_k, streamed from HBM (prefetched into L2 at
+// entry) by all of the element's threads; otherwise r_q and f_f are
+// component-major and the tail applies R^T, the sum-factorised V^T and the
+// mass solve in turn.
 // ---------------------------------------------------------------------------
-template <int D, int NC>
+
+// acc[e] += E[r, 4q + u] X[4q + u][e] for the four nodes of a column quad
+// (node-major X, 8 floats per node, 16-byte aligned)
+template <int NC>
+__device__ __forceinline__ void quad_fma(const float *Xq, float4 ev, float *acc) {
+  const float w[4] = {ev.x, ev.y, ev.z, ev.w};
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const float4 x0 = *reinterpret_cast<const float4 *>(Xq + 8 * u);
+    acc[0] = fmaf(w[u], x0.x, acc[0]);
+    acc[1] = fmaf(w[u], x0.y, acc[1]);
+    acc[2] = fmaf(w[u], x0.z, acc[2]);
+    acc[3] = fmaf(w[u], x0.w, acc[3]);
+    if constexpr (NC > 4) {
+      const float4 x1 = *reinterpret_cast<const float4 *>(Xq + 8 * u + 4);
+      acc[4] = fmaf(w[u], x1.x, acc[4]);
+      if constexpr (NC > 5) acc[5] = fmaf(w[u], x1.y, acc[5]);
+    }
+  }
+}
+
+// one node's NC values into its 8-float node-major slot
+template <int NC>
+__device__ __forceinline__ void store_node(float *x, const float *v) {
+  *reinterpret_cast<float4 *>(x) = make_float4(v[0], v[1], v[2], v[3]);
+#pragma unroll
+  for (int e = 4; e < NC; ++e) x[e] = v[e];
+}
+
+template <int D, int NC, bool ET>
 __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(KernelArgs ka) {
   static_assert(NC == D + 2, "the mixed form covers the Euler equations");
   extern __shared__ __align__(16) double smem_raw[];
@@ -727,6 +764,22 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   const float rnpf = qrcp(npf > 0 ? npf : 1);
   float *base = smem + (size_t)team * L.team_doubles;  // team size in floats for this layout
   float *rq = base + L.off[0], *ff = base + L.off[2], *diff = base + L.off[4], *prim = base + L.off[7];
+  float *X = base + L.off[2];  // ET: node-major residuals (region 2)
+  // residual entries of volume node i / facet node j, component e
+  auto RQ = [&](int e, int i) -> float & {
+    if constexpr (ET) return X[i * 8 + e];
+    else return rq[e * nq + i];
+  };
+  auto FF = [&](int e, int j) -> float & {
+    if constexpr (ET) return X[(nq + j) * 8 + e];
+    else return ff[e * nf + j];
+  };
+  const float *Ekg = ET ? ka.Ekf + (size_t)kk * ka.ek_quads * np * 4 : nullptr;
+  if constexpr (ET) {
+    if (lane == 0) prefetch_l2(Ekg, (uint32_t)ka.ek_quads * np * 16);
+    // padding nodes of the last column quad: zero (E_k is zero there too)
+    for (int t = lane; t < (4 * ka.ek_quads - nq - nf) * 8; t += tpe) X[(nq + nf) * 8 + t] = 0.f;
+  }
   uint64_t *bar = reinterpret_cast<uint64_t *>(base + L.off[10]);
   const int PS = 4 + D;
   const float gm1 = ph.f_gm1, igm1 = ph.f_igm1, gam = ph.f_gamma;
@@ -837,7 +890,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
 #pragma unroll
     for (int e = 0; e < NC; ++e) {
       float fs = (ph.nflux == 0) ? fmaf(a, jump[e], out[e]) : out[e];
-      ff[e * nf + j] = fs * bj;
+      FF(e, j) = fs * bj;
     }
   }
 
@@ -851,7 +904,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
     const int i = lane + sl * tpe;
     cur[sl] = i < nq ? op.vp_inc_ptr[i] : 0;
     if (i < nq && CH < op.nvp)
-      for (int e = 0; e < NC; ++e) rq[e * nq + i] = 0.f;
+      for (int e = 0; e < NC; ++e) RQ(e, i) = 0.f;
   }
   for (int c0 = 0; c0 < op.nvp; c0 += CH) {
     const int c1 = min(op.nvp, c0 + CH);
@@ -912,8 +965,10 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
 #pragma unroll
           for (int e = 0; e < NC; ++e) acc[e] = fmaf(sg, dp[e], acc[e]);
         }
+        if constexpr (ET) store_node<NC>(X + i * 8, acc);
+        else
 #pragma unroll
-        for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
+          for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
       }
       __syncthreads();
       continue;
@@ -924,7 +979,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
       if (i >= nq) continue;
       float acc[NC];
 #pragma unroll
-      for (int e = 0; e < NC; ++e) acc[e] = rq[e * nq + i];
+      for (int e = 0; e < NC; ++e) acc[e] = RQ(e, i);
       int q = cur[sl];
       const int qe = op.vp_inc_ptr[i + 1];
       for (; q < qe; ++q) {
@@ -942,7 +997,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
       }
       cur[sl] = q;
 #pragma unroll
-      for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
+      for (int e = 0; e < NC; ++e) RQ(e, i) = acc[e];
     }
     __syncthreads();
   }
@@ -1013,10 +1068,15 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
               for (int e = 0; e < NC; ++e) acc[e] += dp[e];
             }
           }
-          float *dst = vol ? rq + r : ff + r;
-          const int stride = vol ? nq : nf;
+          if constexpr (ET) {
 #pragma unroll
-          for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+            for (int e = 0; e < NC; ++e) X[t * 8 + e] -= acc[e];
+          } else {
+            float *dst = vol ? rq + r : ff + r;
+            const int stride = vol ? nq : nf;
+#pragma unroll
+            for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+          }
         }
         __syncthreads();
         continue;
@@ -1041,15 +1101,69 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
           for (int e = 0; e < NC; ++e) acc[e] += dp[e];
         }
         cur[sl] = q;
-        float *dst = vol ? rq + r : ff + r;
-        const int stride = vol ? nq : nf;
+        if constexpr (ET) {
 #pragma unroll
-        for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+          for (int e = 0; e < NC; ++e) X[t * 8 + e] -= acc[e];
+        } else {
+          float *dst = vol ? rq + r : ff + r;
+          const int stride = vol ? nq : nf;
+#pragma unroll
+          for (int e = 0; e < NC; ++e) dst[e * stride] -= acc[e];
+        }
       }
       __syncthreads();
     }
   }
 
+  // energy residual = H_ref x density residual + reduced-flux residual, in
+  // FP64, plus the reference state's own FP64 residual (the dropped
+  // reference-pressure terms)
+  double *outp = ka.dudt + (size_t)kk * NC * np;
+  const double *rref = Rs;
+  if constexpr (ET) {
+    // out = E_k [r_q ; f_f]: thread (g, r) sums the column quads g, g + G,
+    // ... of row r (three loads in flight), the G partial rows are added
+    // in a fixed order by the row's thread
+    const int G = tpe / np, gq = lane / np, r = lane - gq * np;
+    const int nquad = ka.ek_quads;
+    const float4 *E4 = reinterpret_cast<const float4 *>(Ekg);
+    float acc[NC];
+#pragma unroll
+    for (int e = 0; e < NC; ++e) acc[e] = 0.f;
+    if (gq < G) {
+      int q = gq;
+      for (; q + 2 * G < nquad; q += 3 * G) {
+        const float4 ea = __ldg(E4 + (size_t)q * np + r);
+        const float4 eb = __ldg(E4 + (size_t)(q + G) * np + r);
+        const float4 ec = __ldg(E4 + (size_t)(q + 2 * G) * np + r);
+        quad_fma<NC>(X + q * 32, ea, acc);
+        quad_fma<NC>(X + (q + G) * 32, eb, acc);
+        quad_fma<NC>(X + (q + 2 * G) * 32, ec, acc);
+      }
+      for (; q < nquad; q += G) quad_fma<NC>(X + q * 32, __ldg(E4 + (size_t)q * np + r), acc);
+      store_node<NC>(diff + (gq * np + r) * 8, acc);
+    }
+    __syncthreads();
+    if (live && lane < np) {
+      float s[NC];
+#pragma unroll
+      for (int e = 0; e < NC; ++e) s[e] = 0.f;
+      for (int gg = 0; gg < G; ++gg) {
+        const float *pr = diff + (gg * np + lane) * 8;
+#pragma unroll
+        for (int e = 0; e < NC; ++e) s[e] += pr[e];
+      }
+#pragma unroll
+      for (int e = 0; e < NC; ++e) {
+        double v = (double)s[e];
+        if (e == NC - 1) v = fma(ph.H_ref, (double)s[0], v);
+        if (rref) v += rref[e * np + lane];
+        outp[e * np + lane] = v;
+        if (!isfinite(s[e])) ka.flag_nonphysical();
+      }
+    }
+    return;
+  }
   // r_q -= R^T f_f
   const float *Rt = OpVals<float>::Rt(op);
   rt_apply<float, NC>(op, Rt, ff, lane, tpe, [&](int t, float v) { rq[t] -= v; });
@@ -1063,11 +1177,6 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   mass_solve<float, D, NC>(op, g.JinvWf ? g.JinvWf + (size_t)kk * nq : nullptr,
                            g.WJinvf ? g.WJinvf + (size_t)kk * nq : nullptr, ka.mass_wa, Xm, Yq, Z,
                            Wb, lane, tpe, Aks);
-  // energy residual = H_ref x density residual + reduced-flux residual, in
-  // FP64, plus the reference state's own FP64 residual (the dropped
-  // reference-pressure terms)
-  double *outp = ka.dudt + (size_t)kk * NC * np;
-  const double *rref = Rs;
   if (live)
     for (int t = lane; t < NC * np; t += tpe) {
       double v = (double)Xm[t];
@@ -1390,25 +1499,31 @@ cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka) {
   return e;
 }
 
+// the mixed phase-B instantiation of this configuration (with the tail
+// operator where ka.Ekf is set), or null
+static const void *mixed_b_kernel(const KernelArgs &ka) {
+  const bool et = ka.Ekf != nullptr;
+  if (ka.op.d == 2 && ka.op.nc == 4)
+    return et ? (const void *)fd_time_derivative_mixed_kernel<2, 4, true>
+              : (const void *)fd_time_derivative_mixed_kernel<2, 4, false>;
+  if (ka.op.d == 3 && ka.op.nc == 5)
+    return et ? (const void *)fd_time_derivative_mixed_kernel<3, 5, true>
+              : (const void *)fd_time_derivative_mixed_kernel<3, 5, false>;
+  return nullptr;
+}
+
 cudaError_t sse_mixed_b_blocks_per_sm(const KernelArgs &ka, size_t smBm, int *blocks) {
-  const void *f = nullptr;
-  if (ka.op.d == 2 && ka.op.nc == 4) f = (const void *)fd_time_derivative_mixed_kernel<2, 4>;
-  else if (ka.op.d == 3 && ka.op.nc == 5) f = (const void *)fd_time_derivative_mixed_kernel<3, 5>;
-  else return cudaErrorInvalidValue;
+  const void *f = mixed_b_kernel(ka);
+  if (!f) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, f, ka.tpb, smBm);
 }
 
 cudaError_t sse_set_smem_limit_mixed(const KernelArgs &ka, size_t smBm) {
-  cudaError_t e = cudaErrorInvalidValue;
-  if (ka.op.d == 2 && ka.op.nc == 4)
-    e = cudaFuncSetAttribute((const void *)fd_time_derivative_mixed_kernel<2, 4>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smBm);
-  else if (ka.op.d == 3 && ka.op.nc == 5)
-    e = cudaFuncSetAttribute((const void *)fd_time_derivative_mixed_kernel<3, 5>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smBm);
-  return e;
+  const void *f = mixed_b_kernel(ka);
+  if (!f) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smBm);
 }
 
 cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st) {
@@ -1421,9 +1536,16 @@ cudaError_t launch_time_derivative(const KernelArgs &ka, cudaStream_t st) {
     km.epb = ka.epb_bm;
     const int gridm = (ka.ne + km.epb - 1) / km.epb;
     size_t smm = (size_t)km.epb * ka.layBm.team_doubles * sizeof(float);
-    if (ka.op.d == 2 && ka.op.nc == 4) fd_time_derivative_mixed_kernel<2, 4><<<gridm, ka.tpb, smm, st>>>(km);
-    else if (ka.op.d == 3 && ka.op.nc == 5) fd_time_derivative_mixed_kernel<3, 5><<<gridm, ka.tpb, smm, st>>>(km);
-    else return cudaErrorInvalidValue;
+    const bool et = ka.Ekf != nullptr;
+    if (ka.op.d == 2 && ka.op.nc == 4) {
+      if (et) fd_time_derivative_mixed_kernel<2, 4, true><<<gridm, ka.tpb, smm, st>>>(km);
+      else fd_time_derivative_mixed_kernel<2, 4, false><<<gridm, ka.tpb, smm, st>>>(km);
+    } else if (ka.op.d == 3 && ka.op.nc == 5) {
+      if (et) fd_time_derivative_mixed_kernel<3, 5, true><<<gridm, ka.tpb, smm, st>>>(km);
+      else fd_time_derivative_mixed_kernel<3, 5, false><<<gridm, ka.tpb, smm, st>>>(km);
+    } else {
+      return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
   }
   if (ka.fd) {
@@ -1502,6 +1624,65 @@ cudaError_t launch_fill_constant_state(double *buf, int nodes, int nc, size_t ne
 cudaError_t launch_round_transpose(const double *in, float *out, size_t nmat, int n, cudaStream_t st) {
   if (nmat == 0 || n == 0) return cudaSuccess;
   round_transpose_kernel<<<elementwise_grid(nmat * n * n), 256, 0, st>>>(in, out, nmat, n);
+  return cudaGetLastError();
+}
+
+// Columns of M = V^T [I | -R^T] (n_p rows; column c at M + c n_p): V^T e_c
+// for a volume node c, -(R V)^T e_j for facet node j = c - n_q, zero for the
+// padding columns up to ncol.  Vd: dense V (n_q x n_p, column-major).
+__global__ void tail_matrix_kernel(DevOps op, const double *__restrict__ Vd, double *__restrict__ M, int ncol) {
+  const int np = op.np, nq = op.nq, nf = op.nf;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < np * ncol; t += gridDim.x * blockDim.x) {
+    const int c = t / np, b = t - c * np;
+    double v = 0.0;
+    if (c < nq) {
+      v = Vd[c + (size_t)nq * b];
+    } else if (c < nq + nf) {
+      const int j = c - nq;
+      for (int q = op.R_ptr[j]; q < op.R_ptr[j + 1]; ++q) v = fma(-op.R_val[q], Vd[op.R_idx[q] + (size_t)nq * b], v);
+    }
+    M[t] = v;
+  }
+}
+
+// E_k = A_k M for element k = blockIdx.x in FP64 (A_k column-major, staged in
+// shared memory), rounded to FP32 in column quads: float4 (q, r) holds
+// E_k[r, 4q .. 4q+3].
+__global__ void __launch_bounds__(256) tail_operator_kernel(const double *__restrict__ Ak,
+                                                            const double *__restrict__ M, float4 *__restrict__ E,
+                                                            int np, int quads) {
+  extern __shared__ double a_s[];
+  const size_t k = blockIdx.x;
+  const double *A = Ak + k * np * np;
+  for (int t = threadIdx.x; t < np * np; t += blockDim.x) a_s[t] = A[t];
+  __syncthreads();
+  float4 *Ek = E + k * quads * np;
+  for (int t = threadIdx.x; t < quads * np; t += blockDim.x) {
+    const int q = t / np, r = t - q * np;
+    const double *m0 = M + (size_t)(4 * q) * np;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int b = 0; b < np; ++b) {
+      const double a = a_s[b * np + r];
+      s0 = fma(a, m0[b], s0);
+      s1 = fma(a, m0[np + b], s1);
+      s2 = fma(a, m0[2 * np + b], s2);
+      s3 = fma(a, m0[3 * np + b], s3);
+    }
+    Ek[t] = make_float4((float)s0, (float)s1, (float)s2, (float)s3);
+  }
+}
+
+cudaError_t launch_tail_operators(const KernelArgs &ka, const double *Vd, double *M, float *E, int quads,
+                                  cudaStream_t st) {
+  const int np = ka.op.np, ncol = 4 * quads;
+  tail_matrix_kernel<<<(np * ncol + 255) / 256, 256, 0, st>>>(ka.op, Vd, M, ncol);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const size_t sm = (size_t)np * np * sizeof(double);
+  if ((e = cudaFuncSetAttribute((const void *)tail_operator_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sm)))
+    return e;
+  tail_operator_kernel<<<ka.ne, 256, sm, st>>>(ka.Ak, M, reinterpret_cast<float4 *>(E), np, quads);
   return cudaGetLastError();
 }
 

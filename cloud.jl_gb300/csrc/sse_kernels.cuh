@@ -36,6 +36,11 @@ struct KernelArgs {
   int ne, epb, tpb;
   const double *Ak;  // per-element weight-adjusted mass operators (n_p x n_p, column-major), or null
   const float *Akf;  // their FP32 roundings for the mixed form (row-major), or null
+  // mixed form: per-element tail operators E_k = A_k V^T [I | -R^T] (n_p rows,
+  // the volume then facet nodes as columns, padded to ek_quads column quads;
+  // float4 (q, r) = E_k[r, 4q .. 4q+3]), or null
+  const float *Ekf;
+  int ek_quads;
   int fd, project_entropy, mass_wa;
   const double *u;   // modal state (np x nc x ne)
   double *dudt;      // residual   (np x nc x ne)
@@ -132,6 +137,11 @@ cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaSt
 cudaError_t launch_fill_constant_state(double *buf, int nodes, int nc, size_t ne, const double *state,
                                        cudaStream_t st);
 cudaError_t launch_round_transpose(const double *in, float *out, size_t nmat, int n, cudaStream_t st);
+// the mixed form's per-element tail operators (KernelArgs::Ekf) from the
+// FP64 mass operators ka.Ak and the dense V (Vd, n_q x n_p column-major);
+// M is FP64 scratch of n_p x 4 quads doubles
+cudaError_t launch_tail_operators(const KernelArgs &ka, const double *Vd, double *M, float *E, int quads,
+                                  cudaStream_t st);
 cudaError_t launch_nodal_values(const KernelArgs &ka, cudaStream_t st);
 cudaError_t launch_projection_of_one(const KernelArgs &ka, double *P1, double *RP1, cudaStream_t st);
 cudaError_t sse_set_smem_limits_mixed_a(const KernelArgs &ka);

@@ -69,6 +69,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   return false;
 }
 
+// Prefetch `bytes` (a multiple of 16) of global memory from the 16-byte
+// aligned address src into L2 through the copy engine; nothing waits on it.
+__device__ __forceinline__ void prefetch_l2(const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // Where a slab starting at global address src lands in a shared region
 // (the region base is 16-byte aligned).
 template <typename T>
