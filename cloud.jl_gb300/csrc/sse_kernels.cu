@@ -834,20 +834,24 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
     if (st_ak) stage_slab(base + L.off[3], Akg, ba, bar);
     if (st_rref) stage_slab(base + L.off[9], Rg, br, bar);
   }
-  // meanwhile: where the neighbour's facet state of this thread's first
-  // facet node lives (its gather overlaps the primitives below)
-  const int P0 = lane < nf ? __ldg(g.mapP + (size_t)kk * nf + lane) : 0;
-  __syncthreads();  // the mbarrier is initialised
-  if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
-    if (lane == 0) ka.flag_timeout();
-    mbar_wait_bounded(bar, 0);  // give copies still in flight a bounded time to land
-    return;
-  }
+  // meanwhile: the neighbour's facet state of this thread's first facet
+  // node (its gather overlaps the bulk copies)
   float uo0[NC];
   if (lane < nf) {
+    const int P0 = __ldg(g.mapP + (size_t)kk * nf + lane);
     const int jn = P0 % nf, kn = P0 / nf;
 #pragma unroll
     for (int e = 0; e < NC; ++e) uo0[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
+  }
+  __syncthreads();  // the mbarrier is initialised
+  // one thread of the team waits for the copies; the others wait at the
+  // barrier, where they take no issue slots (the barrier then orders the
+  // landed data before their reads)
+  const bool landed = lane != 0 ? true : mbar_wait_bounded(bar, 0);
+  if (!__syncthreads_and(landed)) {
+    if (lane == 0) ka.flag_timeout();
+    mbar_wait_bounded(bar, 0);  // give copies still in flight a bounded time to land
+    return;
   }
   for (int i = lane; i < nq + nf; i += tpe) {
     float du[NC];
