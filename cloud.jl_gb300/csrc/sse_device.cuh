@@ -178,18 +178,31 @@ __device__ __forceinline__ double inv_logmean(double x, double y) {
 // ---------------------------------------------------------------------------
 // FP64 fast path.  GB300 issues FP64 at 1/62 of its FP32 rate, so the
 // residual's cost is its FP64 instruction count.  The functions below compute
-// the reference's quantities with fewer FP64 instructions: one correctly
-// rounded reciprocal shared by the logarithmic mean's series branch, the
-// two-point flux contracted with its metric vector before the flux tensor is
-// formed, and logarithms/exponentials instead of pow.  They agree with the
-// reference's formulas to a few ulps (checked on the host in
-// tests/test_device_math.py and against the oracle on the GPU).
+// the reference's quantities with fewer FP64 instructions: one reciprocal
+// shared by the logarithmic mean's series branch, the two-point flux
+// contracted with its metric vector before the flux tensor is formed, and
+// logarithms/exponentials instead of pow.  They agree with the reference's
+// formulas to a few ulps (checked on the host in tests/test_device_math.py
+// and against the oracle on the GPU).
 // ---------------------------------------------------------------------------
 #define SSE_HD __host__ __device__ __forceinline__
 
+// 1/s for the positive, normal arguments of the flux and entropy algebra
+// (sums of densities, pressures, temperatures, entropy variables): the
+// hardware reciprocal approximation (PTX rcp.approx.ftz.f64) refined by two
+// Newton-Raphson steps y <- y + y (1 - s y), each of which squares the
+// relative error, which leaves the result within about an ulp of 1/s -- four
+// FMAs, where a correctly rounded reciprocal needs a longer sequence on the
+// FP64 pipe.  Zero, infinite and subnormal arguments (never physical here)
+// give NaN or flush, which the non-physical flag reports.
 SSE_HD double sse_rcp(double s) {
 #ifdef __CUDA_ARCH__
-  return __drcp_rn(s);
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(s));
+  double e = fma(-s, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-s, y, 1.0);
+  return fma(y, e, y);
 #else
   return 1.0 / s;
 #endif
@@ -207,7 +220,9 @@ SSE_HD double logmean_fast(double x, double y) {
   const double s = x + y;
   const double f = (x - y) * sse_rcp(s);
   const double z = f * f;
-  if (z < 1.0e-4) return 0.5 * s * fma(z, fma(z, fma(z, kInvQ3, kInvQ2), kInvQ1), 1.0);
+  // (s / 2) (1/q) with the 1/2 taken by the coefficients: the same bits
+  // (halving is exact), one multiplication fewer
+  if (z < 1.0e-4) return s * fma(z, fma(z, fma(z, 0.5 * kInvQ3, 0.5 * kInvQ2), 0.5 * kInvQ1), 0.5);
   return (y - x) / log(y / x);
 }
 
@@ -217,7 +232,8 @@ SSE_HD double inv_logmean_fast(double x, double y) {
   const double r = sse_rcp(s);
   const double f = (x - y) * r;
   const double z = f * f;
-  if (z < 1.0e-4) return 2.0 * r * fma(z, fma(z, fma(z, 1.0 / 7.0, 0.2), 1.0 / 3.0), 1.0);
+  // (2 r) q with the 2 taken by the coefficients: the same bits
+  if (z < 1.0e-4) return r * fma(z, fma(z, fma(z, 2.0 * (1.0 / 7.0), 2.0 * 0.2), 2.0 * (1.0 / 3.0)), 2.0);
   return log(y / x) / (y - x);
 }
 
