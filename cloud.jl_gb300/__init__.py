@@ -5,7 +5,7 @@ reference's API plus the C-ABI CUDA library ``libsse_gb300.so``.
 The directory name contains a dot, so it is loaded as the module
 ``cloud_jl_gb300`` (see ``__graft_entry__.load_package``).
 """
-from . import (abi, build, flops_model, gb300, mesh, objectives, polynomials, reference,  # noqa: F401
+from . import (abi, build, flops_model, gb300, jld2, mesh, objectives, polynomials, reference,  # noqa: F401
                setups, solver, timestepping)
 from .gb300 import (GB300Solver, ODEProblem, SSEError, load_library,  # noqa: F401
                     semi_discrete_residual, semidiscretize)
