@@ -887,19 +887,84 @@ int enable_mixed(sse_solver *s) {
   const int tpe_fp64 = ka.tpb / ka.epb;
   const int tpe_m = std::max(32, tpe_fp64);
   ka.epb_bm = std::max(1, ka.epb * tpe_fp64 / tpe_m);
+  // Shared regions of the staged slabs: n floats plus the alignment margin
+  // of a bulk copy (the slab lands at its source address modulo 16).
+  auto staged = [&](int n) { return r4(n + 8); };
+  const int quads = (int)((nq + nf + 3) / 4);
+  // phase-B layout, pair chunk and optional staged slabs for the
+  // sum-factorised tail (et = false) or the tail operators (et = true: region
+  // 2 holds the node-major residuals, 8 floats per node with the last column
+  // quad's padding nodes, and the pair buffer later the G = tpe / n_p partial
+  // rows of the tail product)
+  struct Plan { int chunk, blocks, off; bool geo, rref, ak; };
+  auto plan = [&](bool et) {
+    const int np2 = ka.Akf && !et ? np * np : 0;
+    const int region2 = et ? 32 * quads : nc * (int)nf;
+    const int final_e = et ? (tpe_m / np) * np * 8 : final_m;
+    auto layout_m = [&](int chunk, bool geo, bool rref, bool ak) {
+      const int sizes[11] = {staged(nc * (int)nq), staged(nc * (int)nf), region2,
+                             ak && np2 ? staged(np2) : 0, std::max(chunk * nc, final_e),
+                             staged((int)(d * d * nq)), op.nfp > 0 ? staged((int)(d * c.num_faces * nq)) : 0,
+                             (int)((nq + nf) * (4 + d)),
+                             geo ? 2 * staged((int)(d * nf)) + staged((int)nf) : 0,
+                             rref ? staged(2 * nc * np) : 0, 4};
+      int off = 0, i = 0;
+      for (int sz : sizes) { ka.layBm.off[i++] = off; off += r4(sz); }
+      for (; i < 12; ++i) ka.layBm.off[i] = off;
+      ka.layBm.team_doubles = off;  // counted in floats for this layout
+      return off;
+    };
+    const int budget_m = (int)((size_t)55 * 1024 / 4 / ka.epb_bm);
+    int chunk_m = max_pairs;
+    if (layout_m(chunk_m, false, false, false) > budget_m) {
+      // four blocks per SM when chunks of at least one pass of the element's
+      // threads fit, else two, else one
+      const int fixed = layout_m(0, false, false, false) - r4(final_e);
+      const int need = std::min(tpe_m, max_pairs) * nc;
+      int room = budget_m - fixed;
+      if (room < need) room = 2 * budget_m - fixed;
+      if (room < need) room = (int)((size_t)220 * 1024 / 4 / ka.epb_bm) - fixed;
+      chunk_m = std::max(1, room / nc);
+      if (chunk_m >= tpe_m) chunk_m = chunk_m / tpe_m * tpe_m;
+      chunk_m = std::max(1, std::min(chunk_m, max_pairs));
+    }
+    // The facet geometry, the reference residual and the mass operator are
+    // staged as well where that keeps the resident blocks per SM (shared
+    // memory, registers and threads together), else read from global memory.
+    auto blocks_per_sm = [&](int floats) {
+      int nb = 0;
+      if (sse_mixed_b_blocks_per_sm(ka, (size_t)ka.epb_bm * floats * 4, &nb) != cudaSuccess) return 0;
+      return nb;
+    };
+    Plan pl{chunk_m, 0, 0, false, false, false};
+    pl.blocks = blocks_per_sm(layout_m(chunk_m, false, false, false));
+    if (blocks_per_sm(layout_m(chunk_m, true, false, false)) >= pl.blocks) pl.geo = true;
+    if (blocks_per_sm(layout_m(chunk_m, pl.geo, true, false)) >= pl.blocks) pl.rref = true;
+    if (blocks_per_sm(layout_m(chunk_m, pl.geo, pl.rref, true)) >= pl.blocks) pl.ak = true;
+    pl.off = layout_m(chunk_m, pl.geo, pl.rref, pl.ak);
+    return pl;
+  };
   // The tail operators E_k = A_k V^T [I | -R^T]: phase B's lift, V^T and
   // weight-adjusted mass solve as one per-element product, built once in
   // FP64 and rounded to FP32, where the FP64 mass operators exist, the
-  // element's threads cover its n_p rows, and the operators take at most a
-  // quarter of the free device memory.
+  // element's threads cover its n_p rows, the operators take at most a
+  // quarter of the free device memory, and the node-major residuals keep
+  // the blocks per SM and the pair chunk of the sum-factorised tail (p = 5
+  // tets: the tail operators cost a smaller chunk, and phase B took 10.7
+  // instead of 5.3 ms).
   ka.Ekf = nullptr;
   ka.ek_quads = 0;
+  Plan chosen = plan(false);
   if (ka.Ak && ka.Akf && op.has_vdm && tpe_m >= np) {
-    const int quads = (int)((nq + nf + 3) / 4);
     const size_t bytes = (size_t)ne * quads * np * 16;
     size_t freeb = 0, totalb = 0;
     if ((e = cudaMemGetInfo(&freeb, &totalb))) return cuda_fail(s, e, "cudaMemGetInfo");
-    if (bytes <= freeb / 4) {
+    ka.Ekf = reinterpret_cast<const float *>(16);  // selects the instantiation for the occupancy query
+    ka.ek_quads = quads;
+    const Plan withE = plan(true);
+    ka.Ekf = nullptr;
+    ka.ek_quads = 0;
+    if (bytes <= freeb / 4 && withE.chunk >= chosen.chunk && withE.blocks >= chosen.blocks) {
       const double *Vd = op.dense_v ? op.Vd : nullptr;
       if (!Vd) {
         if ((e = alloc(s, nq * np * sizeof(double), &p))) return cuda_fail(s, e, "alloc dense V");
@@ -912,61 +977,14 @@ int enable_mixed(sse_solver *s) {
         return cuda_fail(s, e, "mixed tail operators");
       ka.Ekf = (const float *)pe;
       ka.ek_quads = quads;
+      chosen = plan(true);
+    } else {
+      chosen = plan(false);  // restores the layout of the sum-factorised tail
     }
   }
-  const bool et = ka.Ekf != nullptr;
-  // Shared regions of the staged slabs: n floats plus the alignment margin
-  // of a bulk copy (the slab lands at its source address modulo 16).
-  auto staged = [&](int n) { return r4(n + 8); };
-  const int np2 = ka.Akf && !et ? np * np : 0;
-  // with the tail operators: region 2 holds the node-major residuals (8
-  // floats per node, the last column quad's padding nodes included) and the
-  // pair buffer later the G = tpe / n_p partial rows of the tail product
-  const int region2 = et ? 32 * ka.ek_quads : nc * (int)nf;
-  const int final_e = et ? (tpe_m / np) * np * 8 : final_m;
-  auto layout_m = [&](int chunk, bool geo, bool rref, bool ak) {
-    const int sizes[11] = {staged(nc * (int)nq), staged(nc * (int)nf), region2,
-                           ak && np2 ? staged(np2) : 0, std::max(chunk * nc, final_e),
-                           staged((int)(d * d * nq)), op.nfp > 0 ? staged((int)(d * c.num_faces * nq)) : 0,
-                           (int)((nq + nf) * (4 + d)),
-                           geo ? 2 * staged((int)(d * nf)) + staged((int)nf) : 0,
-                           rref ? staged(2 * nc * np) : 0, 4};
-    int off = 0, i = 0;
-    for (int sz : sizes) { ka.layBm.off[i++] = off; off += r4(sz); }
-    for (; i < 12; ++i) ka.layBm.off[i] = off;
-    ka.layBm.team_doubles = off;  // counted in floats for this layout
-    return off;
-  };
-  const int budget_m = (int)((size_t)55 * 1024 / 4 / ka.epb_bm);
-  int chunk_m = max_pairs;
-  if (layout_m(chunk_m, false, false, false) > budget_m) {
-    // four blocks per SM when chunks of at least one pass of the element's
-    // threads fit, else two, else one
-    const int fixed = layout_m(0, false, false, false) - r4(final_e);
-    const int need = std::min(tpe_m, max_pairs) * nc;
-    int room = budget_m - fixed;
-    if (room < need) room = 2 * budget_m - fixed;
-    if (room < need) room = (int)((size_t)220 * 1024 / 4 / ka.epb_bm) - fixed;
-    chunk_m = std::max(1, room / nc);
-    if (chunk_m >= tpe_m) chunk_m = chunk_m / tpe_m * tpe_m;
-    chunk_m = std::max(1, std::min(chunk_m, max_pairs));
-  }
-  ka.fd_chunk_mixed = chunk_m;
+  ka.fd_chunk_mixed = chosen.chunk;
   ka.vdm_zsz_mixed = zsz4;
-  // The facet geometry, the reference residual and the mass operator are
-  // staged as well where that keeps the resident blocks per SM (shared
-  // memory, registers and threads together), else read from global memory.
-  auto blocks_per_sm = [&](int floats) {
-    int nb = 0;
-    if (sse_mixed_b_blocks_per_sm(ka, (size_t)ka.epb_bm * floats * 4, &nb) != cudaSuccess) return 0;
-    return nb;
-  };
-  bool geo = false, rref = false, ak = false;
-  const int blocks0 = blocks_per_sm(layout_m(chunk_m, false, false, false));
-  if (blocks_per_sm(layout_m(chunk_m, true, false, false)) >= blocks0) geo = true;
-  if (blocks_per_sm(layout_m(chunk_m, geo, true, false)) >= blocks0) rref = true;
-  if (blocks_per_sm(layout_m(chunk_m, geo, rref, true)) >= blocks0) ak = true;
-  const int off = layout_m(chunk_m, geo, rref, ak);
+  const int off = chosen.off;
   size_t smm = (size_t)ka.epb_bm * off * sizeof(float);
   if (smm > 220 * 1024) return fail(s, SSE_ERR_UNSUPPORTED, "element too large for the mixed kernel");
   if ((e = sse_set_smem_limit_mixed(ka, smm))) return cuda_fail(s, e, "cudaFuncSetAttribute");
