@@ -208,6 +208,20 @@ SSE_HD double sse_rcp(double s) {
 #endif
 }
 
+// 1/s to about 2^-38 relative: one Newton-Raphson step on the hardware
+// approximation, for a quotient that only enters through the square of a
+// ratio below 1e-2 (the logarithmic mean's f = (x - y)/(x + y) on its
+// series branch), where that error moves the result by about 1e-16.
+SSE_HD double sse_rcp_coarse(double s) {
+#ifdef __CUDA_ARCH__
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(s));
+  return fma(y, fma(-s, y, 1.0), y);
+#else
+  return 1.0 / s;
+#endif
+}
+
 // 1/q(z) for q(z) = 1 + z/3 + z^2/5 + z^3/7 by its power series; for
 // z < 1e-4 the first omitted term is below 1e-17 relative.
 constexpr double kInvQ1 = -1.0 / 3.0;
@@ -218,7 +232,7 @@ constexpr double kInvQ3 = -44.0 / 945.0;
 // f = (x - y)/(x + y) on the series branch, (y - x)/log(y/x) otherwise.
 SSE_HD double logmean_fast(double x, double y) {
   const double s = x + y;
-  const double f = (x - y) * sse_rcp(s);
+  const double f = (x - y) * sse_rcp_coarse(s);
   const double z = f * f;
   // (s / 2) (1/q) with the 1/2 taken by the coefficients: the same bits
   // (halving is exact), one multiplication fewer
