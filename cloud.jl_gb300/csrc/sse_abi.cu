@@ -1556,6 +1556,25 @@ int32_t sse_set_precision(sse_solver *s, int32_t precision) {
   return SSE_OK;
 }
 
+// The device address of a host buffer of `bytes` bytes that kernels can reach
+// in place: page-locked host memory mapped into the device's address space
+// (cudaHostAlloc, or cudaHostRegister with mapping), first and last byte in
+// the same mapping; null for pageable or unknown memory.
+const void *mapped_host(const void *p, size_t bytes) {
+  cudaPointerAttributes a{}, z{};
+  const char *last = static_cast<const char *>(p) + (bytes ? bytes - 1 : 0);
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaPointerGetAttributes(&z, last) != cudaSuccess) {
+    cudaGetLastError();  // clear the query's error for unknown (pageable) pointers
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || z.type != cudaMemoryTypeHost || !a.devicePointer || !z.devicePointer)
+    return nullptr;
+  if (static_cast<const char *>(z.devicePointer) - static_cast<const char *>(a.devicePointer) !=
+      last - static_cast<const char *>(p))
+    return nullptr;
+  return a.devicePointer;
+}
+
 int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t, int32_t memory) {
   (void)t;  // the supported laws carry no source term
   if (!s) return SSE_ERR_INVALID_ARGUMENT;
@@ -1565,9 +1584,19 @@ int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t, int
   if (memory == SSE_DEVICE) {
     if ((e = residual_device(s, u, dudt)) != cudaSuccess) return cuda_fail(s, e, "residual");
   } else if (memory == SSE_HOST) {
-    if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
-    if ((e = residual_device(s, s->d_u, s->d_dudt)) != cudaSuccess) return cuda_fail(s, e, "residual");
-    if ((e = cudaMemcpyAsync(dudt, s->d_dudt, n * 8, cudaMemcpyDeviceToHost, s->stream))) return cuda_fail(s, e, "D2H");
+    const double *hu = static_cast<const double *>(mapped_host(u, n * 8));
+    double *hd = static_cast<double *>(const_cast<void *>(mapped_host(dudt, n * 8)));
+    if (hu && hd) {
+      // page-locked caller buffers: phase A reads the state and phase B
+      // writes the residual across the host link while they compute (GB300:
+      // NVLink-C2C, ~190 GB/s either way, the rate of the staging copies),
+      // so no copy stands between the stages
+      if ((e = residual_device(s, hu, hd)) != cudaSuccess) return cuda_fail(s, e, "residual");
+    } else {
+      if ((e = cudaMemcpyAsync(s->d_u, u, n * 8, cudaMemcpyHostToDevice, s->stream))) return cuda_fail(s, e, "H2D");
+      if ((e = residual_device(s, s->d_u, s->d_dudt)) != cudaSuccess) return cuda_fail(s, e, "residual");
+      if ((e = cudaMemcpyAsync(dudt, s->d_dudt, n * 8, cudaMemcpyDeviceToHost, s->stream))) return cuda_fail(s, e, "D2H");
+    }
   } else {
     return fail(s, SSE_ERR_INVALID_ARGUMENT, "memory must be SSE_HOST or SSE_DEVICE");
   }

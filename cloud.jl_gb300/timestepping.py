@@ -68,6 +68,23 @@ class _Ops:
             np.multiply(x, b, out=scratch)
             y += scratch
 
+    def axpy_into(self, q, a, k):
+        """q <- a q + k (one pass on torch tensors)"""
+        if self.torch:
+            import torch
+            torch.add(k, q, alpha=a, out=q)
+        else:
+            q *= a
+            q += k
+
+    def add_scaled(self, u, q, c, scratch):
+        """u <- u + c q (one pass on torch tensors)"""
+        if self.torch:
+            u.add_(q, alpha=c)
+        else:
+            np.multiply(q, c, out=scratch)
+            u += scratch
+
     def set_scaled(self, y, x, b):
         """y <- b x"""
         if self.torch:
@@ -95,15 +112,19 @@ def solve(ode, dt: float, n_steps: int, alg: str = "CarpenterKennedy2N54", u=Non
     k = ops.empty(u)
     scratch = ops.empty(u)
     if alg == "CarpenterKennedy2N54":
+        # the 2N recurrence q <- a q + dt k, u <- u + b q on the register
+        # scaled by 1/dt (q' <- a q' + k, u <- u + (b dt) q'): two passes
+        # over the state per stage, as OrdinaryDiffEq's fused broadcasts; on
+        # the first stage (a = 0) the residual buffer itself becomes q'
         q = ops.empty(u)
         for _ in range(n_steps):
             for s, (a, b, c) in enumerate(zip(CK_A, CK_B, CK_C)):
                 ode.f(k, u, ode.p, t + c * dt)
                 if s == 0:
-                    ops.set_scaled(q, k, dt)
+                    q, k = k, q
                 else:
-                    ops.scale_add(q, a, k, dt, scratch)
-                ops.scale_add(u, 1.0, q, b, scratch)
+                    ops.axpy_into(q, a, k)
+                ops.add_scaled(u, q, b * dt, scratch)
             t += dt
     elif alg == "RK4":
         acc, ust = ops.empty(u), ops.empty(u)

@@ -68,6 +68,12 @@ def test_rejects_invalid_arguments_on_host(pkg, lib):
     rc, msg, _ = _create(pkg, lib, host)
     host.cfg.n_c = 4
     assert rc == abi.SSE_ERR_UNSUPPORTED
+    # an empty mesh (no elements) is rejected on the host
+    ne = host.cfg.n_e
+    host.cfg.n_e = 0
+    rc, msg, h0 = _create(pkg, lib, host)
+    host.cfg.n_e = ne
+    assert rc == abi.SSE_ERR_INVALID_ARGUMENT and not h0.value
     # inconsistent facet count
     host.cfg.nodes_per_face += 1
     rc, msg, _ = _create(pkg, lib, host)

@@ -112,6 +112,29 @@ def test_device_memory_path_and_determinism(built, pkg):
     assert np.array_equal(a.cpu().numpy(), host_res)       # host and device paths agree
 
 
+@pytest.mark.parametrize("name,mixed", [("tgv_tet_modal", False), ("tgv_tet_modal", True),
+                                        ("vortex_tri_modal", False), ("adv_tri_modal", False)])
+def test_pinned_host_buffers_are_used_in_place(built, pkg, name, mixed):
+    """sse_residual on page-locked host buffers: the kernels read the state
+    and write the residual in host memory (no staging copies), with the bits
+    of the device-memory path; also with the residual written over the
+    state, and for pageable buffers (staging copies)."""
+    import torch
+    host, u = cases.make(name)
+    gpu = pkg.GB300Solver(host)
+    if mixed:
+        gpu.set_precision(pkg.abi.SSE_MIXED)
+    want = gpu.residual(torch.from_numpy(u).cuda()).cpu().numpy()
+    up = torch.from_numpy(u.copy()).pin_memory()
+    out = torch.full_like(up, float("nan")).pin_memory()
+    gpu.residual(up, out)
+    assert np.array_equal(out.numpy(), want)
+    assert np.array_equal(up.numpy(), u)                   # the state is left as it was
+    assert np.array_equal(gpu.residual(u.copy()), want)    # pageable: staging copies
+    gpu.residual(up, up)                                   # in place (two-phase kernels
+    assert rel2(up.numpy(), want) <= 1e-13                 # where the one-kernel path ran)
+
+
 @pytest.mark.parametrize("name,scheme,steps", [("adv_tri_modal", 1, 3), ("vortex_tri_modal", 0, 3),
                                                ("tgv_tet_modal", 0, 2)])
 def test_rk_steps_match_oracle(built, pkg, name, scheme, steps):
