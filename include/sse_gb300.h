@@ -152,7 +152,11 @@ int32_t sse_create(const sse_config *cfg, const sse_operators *ops,
 int32_t sse_destroy(sse_solver *s);
 
 /* dudt <- R(u): semi_discrete_residual!(dudt, u, solver, t), Solvers.jl:474-514.
- * u and dudt are N_p x N_c x N_e column-major FP64, host or device memory. */
+ * u and dudt are N_p x N_c x N_e column-major FP64, host or device memory.
+ * SSE_HOST buffers that are page-locked and mapped into the device's address
+ * space (cudaHostAlloc, cudaHostRegister with mapping) are read and written
+ * in place by the kernels over the host link; other host buffers go through
+ * the handle's device buffers with one copy each way.  dudt may be u. */
 int32_t sse_residual(sse_solver *s, const double *u, double *dudt, double t,
                      int32_t memory);
 
