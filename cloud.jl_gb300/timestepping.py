@@ -59,15 +59,6 @@ class _Ops:
             return u.new_empty(u.shape).pin_memory() if u.is_pinned() else u.new_empty(u.shape)
         return np.empty_like(u)
 
-    def scale_add(self, y, a, x, b, scratch):
-        """y <- a y + b x"""
-        if self.torch:
-            y.mul_(a).add_(x, alpha=b)
-        else:
-            y *= a
-            np.multiply(x, b, out=scratch)
-            y += scratch
-
     def axpy_into(self, q, a, k):
         """q <- a q + k (one pass on torch tensors)"""
         if self.torch:
@@ -85,17 +76,11 @@ class _Ops:
             np.multiply(q, c, out=scratch)
             u += scratch
 
-    def set_scaled(self, y, x, b):
-        """y <- b x"""
-        if self.torch:
-            y.copy_(x).mul_(b)
-        else:
-            np.multiply(x, b, out=y)
-
     def lincomb(self, y, x, b, z):
-        """y <- x + b z"""
+        """y <- x + b z (one pass on torch tensors)"""
         if self.torch:
-            y.copy_(x).add_(z, alpha=b)
+            import torch
+            torch.add(x, z, alpha=b, out=y)
         else:
             np.multiply(z, b, out=y)
             y += x
@@ -127,20 +112,23 @@ def solve(ode, dt: float, n_steps: int, alg: str = "CarpenterKennedy2N54", u=Non
                 ops.add_scaled(u, q, b * dt, scratch)
             t += dt
     elif alg == "RK4":
+        # one fused pass per update: the stage states ust = u + c k, the
+        # accumulator acc = k1 + 2 k2 + 2 k3 + k4 (k1's buffer becomes acc),
+        # and u <- u + dt/6 (acc + k4)
         acc, ust = ops.empty(u), ops.empty(u)
         for _ in range(n_steps):
             ode.f(k, u, ode.p, t)
-            ops.set_scaled(acc, k, 1.0)
+            acc, k = k, acc
+            ops.lincomb(ust, u, 0.5 * dt, acc)
+            ode.f(k, ust, ode.p, t + 0.5 * dt)
+            ops.add_scaled(acc, k, 2.0, scratch)
             ops.lincomb(ust, u, 0.5 * dt, k)
             ode.f(k, ust, ode.p, t + 0.5 * dt)
-            ops.scale_add(acc, 1.0, k, 2.0, scratch)
-            ops.lincomb(ust, u, 0.5 * dt, k)
-            ode.f(k, ust, ode.p, t + 0.5 * dt)
-            ops.scale_add(acc, 1.0, k, 2.0, scratch)
+            ops.add_scaled(acc, k, 2.0, scratch)
             ops.lincomb(ust, u, dt, k)
             ode.f(k, ust, ode.p, t + dt)
-            ops.scale_add(acc, 1.0, k, 1.0, scratch)
-            ops.scale_add(u, 1.0, acc, dt / 6.0, scratch)
+            ops.add_scaled(acc, k, 1.0, scratch)
+            ops.add_scaled(u, acc, dt / 6.0, scratch)
             t += dt
     else:
         raise ValueError(f"unknown time integrator {alg!r}")
