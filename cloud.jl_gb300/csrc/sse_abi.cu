@@ -637,6 +637,10 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   ph.gamma = c.gamma;
   ph.gm1 = c.gamma - 1.0;
   ph.igm1 = c.law == SSE_EULER ? 1.0 / (c.gamma - 1.0) : 0.0;
+  ph.ilm_q[0] = ph.igm1 * 2.0;
+  ph.ilm_q[1] = ph.igm1 * (2.0 / 3.0);
+  ph.ilm_q[2] = ph.igm1 * 0.4;
+  ph.ilm_q[3] = ph.igm1 * (2.0 / 7.0);
   ph.log_gm1 = c.law == SSE_EULER ? std::log(c.gamma - 1.0) : 0.0;
   for (int m = 0; m < 3; ++m) ph.a[m] = c.a[m];
   ka.fd = fd;

@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
             for (int n = 0; n < D; ++n)
               G[n] = fma(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
           }
-          ec_flux_dot_half<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)j * PS, G, dp);
+          ec_flux_dot_half<D>(ph.igm1, ph.ilm_q, prim + (size_t)i * PS, prim + (size_t)j * PS, G, dp);
           continue;
         }
       }
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(256) fd_time_derivative_kernel(KernelArgs ka) 
             double G[D];
 #pragma unroll
             for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
-            ec_flux_dot_half<D>(ph.igm1, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, dp);
+            ec_flux_dot_half<D>(ph.igm1, ph.ilm_q, prim + (size_t)i * PS, prim + (size_t)(nq + j) * PS, G, dp);
             continue;
           }
         }
