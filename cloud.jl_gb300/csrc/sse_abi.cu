@@ -16,6 +16,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>  // header-only NVTX ranges (no link dependency)
+
 #include <cuda_runtime.h>
 
 #include "../../include/sse_gb300.h"
@@ -1143,9 +1145,16 @@ cudaError_t residual_device(sse_solver *s, const double *u, double *dudt, double
     ka.u_q = u_q;
     ka.u_f = u_f;
   }
+  // NVTX ranges named like the reference's TimerOutputs sections
+  // (Solvers.jl:474-489), around each phase's launch
+  nvtxRangePushA("nodal values");
   cudaError_t e = launch_nodal_values(ka, s->stream);
+  nvtxRangePop();
   if (e != cudaSuccess) return e;
-  return launch_time_derivative(ka, s->stream);
+  nvtxRangePushA("time deriv.");
+  e = launch_time_derivative(ka, s->stream);
+  nvtxRangePop();
+  return e;
 }
 
 // ---------------------------------------------------------------------------

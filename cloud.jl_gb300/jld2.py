@@ -51,7 +51,7 @@ UNDEF = 0xFFFFFFFFFFFFFFFF
 SINGLE_OBJECT = "single_stored_object"   # JLD2's key of save_object / load_object
 
 # header message types
-MSG_NIL, MSG_DATASPACE, MSG_LINK_INFO, MSG_DATATYPE, MSG_FILL_OLD, MSG_FILL = 0x00, 0x01, 0x02, 0x03, 0x04, 0x05
+MSG_DATASPACE, MSG_LINK_INFO, MSG_DATATYPE, MSG_FILL = 0x01, 0x02, 0x03, 0x05
 MSG_LINK, MSG_LAYOUT, MSG_GROUP_INFO, MSG_CONTINUATION, MSG_SYMBOL_TABLE = 0x06, 0x08, 0x0A, 0x10, 0x11
 
 
@@ -604,14 +604,23 @@ def save_callback(solver, results_path: str, u0, n_steps: int, dt: float, interv
     ``iter % interval == 0``) and PresetTimeCallback (tspan ends) do; each
     step number is appended to time_steps.jld2.  Returns (u, t) at the end.
     ``scheme``: 0 CarpenterKennedy2N54, 1 RK4 (the library's sse_scheme)."""
+    def write(u_s, t_s, step, du_s):
+        # the integrator form of save_solution: skip a step already on disk,
+        # log the step to screen.txt (File/save.jl:45-66)
+        if os.path.exists(os.path.join(results_path, f"sol_{step}.jld2")):
+            return
+        with open(os.path.join(results_path, "screen.txt"), "a") as log:
+            log.write(f"writing time step {step}  t = {t_s}\n")
+        save_solution(u_s, t_s, results_path, step, du_s)
+
     u = np.array(u0, dtype=np.float64, order="C", copy=True)
-    save_solution(u, t0, results_path, 0, solver.residual(u))
+    write(u, t0, 0, solver.residual(u))
     t, snaps, res = solver.rk_steps_snapshots(u, n_steps, dt, interval, scheme, with_residuals=True, t=t0)
     for k in range(len(snaps)):
         step = (k + 1) * interval
-        save_solution(snaps[k], t0 + step * dt, results_path, step, res[k])
+        write(snaps[k], t0 + step * dt, step, res[k])
     if n_steps % interval:
-        save_solution(u, t, results_path, n_steps, solver.residual(u))
+        write(u, t, n_steps, solver.residual(u))
     return u, t
 
 

@@ -30,3 +30,5 @@ def test_save_callback_writes_the_device_trajectory(gpu_lib, pkg, tmp_path):
         assert np.array_equal(us, w)
         assert np.array_equal(dus, G.residual(w))
     assert np.array_equal(u, w)
+    log = open(path + "screen.txt").read().splitlines()
+    assert [ln.split()[3] for ln in log] == ["0", "3", "6", "7"]
