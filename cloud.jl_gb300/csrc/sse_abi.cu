@@ -517,6 +517,13 @@ int build(sse_solver *s, const sse_config *cfg, const sse_operators *ops, const 
   s->nnzR = (size_t)(ops->R.colptr[ops->R.n] - 1);
   for (size_t t = 0; t < (size_t)c.n_q * c.n_e; ++t) s->volume += geo->WJ[t];
 
+  // ---- the tables of the FP64 logarithm and exponential of the entropy maps
+  {
+    std::vector<double> mt(3 * kLogTab + 2 * kExpTab);
+    sse_build_math_tables(mt.data());
+    if ((e = upload(s, mt.data(), mt.size(), &op.math_tab)) != cudaSuccess) return cuda_fail(s, e, "upload");
+  }
+
   // ---- R, R^T, D, D^T
   int rc;
   if ((rc = upload_csr(s, csc_to_csr(ops->R, false), &op.R_ptr, &op.R_idx, &op.R_val))) return rc;

@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
     double ui[NC], wi[NC];
 #pragma unroll
     for (int e = 0; e < NC; ++e) ui[e] = Uq0[e * nq + i];
-    cons_to_entropy_fast<D>(ph.gamma, ph.gm1, ph.igm1, ui, wi);
+    cons_to_entropy_fast<D>(ph.gamma, ph.gm1, ph.igm1, ui, wi, ka.op.math_tab);
     const double s = op.has_vdm ? WJ[i] : 1.0;
 #pragma unroll
     for (int e = 0; e < NC; ++e) X[e * nq + i] = wi[e] * s;

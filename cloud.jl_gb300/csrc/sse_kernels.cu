@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
 #pragma unroll
         for (int e = 0; e < NC; ++e) ui[e] = Y[e * nq + i];
         if (!(ui[0] > 0.0)) ka.flag_nonphysical();
-        cons_to_entropy_fast<D>(ph.gamma, ph.gm1, ph.igm1, ui, wi);
+        cons_to_entropy_fast<D>(ph.gamma, ph.gm1, ph.igm1, ui, wi, op.math_tab);
         double s = op.has_vdm ? WJ[i] : 1.0;
 #pragma unroll
         for (int e = 0; e < NC; ++e) X[e * nq + i] = wi[e] * s;
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
           double wi[NC], ui[NC];
 #pragma unroll
           for (int e = 0; e < NC; ++e) wi[e] = X[e * nq + i];
-          entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui);
+          entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui, op.math_tab);
 #pragma unroll
           for (int e = 0; e < NC; ++e) {
             if (live) store_state<NC>(ka, ka.u_q, ka.u_qf, (size_t)kk * NC * nq + e * nq + i, e, ui[e]);
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(256) nodal_values_kernel(KernelArgs ka) {
         double wi[NC], ui[NC];
 #pragma unroll
         for (int e = 0; e < NC; ++e) wi[e] = F[e * nf + j];
-        entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui);
+        entropy_to_cons_fast<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, ui, op.math_tab);
 #pragma unroll
         for (int e = 0; e < NC; ++e) {
           if (live) store_state<NC>(ka, ka.u_f, ka.u_ff, (size_t)kk * NC * nf + e * nf + j, e, ui[e]);

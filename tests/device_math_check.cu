@@ -403,9 +403,42 @@ static void check_entropy_pert(std::mt19937_64 &rng, double *worst) {
   }
 }
 
+// the table-driven logarithm / exponential against the C library's in
+// extended precision: ulps of the double result, over the ranges the
+// entropy maps see and far beyond; out-of-range arguments take the library
+// functions (NaN for negative logs, which the non-physical flag relies on)
+void check_logexp(std::mt19937_64 &rng, double *worst) {
+  static double tab[3 * sse::kLogTab + 2 * sse::kExpTab];
+  sse::sse_build_math_tables(tab);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  auto ulps = [](double got, long double want) {
+    const double w = (double)want;
+    const double ulp = std::nextafter(std::fabs(w), INFINITY) - std::fabs(w);
+    return (double)(std::fabs((long double)got - want) / ulp);
+  };
+  for (int i = 0; i < 2000000; ++i) {
+    const double x = std::exp(40.0 * U(rng));                 // 4e-18 .. 2e17
+    const long double lw = std::log((long double)x);
+    // log: ulps of the result, or of 1 where the result is below 1 in
+    // magnitude (an absolute-accuracy form: e ln2 + log F is not formed
+    // relative to a result near zero)
+    const double g = sse::sse_log(x, tab);
+    const double ul = std::fabs((double)lw) >= 1.0 ? ulps(g, lw) : (double)(std::fabs((long double)g - lw) / 0x1p-52);
+    worst[16] = std::fmax(worst[16], ul);
+    const double y = 700.0 * U(rng);
+    worst[17] = std::fmax(worst[17], ulps(sse::sse_exp(y, tab), std::exp((long double)y)));
+  }
+  // arguments outside the table range go to the library functions
+  if (!std::isnan(sse::sse_log(-1.0, tab)) || sse::sse_log(0.0, tab) != -INFINITY ||
+      sse::sse_exp(800.0, tab) != INFINITY || sse::sse_exp(-800.0, tab) != 0.0 ||
+      !std::isnan(sse::sse_exp(NAN, tab)) || sse::sse_log(5e-320, tab) != std::log(5e-320))
+    worst[18] += 1.0;
+}
+
 int main() {
   std::mt19937_64 rng(20261203);
-  double worst[16] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double worst[19] = {0};
+  check_logexp(rng, worst);
   check<2>(rng, worst);
   check<3>(rng, worst);
   check_mixed<2>(rng, worst);
@@ -422,8 +455,10 @@ int main() {
               "\"mixed_flux_vjp\": %.3e, \"ec_flux_half_mismatches\": %.0f, "
               "\"cons_to_entropy_pert\": %.3e, \"entropy_to_cons_pert\": %.3e, "
               "\"cons_to_entropy_jvp_f\": %.3e, \"entropy_to_cons_jvp_f\": %.3e, "
-              "\"ec_flux_half_energy\": %.3e}\n",
+              "\"ec_flux_half_energy\": %.3e, \"table_log_ulps\": %.3f, \"table_exp_ulps\": %.3f, "
+              "\"table_logexp_special_mismatches\": %.0f}\n",
               worst[0], worst[1], worst[2], worst[3], worst[4], worst[5], worst[6], worst[7], worst[8],
-              worst[9], worst[10], worst[11], worst[12], worst[13], worst[14], worst[15]);
+              worst[9], worst[10], worst[11], worst[12], worst[13], worst[14], worst[15], worst[16], worst[17],
+              worst[18]);
   return 0;
 }

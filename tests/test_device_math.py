@@ -87,3 +87,14 @@ def test_fp32_entropy_map_jvps(results):
     # component
     assert results["cons_to_entropy_jvp_f"] < 1e-5
     assert results["entropy_to_cons_jvp_f"] < 1e-5
+
+
+def test_table_driven_log_and_exp(results):
+    # sse_log / sse_exp (Tang's table-driven methods) against the C library
+    # in extended precision: within 2 ulp of the result (for |log| < 1,
+    # 2 ulp of 1: the entropy maps need absolute accuracy there), and every
+    # out-of-range argument handed to the library functions (NaN logs of
+    # negative pressures, which the non-physical flag relies on)
+    assert results["table_log_ulps"] < 2.0
+    assert results["table_exp_ulps"] < 2.0
+    assert results["table_logexp_special_mismatches"] == 0
