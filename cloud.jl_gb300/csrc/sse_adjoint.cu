@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
     double wi[NC], bi[NC], ri[NC];
 #pragma unroll
     for (int e = 0; e < NC; ++e) { wi[e] = Wf[e * nf + j]; bi[e] = Bf[e * nf + j]; }
-    entropy_to_cons_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, bi, ri);
+    entropy_to_cons_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, bi, ri, ka.op.math_tab);
 #pragma unroll
     for (int e = 0; e < NC; ++e) Bf[e * nf + j] = ri[e];
   }
@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(256) adj_projection_kernel(KernelArgs ka) {
       double wi[NC], bi[NC], ri[NC];
 #pragma unroll
       for (int e = 0; e < NC; ++e) { wi[e] = Wq[e * nq + i]; bi[e] = Bq[e * nq + i]; }
-      entropy_to_cons_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, bi, ri);
+      entropy_to_cons_jvp<D>(ph.gamma, ph.gm1, ph.igm1, ph.log_gm1, wi, bi, ri, ka.op.math_tab);
 #pragma unroll
       for (int e = 0; e < NC; ++e) Bq[e * nq + i] = ri[e];
     }

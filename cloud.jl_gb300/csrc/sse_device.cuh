@@ -638,7 +638,8 @@ SSE_HD void cons_to_entropy_jvp(double gamma, double gm1, double igm1, const dou
 // Jacobian: the inverse of the entropy Hessian).
 template <int D>
 SSE_HD void entropy_to_cons_jvp(double gamma, double gm1, double igm1, double log_gm1,
-                                const double *w_in, const double *dw_in, double *du) {
+                                const double *w_in, const double *dw_in, double *du,
+                                const double *mt = nullptr) {
   double w[D + 2], dw[D + 2];
 #pragma unroll
   for (int e = 0; e < D + 2; ++e) {
@@ -656,7 +657,7 @@ SSE_HD void entropy_to_cons_jvp(double gamma, double gm1, double igm1, double lo
   const double dk = ds * iwE - k * dw[D + 1] * iwE;
   const double sv = gamma - w[0] + k;
   const double dsv = -dw[0] + dk;
-  const double rhoe = exp(igm1 * (log_gm1 - gamma * log(-w[D + 1]) - sv));
+  const double rhoe = sse_exp(igm1 * (log_gm1 - gamma * sse_log(-w[D + 1], mt) - sv), mt);
   const double drhoe = rhoe * igm1 * (-gamma * dw[D + 1] * iwE - dsv);
   du[0] = -dw[D + 1] * rhoe - w[D + 1] * drhoe;
 #pragma unroll
