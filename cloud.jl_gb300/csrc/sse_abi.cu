@@ -860,6 +860,13 @@ int enable_mixed(sse_solver *s) {
       return cuda_fail(s, e, "mixed mass operators");
     ka.Akf = (const float *)p;
   }
+  g.halfnJqt = nullptr;
+  if (g.halfnJq) {
+    if ((e = alloc(s, (size_t)d * c.num_faces * nq * ne * sizeof(float), &p)) ||
+        (e = launch_halfnjq_transpose(g.halfnJq, (float *)p, ne, (int)nq, (int)d, c.num_faces, s->stream)))
+      return cuda_fail(s, e, "mixed metric terms");
+    g.halfnJqt = (const float *)p;
+  }
   if ((e = rounded(g.BJf, nf * ne, &g.BJff)) || (e = rounded(g.n_f, d * nf * ne, &g.n_ff)) ||
       (e = rounded(g.Lambda_q, nq * d * d * ne, &g.Lambda_qf)) ||
       (e = rounded(g.halfnJf, d * nf * ne, &g.halfnJff)) ||
@@ -912,7 +919,7 @@ int enable_mixed(sse_solver *s) {
   struct Plan { int chunk, blocks, off; bool geo, rref, ak; };
   auto plan = [&](bool et) {
     const int np2 = ka.Akf && !et ? np * np : 0;
-    const int region2 = et ? 32 * quads : nc * (int)nf;
+    const int region2 = et ? (nc > 4 ? 20 : 16) * quads : nc * (int)nf;  // quads of node-major residuals
     const int final_e = et ? (tpe_m / np) * np * 8 : final_m;
     auto layout_m = [&](int chunk, bool geo, bool rref, bool ak) {
       const int sizes[11] = {staged(nc * (int)nq), staged(nc * (int)nf), region2,

@@ -104,8 +104,10 @@ struct DevGeo {
   const double *halfnJq;      // d x nfac x nq x ne
   const double *JinvW;        // nq x ne
   const double *WJinv;        // nq x ne
-  // FP32 roundings of the FP64 metric terms for the mixed form
-  const float *BJff, *n_ff, *Lambda_qf, *halfnJff, *halfnJqf, *JinvWf, *WJinvf;
+  // FP32 roundings of the FP64 metric terms for the mixed form; halfnJqt:
+  // halfnJq transposed to (f D + m) n_q + i per element, so that the lanes
+  // of a warp (different volume nodes i) read different banks
+  const float *BJff, *n_ff, *Lambda_qf, *halfnJff, *halfnJqf, *halfnJqt, *JinvWf, *WJinvf;
   // mixed form: the entropy projection of the constant function 1 at the
   // volume nodes (V M^-1 V^T (W J), nq x ne) and its facet values (R P1, nf x ne)
   const double *P1, *RP1;
@@ -907,8 +909,29 @@ SSE_HD float inv_logmean_beta_minus_ref(float theta_ref, float dti, float dtj) {
 template <int D>
 SSE_HD void ec_flux_dot_mixed(float igm1, float rho_ref, float theta_ref, const float *Pi,
                               const float *Pj, const float *G, float *out) {
-  const float drho_hat = logmean_minus_ref(rho_ref, Pi[0], Pj[0], Pi[1], Pj[1]);
-  const float dilm = inv_logmean_beta_minus_ref(theta_ref, Pi[2], Pj[2]);
+  // both means by their series when both pairs of arguments are close (one
+  // branch per flux; the same expressions as logmean_minus_ref and
+  // inv_logmean_beta_minus_ref, which take the other cases)
+  float drho_hat, dilm;
+  {
+    const float dri = Pi[1], drj = Pj[1], dti = Pi[2], dtj = Pj[2];
+    const float fr = sse_fdiv(dri - drj, 2.f * rho_ref + (dri + drj));
+    const float zr = fr * fr;
+    const float sig = dti + dtj;
+    const float rden = sse_fdiv(1.f, 2.f * theta_ref + sig);
+    const float ft = (dtj - dti) * rden;
+    const float zt = ft * ft;
+    if (zr < 0.05f && zt < 0.05f) {
+      const float qm1 = q_minus_one_f(zr);
+      drho_hat = sse_fdiv(0.5f * (dri + drj) - rho_ref * qm1, 1.f + qm1);
+      const float hm_minus = (theta_ref * sig + 2.f * dti * dtj) * rden;
+      const float hm = theta_ref + hm_minus;
+      dilm = fmaf(q_minus_one_f(zt), hm, hm_minus);
+    } else {
+      drho_hat = logmean_minus_ref(rho_ref, Pi[0], Pj[0], dri, drj);
+      dilm = inv_logmean_beta_minus_ref(theta_ref, dti, dtj);
+    }
+  }
   float vs[D];
   float vv = 0.f, gvs = 0.f, gvi = 0.f, gvj = 0.f;
 #pragma unroll

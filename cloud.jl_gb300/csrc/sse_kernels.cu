@@ -718,27 +718,76 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
 // mass solve in turn.
 // ---------------------------------------------------------------------------
 
-// acc[e] += E[r, 4q + u] X[4q + u][e] for the four nodes of a column quad
-// (node-major X, 8 floats per node, 16-byte aligned)
+// Node-major residuals of the tail product, in quads of four nodes: the
+// first four components of node n are float4 (n & 3) of quad n >> 2, the
+// fifth (NC = 5) is entry n & 3 of the quad's fifth float4, so that one
+// column quad of E_k meets its 4 x NC values in NC / 4 rounded up + 4
+// vector loads
+template <int NC>
+constexpr int kQuadFloats = NC > 4 ? 20 : 16;
+
+template <int NC>
+__device__ __forceinline__ int xq_index(int n, int e) {
+  return (n >> 2) * kQuadFloats<NC> + (e < 4 ? (n & 3) * 4 + e : 16 + (n & 3));
+}
+
+template <int NC>
+__device__ __forceinline__ void store_xq(float *X, int n, const float *v) {
+  float *q = X + (n >> 2) * kQuadFloats<NC>;
+  *reinterpret_cast<float4 *>(q + (n & 3) * 4) = make_float4(v[0], v[1], v[2], v[3]);
+  if constexpr (NC > 4) q[16 + (n & 3)] = v[4];
+}
+
+template <int NC>
+__device__ __forceinline__ void load_xq(const float *X, int n, float *v) {
+  const float *q = X + (n >> 2) * kQuadFloats<NC>;
+  const float4 a = *reinterpret_cast<const float4 *>(q + (n & 3) * 4);
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+  v[3] = a.w;
+  if constexpr (NC > 4) v[4] = q[16 + (n & 3)];
+}
+
+// x[n] -= v for node n
+template <int NC>
+__device__ __forceinline__ void sub_xq(float *X, int n, const float *v) {
+  float *q = X + (n >> 2) * kQuadFloats<NC>;
+  float4 *p = reinterpret_cast<float4 *>(q + (n & 3) * 4);
+  float4 a = *p;
+  a.x -= v[0];
+  a.y -= v[1];
+  a.z -= v[2];
+  a.w -= v[3];
+  *p = a;
+  if constexpr (NC > 4) q[16 + (n & 3)] -= v[4];
+}
+
+// acc[e] += E[r, 4q + u] X[4q + u][e] for the four nodes of the column quad
+// at Xq
 template <int NC>
 __device__ __forceinline__ void quad_fma(const float *Xq, float4 ev, float *acc) {
   const float w[4] = {ev.x, ev.y, ev.z, ev.w};
+  float c4[4] = {0.f, 0.f, 0.f, 0.f};
+  if constexpr (NC > 4) {
+    const float4 t = *reinterpret_cast<const float4 *>(Xq + 16);
+    c4[0] = t.x;
+    c4[1] = t.y;
+    c4[2] = t.z;
+    c4[3] = t.w;
+  }
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
-    const float4 x0 = *reinterpret_cast<const float4 *>(Xq + 8 * u);
+    const float4 x0 = *reinterpret_cast<const float4 *>(Xq + 4 * u);
     acc[0] = fmaf(w[u], x0.x, acc[0]);
     acc[1] = fmaf(w[u], x0.y, acc[1]);
     acc[2] = fmaf(w[u], x0.z, acc[2]);
     acc[3] = fmaf(w[u], x0.w, acc[3]);
-    if constexpr (NC > 4) {
-      const float4 x1 = *reinterpret_cast<const float4 *>(Xq + 8 * u + 4);
-      acc[4] = fmaf(w[u], x1.x, acc[4]);
-      if constexpr (NC > 5) acc[5] = fmaf(w[u], x1.y, acc[5]);
-    }
+    if constexpr (NC > 4) acc[4] = fmaf(w[u], c4[u], acc[4]);
   }
 }
 
-// one node's NC values into its 8-float node-major slot
+// one node's NC values into an 8-float slot (the tail's partial rows)
 template <int NC>
 __device__ __forceinline__ void store_node(float *x, const float *v) {
   *reinterpret_cast<float4 *>(x) = make_float4(v[0], v[1], v[2], v[3]);
@@ -746,9 +795,29 @@ __device__ __forceinline__ void store_node(float *x, const float *v) {
   for (int e = 4; e < NC; ++e) x[e] = v[e];
 }
 
+// Pair buffer of the mixed phase B: the first four components of pair p as
+// float4 p of the buffer, the fifth (NC = 5) at 4 ch + p (ch pairs per chunk)
+template <int NC>
+__device__ __forceinline__ void store_pair(float *d, int ch, int p, const float *v) {
+  reinterpret_cast<float4 *>(d)[p] = make_float4(v[0], v[1], v[2], v[3]);
+  if constexpr (NC > 4) d[4 * ch + p] = v[4];
+}
+
+template <int NC>
+__device__ __forceinline__ void load_pair(const float *d, int ch, int p, float *v) {
+  const float4 a = reinterpret_cast<const float4 *>(d)[p];
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+  v[3] = a.w;
+  if constexpr (NC > 4) v[4] = d[4 * ch + p];
+}
+
+
 template <int D, int NC, bool ET>
 __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(KernelArgs ka) {
   static_assert(NC == D + 2, "the mixed form covers the Euler equations");
+  static_assert(NC <= 5, "pair buffer and primitives hold at most five components");
   extern __shared__ __align__(16) double smem_raw[];
   float *smem = reinterpret_cast<float *>(smem_raw);
   const DevOps &op = ka.op;
@@ -767,21 +836,21 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   float *X = base + L.off[2];  // ET: node-major residuals (region 2)
   // residual entries of volume node i / facet node j, component e
   auto RQ = [&](int e, int i) -> float & {
-    if constexpr (ET) return X[i * 8 + e];
+    if constexpr (ET) return X[xq_index<NC>(i, e)];
     else return rq[e * nq + i];
   };
   auto FF = [&](int e, int j) -> float & {
-    if constexpr (ET) return X[(nq + j) * 8 + e];
+    if constexpr (ET) return X[xq_index<NC>(nq + j, e)];
     else return ff[e * nf + j];
   };
   const float *Ekg = ET ? ka.Ekf + (size_t)kk * ka.ek_quads * np * 4 : nullptr;
   if constexpr (ET) {
     if (lane == 0) prefetch_l2(Ekg, (uint32_t)ka.ek_quads * np * 16);
     // padding nodes of the last column quad: zero (E_k is zero there too)
-    for (int t = lane; t < (4 * ka.ek_quads - nq - nf) * 8; t += tpe) X[(nq + nf) * 8 + t] = 0.f;
+    for (int t = lane; t < (4 * ka.ek_quads - nq - nf) * NC; t += tpe) X[xq_index<NC>(nq + nf + t / NC, t % NC)] = 0.f;
   }
   uint64_t *bar = reinterpret_cast<uint64_t *>(base + L.off[10]);
-  const int PS = 4 + D;
+  constexpr int PS = 4 + D;
   const float gm1 = ph.f_gm1, igm1 = ph.f_igm1, gam = ph.f_gamma;
   const float rho_ref = ph.f_rho_ref, p_ref = ph.f_p_ref, hl = ph.f_half_lambda;
   const float theta_ref = ph.f_theta_ref, H_ref = ph.f_H_ref;
@@ -793,7 +862,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   const float *uqg = ka.u_qf + (size_t)kk * NC * nq;
   const float *ufg = ka.u_ff + (size_t)kk * NC * nf;
   const float *Lg = g.Lambda_qf + (size_t)kk * nq * D * D;
-  const float *Hg = g.halfnJqf + (size_t)kk * D * nfac * nq;
+  const float *Hg = g.halfnJqt + (size_t)kk * D * nfac * nq;
   const float *nfg = g.n_ff + (size_t)kk * D * nf, *bjg = g.BJff + (size_t)kk * nf;
   const float *hfg = g.halfnJff + (size_t)kk * D * nf;
   const float *Akg = ka.Akf ? ka.Akf + (size_t)kk * np * np : nullptr;
@@ -806,7 +875,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   float *geo_b = geo_r + ((D * nf + 8 + 3) & ~3), *geo_h = geo_b + ((nf + 8 + 3) & ~3);
   const float *uq = staged_ptr(base + L.off[0], uqg), *uf = staged_ptr(base + L.off[1], ufg);
   const float *Lam = staged_ptr(base + L.off[5], Lg);
-  const float *hnq = st_hnq ? staged_ptr(base + L.off[6], Hg) : Hg;
+  const float *hnq = staged_ptr(base + L.off[6], Hg);  // read only where there are facet pairs
   const float *nfv = st_geo ? staged_ptr(geo_r, nfg) : nfg, *bjf = st_geo ? staged_ptr(geo_b, bjg) : bjg;
   const float *hnf = st_geo ? staged_ptr(geo_h, hfg) : hfg;
   const float *Aks = st_ak ? staged_ptr(base + L.off[3], Akg) : Akg;
@@ -834,14 +903,27 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
     if (st_ak) stage_slab(base + L.off[3], Akg, ba, bar);
     if (st_rref) stage_slab(base + L.off[9], Rg, br, bar);
   }
-  // meanwhile: the neighbour's facet state of this thread's first facet
-  // node (its gather overlaps the bulk copies)
+  // With all volume pairs in one chunk, the interface flux of facet node j
+  // runs in the volume-sum phase, on the thread of node n_q + j of the node
+  // loop (threads past the n_q volume nodes are idle there); else before
+  // the pairs, on thread j.  Meanwhile: the neighbour's facet state of this
+  // thread's first facet node (its gather overlaps the bulk copies), kept
+  // in the node's residual slot (not staged, written by the interface flux
+  // only) when the flux comes late.
+  const bool iface_late = op.nvp > 0 && ka.fd_chunk_mixed >= op.nvp;
+  const int j0 = iface_late ? lane + (lane >= nq ? 0 : (nq - lane + tpe - 1) / tpe) * tpe - nq : lane;
   float uo0[NC];
-  if (lane < nf) {
-    const int P0 = __ldg(g.mapP + (size_t)kk * nf + lane);
+  if (j0 < nf) {
+    const int P0 = __ldg(g.mapP + (size_t)kk * nf + j0);
     const int jn = P0 % nf, kn = P0 / nf;
 #pragma unroll
     for (int e = 0; e < NC; ++e) uo0[e] = ka.u_ff[((size_t)kn * NC + e) * nf + jn];
+    if (iface_late) {
+      if constexpr (ET) store_xq<NC>(X, nq + j0, uo0);
+      else
+#pragma unroll
+        for (int e = 0; e < NC; ++e) FF(e, j0) = uo0[e];
+    }
   }
   __syncthreads();  // the mbarrier is initialised
   // one thread of the team waits for the copies; the others wait at the
@@ -862,11 +944,13 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   __syncthreads();
 
   // interface flux: EC flux . n + Lax-Friedrichs, scaled by BJf
-  for (int j = lane; j < nf; j += tpe) {
+  auto interface_flux = [&](int j, bool late) {
     float uo[NC], n[D], Po[4 + D], out[NC];
-    if (j == lane) {
+    if (j == j0) {
+      if (late && ET) load_xq<NC>(X, nq + j, uo);
+      else
 #pragma unroll
-      for (int e = 0; e < NC; ++e) uo[e] = uo0[e];
+        for (int e = 0; e < NC; ++e) uo[e] = late ? FF(e, j) : uo0[e];
     } else {
       const int P = g.mapP[(size_t)kk * nf + j];
       const int jn = P % nf, kn = P / nf;
@@ -891,12 +975,16 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
 #pragma unroll
     for (int e = 0; e < NC; ++e) jump[e] = uf[e * nf + j] - uo[e];
     jump[NC - 1] = fmaf(-H_ref, jump[0], jump[NC - 1]);  // reduced energy: E' - H_ref rho'
+    float res[NC];
 #pragma unroll
-    for (int e = 0; e < NC; ++e) {
-      float fs = (ph.nflux == 0) ? fmaf(a, jump[e], out[e]) : out[e];
-      FF(e, j) = fs * bj;
-    }
-  }
+    for (int e = 0; e < NC; ++e) res[e] = ((ph.nflux == 0) ? fmaf(a, jump[e], out[e]) : out[e]) * bj;
+    if constexpr (ET) store_xq<NC>(X, nq + j, res);
+    else
+#pragma unroll
+      for (int e = 0; e < NC; ++e) FF(e, j) = res[e];
+  };
+  if (!iface_late)
+    for (int j = lane; j < nf; j += tpe) interface_flux(j, false);
 
   // volume flux differencing: one contracted EC flux per unique pair, in
   // chunks of at most CH pairs with per-node cursors (ascending pair order)
@@ -938,13 +1026,17 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
       }
       ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (int)i * PS, prim + (int)j * PS, G, out);
-#pragma unroll
-      for (int e = 0; e < NC; ++e) diff[(int)(pidx - c0) * NC + e] = out[e];
+      store_pair<NC>(diff, CH, pidx - c0, out);
     }
     __syncthreads();
     if (CH >= op.nvp) {
-      // one chunk: each node sums its whole incidence list
-      for (int i = lane; i < nq; i += tpe) {
+      // one chunk: each node sums its whole incidence list; the threads of
+      // the facet nodes compute the interface flux meanwhile
+      for (int i = lane; i < nq + nf; i += tpe) {
+        if (i >= nq) {
+          interface_flux(i - nq, true);
+          continue;
+        }
         float acc[NC];
 #pragma unroll
         for (int e = 0; e < NC; ++e) acc[e] = 0.f;
@@ -956,7 +1048,8 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
           for (int r = 0; r < 4; ++r) inc[r] = __ldg(op.vp_inc + q + r);
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
-            const float *dp = diff + (int)(inc[r] >> 1) * NC;
+            float dp[NC];
+            load_pair<NC>(diff, CH, inc[r] >> 1, dp);
             const float sg = (inc[r] & 1) ? -1.f : 1.f;
 #pragma unroll
             for (int e = 0; e < NC; ++e) acc[e] = fmaf(sg, dp[e], acc[e]);
@@ -964,12 +1057,13 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         }
         for (; q < qb; ++q) {
           const int inc = __ldg(op.vp_inc + q);
-          const float *dp = diff + (int)(inc >> 1) * NC;
+          float dp[NC];
+          load_pair<NC>(diff, CH, inc >> 1, dp);
           const float sg = (inc & 1) ? -1.f : 1.f;
 #pragma unroll
           for (int e = 0; e < NC; ++e) acc[e] = fmaf(sg, dp[e], acc[e]);
         }
-        if constexpr (ET) store_node<NC>(X + i * 8, acc);
+        if constexpr (ET) store_xq<NC>(X, i, acc);
         else
 #pragma unroll
           for (int e = 0; e < NC; ++e) rq[e * nq + i] = acc[e];
@@ -990,7 +1084,8 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         const int inc = op.vp_inc[q];
         const int pidx = inc >> 1;
         if (pidx >= c1) break;
-        const float *dp = diff + (int)(pidx - c0) * NC;
+        float dp[NC];
+        load_pair<NC>(diff, CH, pidx - c0, dp);
         if (inc & 1) {
 #pragma unroll
           for (int e = 0; e < NC; ++e) acc[e] -= dp[e];
@@ -1029,10 +1124,9 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         int f = qdiv(j, rnpf);
         float G[D], out[NC];
 #pragma unroll
-        for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[m + D * (f + nfac * i)]);
+        for (int m = 0; m < D; ++m) G[m] = Cij * (hnf[m + D * j] + hnq[(f * D + m) * nq + i]);
         ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (int)i * PS, prim + (int)(nq + j) * PS, G, out);
-#pragma unroll
-        for (int e = 0; e < NC; ++e) diff[(int)(pidx - c0) * NC + e] = out[e];
+        store_pair<NC>(diff, CH, pidx - c0, out);
       }
       __syncthreads();
       if (CH >= op.nfp) {
@@ -1053,13 +1147,15 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
               for (int u = 0; u < 4; ++u) id[u] = __ldg(op.fp_q + q + u);
 #pragma unroll
               for (int u = 0; u < 4; ++u) {
-                const float *dp = diff + id[u] * NC;
+                float dp[NC];
+                load_pair<NC>(diff, CH, id[u], dp);
 #pragma unroll
                 for (int e = 0; e < NC; ++e) acc[e] += dp[e];
               }
             }
             for (; q < qb; ++q) {
-              const float *dp = diff + __ldg(op.fp_q + q) * NC;
+              float dp[NC];
+              load_pair<NC>(diff, CH, __ldg(op.fp_q + q), dp);
 #pragma unroll
               for (int e = 0; e < NC; ++e) acc[e] += dp[e];
             }
@@ -1067,14 +1163,14 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
             // the pairs are enumerated facet node by facet node (the columns
             // of C): a facet node's pairs are the consecutive ids qa..qb-1
             for (int q = qa; q < qb; ++q) {
-              const float *dp = diff + q * NC;
+              float dp[NC];
+              load_pair<NC>(diff, CH, q, dp);
 #pragma unroll
               for (int e = 0; e < NC; ++e) acc[e] += dp[e];
             }
           }
           if constexpr (ET) {
-#pragma unroll
-            for (int e = 0; e < NC; ++e) X[t * 8 + e] -= acc[e];
+            sub_xq<NC>(X, t, acc);
           } else {
             float *dst = vol ? rq + r : ff + r;
             const int stride = vol ? nq : nf;
@@ -1100,14 +1196,14 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
           // a facet node's pairs are its consecutive ids (C's columns)
           const int pidx = vol ? __ldg(op.fp_q + q) : q;
           if (pidx >= c1) break;
-          const float *dp = diff + (int)(pidx - c0) * NC;
+          float dp[NC];
+          load_pair<NC>(diff, CH, pidx - c0, dp);
 #pragma unroll
           for (int e = 0; e < NC; ++e) acc[e] += dp[e];
         }
         cur[sl] = q;
         if constexpr (ET) {
-#pragma unroll
-          for (int e = 0; e < NC; ++e) X[t * 8 + e] -= acc[e];
+          sub_xq<NC>(X, t, acc);
         } else {
           float *dst = vol ? rq + r : ff + r;
           const int stride = vol ? nq : nf;
@@ -1140,11 +1236,11 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         const float4 ea = __ldg(E4 + (size_t)q * np + r);
         const float4 eb = __ldg(E4 + (size_t)(q + G) * np + r);
         const float4 ec = __ldg(E4 + (size_t)(q + 2 * G) * np + r);
-        quad_fma<NC>(X + q * 32, ea, acc);
-        quad_fma<NC>(X + (q + G) * 32, eb, acc);
-        quad_fma<NC>(X + (q + 2 * G) * 32, ec, acc);
+        quad_fma<NC>(X + q * kQuadFloats<NC>, ea, acc);
+        quad_fma<NC>(X + (q + G) * kQuadFloats<NC>, eb, acc);
+        quad_fma<NC>(X + (q + 2 * G) * kQuadFloats<NC>, ec, acc);
       }
-      for (; q < nquad; q += G) quad_fma<NC>(X + q * 32, __ldg(E4 + (size_t)q * np + r), acc);
+      for (; q < nquad; q += G) quad_fma<NC>(X + q * kQuadFloats<NC>, __ldg(E4 + (size_t)q * np + r), acc);
       store_node<NC>(diff + (gq * np + r) * 8, acc);
     }
     __syncthreads();
@@ -1239,6 +1335,21 @@ __global__ void round_to_float_kernel(const double *__restrict__ in, float *__re
                                       double shift) {
   for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x)
     out[x] = (float)(in[x] + shift);
+}
+
+// FP64 -> FP32 rounding of halfnJq (m + D (f + nfac i) per element) into the
+// layout (f D + m) n_q + i; one thread per output float
+__global__ void halfnjq_transpose_kernel(const double *__restrict__ in, float *__restrict__ out, size_t ne,
+                                         int nq, int d, int nfac) {
+  const int per = d * nfac * nq;
+  const size_t n = ne * (size_t)per;
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = x / per;
+    const int t = (int)(x - k * per);
+    const int fm = t / nq, i = t - fm * nq;
+    const int f = fm / d, m = fm - f * d;
+    out[x] = (float)in[k * per + m + d * (f + nfac * i)];
+  }
 }
 
 // FP64 -> FP32 rounding of nmat n x n matrices with a transpose of each: the
@@ -1606,6 +1717,14 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
                                         double a, double b, double dt, int first, size_t n,
                                         cudaStream_t st) {
   ck_stage_compensated_kernel<<<elementwise_grid(n), 256, 0, st>>>(u, comp, tmp, k, a, b, dt, first, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_halfnjq_transpose(const double *in, float *out, size_t ne, int nq, int d, int nfac,
+                                     cudaStream_t st) {
+  const size_t n = ne * (size_t)d * nfac * nq;
+  if (n == 0) return cudaSuccess;
+  halfnjq_transpose_kernel<<<elementwise_grid(n), 256, 0, st>>>(in, out, ne, nq, d, nfac);
   return cudaGetLastError();
 }
 

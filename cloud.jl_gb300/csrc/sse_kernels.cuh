@@ -134,6 +134,10 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
                                         cudaStream_t st);
 // out = (float)(in + shift)
 cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st, double shift = 0.0);
+// FP64 halfnJq (d x nfac x n_q per element) rounded to FP32 and transposed to
+// (f d + m) n_q + i
+cudaError_t launch_halfnjq_transpose(const double *in, float *out, size_t ne, int nq, int d, int nfac,
+                                     cudaStream_t st);
 cudaError_t launch_fill_constant_state(double *buf, int nodes, int nc, size_t ne, const double *state,
                                        cudaStream_t st);
 cudaError_t launch_round_transpose(const double *in, float *out, size_t nmat, int n, cudaStream_t st);
