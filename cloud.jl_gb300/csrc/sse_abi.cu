@@ -851,6 +851,16 @@ int enable_mixed(sse_solver *s) {
       (e = rounded(op.Rt_val, s->nnzR, &op.Rt_valf)) || (e = rounded(op.vp_S, s->nvpS, &op.vp_Sf)) ||
       (e = rounded(op.fp_C, s->nfpC, &op.fp_Cf)) || (e = rounded(op.Vd, s->nVd, &op.Vdf)))
     return cuda_fail(s, e, "mixed operators");
+  op.vp_pkf = op.fp_pkf = nullptr;
+  if (op.nvp + op.nfp > 0) {
+    void *pv = nullptr, *pf = nullptr;
+    if ((e = alloc(s, (size_t)std::max(op.nvp, 1) * 4 * sizeof(float), &pv)) ||
+        (e = alloc(s, (size_t)std::max(op.nfp, 1) * 2 * sizeof(float), &pf)) ||
+        (e = launch_pack_pairs(op, (float *)pv, (float *)pf, s->stream)))
+      return cuda_fail(s, e, "mixed pair tables");
+    op.vp_pkf = (const float *)pv;
+    op.fp_pkf = (const float *)pf;
+  }
   // the per-element mass operators in FP32, transposed to row-major (the FP32
   // dense solve gives each thread one row)
   ka.Akf = nullptr;
@@ -867,8 +877,14 @@ int enable_mixed(sse_solver *s) {
       return cuda_fail(s, e, "mixed metric terms");
     g.halfnJqt = (const float *)p;
   }
+  g.Lambda_qn = nullptr;
+  if (g.Lambda_q) {
+    if ((e = alloc(s, (size_t)lambda_stride((int)d) * nq * ne * sizeof(float), &p)) ||
+        (e = launch_lambda_node_major(g.Lambda_q, (float *)p, ne, (int)nq, (int)d, s->stream)))
+      return cuda_fail(s, e, "mixed metric terms");
+    g.Lambda_qn = (const float *)p;
+  }
   if ((e = rounded(g.BJf, nf * ne, &g.BJff)) || (e = rounded(g.n_f, d * nf * ne, &g.n_ff)) ||
-      (e = rounded(g.Lambda_q, nq * d * d * ne, &g.Lambda_qf)) ||
       (e = rounded(g.halfnJf, d * nf * ne, &g.halfnJff)) ||
       (e = rounded(g.halfnJq, d * c.num_faces * nq * ne, &g.halfnJqf)) ||
       (e = rounded(g.JinvW, g.JinvW ? nq * ne : 0, &g.JinvWf)) ||
@@ -924,7 +940,7 @@ int enable_mixed(sse_solver *s) {
     auto layout_m = [&](int chunk, bool geo, bool rref, bool ak) {
       const int sizes[11] = {staged(nc * (int)nq), staged(nc * (int)nf), region2,
                              ak && np2 ? staged(np2) : 0, std::max(chunk * nc, final_e),
-                             staged((int)(d * d * nq)), op.nfp > 0 ? staged((int)(d * c.num_faces * nq)) : 0,
+                             staged(lambda_stride((int)d) * (int)nq), op.nfp > 0 ? staged((int)(d * c.num_faces * nq)) : 0,
                              (int)((nq + nf) * (4 + d)),
                              geo ? 2 * staged((int)(d * nf)) + staged((int)nf) : 0,
                              rref ? staged(2 * nc * np) : 0, 4};

@@ -969,7 +969,10 @@ __global__ void __launch_bounds__(256) adj_flux_mixed_kernel(KernelArgs ka) {
     uf[t] = ka.u_ff[(size_t)kk * NC * nf + t];
     ubd[t] = 0.f;
   }
-  for (int t = lane; t < nq * D * D; t += tpe) Lam[t] = g.Lambda_qf[(size_t)kk * nq * D * D + t];
+  for (int t = lane; t < nq * D * D; t += tpe) {
+    const int v = t / nq, i = t - v * nq;
+    Lam[t] = g.Lambda_qn[((size_t)kk * nq + i) * lambda_stride(D) + v];
+  }
   // halfnJq is staged when the layout has room for it, else read from global
   // memory (the host drops it from the layout to keep more blocks per SM)
   const float *hnq_src = hnq;

@@ -53,6 +53,10 @@ struct DevOps {
   const int *fp_f_ptr, *fp_f;  // per facet node: incident pair ids
   // FP32 copies of the operator values for the mixed form (rounded from FP64)
   const float *Af, *Bf, *Cf, *R_valf, *Rt_valf, *vp_Sf, *fp_Cf;
+  // the mixed phase B's pair tables, one vector load per pair: volume pairs
+  // as float4 (S_1..S_D in FP32, zero-padded, and vp_ij's bits in w), facet
+  // pairs as float2 (C in FP32, fp_ij's bits in y)
+  const float *vp_pkf, *fp_pkf;
   // dense V (nq x np, column-major) of a multidimensional modal basis:
   // has_vdm == 1 and dense_v == 1, the warped factors unused
   int dense_v;
@@ -106,8 +110,10 @@ struct DevGeo {
   const double *WJinv;        // nq x ne
   // FP32 roundings of the FP64 metric terms for the mixed form; halfnJqt:
   // halfnJq transposed to (f D + m) n_q + i per element, so that the lanes
-  // of a warp (different volume nodes i) read different banks
-  const float *BJff, *n_ff, *Lambda_qf, *halfnJff, *halfnJqf, *halfnJqt, *JinvWf, *WJinvf;
+  // of a warp (different volume nodes i) read different banks; Lambda_qn:
+  // Lambda_q node-major, value v = m + D n of node i at lambda_stride(D) i +
+  // v (an odd stride: distinct nodes of a warp meet distinct banks)
+  const float *BJff, *n_ff, *Lambda_qn, *halfnJff, *halfnJqf, *halfnJqt, *JinvWf, *WJinvf;
   // mixed form: the entropy projection of the constant function 1 at the
   // volume nodes (V M^-1 V^T (W J), nq x ne) and its facet values (R P1, nf x ne)
   const double *P1, *RP1;
@@ -121,6 +127,9 @@ struct DevGeo {
   // epilogue; null until the reference state is chosen.
   const double *Rref;
 };
+
+// floats per node of the node-major FP32 metric terms Lambda_qn
+__host__ __device__ constexpr int lambda_stride(int D) { return (D * D) % 2 ? D * D : D * D + 1; }
 
 // Constants of the FP32 perturbation entropy maps, rounded once from the FP64
 // reference state (w_ref: its entropy variables).
@@ -928,7 +937,7 @@ SSE_HD void ec_flux_dot_mixed(float igm1, float rho_ref, float theta_ref, const 
       const float hm = theta_ref + hm_minus;
       dilm = fmaf(q_minus_one_f(zt), hm, hm_minus);
     } else {
-      drho_hat = logmean_minus_ref(rho_ref, Pi[0], Pj[0], dri, drj);
+      drho_hat = logmean_minus_ref(rho_ref, rho_ref + dri, rho_ref + drj, dri, drj);  // = P[0] (no load)
       dilm = inv_logmean_beta_minus_ref(theta_ref, dti, dtj);
     }
   }

@@ -861,7 +861,8 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   // thread of the team, completed on the team's mbarrier.
   const float *uqg = ka.u_qf + (size_t)kk * NC * nq;
   const float *ufg = ka.u_ff + (size_t)kk * NC * nf;
-  const float *Lg = g.Lambda_qf + (size_t)kk * nq * D * D;
+  constexpr int LS = lambda_stride(D);
+  const float *Lg = g.Lambda_qn + (size_t)kk * nq * LS;
   const float *Hg = g.halfnJqt + (size_t)kk * D * nfac * nq;
   const float *nfg = g.n_ff + (size_t)kk * D * nf, *bjg = g.BJff + (size_t)kk * nf;
   const float *hfg = g.halfnJff + (size_t)kk * D * nf;
@@ -883,7 +884,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   if (lane == 0) {
     mbar_init(bar, 1);
     mbar_fence_init();
-    const uint32_t bq = NC * nq * 4, bf = NC * nf * 4, bl = nq * D * D * 4, bh = D * nfac * nq * 4;
+    const uint32_t bq = NC * nq * 4, bf = NC * nf * 4, bl = nq * LS * 4, bh = D * nfac * nq * 4;
     const uint32_t bn = D * nf * 4, bb = nf * 4, ba = np * np * 4, br = NC * np * 8;
     uint32_t tx = staged_span(uqg, bq) + staged_span(ufg, bf) + staged_span(Lg, bl);
     if (st_hnq) tx += staged_span(Hg, bh);
@@ -988,7 +989,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
 
   // volume flux differencing: one contracted EC flux per unique pair, in
   // chunks of at most CH pairs with per-node cursors (ascending pair order)
-  const float *vpS = OpVals<float>::vpS(op);
+  const float4 *vpk = reinterpret_cast<const float4 *>(op.vp_pkf);
   const int CH = ka.fd_chunk_mixed;
   int cur[kMaxNodeSlots];
 #pragma unroll
@@ -1000,20 +1001,12 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
   }
   for (int c0 = 0; c0 < op.nvp; c0 += CH) {
     const int c1 = min(op.nvp, c0 + CH);
-    int ijn = c0 + lane < c1 ? __ldg(op.vp_ij + c0 + lane) : 0;
-    float Sn[D];
-#pragma unroll
-    for (int m = 0; m < D; ++m) Sn[m] = c0 + lane < c1 ? __ldg(vpS + (c0 + lane) * D + m) : 0.f;
+    float4 nx = c0 + lane < c1 ? __ldg(vpk + c0 + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
-      const int ij = ijn;
-      float Sv[D];
-#pragma unroll
-      for (int m = 0; m < D; ++m) Sv[m] = Sn[m];
-      if (pidx + tpe < c1) {
-        ijn = __ldg(op.vp_ij + pidx + tpe);
-#pragma unroll
-        for (int m = 0; m < D; ++m) Sn[m] = __ldg(vpS + (pidx + tpe) * D + m);
-      }
+      const float4 cu = nx;
+      if (pidx + tpe < c1) nx = __ldg(vpk + pidx + tpe);
+      const int ij = __float_as_int(cu.w);
+      const float Sv[3] = {cu.x, cu.y, cu.z};
       int i = ij & 0xffff, j = ij >> 16;
       float G[D], out[NC];
 #pragma unroll
@@ -1023,7 +1016,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
         const float Sm = Sv[m];
         if (Sm == 0.f) continue;
 #pragma unroll
-        for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i + nq * (m + D * n)] + Lam[j + nq * (m + D * n)], G[n]);
+        for (int n = 0; n < D; ++n) G[n] = fmaf(Sm, Lam[i * LS + m + D * n] + Lam[j * LS + m + D * n], G[n]);
       }
       ec_flux_dot_mixed<D>(igm1, rho_ref, theta_ref, prim + (int)i * PS, prim + (int)j * PS, G, out);
       store_pair<NC>(diff, CH, pidx - c0, out);
@@ -1103,7 +1096,7 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
 
   // facet correction, chunked the same way
   if (op.nfp > 0) {
-    const float *fpC = OpVals<float>::fpC(op);
+    const float2 *fpk = reinterpret_cast<const float2 *>(op.fp_pkf);
 #pragma unroll
     for (int sl = 0; sl < kMaxNodeSlots; ++sl) {
       const int t = lane + sl * tpe;
@@ -1111,15 +1104,12 @@ __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(Kernel
     }
     for (int c0 = 0; c0 < op.nfp; c0 += CH) {
       const int c1 = min(op.nfp, c0 + CH);
-      int ijn = c0 + lane < c1 ? __ldg(op.fp_ij + c0 + lane) : 0;
-      float Cn = c0 + lane < c1 ? __ldg(fpC + c0 + lane) : 0.f;
+      float2 nx = c0 + lane < c1 ? __ldg(fpk + c0 + lane) : make_float2(0.f, 0.f);
       for (int pidx = c0 + lane; pidx < c1; pidx += tpe) {
-        const int ij = ijn;
-        const float Cij = Cn;
-        if (pidx + tpe < c1) {
-          ijn = __ldg(op.fp_ij + pidx + tpe);
-          Cn = __ldg(fpC + pidx + tpe);
-        }
+        const float2 cu = nx;
+        if (pidx + tpe < c1) nx = __ldg(fpk + pidx + tpe);
+        const int ij = __float_as_int(cu.y);
+        const float Cij = cu.x;
         int i = ij & 0xffff, j = ij >> 16;
         int f = qdiv(j, rnpf);
         float G[D], out[NC];
@@ -1335,6 +1325,37 @@ __global__ void round_to_float_kernel(const double *__restrict__ in, float *__re
                                       double shift) {
   for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x)
     out[x] = (float)(in[x] + shift);
+}
+
+// FP64 -> FP32 rounding of Lambda_q (v n_q + i per element) into the
+// node-major layout lambda_stride(d) i + v (padding entries zero)
+__global__ void lambda_node_major_kernel(const double *__restrict__ in, float *__restrict__ out, size_t ne,
+                                         int nq, int d) {
+  const int ls = lambda_stride(d), dd = d * d, per = nq * ls;
+  const size_t n = ne * (size_t)per;
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = x / per;
+    const int t = (int)(x - k * per);
+    const int i = t / ls, v = t - i * ls;
+    out[x] = v < dd ? (float)in[k * (size_t)nq * dd + (size_t)v * nq + i] : 0.f;
+  }
+}
+
+// The mixed phase B's packed pair tables (FP32 roundings of S and C with
+// the packed node indices' bits)
+__global__ void pack_pairs_kernel(const int *__restrict__ vp_ij, const double *__restrict__ vp_S, int nvp,
+                                  const int *__restrict__ fp_ij, const double *__restrict__ fp_C, int nfp, int d,
+                                  float4 *__restrict__ vpk, float2 *__restrict__ fpk) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvp + nfp; t += gridDim.x * blockDim.x) {
+    if (t < nvp) {
+      float s[3] = {0.f, 0.f, 0.f};
+      for (int m = 0; m < d; ++m) s[m] = (float)vp_S[(size_t)t * d + m];
+      vpk[t] = make_float4(s[0], s[1], s[2], __int_as_float(vp_ij[t]));
+    } else {
+      const int q = t - nvp;
+      fpk[q] = make_float2((float)fp_C[q], __int_as_float(fp_ij[q]));
+    }
+  }
 }
 
 // FP64 -> FP32 rounding of halfnJq (m + D (f + nfac i) per element) into the
@@ -1717,6 +1738,22 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
                                         double a, double b, double dt, int first, size_t n,
                                         cudaStream_t st) {
   ck_stage_compensated_kernel<<<elementwise_grid(n), 256, 0, st>>>(u, comp, tmp, k, a, b, dt, first, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lambda_node_major(const double *in, float *out, size_t ne, int nq, int d, cudaStream_t st) {
+  const size_t n = ne * (size_t)nq * lambda_stride(d);
+  if (n == 0) return cudaSuccess;
+  lambda_node_major_kernel<<<elementwise_grid(n), 256, 0, st>>>(in, out, ne, nq, d);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_pairs(const DevOps &op, float *vpk, float *fpk, cudaStream_t st) {
+  const int n = op.nvp + op.nfp;
+  if (n == 0) return cudaSuccess;
+  pack_pairs_kernel<<<(n + 255) / 256, 256, 0, st>>>(op.vp_ij, op.vp_S, op.nvp, op.fp_ij, op.fp_C, op.nfp, op.d,
+                                                     reinterpret_cast<float4 *>(vpk),
+                                                     reinterpret_cast<float2 *>(fpk));
   return cudaGetLastError();
 }
 

@@ -134,6 +134,12 @@ cudaError_t launch_ck_stage_compensated(double *u, double *comp, double *tmp, co
                                         cudaStream_t st);
 // out = (float)(in + shift)
 cudaError_t launch_round_to_float(const double *in, float *out, size_t n, cudaStream_t st, double shift = 0.0);
+// FP64 Lambda_q (n_q x d x d per element) rounded to FP32, node-major with
+// lambda_stride(d) floats per node
+cudaError_t launch_lambda_node_major(const double *in, float *out, size_t ne, int nq, int d, cudaStream_t st);
+// the mixed phase B's packed pair tables: 4 floats per volume pair, 2 per
+// facet pair
+cudaError_t launch_pack_pairs(const DevOps &op, float *vpk, float *fpk, cudaStream_t st);
 // FP64 halfnJq (d x nfac x n_q per element) rounded to FP32 and transposed to
 // (f d + m) n_q + i
 cudaError_t launch_halfnjq_transpose(const double *in, float *out, size_t ne, int nq, int d, int nfac,
