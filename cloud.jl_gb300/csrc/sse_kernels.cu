@@ -721,8 +721,8 @@ __global__ void __launch_bounds__(256) std_time_derivative_kernel(KernelArgs ka)
 // Node-major residuals of the tail product, in quads of four nodes: the
 // first four components of node n are float4 (n & 3) of quad n >> 2, the
 // fifth (NC = 5) is entry n & 3 of the quad's fifth float4, so that one
-// column quad of E_k meets its 4 x NC values in NC / 4 rounded up + 4
-// vector loads
+// column quad of E_k meets its 4 x NC values in four vector loads, plus one
+// for the fifth components
 template <int NC>
 constexpr int kQuadFloats = NC > 4 ? 20 : 16;
 
@@ -812,7 +812,6 @@ __device__ __forceinline__ void load_pair(const float *d, int ch, int p, float *
   v[3] = a.w;
   if constexpr (NC > 4) v[4] = d[4 * ch + p];
 }
-
 
 template <int D, int NC, bool ET>
 __global__ void __launch_bounds__(256, 4) fd_time_derivative_mixed_kernel(KernelArgs ka) {
