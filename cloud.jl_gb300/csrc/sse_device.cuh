@@ -73,20 +73,14 @@ template <> struct OpVals<double> {
   __device__ static const double *A(const DevOps &o) { return o.A; }
   __device__ static const double *B(const DevOps &o) { return o.B; }
   __device__ static const double *C(const DevOps &o) { return o.C; }
-  __device__ static const double *R(const DevOps &o) { return o.R_val; }
   __device__ static const double *Rt(const DevOps &o) { return o.Rt_val; }
-  __device__ static const double *vpS(const DevOps &o) { return o.vp_S; }
-  __device__ static const double *fpC(const DevOps &o) { return o.fp_C; }
   __device__ static const double *Vd(const DevOps &o) { return o.Vd; }
 };
 template <> struct OpVals<float> {
   __device__ static const float *A(const DevOps &o) { return o.Af; }
   __device__ static const float *B(const DevOps &o) { return o.Bf; }
   __device__ static const float *C(const DevOps &o) { return o.Cf; }
-  __device__ static const float *R(const DevOps &o) { return o.R_valf; }
   __device__ static const float *Rt(const DevOps &o) { return o.Rt_valf; }
-  __device__ static const float *vpS(const DevOps &o) { return o.vp_Sf; }
-  __device__ static const float *fpC(const DevOps &o) { return o.fp_Cf; }
   __device__ static const float *Vd(const DevOps &o) { return o.Vdf; }
 };
 
